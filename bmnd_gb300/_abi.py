@@ -1,0 +1,179 @@
+"""ctypes view of the C ABI in include/bmnd_gb300.h and the library loader.
+
+The library (``bmnd_gb300/libbmnd_gb300.so``) is built in-tree by
+:mod:`bmnd_gb300.build`.  There is no fallback: if it is missing or was built
+for another ABI version, :func:`lib` raises ``RuntimeError``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+ABI_VERSION = 1
+MAX_DIMS = 3
+MAX_EDGE = 8
+MAX_PATCH = 512
+MAX_STACK = 32
+
+OK = 0
+ERR_INVALID_ARG = -1
+ERR_UNSUPPORTED = -2
+ERR_WORKSPACE = -3
+ERR_CUDA = -4
+ERR_TIMEOUT = -5
+
+DIST_SSD = 0
+DIST_POISSON_DEVIANCE = 1
+DIST_PEARSON = 2
+DIST_ANSCOMBE_SSD = 3
+
+FILTER_HARD_THRESHOLD = 0
+FILTER_WIENER = 1
+
+GROUP_HAAR = 0
+GROUP_DCT = 1
+GROUP_NONE = 2
+
+WEIGHT_CLASSIC = 0
+WEIGHT_VARIANCE = 1
+
+MATCH_EXACT = 0
+MATCH_FAST = 1
+
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_U64 = ctypes.c_uint64
+_F32P = ctypes.POINTER(ctypes.c_float)
+_I32P = ctypes.POINTER(ctypes.c_int32)
+_I64P = ctypes.POINTER(ctypes.c_int64)
+_U64P = ctypes.POINTER(ctypes.c_uint64)
+
+
+class MatchParams(ctypes.Structure):
+    _fields_ = [
+        ("ndim", _I32),
+        ("counts", _I32 * MAX_DIMS),
+        ("search_radius", _I32 * MAX_DIMS),
+        ("max_matches", _I32),
+        ("min_matches", _I32),
+        ("prefer_power_of_two", _I32),
+        ("distance", _I32),
+        ("stabilize_ties", _I32),
+        ("precision", _I32),
+        ("count_scale", ctypes.c_double),
+    ]
+
+
+class StageParams(ctypes.Structure):
+    _fields_ = [
+        ("ndim", _I32),
+        ("shape", _I32 * MAX_DIMS),
+        ("block", _I32 * MAX_DIMS),
+        ("search_radius", _I32 * MAX_DIMS),
+        ("max_stack", _I32),
+        ("min_stack", _I32),
+        ("distance", _I32),
+        ("stabilize_ties", _I32),
+        ("match_precision", _I32),
+        ("filter", _I32),
+        ("group_transform", _I32),
+        ("variance_k", _I32),
+        ("weight_model", _I32),
+        ("windowed_synthesis", _I32),
+        ("match_threshold", ctypes.c_float),
+        ("ht_lambda", ctypes.c_float),
+        ("wiener_scale", ctypes.c_float),
+        ("reserved0", ctypes.c_float),
+        ("count_scale", ctypes.c_double),
+        ("variance_floor", ctypes.c_double),
+        ("eps", ctypes.c_double),
+        ("spatial_fwd", (ctypes.c_float * (MAX_EDGE * MAX_EDGE)) * MAX_DIMS),
+        ("spatial_inv", (ctypes.c_float * (MAX_EDGE * MAX_EDGE)) * MAX_DIMS),
+        ("window", ctypes.c_float * MAX_PATCH),
+        ("spatial_metric_diag", ctypes.c_double * MAX_PATCH),
+    ]
+
+
+# name -> (restype, argtypes); every symbol include/bmnd_gb300.h declares
+SIGNATURES = {
+    "bmnd_abi_version": (_I32, []),
+    "bmnd_last_error": (ctypes.c_char_p, []),
+    "bmnd_reference_schedule": (
+        _I32,
+        [_I32, _I32P, _I32P, _I32P, ctypes.c_double, _I32, _I32P, _I32P, _I32P, _I64, _I64P],
+    ),
+    "bmnd_blockmatch_patches": (
+        _I32,
+        [ctypes.POINTER(MatchParams), ctypes.c_void_p, _I32, ctypes.c_void_p, _I64,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _U64],
+    ),
+    "bmnd_blockmatch_volume": (
+        _I32,
+        [ctypes.POINTER(MatchParams), ctypes.c_void_p, _I32P, _I32P, ctypes.c_void_p, _I64,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _U64],
+    ),
+    "bmnd_stage_workspace_bytes": (_I32, [ctypes.POINTER(StageParams), _I64, _U64P]),
+    "bmnd_stage": (
+        _I32,
+        [ctypes.POINTER(StageParams), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _I64,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+         _U64, _U64],
+    ),
+    "bmnd_run": (
+        _I32,
+        [ctypes.POINTER(StageParams), ctypes.POINTER(StageParams), ctypes.c_void_p,
+         ctypes.c_void_p, _I64, ctypes.c_void_p, _I64, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_void_p, _U64, _U64],
+    ),
+}
+
+LIB_NAME = "libbmnd_gb300.so"
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> str:
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), LIB_NAME)
+
+
+def lib() -> ctypes.CDLL:
+    """Load the native library once; raise if it is absent or mismatched."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"{LIB_NAME} is not built ({path} missing); run "
+                "`python -c 'import __graft_entry__ as g; g.build()'` or "
+                "`python -m bmnd_gb300.build`"
+            )
+        handle = ctypes.CDLL(path)
+        for name, (restype, argtypes) in SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = restype
+            fn.argtypes = argtypes
+        version = handle.bmnd_abi_version()
+        if version != ABI_VERSION:
+            raise RuntimeError(f"{LIB_NAME} has ABI version {version}, expected {ABI_VERSION}")
+        _lib = handle
+        return _lib
+
+
+class BmndError(RuntimeError):
+    """A non-zero status returned by the native library."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"bmnd_gb300 native call failed ({code}): {message}")
+        self.code = code
+
+
+def check(code: int) -> None:
+    if code != OK:
+        msg = lib().bmnd_last_error()
+        raise BmndError(code, msg.decode() if msg else "")

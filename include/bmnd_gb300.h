@@ -1,0 +1,212 @@
+/*
+ * bmnd_gb300.h -- C ABI of the GB300 (sm_103a) BMND collaborative-filtering path.
+ *
+ * The reference (cduhme/bmnd) is a pure-Python/Numba package whose only
+ * boundary is the Python function bmnd() (src/bmnd/bmndalgo.py:71-83).  This
+ * library replaces the work that function does below its argument validation:
+ * the reference schedule, block matching, group filtering (transforms,
+ * direct-Poisson noise statistics, hard thresholding / Wiener shrinkage,
+ * aggregation weights) and the weighted aggregation with the final division.
+ *
+ * Conventions
+ *   - Plain C types only.  Volumes are C-ordered float32, patch-grid indices
+ *     ("lin") are C-ordered int32 over the patch grid counts[a] = shape[a] -
+ *     block[a] + 1, exactly the linear index the reference uses
+ *     (src/bmnd/blockmatching.py:1112-1114).
+ *   - Device pointers are CUDA device (or managed) memory owned by the caller;
+ *     the library never allocates or frees caller memory and never calls
+ *     cudaMalloc.  Scratch space is a caller-provided workspace whose size
+ *     bmnd_workspace_bytes() reports.
+ *   - "stream" is a cudaStream_t passed as uint64_t (0 = legacy default stream).
+ *     Every launch of a call goes on that stream; calls return after
+ *     enqueueing (device work is asynchronous) unless stated otherwise.
+ *   - Every function returns BMND_OK (0) or a negative BMND_ERR_* code; the
+ *     message of the last failure on the calling thread is bmnd_last_error().
+ */
+#ifndef BMND_GB300_H
+#define BMND_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BMND_ABI_VERSION 1
+#define BMND_MAX_DIMS 3
+#define BMND_MAX_EDGE 8       /* largest patch edge per axis */
+#define BMND_MAX_PATCH 512    /* largest patch volume */
+#define BMND_MAX_STACK 32     /* largest group size */
+
+/* return codes */
+#define BMND_OK 0
+#define BMND_ERR_INVALID_ARG (-1)
+#define BMND_ERR_UNSUPPORTED (-2)
+#define BMND_ERR_WORKSPACE (-3)
+#define BMND_ERR_CUDA (-4)
+#define BMND_ERR_TIMEOUT (-5)
+
+/* block-matching distances (src/bmnd/blockmatching.py:13-16) */
+#define BMND_DIST_SSD 0
+#define BMND_DIST_POISSON_DEVIANCE 1
+#define BMND_DIST_PEARSON 2
+#define BMND_DIST_ANSCOMBE_SSD 3
+
+/* group filters */
+#define BMND_FILTER_HARD_THRESHOLD 0 /* src/bmnd/bmndalgo.py:335-559 */
+#define BMND_FILTER_WIENER 1         /* src/bmnd/bmndalgo.py:760-981 */
+
+/* transform along the group axis (src/bmnd/transforms.py:393-440) */
+#define BMND_GROUP_HAAR 0 /* hierarchical Haar for power-of-two sizes, DCT-II otherwise */
+#define BMND_GROUP_DCT 1  /* orthonormal DCT-II for every size */
+#define BMND_GROUP_NONE 2 /* identity */
+
+/* aggregation weight model (src/bmnd/enums.py:30-33); scope is always "patch" */
+#define BMND_WEIGHT_CLASSIC 0
+#define BMND_WEIGHT_VARIANCE 1
+
+/* matching precision */
+#define BMND_MATCH_EXACT 0 /* FP32 per-term distances for every candidate */
+#define BMND_MATCH_FAST 1  /* approximate screening pass + exact FP32 rescoring inside a margin */
+
+/*
+ * Block matching on one patch grid.  Replaces
+ * _fused_blockmatch_groups_batch_numba (src/bmnd/blockmatching.py:1045-1205)
+ * as driven by blockmatch_groups (:1393-1511).
+ */
+typedef struct BmndMatchParams {
+    int32_t ndim;                          /* 1..BMND_MAX_DIMS */
+    int32_t counts[BMND_MAX_DIMS];         /* patch-grid extents */
+    int32_t search_radius[BMND_MAX_DIMS];  /* window = clip(center +- radius) */
+    int32_t max_matches;                   /* 1..BMND_MAX_STACK */
+    int32_t min_matches;                   /* >= 1 */
+    int32_t prefer_power_of_two;           /* truncate to the largest 2^j (>= min) */
+    int32_t distance;                      /* BMND_DIST_* */
+    int32_t stabilize_ties;                /* canonical-key comparisons (Poisson) */
+    int32_t precision;                     /* BMND_MATCH_* */
+    double count_scale;                    /* poisson_count_scale (> 0) */
+} BmndMatchParams;
+
+/*
+ * One filtering stage (hard thresholding or Wiener) on a volume.
+ * Replaces bmndalgo.py:230-633 (stage 1) and :648-1046 (stage 2).
+ */
+typedef struct BmndStageParams {
+    int32_t ndim;                            /* 1..BMND_MAX_DIMS */
+    int32_t shape[BMND_MAX_DIMS];            /* volume extents */
+    int32_t block[BMND_MAX_DIMS];            /* patch extents */
+    int32_t search_radius[BMND_MAX_DIMS];
+    int32_t max_stack;                       /* 1..BMND_MAX_STACK */
+    int32_t min_stack;
+    int32_t distance;                        /* BMND_DIST_* */
+    int32_t stabilize_ties;
+    int32_t match_precision;                 /* BMND_MATCH_* */
+    int32_t filter;                          /* BMND_FILTER_* */
+    int32_t group_transform;                 /* BMND_GROUP_* */
+    int32_t variance_k;                      /* exact overlap-aware planes (k) */
+    int32_t weight_model;                    /* BMND_WEIGHT_* */
+    int32_t windowed_synthesis;              /* weight domain windowed_synthesis */
+    float match_threshold;                   /* raw distance threshold (non-SSD) */
+    float ht_lambda;                         /* hard-threshold multiplier */
+    float wiener_scale;                      /* mu^2 */
+    float reserved0;
+    double count_scale;                      /* poisson_count_scale (> 0) */
+    double variance_floor;                   /* poisson_variance_floor (>= 0) */
+    double eps;                              /* 1e-10 in the reference */
+    /* per-axis spatial transforms, row-major edge x edge, float32 */
+    float spatial_fwd[BMND_MAX_DIMS][BMND_MAX_EDGE * BMND_MAX_EDGE];
+    float spatial_inv[BMND_MAX_DIMS][BMND_MAX_EDGE * BMND_MAX_EDGE];
+    /* Kaiser aggregation window (C order over the patch), float32 */
+    float window[BMND_MAX_PATCH];
+    /* diag(S_inv^T diag(w^2) S_inv), float64; used only for windowed_synthesis */
+    double spatial_metric_diag[BMND_MAX_PATCH];
+} BmndStageParams;
+
+/* ABI version this library was built with (BMND_ABI_VERSION). */
+int32_t bmnd_abi_version(void);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* bmnd_last_error(void);
+
+/*
+ * Host-only.  GENERATED reference schedule: replaces get_reference_schedule
+ * with mode="generated" (src/bmnd/shifts.py:405-423, :519-576, :229-266).
+ * Writes up to `capacity` rows of reference_abs / reference_shifted / shift
+ * (each n x ndim int32, any may be NULL) and the total count to *out_count.
+ * Call with capacity 0 to size the buffers.
+ */
+int32_t bmnd_reference_schedule(int32_t ndim, const int32_t* counts, const int32_t* block,
+                                const int32_t* step, double shift_density,
+                                int32_t schedule_density, int32_t* out_abs,
+                                int32_t* out_shifted, int32_t* out_shift, int64_t capacity,
+                                int64_t* out_count);
+
+/*
+ * Block matching over an explicit patch table d_patches (n_patches x
+ * patch_vol float32, row = patch-grid lin).  Replaces blockmatch_groups
+ * (src/bmnd/blockmatching.py:1393-1511).  d_refs: n_refs x ndim int32 patch-grid
+ * positions; d_thresholds: n_refs float32 raw thresholds.  Outputs (device):
+ * d_sel n_refs x max_matches int32 (selected lins, reference first, -1
+ * padded), d_count n_refs int32 (final_count), d_accepted n_refs int32
+ * (accepted_count).
+ */
+int32_t bmnd_blockmatch_patches(const BmndMatchParams* params, const float* d_patches,
+                                int32_t patch_vol, const int32_t* d_refs, int64_t n_refs,
+                                const float* d_thresholds, int32_t* d_sel, int32_t* d_count,
+                                int32_t* d_accepted, uint64_t stream);
+
+/*
+ * Block matching where the patch at grid position q is the block of
+ * d_volume starting at q (the reference's extract_patches_strided view,
+ * src/bmnd/utils.py:15-31, without materialising it).  Same outputs as
+ * bmnd_blockmatch_patches; `block` gives the patch extents, params->counts
+ * must equal shape - block + 1.
+ */
+int32_t bmnd_blockmatch_volume(const BmndMatchParams* params, const float* d_volume,
+                               const int32_t* shape, const int32_t* block,
+                               const int32_t* d_refs, int64_t n_refs,
+                               const float* d_thresholds, int32_t* d_sel, int32_t* d_count,
+                               int32_t* d_accepted, uint64_t stream);
+
+/*
+ * Workspace bytes bmnd_stage() needs for `params` and n_refs references.
+ */
+int32_t bmnd_stage_workspace_bytes(const BmndStageParams* params, int64_t n_refs,
+                                   uint64_t* out_bytes);
+
+/*
+ * One filtering stage on the device.
+ *   d_noisy     observation (shape), float32
+ *   d_pilot     stage-1 estimate for the Wiener stage (matching source,
+ *               Wiener reference coefficients and variance source), NULL for
+ *               hard thresholding
+ *   d_refs      n_refs x ndim int32 reference positions (patch grid)
+ *   d_out       estimate: where(den > 0, num / (den + eps), noisy)
+ *               (bmndalgo.py:626-631, :1039-1044)
+ *   d_sel/d_count/d_accepted  optional (NULL) copies of the match sets, laid
+ *               out as in bmnd_blockmatch_patches
+ * The workspace must be at least bmnd_stage_workspace_bytes() bytes and
+ * 256-byte aligned.
+ */
+int32_t bmnd_stage(const BmndStageParams* params, const float* d_noisy, const float* d_pilot,
+                   const int32_t* d_refs, int64_t n_refs, float* d_out, int32_t* d_sel,
+                   int32_t* d_count, int32_t* d_accepted, void* d_workspace,
+                   uint64_t workspace_bytes, uint64_t stream);
+
+/*
+ * Both stages back to back (hard thresholding, then Wiener on the pilot),
+ * i.e. the body of bmnd() for a direct-Poisson profile.  ht/wiener are the
+ * stage parameters, refs_ht/refs_wiener their schedules; d_ht_out receives
+ * the stage-1 estimate (required: it is the Wiener pilot), d_out the result.
+ * The workspace must hold max(stage workspaces).
+ */
+int32_t bmnd_run(const BmndStageParams* ht, const BmndStageParams* wiener,
+                 const float* d_noisy, const int32_t* d_refs_ht, int64_t n_refs_ht,
+                 const int32_t* d_refs_wiener, int64_t n_refs_wiener, float* d_ht_out,
+                 float* d_out, void* d_workspace, uint64_t workspace_bytes, uint64_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BMND_GB300_H */

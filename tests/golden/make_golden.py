@@ -1,0 +1,273 @@
+"""Generate the golden fixtures under ``tests/golden/`` from the reference itself.
+
+The reference (cduhme/bmnd, pure Python + Numba) is imported from its source
+tree with the import stand-ins in ``oracle/shim`` (``numba.njit`` = identity,
+``pywt.Wavelet`` metadata only), so every loop runs with NumPy float32
+semantics.  The fixtures are committed; this script is only needed to
+regenerate them and needs the reference checkout, which the GPU machines do
+not have.
+
+Usage::
+
+    python tests/golden/make_golden.py unit
+    python tests/golden/make_golden.py pipeline bm3d_32 [bm4d_16 ...]
+    python tests/golden/make_golden.py list
+
+``unit`` writes ``unit_*.npz`` (distances, canonical keys, transforms, exact
+and approximate Poisson sigma, weights, schedules); ``pipeline`` writes
+``pipe_<case>.npz`` with the noisy input, both stage estimates (via
+``stage_callback``) and both stages' match sets (via ``blockmatch_callback``).
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REFERENCE_SRC = os.environ.get("BMND_REFERENCE_SRC", "/root/reference/src")
+sys.dont_write_bytecode = True
+sys.path.insert(0, os.path.join(REPO, "oracle", "shim"))
+sys.path.insert(1, REFERENCE_SRC)
+sys.path.insert(2, REPO)
+
+from bmnd_gb300 import phantoms  # noqa: E402
+
+# name -> (profile kind, generator, kwargs, extra profile fields)
+PIPELINE_CASES = {
+    "bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=1), {}),
+    "bm3d_48": ("bm3d", phantoms.shapes_2d, dict(size=48, seed=2), {}),
+    "bm3d_64": ("bm3d", phantoms.shapes_2d, dict(size=64, seed=3), {}),
+    "bm3d_40x24": ("bm3d", "ragged2d", dict(shape=(40, 24), seed=6), {}),
+    "bm3d_lowcount_32": ("bm3d", "lowcount2d", dict(size=32, seed=7), {}),
+    "bm4d_16": ("bm4d", phantoms.ellipsoids_3d, dict(size=16, seed=4, count=6), {}),
+    "bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=5), {}),
+    "bm3d_256_cfg": ("bm3d", phantoms.shapes_2d, dict(size=256, seed=0), {}),
+}
+
+
+def _make_input(gen, kwargs):
+    if gen == "ragged2d":
+        shape = kwargs["shape"]
+        clean, _ = phantoms.shapes_2d(size=max(shape), seed=kwargs["seed"])
+        clean = np.ascontiguousarray(clean[: shape[0], : shape[1]])
+        return clean, phantoms.poisson_noise(clean, kwargs["seed"])
+    if gen == "lowcount2d":
+        clean, _ = phantoms.shapes_2d(size=kwargs["size"], seed=kwargs["seed"])
+        clean = clean * np.float32(2.0 / float(clean.max()))
+        return clean, phantoms.poisson_noise(clean, kwargs["seed"])
+    if gen == "ragged3d":
+        shape = kwargs["shape"]
+        clean, _ = phantoms.ellipsoids_3d(size=shape, seed=kwargs["seed"], count=6)
+        return clean, phantoms.poisson_noise(clean, kwargs["seed"])
+    return gen(**kwargs)
+
+
+def _pack_matches(result, max_stack, ndim):
+    groups = result.groups
+    n = len(groups)
+    sel = np.full((n, max_stack), -1, dtype=np.int32)
+    counts = np.zeros(n, dtype=np.int32)
+    accepted = np.zeros(n, dtype=np.int32)
+    refs = np.zeros((n, ndim), dtype=np.int32)
+    for i, group in enumerate(groups):
+        k = int(group.final_count)
+        sel[i, :k] = group.selected_lin_indices[:k]
+        counts[i] = k
+        accepted[i] = int(group.accepted_count)
+        refs[i] = group.reference_abs
+    return sel, counts, accepted, refs
+
+
+def run_pipeline(name: str) -> None:
+    import bmnd as ref
+
+    kind, gen, kwargs, extra = PIPELINE_CASES[name]
+    clean, noisy = _make_input(gen, kwargs)
+    profile_cls = ref.BM3DProfile if kind == "bm3d" else ref.BM4DProfile
+    profile = profile_cls(noise_model=ref.NoiseModel.POISSON, **extra)
+    stages = {}
+    matches = {}
+
+    def stage_cb(stage, est):
+        stages[stage] = np.asarray(est, dtype=np.float32)
+
+    def bm_cb(stage, result):
+        max_stack = profile.ht_max_stack_size if stage == "ht" else profile.wiener_max_stack_size
+        matches[stage] = _pack_matches(result, max_stack, noisy.ndim)
+
+    t0 = time.time()
+    out = ref.bmnd(noisy, profile, stage_callback=stage_cb, blockmatch_callback=bm_cb)
+    elapsed = time.time() - t0
+    payload = dict(
+        kind=np.array(kind),
+        clean=clean,
+        noisy=noisy,
+        ht=stages["ht"],
+        wiener=stages["wiener"],
+        out=np.asarray(out, dtype=np.float32),
+        seconds=np.float64(elapsed),
+    )
+    for stage, (sel, counts, accepted, refs) in matches.items():
+        payload[f"{stage}_sel"] = sel
+        payload[f"{stage}_count"] = counts
+        payload[f"{stage}_accepted"] = accepted
+        payload[f"{stage}_refs"] = refs
+    path = os.path.join(HERE, f"pipe_{name}.npz")
+    np.savez_compressed(path, **payload)
+    print(f"{name}: {noisy.shape} in {elapsed:.1f} s -> {path}")
+
+
+def run_unit() -> None:
+    from bmnd import blockmatching as bm
+    from bmnd import shifts, transforms, utils, variance, aggregationweights, wiener, poisson
+    from bmnd.enums import AggregationWeightDomain, AggregationWeightModel, AggregationWeightScope
+    from bmnd.profiles import BM3DProfile, BM4DProfile
+
+    rng = np.random.default_rng(1234)
+    out = {}
+
+    # --- patch distances and canonical keys (all four distance codes) ---
+    for patch_vol in (64, 125):
+        n_pairs = 1000
+        lam = rng.uniform(0.0, 60.0, size=(n_pairs, 1))
+        ref_p = rng.poisson(lam, size=(n_pairs, patch_vol)).astype(np.float32)
+        cand = rng.poisson(lam * rng.uniform(0.6, 1.4, size=(n_pairs, 1)), size=(n_pairs, patch_vol)).astype(np.float32)
+        # a share of real-valued (pilot-like) patches
+        ref_p[: n_pairs // 3] += rng.uniform(0.0, 1.0, size=(n_pairs // 3, patch_vol)).astype(np.float32)
+        cand[: n_pairs // 3] += rng.uniform(0.0, 1.0, size=(n_pairs // 3, patch_vol)).astype(np.float32)
+        # zero patches and identical pairs
+        ref_p[-20:] = 0.0
+        cand[-40:-20] = ref_p[-40:-20]
+        for code in range(4):
+            d = np.array(
+                [bm._patch_distance_numba(ref_p[i], cand[i], code, 1.0) for i in range(n_pairs)],
+                dtype=np.float32,
+            )
+            out[f"dist_p{patch_vol}_c{code}"] = d
+        out[f"dist_p{patch_vol}_ref"] = ref_p
+        out[f"dist_p{patch_vol}_cand"] = cand
+    keys_in = np.concatenate(
+        [
+            rng.uniform(0.0, 1.0, 2000),
+            rng.uniform(1.0, 8.0, 2000),
+            rng.uniform(8.0, 1e4, 1000),
+            np.array([0.0, 1.0, 2.0, 2.9527, 0.3937, 0.7689, 3.0, 4.0 - 1e-6]),
+        ]
+    ).astype(np.float32)
+    out["canon_in"] = keys_in
+    out["canon_out"] = np.array([bm._canonicalize_poisson_distance_numba(np.float32(v)) for v in keys_in], dtype=np.float32)
+
+    # --- transforms ---
+    for n in (4, 8):
+        f, i = transforms.get_transform_matrix((1, n), [transforms.Transform(transforms.TransformType.BIOR15, transforms.TransformMode.SPATIAL)])
+        out[f"bior15_fwd_{n}"] = np.asarray(f[1], dtype=np.float32)
+        out[f"bior15_inv_{n}"] = np.asarray(i[1], dtype=np.float32)
+    for n in (4, 5, 8):
+        f, i = transforms.get_transform_matrix((1, n), [transforms.Transform(transforms.TransformType.DCT, transforms.TransformMode.SPATIAL)])
+        out[f"dct_fwd_{n}"] = np.asarray(f[1], dtype=np.float32)
+        out[f"dct_inv_{n}"] = np.asarray(i[1], dtype=np.float32)
+    for n in (1, 2, 4, 8, 16, 32, 3, 6):
+        f, i = transforms.get_transform_matrix((n, 4), [transforms.Transform(transforms.TransformType.HAAR, transforms.TransformMode.GROUP)])
+        out[f"haar_fwd_{n}"] = np.asarray(f[0], dtype=np.float32)
+        out[f"haar_inv_{n}"] = np.asarray(i[0], dtype=np.float32)
+    for shape in ((8, 8), (4, 4, 4), (5, 5, 5)):
+        out["kaiser_" + "x".join(map(str, shape))] = utils.kaiser_window_nd(shape, beta=2.0)
+
+    # --- schedules (GENERATED, defaults) ---
+    sched_cases = [
+        ((25, 25), (8, 8), (3, 3)),
+        ((17, 41), (8, 8), (3, 3)),
+        ((249, 249), (8, 8), (3, 3)),
+        ((13, 13, 13), (4, 4, 4), (3, 3, 3)),
+        ((9, 13, 17), (5, 5, 5), (3, 3, 3)),
+        ((1, 7), (8, 8), (3, 3)),
+    ]
+    for idx, (counts, block, step) in enumerate(sched_cases):
+        items = shifts.get_reference_schedule(counts, block, step, mode="generated", shift_density=2.0, schedule_density=2)
+        out[f"sched{idx}_counts"] = np.array(counts, dtype=np.int64)
+        out[f"sched{idx}_block"] = np.array(block, dtype=np.int64)
+        out[f"sched{idx}_step"] = np.array(step, dtype=np.int64)
+        out[f"sched{idx}_abs"] = np.array([it.reference_abs for it in items], dtype=np.int64).reshape(-1, len(counts))
+        out[f"sched{idx}_shifted"] = np.array([it.reference_shifted for it in items], dtype=np.int64).reshape(-1, len(counts))
+        out[f"sched{idx}_shift"] = np.array([it.shift for it in items], dtype=np.int64).reshape(-1, len(counts))
+
+    # --- group filtering pieces: approximate and exact Poisson sigma, weights, gains ---
+    cases = [
+        ("ht2d", BM3DProfile().ht_transform, (8, 8), 16, 19),
+        ("wi2d", BM3DProfile().wiener_transform, (8, 8), 32, 19),
+        ("ht3d", BM4DProfile().ht_transform, (4, 4, 4), 16, 7),
+        ("wi3d", BM4DProfile().wiener_transform, (5, 5, 5), 32, 7),
+    ]
+    for tag, tlist, block, nmax, radius in cases:
+        ndim = len(block)
+        vol_shape = tuple(b + 2 * radius + 3 for b in block)
+        vol = rng.poisson(20.0, size=vol_shape).astype(np.float32)
+        vmodel = variance.build_poisson_variance_model(vol, variance_floor=1e-10, scale=1.0, source_name="observation")
+        counts = tuple(s - b + 1 for s, b in zip(vol_shape, block))
+        for n in sorted({1, 2, 4, 8, nmax}):
+            if n > nmax:
+                continue
+            # random distinct positions in the counts grid, clustered to create overlap
+            lin = rng.choice(int(np.prod(counts)), size=n, replace=False)
+            abs_pos = np.array(np.unravel_index(lin, counts)).T.astype(np.int64)
+            shifted = abs_pos - abs_pos.min(axis=0, keepdims=True)
+            group_shape = (n,) + block
+            fwd, inv = transforms.get_transform_matrix(group_shape, tlist)
+            patches = np.stack([vol[tuple(slice(a, a + b) for a, b in zip(p, block))] for p in abs_pos])
+            vpatches = np.stack([vmodel.variance_volume[tuple(slice(a, a + b) for a, b in zip(p, block))] for p in abs_pos])
+            coef = transforms.apply_transform_nd(patches, fwd)
+            sigma_approx = variance.get_direct_poisson_noise_std(vpatches, fwd, k=0)
+            sigma = variance.get_direct_poisson_noise_std(
+                vpatches, fwd, k=4, variance_model=vmodel,
+                selected_abs_positions=abs_pos, selected_shifted_positions=shifted, group_shape=group_shape,
+            )
+            thr = np.float32(3.0) * sigma
+            mask = poisson._poisson_hard_threshold_mask(np.abs(coef), thr, 1.0)
+            w_patch = utils.kaiser_window_nd(block, beta=2.0)
+            metric = aggregationweights.get_synthesis_risk_metric_factors(group_shape, inv, w_patch)
+            att = np.asarray(mask, dtype=np.float32)
+            weights_ht = aggregationweights.compute_aggregation_weights(
+                att, model=AggregationWeightModel.VARIANCE, domain=AggregationWeightDomain.COEFFICIENT,
+                scope=AggregationWeightScope.PATCH, noise_variance=np.asarray(sigma, dtype=np.float32) ** 2,
+                signal_power=None, inverse_transform=inv, w_patch=w_patch, metric_factors=metric,
+                mass_functional=None, eps=1e-10,
+            )
+            filt = transforms.apply_transform_nd(coef * mask, inv)
+            gain = wiener.compute_poisson_wiener_gain(coef, sigma, 0.4, eps=1e-10)
+            key = f"grp_{tag}_n{n}"
+            out[key + "_vol"] = vol
+            out[key + "_abs"] = abs_pos
+            out[key + "_coef"] = np.asarray(coef, dtype=np.float32)
+            out[key + "_sigma_approx"] = sigma_approx
+            out[key + "_sigma"] = np.asarray(sigma, dtype=np.float32)
+            out[key + "_mask"] = np.asarray(mask, dtype=np.uint8)
+            out[key + "_weights_ht"] = np.asarray(weights_ht, dtype=np.float32)
+            out[key + "_filt_ht"] = np.asarray(filt, dtype=np.float32)
+            out[key + "_gain"] = np.asarray(gain, dtype=np.float32)
+
+    path = os.path.join(HERE, "unit_reference.npz")
+    np.savez_compressed(path, **out)
+    print(f"unit fixtures -> {path} ({len(out)} arrays)")
+
+
+def main(argv: list[str]) -> None:
+    if not argv or argv[0] == "list":
+        print("\n".join(PIPELINE_CASES))
+        return
+    if argv[0] == "unit":
+        run_unit()
+        return
+    if argv[0] == "pipeline":
+        for name in argv[1:]:
+            run_pipeline(name)
+        return
+    raise SystemExit(f"unknown command {argv[0]!r}")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
