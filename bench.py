@@ -1,0 +1,451 @@
+"""Benchmark: Mvoxel/s of the BMND direct-Poisson path on one GB300.
+
+Workload (default): 256^3 float32 BM4D-Poisson volume of 30 random ellipsoids
+(semi-axes 10-80 voxels, intensities U[5, 30], background 2, Poisson noise;
+seeded synthetic data, see bmnd_gb300/phantoms.py) denoised with
+BM4DProfile(noise_model="poisson") defaults: both stages (hard thresholding,
+then Wiener on the pilot).  One step = one full bmnd() call.
+
+* ``value``  -- voxels / device time of bmnd_device() with the input resident
+  in HBM (CUDA events on the launching stream; L2 flushed between steps).
+* ``e2e``    -- the same metric through the public bmnd() call on a host
+  NumPy array: host->device copy, both stages, device->host copy.
+* ``roofline`` -- the dominant kernel (largest share of the step), timed with
+  CUDA events inside this script.
+* ``cpu_baseline`` -- the C oracle (the reference algorithm restated in C,
+  OpenMP on every host core) on a bounded sample of the same workload.
+
+``--impl reference`` times that CPU implementation alone (rank 0).  Multi-GPU
+runs are independent replicas (one volume per rank, weak scaling).
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "bm4d256": dict(kind="bm4d", size=256, desc="256^3 BM4D-Poisson, 30 ellipsoids"),
+    "bm4d128": dict(kind="bm4d", size=128, desc="128^3 BM4D-Poisson, 30 ellipsoids"),
+    "bm3d2048": dict(kind="bm3d", size=2048, desc="2048^2 BM3D-Poisson, 40 blobs + 60 rectangles"),
+    "bm3d256": dict(kind="bm3d", size=256, desc="256^2 BM3D-Poisson, 12 rectangles/discs"),
+}
+
+
+def make_input(name: str, seed: int):
+    from bmnd_gb300 import phantoms
+
+    w = WORKLOADS[name]
+    if w["kind"] == "bm4d":
+        return phantoms.ellipsoids_3d(w["size"], seed=seed)
+    if w["size"] == 2048:
+        return phantoms.blobs_2d(2048, seed=seed)
+    return phantoms.shapes_2d(w["size"], seed=seed)
+
+
+def make_profile(name: str):
+    import bmnd_gb300 as bg
+
+    cls = bg.BM4DProfile if WORKLOADS[name]["kind"] == "bm4d" else bg.BM3DProfile
+    return cls(noise_model=bg.NoiseModel.POISSON)
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {
+            "sm_mhz": float(np.median(sm)) if sm else None,
+            "sm_max_mhz": float(max(smax)) if smax else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def load_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def profile_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_launch:"):
+                try:
+                    return float(line.split(":", 1)[1].strip())
+                except ValueError:
+                    return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the C oracle on a bounded sample)
+# ---------------------------------------------------------------------------
+def cpu_baseline(workload: str, seed: int, budget_s: float = 20.0) -> dict:
+    import oracle
+
+    _, noisy = make_input(workload, seed) if WORKLOADS[workload]["size"] <= 256 else make_input("bm3d256", seed)
+    if noisy.ndim == 3:
+        crop = 48
+        sample = noisy[:crop, :crop, :crop].copy()
+        desc = f"{crop}^3 corner crop of the same volume, both stages"
+    else:
+        crop = 128
+        sample = noisy[:crop, :crop].copy()
+        desc = f"{crop}^2 corner crop, both stages"
+    threads = os.cpu_count() or 1
+    oracle.build()
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        oracle.bmnd(sample, make_profile(workload), threads=threads)
+        reps += 1
+        if time.perf_counter() - t0 > budget_s or reps >= 3:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    return {
+        "value": sample.size / dt / 1e6,
+        "unit": "Mvoxel/s",
+        "cores": threads,
+        "kind": "port",
+        "sample": desc,
+        "seconds_per_call": dt,
+    }
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def time_kernels(torch, noisy_t, profile, reps: int = 3) -> dict:
+    """CUDA-event times of the block-matching kernels and of each stage."""
+    import bmnd_gb300 as bg
+    from bmnd_gb300 import _abi, plan
+    from bmnd_gb300.validation import resolve_profile
+
+    L = _abi.lib()
+    shape = tuple(noisy_t.shape)
+    resolved = resolve_profile(profile, shape)
+    stream = torch.cuda.current_stream()
+    res = {}
+    pilot = bg.bmnd_device(noisy_t, profile)  # any pilot with the right statistics
+    for stage in ("ht", "wiener"):
+        p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k)
+        block = tuple(getattr(profile, f"{stage}_block_size"))
+        counts = tuple(s - b + 1 for s, b in zip(shape, block))
+        sched = plan.reference_schedule(profile, counts, stage)
+        n = len(sched)
+        refs = torch.from_numpy(np.array(sched.reference_abs, dtype=np.int32)).cuda()
+        thr = torch.full((n,), float(p.match_threshold), device="cuda")
+        sel = torch.empty((n, p.max_stack), dtype=torch.int32, device="cuda")
+        cnt = torch.empty(n, dtype=torch.int32, device="cuda")
+        acc = torch.empty(n, dtype=torch.int32, device="cuda")
+        mp = _abi.MatchParams()
+        mp.ndim = len(shape)
+        for a in range(len(shape)):
+            mp.counts[a] = counts[a]
+            mp.search_radius[a] = p.search_radius[a]
+        mp.max_matches, mp.min_matches, mp.prefer_power_of_two = p.max_stack, p.min_stack, 1
+        mp.distance, mp.stabilize_ties, mp.count_scale = p.distance, 1, p.count_scale
+        sh = (ctypes.c_int32 * len(shape))(*shape)
+        bl = (ctypes.c_int32 * len(shape))(*block)
+        src = noisy_t if stage == "ht" else pilot
+        times = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _abi.check(L.bmnd_blockmatch_volume(ctypes.byref(mp), src.data_ptr(), sh, bl, refs.data_ptr(), n,
+                                                thr.data_ptr(), sel.data_ptr(), cnt.data_ptr(), acc.data_ptr(),
+                                                int(stream.cuda_stream)))
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        nbytes = ctypes.c_uint64(0)
+        _abi.check(L.bmnd_stage_workspace_bytes(ctypes.byref(p), n, ctypes.byref(nbytes)))
+        ws = torch.empty(nbytes.value, dtype=torch.uint8, device="cuda")
+        out = torch.empty_like(noisy_t)
+        stimes = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _abi.check(L.bmnd_stage(ctypes.byref(p), noisy_t.data_ptr(),
+                                    None if stage == "ht" else pilot.data_ptr(), refs.data_ptr(), n,
+                                    out.data_ptr(), None, None, None, ws.data_ptr(), ws.numel(),
+                                    int(stream.cuda_stream)))
+            e1.record(stream)
+            e1.synchronize()
+            stimes.append(e0.elapsed_time(e1))
+        counts_h = cnt.cpu().numpy()
+        windows = 1
+        for a in range(len(shape)):
+            pass
+        # candidate pairs actually scored (clipped windows) -> deviance voxel-terms
+        refs_h = np.array(sched.reference_abs, dtype=np.int64)
+        pairs = np.ones(n, dtype=np.int64)
+        for a in range(len(shape)):
+            lo = np.maximum(refs_h[:, a] - p.search_radius[a], 0)
+            hi = np.minimum(refs_h[:, a] + p.search_radius[a], counts[a] - 1)
+            pairs *= hi - lo + 1
+        P = int(np.prod(block))
+        res[stage] = {
+            "match_ms": float(np.median(times)),
+            "stage_ms": float(np.median(stimes)),
+            "groups": n,
+            "pairs": int(pairs.sum()),
+            "voxel_terms": int(pairs.sum()) * P,
+            "mean_group": float(counts_h.mean()),
+            "P": P,
+        }
+    return res
+
+
+def run_gpu(args, rank: int, world: int) -> dict | None:
+    import torch
+
+    import bmnd_gb300 as bg
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("nccl")
+        dist = dist_mod
+    clean, noisy = make_input(args.workload, seed=rank)
+    profile = make_profile(args.workload)
+    x = torch.from_numpy(noisy).cuda()
+    nvox = noisy.size
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        out = bg.bmnd_device(x, profile, match_precision=args.precision)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(torch.cuda.current_device())
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = bg.bmnd_device(x, profile, match_precision=args.precision)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    if dist:
+        dist.barrier()
+    ms = total_ms / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # end to end through the public API (host array in, host array out)
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        host_out = bg.bmnd(noisy, profile, match_precision=args.precision)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return None
+
+    from bmnd_gb300.phantoms import psnr
+
+    kt = time_kernels(torch, x, profile)
+    peaks = load_peaks()
+    # dominant kernel: the larger of the two matching launches or group-filter launches
+    cands = []
+    for stage in ("ht", "wiener"):
+        k = kt[stage]
+        cands.append((k["match_ms"], f"blockmatch_{stage}", stage))
+        cands.append((k["stage_ms"] - k["match_ms"], f"groupfilter_{stage}", stage))
+    dom_ms, dom_name, dom_stage = max(cands)
+    k = kt[dom_stage]
+    if dom_name.startswith("blockmatch"):
+        # algorithmic bytes: read the matching source once, write the match table
+        alg_bytes = nvox * 4 + k["groups"] * (int(profile.ht_max_stack_size if dom_stage == "ht" else profile.wiener_max_stack_size) + 2) * 4
+    else:
+        # read noisy (+ pilot) once, write float64 numerator and denominator once
+        alg_bytes = nvox * (4 if dom_stage == "ht" else 8) + nvox * 16
+    achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = profile_traffic(dom_name, args.workload)
+    launches_per_step = 6  # per stage: blockmatch, group filter, finalize
+    result = {
+        "metric": "Mvoxel/s at 256^3 BM4D" if args.workload == "bm4d256" else f"Mvoxel/s at {WORKLOADS[args.workload]['desc']}",
+        "value": nvox * world / (ms * 1e-3) / 1e6,
+        "unit": "Mvoxel/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded phantom, Poisson counts)",
+        "config": {
+            "workload": WORKLOADS[args.workload]["desc"],
+            "shape": list(noisy.shape),
+            "profile": "BM4DProfile(noise_model=poisson) defaults" if WORKLOADS[args.workload]["kind"] == "bm4d"
+            else "BM3DProfile(noise_model=poisson) defaults",
+            "match_precision": args.precision,
+            "parallelism": f"replicas{world}",
+            "l2": "flushed between timed steps (256 MiB write)",
+        },
+        "e2e": {
+            "value": nvox * world / e2e_s / 1e6,
+            "unit": "Mvoxel/s",
+            "h2d_bytes_per_step": nvox * 4,
+            "d2h_bytes_per_step": nvox * 4,
+        },
+        "roofline": {
+            "kernel": dom_name,
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peaks["hbm_gbs"],
+            "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"],
+            "traffic": traffic,
+            "peak_source": peaks["source"],
+            "ms_per_launch": dom_ms,
+            "algorithmic_bytes": alg_bytes,
+        },
+        "kernels": kt,
+        "clocks": clocks,
+        "gpu_launches": launches_per_step * args.steps,
+        "psnr_db": psnr(out.cpu().numpy(), clean),
+    }
+    if not args.skip_cpu:
+        result["cpu_baseline"] = cpu_baseline(args.workload, seed=0)
+    if dist:
+        dist.destroy_process_group()
+    return result
+
+
+def run_reference(args, rank: int, world: int) -> dict | None:
+    if rank != 0:
+        return None
+    per = []
+    for _ in range(args.warmup):
+        cpu_baseline(args.workload, seed=0, budget_s=5.0)
+    for _ in range(args.steps):
+        per.append(cpu_baseline(args.workload, seed=0, budget_s=10.0))
+    v = float(np.median([p["value"] for p in per]))
+    cb = dict(per[0])
+    cb["value"] = v
+    return {
+        "impl": "reference",
+        "metric": "Mvoxel/s at 256^3 BM4D" if args.workload == "bm4d256" else f"Mvoxel/s at {WORKLOADS[args.workload]['desc']}",
+        "value": v,
+        "unit": "Mvoxel/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * float(np.median([p["seconds_per_call"] for p in per])),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded phantom, Poisson counts)",
+        "config": {"workload": WORKLOADS[args.workload]["desc"], "sample": cb["sample"]},
+        "cpu_baseline": cb,
+        "e2e": {"value": v, "unit": "Mvoxel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="bm4d256", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="exact", choices=["exact", "fast"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", args.gpus))
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        res = run_gpu(args, rank, world)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

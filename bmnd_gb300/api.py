@@ -1,0 +1,308 @@
+"""``bmnd()``: the reference's public entry point, executed on one GB300.
+
+Same signature, argument checks (in the same order, with the same
+``ValueError`` texts), return contract and callbacks as the reference
+(src/bmnd/bmndalgo.py:71-183, :325-326, :632-633, :742-743, :1045-1046).
+Below the validation every step runs in the native library
+(``libbmnd_gb300.so``) on the current CUDA device; PyTorch only provides the
+device buffers and the stream.  There is no CPU fallback: without a CUDA
+device, or without the built library, the call raises.
+
+Scope of the GPU path: direct-Poisson profiles (``noise_model="poisson"``)
+with the default Poisson options, 1-3 dimensional volumes, patch edges up to
+8 and stacks up to 32.  Anything else raises ``NotImplementedError`` after
+validation.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from collections.abc import Callable
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi, plan
+from .enums import CacheMode, coerce_enum
+from .validation import resolve_profile
+
+__all__ = ["bmnd", "BlockMatchGroup", "BlockMatchResult", "bmnd_device"]
+
+
+@dataclass
+class BlockMatchGroup:
+    """One matched group, as the reference reports it (blockmatching.py:151-160)."""
+
+    reference_abs: tuple[int, ...]
+    reference_shift: tuple[int, ...]
+    reference_shifted: tuple[int, ...]
+    selected_lin_indices: np.ndarray
+    selected_abs_positions: np.ndarray
+    selected_shifted_positions: np.ndarray
+    accepted_count: int
+    final_count: int
+
+
+@dataclass
+class BlockMatchResult:
+    groups: list[BlockMatchGroup]
+
+
+def _validate_sigma(sigma: object) -> float:
+    if isinstance(sigma, (bool, np.bool_)):
+        raise ValueError(f"sigma must be finite and non-negative, got {sigma!r}.")
+    try:
+        value = float(sigma)
+    except (TypeError, ValueError) as exc:
+        raise ValueError(f"sigma must be finite and non-negative, got {sigma!r}.") from exc
+    if not np.isfinite(value) or value < 0.0:
+        raise ValueError(f"sigma must be finite and non-negative, got {sigma!r}.")
+    return value
+
+
+def _validate_max_cache_bytes(budget):
+    """Same accepted values as the reference (cache.py:65-83); the budget itself
+    governs CPU-side covariance caches the GPU path does not have."""
+    if isinstance(budget, str):
+        budget = coerce_enum(budget, CacheMode, "max_cache_bytes mode")
+    if budget is None or budget is CacheMode.AUTO:
+        return budget
+    if isinstance(budget, bool) or not isinstance(budget, (int, np.integer)) or int(budget) < 0:
+        raise ValueError(
+            "max_cache_bytes must be a non-negative integer, 'auto', or None, "
+            f"got {budget!r}."
+        )
+    return int(budget)
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+class _Workspace:
+    """Per-device scratch buffer, grown on demand and reused across calls."""
+
+    def __init__(self):
+        self._lock = threading.Lock()
+        self._buffers = {}
+
+    def get(self, device, nbytes: int):
+        torch = _torch()
+        key = str(device)
+        with self._lock:
+            buf = self._buffers.get(key)
+            if buf is None or buf.numel() < nbytes:
+                buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+                if buf.data_ptr() % 256:
+                    raise RuntimeError("workspace allocation is not 256-byte aligned")
+                self._buffers[key] = buf
+            return buf
+
+
+_WORKSPACE = _Workspace()
+_REFS_CACHE: dict = {}
+
+
+def _device_refs(schedule: plan.Schedule, device):
+    torch = _torch()
+    key = (id(schedule), str(device))
+    hit = _REFS_CACHE.get(key)
+    if hit is not None and hit[0] is schedule:
+        return hit[1]
+    t = torch.from_numpy(np.array(schedule.reference_abs, dtype=np.int32, copy=True)).to(device)
+    if len(_REFS_CACHE) > 64:
+        _REFS_CACHE.clear()
+    _REFS_CACHE[key] = (schedule, t)
+    return t
+
+
+def _match_result(schedule: plan.Schedule, counts, sel, cnt, acc) -> BlockMatchResult:
+    ndim = len(counts)
+    groups = []
+    counts_arr = np.asarray(counts, dtype=np.int64)
+    for i in range(len(schedule)):
+        k = int(cnt[i])
+        lins = sel[i, :k].astype(np.int64)
+        abs_pos = np.stack(np.unravel_index(lins, counts_arr), axis=1).astype(np.int64) if k else np.empty(
+            (0, ndim), dtype=np.int64
+        )
+        if k:
+            shifted = abs_pos - abs_pos.min(axis=0, keepdims=True)
+            ref_shifted = tuple(int(x) for x in shifted[0])
+        else:
+            shifted = abs_pos.copy()
+            ref_shifted = tuple(int(x) for x in schedule.reference_shifted[i])
+        groups.append(
+            BlockMatchGroup(
+                reference_abs=tuple(int(x) for x in schedule.reference_abs[i]),
+                reference_shift=tuple(int(x) for x in schedule.shift[i]),
+                reference_shifted=ref_shifted,
+                selected_lin_indices=lins,
+                selected_abs_positions=abs_pos,
+                selected_shifted_positions=shifted,
+                accepted_count=int(acc[i]),
+                final_count=k,
+            )
+        )
+    return BlockMatchResult(groups=groups)
+
+
+_MATCH_PRECISIONS = {"exact": _abi.MATCH_EXACT, "fast": _abi.MATCH_FAST}
+
+
+def bmnd_device(noisy, profile, *, resolved=None, match_precision: str = "exact",
+                stage_callback=None, blockmatch_callback=None, stream=None):
+    """Run both stages on a float32 CUDA tensor and return the CUDA result tensor.
+
+    ``noisy`` must be a C-contiguous float32 CUDA tensor holding a validated,
+    non-negative, non-zero volume.  This is the device-resident core of
+    :func:`bmnd` (no host copies unless a callback is given).
+    """
+    torch = _torch()
+    shape = tuple(int(s) for s in noisy.shape)
+    if resolved is None:
+        resolved = resolve_profile(profile, shape)
+    precision = _MATCH_PRECISIONS[match_precision]
+    device = noisy.device
+    L = _abi.lib()
+    if stream is None:
+        stream = torch.cuda.current_stream(device)
+    sptr = int(stream.cuda_stream)
+    params = {}
+    schedules = {}
+    need = 0
+    for stage in ("ht", "wiener"):
+        p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance,
+                              resolved.variance_k, precision)
+        block = tuple(int(b) for b in getattr(profile, f"{stage}_block_size"))
+        counts = tuple(s - b + 1 for s, b in zip(shape, block))
+        sched = plan.reference_schedule(profile, counts, stage)
+        nbytes = ctypes.c_uint64(0)
+        _abi.check(L.bmnd_stage_workspace_bytes(ctypes.byref(p), len(sched), ctypes.byref(nbytes)))
+        need = max(need, nbytes.value)
+        params[stage] = (p, counts)
+        schedules[stage] = sched
+    ws = _WORKSPACE.get(device, need)
+    ht_out = torch.empty_like(noisy)
+    out = torch.empty_like(noisy)
+    pilot = None
+    for stage, dst in (("ht", ht_out), ("wiener", out)):
+        p, counts = params[stage]
+        sched = schedules[stage]
+        refs = _device_refs(sched, device)
+        sel = cnt = acc = None
+        if blockmatch_callback is not None:
+            n = len(sched)
+            sel = torch.empty((n, p.max_stack), dtype=torch.int32, device=device)
+            cnt = torch.empty(n, dtype=torch.int32, device=device)
+            acc = torch.empty(n, dtype=torch.int32, device=device)
+        _abi.check(L.bmnd_stage(
+            ctypes.byref(p), noisy.data_ptr(), None if pilot is None else pilot.data_ptr(),
+            refs.data_ptr(), len(sched), dst.data_ptr(),
+            None if sel is None else sel.data_ptr(), None if cnt is None else cnt.data_ptr(),
+            None if acc is None else acc.data_ptr(), ws.data_ptr(), ws.numel(), sptr))
+        if blockmatch_callback is not None:
+            blockmatch_callback(stage, _match_result(sched, counts, sel.cpu().numpy(),
+                                                     cnt.cpu().numpy(), acc.cpu().numpy()))
+        if stage_callback is not None:
+            stage_callback(stage, dst.cpu().numpy().copy())
+        pilot = dst
+    return out
+
+
+def bmnd(
+    volume,
+    profile,
+    sigma: float | None = None,
+    sigma_psd=None,
+    return_sigma_map: bool = False,
+    stage_callback: Callable[[str, np.ndarray], None] | None = None,
+    blockmatch_callback: Callable[[str, BlockMatchResult], None] | None = None,
+    max_cache_bytes=CacheMode.AUTO,
+    *,
+    match_precision: str = "exact",
+):
+    """Denoise ``volume`` with ``profile`` (drop-in for the reference ``bmnd``).
+
+    ``volume`` may be a NumPy array (the result is a NumPy float32 array of
+    the same shape) or a CUDA tensor (the result stays on that device).
+    ``match_precision`` selects exact float32 matching for every candidate
+    ("exact") or screening plus exact rescoring near the selection boundary
+    ("fast").
+    """
+    if sigma is not None and sigma_psd is not None:
+        raise ValueError("sigma and sigma_psd are mutually exclusive.")
+    if sigma is not None:
+        _validate_sigma(sigma)
+    _validate_max_cache_bytes(max_cache_bytes)
+    if match_precision not in _MATCH_PRECISIONS:
+        raise ValueError(f"match_precision must be 'exact' or 'fast', got {match_precision!r}.")
+
+    torch_input = type(volume).__module__.startswith("torch")
+    shape = tuple(int(s) for s in volume.shape)
+    resolved = resolve_profile(profile, shape)
+    if resolved.is_poisson and sigma_psd is not None:
+        raise ValueError(
+            "sigma_psd is only supported for stationary additive noise; "
+            "direct Poisson mode uses a variance volume instead."
+        )
+    if torch_input:
+        torch = _torch()
+        dev_vol = volume.detach()
+        if not bool(torch.isfinite(dev_vol).all()):
+            raise ValueError("volume must contain only finite values.")
+        dev_vol = dev_vol.to(torch.float32)
+        if not bool(torch.isfinite(dev_vol).all()):
+            raise ValueError("volume values must be representable as finite float32 values.")
+        if resolved.is_poisson and bool((dev_vol < 0).any()):
+            raise ValueError("Direct Poisson input must contain only non-negative values.")
+        all_zero = not bool((dev_vol != 0).any())
+    else:
+        arr = np.asarray(volume)
+        if not np.all(np.isfinite(arr)):
+            raise ValueError("volume must contain only finite values.")
+        with np.errstate(over="ignore", invalid="ignore"):
+            vol = arr.astype(np.float32, copy=False)
+        if not np.all(np.isfinite(vol)):
+            raise ValueError("volume values must be representable as finite float32 values.")
+        if resolved.is_poisson and np.any(vol < 0.0):
+            raise ValueError("Direct Poisson input must contain only non-negative values.")
+        all_zero = not np.any(vol != 0.0)
+
+    if all_zero:
+        zero = volume if torch_input else vol
+        if stage_callback is not None:
+            copy = (lambda z: z.cpu().numpy().copy()) if torch_input else (lambda z: z.copy())
+            stage_callback("ht", copy(zero))
+            stage_callback("wiener", copy(zero))
+        if return_sigma_map:
+            smap = np.zeros(shape, dtype=np.float32)
+            return zero, {"ht": smap, "wiener": smap}
+        return zero
+
+    if not resolved.is_poisson:
+        raise plan.unsupported(
+            "Gaussian noise profiles are not on the GPU path; use noise_model='poisson'"
+        )
+    plan.check_poisson_options(profile)
+    if return_sigma_map:
+        raise plan.unsupported("return_sigma_map is not on the GPU path")
+
+    torch = _torch()
+    if not torch.cuda.is_available():
+        raise RuntimeError("bmnd_gb300 needs a CUDA device; no CPU fallback exists")
+    if torch_input:
+        dev = dev_vol.contiguous()
+        if not dev.is_cuda:
+            dev = dev.cuda()
+    else:
+        host = torch.from_numpy(np.ascontiguousarray(vol))
+        dev = host.pin_memory().cuda(non_blocking=True)
+    out = bmnd_device(dev, profile, resolved=resolved, match_precision=match_precision,
+                      stage_callback=stage_callback, blockmatch_callback=blockmatch_callback)
+    if torch_input:
+        return out if volume.is_cuda else out.cpu()
+    return out.cpu().numpy()

@@ -1,0 +1,96 @@
+"""Build ``libbmnd_gb300.so`` in-tree with nvcc for sm_103a.
+
+Every ``csrc/*.cu`` file is compiled in parallel to an object under
+``bmnd_gb300/_build/`` and linked into ``bmnd_gb300/libbmnd_gb300.so``.
+Run ``python -m bmnd_gb300.build`` (``--force`` rebuilds everything).
+"""
+
+from __future__ import annotations
+
+import concurrent.futures
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libbmnd_gb300.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = [
+    "-O3",
+    "-lineinfo",
+    "-std=c++17",
+    "-Xcompiler",
+    "-fPIC",
+    "--expt-relaxed-constexpr",
+    "-Xptxas",
+    "-warn-spills",
+]
+
+
+def nvcc() -> str:
+    path = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(path):
+        raise RuntimeError("nvcc not found")
+    return path
+
+
+def _sources() -> list[str]:
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+
+
+def _headers() -> list[str]:
+    return sorted(glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h")))
+
+
+def _compile(src: str, extra: list[str]) -> str:
+    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-I", INCLUDE, "-c", src, "-o", obj]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")
+    return obj
+
+
+def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> str:
+    """Compile and link the library if any source is newer than it; return its path."""
+    extra = list(extra or [])
+    sources = _sources()
+    newest = max(os.path.getmtime(p) for p in sources + _headers() + [__file__])
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    workers = min(len(sources), os.cpu_count() or 4)
+    with concurrent.futures.ThreadPoolExecutor(max_workers=workers) as pool:
+        objs = list(pool.map(lambda s: _compile(s, extra), sources))
+    tmp = LIB + ".tmp"
+    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcuda"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, LIB)
+    if verbose:
+        print(f"built {LIB}")
+    return LIB
+
+
+def ptxas_report() -> str:
+    """Registers / spills / shared memory per kernel (nvcc -Xptxas -v)."""
+    lines = []
+    for src in _sources():
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-Xptxas", "-v", "-I", INCLUDE, "-c", src, "-o", os.devnull]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        lines.append(f"== {os.path.basename(src)}\n{res.stderr}")
+    return "\n".join(lines)
+
+
+if __name__ == "__main__":
+    if "--ptxas" in sys.argv:
+        print(ptxas_report())
+    else:
+        build(force="--force" in sys.argv, verbose=True)

@@ -1,0 +1,312 @@
+// abi.cu -- the extern "C" entry points declared in include/bmnd_gb300.h.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "bmnd_common.cuh"
+
+namespace bmnd {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+void clear_error() { g_last_error.clear(); }
+int32_t fail(int32_t code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+int32_t cuda_fail(cudaError_t err, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorName(err) + " (" + cudaGetErrorString(err) + ")";
+    return BMND_ERR_CUDA;
+}
+
+int64_t group_filter_smem_bytes(const BmndStageParams& sp);
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// GENERATED reference schedule (src/bmnd/shifts.py:229-266, :519-576)
+// ---------------------------------------------------------------------------
+std::vector<int> axis_shifts(int block, int step, bool allow_multiple, double density) {
+    if (!allow_multiple || block < 3 || step < 1 || step > block) return {0};
+    double safe = density > 0.0 ? density : 0.0;
+    int count = static_cast<int>(std::ceil(safe * (block - 1) / static_cast<double>(step)));
+    count = std::max(count, 1);
+    count = std::min(count, block);
+    if (count == 1) return {0};
+    // np.linspace(0, block - 1, count), rounded half to even, plus 0, sorted unique
+    std::set<int> values{0};
+    double stop = static_cast<double>(block - 1);
+    double delta = stop / static_cast<double>(count - 1);
+    for (int i = 0; i < count; ++i) {
+        double v = (i == count - 1) ? stop : i * delta;
+        values.insert(static_cast<int>(std::nearbyint(v)));
+    }
+    return std::vector<int>(values.begin(), values.end());
+}
+
+int32_t validate_stage(const BmndStageParams& sp) {
+    if (sp.ndim < 1 || sp.ndim > BMND_MAX_DIMS) return fail(BMND_ERR_INVALID_ARG, "ndim must be 1..3");
+    int P = 1;
+    int64_t vox = 1;
+    for (int d = 0; d < sp.ndim; ++d) {
+        if (sp.shape[d] < 1) return fail(BMND_ERR_INVALID_ARG, "shape must be positive");
+        if (sp.block[d] < 1 || sp.block[d] > sp.shape[d])
+            return fail(BMND_ERR_INVALID_ARG, "block must be in [1, shape]");
+        if (sp.block[d] > BMND_MAX_EDGE) return fail(BMND_ERR_UNSUPPORTED, "patch edge above 8");
+        if (sp.search_radius[d] < 0) return fail(BMND_ERR_INVALID_ARG, "search radius must be >= 0");
+        if (2 * static_cast<int64_t>(sp.search_radius[d]) + sp.block[d] > 1000)
+            return fail(BMND_ERR_UNSUPPORTED, "search window too large");
+        P *= sp.block[d];
+        vox *= sp.shape[d];
+    }
+    if (P > BMND_MAX_PATCH) return fail(BMND_ERR_UNSUPPORTED, "patch volume above 512");
+    if (vox > 0x7fffffffLL) return fail(BMND_ERR_UNSUPPORTED, "volume above 2^31 voxels");
+    if (sp.max_stack < 1 || sp.max_stack > BMND_MAX_STACK)
+        return fail(BMND_ERR_UNSUPPORTED, "max_stack must be in [1, 32]");
+    if (sp.min_stack < 1 || sp.min_stack > sp.max_stack)
+        return fail(BMND_ERR_INVALID_ARG, "min_stack must be in [1, max_stack]");
+    if (sp.distance < 0 || sp.distance > 3) return fail(BMND_ERR_INVALID_ARG, "unknown distance");
+    if (sp.filter != BMND_FILTER_HARD_THRESHOLD && sp.filter != BMND_FILTER_WIENER)
+        return fail(BMND_ERR_INVALID_ARG, "unknown filter");
+    if (sp.group_transform < 0 || sp.group_transform > 2)
+        return fail(BMND_ERR_INVALID_ARG, "unknown group transform");
+    if (sp.variance_k < 0) return fail(BMND_ERR_INVALID_ARG, "variance_k must be >= 0");
+    if (sp.weight_model != BMND_WEIGHT_CLASSIC && sp.weight_model != BMND_WEIGHT_VARIANCE)
+        return fail(BMND_ERR_INVALID_ARG, "unknown weight model");
+    if (!(sp.count_scale > 0.0) || !std::isfinite(sp.count_scale))
+        return fail(BMND_ERR_INVALID_ARG, "count_scale must be finite and positive");
+    if (!(sp.variance_floor >= 0.0)) return fail(BMND_ERR_INVALID_ARG, "variance_floor must be >= 0");
+    if (!(sp.eps > 0.0)) return fail(BMND_ERR_INVALID_ARG, "eps must be positive");
+    if (!(sp.match_threshold >= 0.0f) || !std::isfinite(sp.match_threshold))
+        return fail(BMND_ERR_INVALID_ARG, "match threshold must be finite and >= 0");
+    if (group_filter_smem_bytes(sp) > 227 * 1024)
+        return fail(BMND_ERR_UNSUPPORTED, "profile needs more than 227 KB of shared memory per group");
+    return BMND_OK;
+}
+
+struct StageWorkspace {
+    double* num;
+    double* den;
+    int32_t* sel;
+    int32_t* count;
+    int32_t* accepted;
+    uint64_t bytes;
+};
+
+uint64_t align256(uint64_t v) { return (v + 255) & ~uint64_t(255); }
+
+StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
+    StageWorkspace w{};
+    uint64_t vox = static_cast<uint64_t>(volume_voxels(sp));
+    uint64_t off = 0;
+    auto take = [&](uint64_t bytes) {
+        uint64_t o = off;
+        off += align256(bytes);
+        return o;
+    };
+    uint64_t o_num = take(8 * vox);
+    uint64_t o_den = take(8 * vox);
+    uint64_t o_sel = take(4ull * n_refs * sp.max_stack);
+    uint64_t o_cnt = take(4ull * n_refs);
+    uint64_t o_acc = take(4ull * n_refs);
+    w.bytes = off;
+    if (base) {
+        char* b = static_cast<char*>(base);
+        w.num = reinterpret_cast<double*>(b + o_num);
+        w.den = reinterpret_cast<double*>(b + o_den);
+        w.sel = reinterpret_cast<int32_t*>(b + o_sel);
+        w.count = reinterpret_cast<int32_t*>(b + o_cnt);
+        w.accepted = reinterpret_cast<int32_t*>(b + o_acc);
+    }
+    return w;
+}
+
+BmndMatchParams match_params_of(const BmndStageParams& sp) {
+    BmndMatchParams mp{};
+    mp.ndim = sp.ndim;
+    for (int d = 0; d < sp.ndim; ++d) {
+        mp.counts[d] = sp.shape[d] - sp.block[d] + 1;
+        mp.search_radius[d] = sp.search_radius[d];
+    }
+    mp.max_matches = sp.max_stack;
+    mp.min_matches = sp.min_stack;
+    mp.prefer_power_of_two = 1;
+    mp.distance = sp.distance;
+    mp.stabilize_ties = sp.stabilize_ties;
+    mp.precision = sp.match_precision;
+    mp.count_scale = sp.count_scale;
+    return mp;
+}
+
+int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pilot,
+                  const int32_t* refs, int64_t n_refs, float* out, int32_t* sel, int32_t* count,
+                  int32_t* accepted, void* ws, uint64_t ws_bytes, cudaStream_t stream) {
+    int32_t rc = validate_stage(sp);
+    if (rc) return rc;
+    if (!noisy || !out) return fail(BMND_ERR_INVALID_ARG, "noisy and out are required");
+    if (sp.filter == BMND_FILTER_WIENER && !pilot)
+        return fail(BMND_ERR_INVALID_ARG, "the Wiener stage needs the pilot estimate");
+    if (n_refs < 0 || (n_refs > 0 && !refs)) return fail(BMND_ERR_INVALID_ARG, "bad reference list");
+    StageWorkspace need = carve(sp, n_refs, nullptr);
+    if (!ws || ws_bytes < need.bytes) return fail(BMND_ERR_WORKSPACE, "workspace too small");
+    if (reinterpret_cast<uintptr_t>(ws) % 256 != 0)
+        return fail(BMND_ERR_INVALID_ARG, "workspace must be 256-byte aligned");
+    StageWorkspace w = carve(sp, n_refs, ws);
+    if (sel) w.sel = sel;
+    if (count) w.count = count;
+    if (accepted) w.accepted = accepted;
+    uint64_t vox = static_cast<uint64_t>(volume_voxels(sp));
+    BMND_CUDA_TRY(cudaMemsetAsync(w.num, 0, 8 * vox, stream));
+    BMND_CUDA_TRY(cudaMemsetAsync(w.den, 0, 8 * vox, stream));
+    BmndMatchParams mp = match_params_of(sp);
+    const float* match_src = sp.filter == BMND_FILTER_WIENER ? pilot : noisy;
+    rc = launch_blockmatch_volume(mp, match_src, sp.shape, sp.block, refs, n_refs, nullptr,
+                                  sp.match_threshold, w.sel, w.count, w.accepted, stream);
+    if (rc) return rc;
+    rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, stream);
+    if (rc) return rc;
+    return launch_finalize(sp, w.num, w.den, noisy, out, stream);
+}
+
+}  // namespace
+}  // namespace bmnd
+
+using namespace bmnd;
+
+extern "C" {
+
+int32_t bmnd_abi_version(void) { return BMND_ABI_VERSION; }
+
+const char* bmnd_last_error(void) { return g_last_error.c_str(); }
+
+int32_t bmnd_reference_schedule(int32_t ndim, const int32_t* counts, const int32_t* block,
+                                const int32_t* step, double shift_density,
+                                int32_t schedule_density, int32_t* out_abs, int32_t* out_shifted,
+                                int32_t* out_shift, int64_t capacity, int64_t* out_count) {
+    clear_error();
+    if (ndim < 1 || ndim > BMND_MAX_DIMS) return fail(BMND_ERR_INVALID_ARG, "ndim must be 1..3");
+    if (!counts || !block || !step || !out_count) return fail(BMND_ERR_INVALID_ARG, "null argument");
+    std::vector<std::vector<int>> shifts(ndim);
+    int last[BMND_MAX_DIMS], slots[BMND_MAX_DIMS];
+    int64_t total_slots = 1, grid = 1;
+    for (int d = 0; d < ndim; ++d) {
+        if (step[d] < 1) return fail(BMND_ERR_INVALID_ARG, "step must be positive");
+        if (counts[d] < 1) return fail(BMND_ERR_INVALID_ARG, "counts must be positive");
+        shifts[d] = axis_shifts(block[d], step[d], d < std::max(ndim - 1, 0), shift_density);
+        last[d] = std::max(counts[d] - 1, 0);
+        slots[d] = (last[d] + step[d] - 1) / step[d] + 1;
+        total_slots *= slots[d];
+        grid *= counts[d];
+    }
+    int phases = std::max(1, static_cast<int>(schedule_density));
+    std::vector<uint8_t> seen(static_cast<size_t>(grid), 0);
+    int64_t n = 0;
+    int slot[BMND_MAX_DIMS];
+    for (int64_t s = 0; s < total_slots; ++s) {
+        int64_t rem = s;
+        for (int d = ndim - 1; d >= 0; --d) {
+            slot[d] = static_cast<int>(rem % slots[d]);
+            rem /= slots[d];
+        }
+        for (int ph = 0; ph < phases; ++ph) {
+            int abs_pos[BMND_MAX_DIMS], base[BMND_MAX_DIMS];
+            int64_t lin = 0;
+            for (int d = 0; d < ndim; ++d) {
+                int b = std::min(slot[d] * step[d], last[d]);
+                int offset = 0;
+                if (d < ndim - 1) {
+                    const std::vector<int>& sh = shifts[d];
+                    offset = sh[(slot[d + 1] + ph) % static_cast<int>(sh.size())];
+                }
+                int a = std::min(std::max(b - offset, 0), last[d]);
+                if (slot[d] == slots[d] - 1) a = last[d];
+                base[d] = b;
+                abs_pos[d] = a;
+                lin = lin * counts[d] + a;
+            }
+            if (seen[lin]) continue;
+            seen[lin] = 1;
+            if (n < capacity) {
+                for (int d = 0; d < ndim; ++d) {
+                    if (out_abs) out_abs[n * ndim + d] = abs_pos[d];
+                    if (out_shifted) out_shifted[n * ndim + d] = base[d];
+                    if (out_shift) out_shift[n * ndim + d] = base[d] - abs_pos[d];
+                }
+            }
+            ++n;
+        }
+    }
+    *out_count = n;
+    return BMND_OK;
+}
+
+int32_t bmnd_blockmatch_patches(const BmndMatchParams* params, const float* d_patches,
+                                int32_t patch_vol, const int32_t* d_refs, int64_t n_refs,
+                                const float* d_thresholds, int32_t* d_sel, int32_t* d_count,
+                                int32_t* d_accepted, uint64_t stream) {
+    clear_error();
+    if (!params || !d_patches || !d_thresholds || !d_sel || !d_count || !d_accepted ||
+        (n_refs > 0 && !d_refs))
+        return fail(BMND_ERR_INVALID_ARG, "null argument");
+    return launch_blockmatch_patches(*params, d_patches, patch_vol, d_refs, n_refs, d_thresholds,
+                                     d_sel, d_count, d_accepted, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int32_t bmnd_blockmatch_volume(const BmndMatchParams* params, const float* d_volume,
+                               const int32_t* shape, const int32_t* block, const int32_t* d_refs,
+                               int64_t n_refs, const float* d_thresholds, int32_t* d_sel,
+                               int32_t* d_count, int32_t* d_accepted, uint64_t stream) {
+    clear_error();
+    if (!params || !d_volume || !shape || !block || !d_thresholds || !d_sel || !d_count ||
+        !d_accepted || (n_refs > 0 && !d_refs))
+        return fail(BMND_ERR_INVALID_ARG, "null argument");
+    return launch_blockmatch_volume(*params, d_volume, shape, block, d_refs, n_refs, d_thresholds,
+                                    0.0f, d_sel, d_count, d_accepted,
+                                    reinterpret_cast<cudaStream_t>(stream));
+}
+
+int32_t bmnd_stage_workspace_bytes(const BmndStageParams* params, int64_t n_refs,
+                                   uint64_t* out_bytes) {
+    clear_error();
+    if (!params || !out_bytes || n_refs < 0) return fail(BMND_ERR_INVALID_ARG, "bad argument");
+    int32_t rc = validate_stage(*params);
+    if (rc) return rc;
+    *out_bytes = carve(*params, n_refs, nullptr).bytes;
+    return BMND_OK;
+}
+
+int32_t bmnd_stage(const BmndStageParams* params, const float* d_noisy, const float* d_pilot,
+                   const int32_t* d_refs, int64_t n_refs, float* d_out, int32_t* d_sel,
+                   int32_t* d_count, int32_t* d_accepted, void* d_workspace,
+                   uint64_t workspace_bytes, uint64_t stream) {
+    clear_error();
+    if (!params) return fail(BMND_ERR_INVALID_ARG, "null params");
+    return run_stage(*params, d_noisy, d_pilot, d_refs, n_refs, d_out, d_sel, d_count, d_accepted,
+                     d_workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int32_t bmnd_run(const BmndStageParams* ht, const BmndStageParams* wiener, const float* d_noisy,
+                 const int32_t* d_refs_ht, int64_t n_refs_ht, const int32_t* d_refs_wiener,
+                 int64_t n_refs_wiener, float* d_ht_out, float* d_out, void* d_workspace,
+                 uint64_t workspace_bytes, uint64_t stream) {
+    clear_error();
+    if (!ht || !wiener || !d_ht_out) return fail(BMND_ERR_INVALID_ARG, "null argument");
+    if (ht->filter != BMND_FILTER_HARD_THRESHOLD || wiener->filter != BMND_FILTER_WIENER)
+        return fail(BMND_ERR_INVALID_ARG, "bmnd_run takes a hard-threshold then a Wiener stage");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int32_t rc = run_stage(*ht, d_noisy, nullptr, d_refs_ht, n_refs_ht, d_ht_out, nullptr, nullptr,
+                           nullptr, d_workspace, workspace_bytes, s);
+    if (rc) return rc;
+    return run_stage(*wiener, d_noisy, d_ht_out, d_refs_wiener, n_refs_wiener, d_out, nullptr,
+                     nullptr, nullptr, d_workspace, workspace_bytes, s);
+}
+
+}  // extern "C"

@@ -1,0 +1,165 @@
+// bmnd_common.cuh -- shared device helpers of the GB300 BMND library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstring>
+#include <string>
+
+#include "../../include/bmnd_gb300.h"
+
+namespace bmnd {
+
+// ---------------------------------------------------------------------------
+// error reporting (thread-local message behind bmnd_last_error)
+// ---------------------------------------------------------------------------
+void set_error(const std::string& msg);
+void clear_error();
+int32_t fail(int32_t code, const std::string& msg);
+int32_t cuda_fail(cudaError_t err, const char* what);
+
+#define BMND_CUDA_TRY(expr)                                      \
+    do {                                                         \
+        cudaError_t _e = (expr);                                 \
+        if (_e != cudaSuccess) return ::bmnd::cuda_fail(_e, #expr); \
+    } while (0)
+
+#define BMND_LAUNCH_CHECK(what)                                   \
+    do {                                                          \
+        cudaError_t _e = cudaGetLastError();                      \
+        if (_e != cudaSuccess) return ::bmnd::cuda_fail(_e, what); \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// canonical Poisson distance keys
+//
+// The reference compares Poisson distances after rounding them to a quantum of
+// 32 * 2^-23 * 2^floor(log2(max(|d|, 1))) with round-half-even
+// (src/bmnd/blockmatching.py:957-964).  For a float32 d that quantum is a
+// power of two, so d / quantum is an exact scaling, rint() is exact in float32
+// (the scaled value is below 2^19) and so is the product back: the key is
+// computed exactly in float32 here.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline float canonical_key(float d) {
+    if (!(d == d) || d == INFINITY || d == -INFINITY) return d;
+    float mag = fabsf(d);
+    int e = 0;
+    if (mag >= 1.0f) {
+        int ex;
+        frexpf(mag, &ex);  // mag = f * 2^ex, f in [0.5, 1)
+        e = ex - 1;
+    }
+    float scaled = ldexpf(d, 18 - e);
+    return ldexpf(rintf(scaled), e - 18);
+}
+
+// order-preserving uint32 image of a float (total order for non-NaN values)
+__host__ __device__ inline uint32_t order_bits(float f) {
+#ifdef __CUDA_ARCH__
+    uint32_t u = __float_as_uint(f);
+#else
+    uint32_t u;
+    memcpy(&u, &f, sizeof(u));
+#endif
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__host__ __device__ inline uint64_t composite_key(float key, int32_t lin) {
+    return (static_cast<uint64_t>(order_bits(key)) << 32) | static_cast<uint32_t>(lin);
+}
+
+// ---------------------------------------------------------------------------
+// group-axis transform entries
+//
+// Hierarchical Haar matrix of a power-of-two size n = 2^L as the reference
+// builds it (src/bmnd/transforms.py:393-408): row 0 is s^L, the detail rows
+// created at level l (rows [2^(l-1), 2^l)) carry +-s^(L-l+1) on a support of
+// 2^(L-l+1) columns.  s^m is the float32 product s*s*...*s evaluated left to
+// right, exactly as the repeated kron products produce it.  Other sizes (and
+// BMND_GROUP_DCT) use the orthonormal DCT-II evaluated in float64 and rounded
+// (transforms.py:424-436).
+// ---------------------------------------------------------------------------
+__host__ __device__ inline bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+__host__ __device__ inline float haar_power(int m) {
+    const float s = 0.70710677f;  // float32(1 / sqrt(2))
+    float p = 1.0f;
+    for (int i = 0; i < m; ++i) p = p * s;
+    return p;
+}
+
+__host__ __device__ inline int ilog2_floor(int v) {
+    int l = 0;
+    while ((1 << (l + 1)) <= v) ++l;
+    return l;
+}
+
+__host__ __device__ inline float haar_entry(int n, int i, int g) {
+    int L = ilog2_floor(n);
+    if (i == 0) return haar_power(L);
+    int l = ilog2_floor(i) + 1;
+    int c = 1 << (l - 1);
+    int j = i - c;
+    int width = n >> (l - 1);
+    int start = j * width;
+    int half = width >> 1;
+    float v = haar_power(L - l + 1);
+    if (g >= start && g < start + half) return v;
+    if (g >= start + half && g < start + width) return -v;
+    return 0.0f;
+}
+
+__host__ __device__ inline float dct_entry(int n, int f, int s) {
+    const double pi = 3.141592653589793;
+    double norm = f == 0 ? sqrt(1.0 / n) : sqrt(2.0 / n);
+    return static_cast<float>(norm * cos(pi * (s + 0.5) * f / n));
+}
+
+__host__ __device__ inline float group_entry(int kind, int n, int i, int g) {
+    if (kind == BMND_GROUP_NONE) return i == g ? 1.0f : 0.0f;
+    if (kind == BMND_GROUP_HAAR && is_pow2(n)) return haar_entry(n, i, g);
+    return dct_entry(n, i, g);
+}
+
+// exact float32 operations that the compiler must not contract into FMAs
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+
+struct Dims {
+    int32_t ndim;
+    int32_t shape[BMND_MAX_DIMS];
+    int32_t block[BMND_MAX_DIMS];
+    int32_t counts[BMND_MAX_DIMS];
+};
+
+inline int64_t volume_voxels(const BmndStageParams& p) {
+    int64_t n = 1;
+    for (int d = 0; d < p.ndim; ++d) n *= p.shape[d];
+    return n;
+}
+
+inline int patch_volume(const BmndStageParams& p) {
+    int n = 1;
+    for (int d = 0; d < p.ndim; ++d) n *= p.block[d];
+    return n;
+}
+
+// launch helpers implemented in the .cu files
+int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume, const int32_t* shape,
+                                 const int32_t* block, const int32_t* refs, int64_t n_refs,
+                                 const float* thresholds, float scalar_threshold, int32_t* sel,
+                                 int32_t* count, int32_t* accepted, cudaStream_t stream);
+int32_t launch_blockmatch_patches(const BmndMatchParams& mp, const float* patches, int32_t patch_vol,
+                                  const int32_t* refs, int64_t n_refs, const float* thresholds,
+                                  int32_t* sel, int32_t* count, int32_t* accepted,
+                                  cudaStream_t stream);
+int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const float* pilot,
+                            const int32_t* sel, const int32_t* count, int64_t n_refs, double* num,
+                            double* den, cudaStream_t stream);
+int32_t launch_finalize(const BmndStageParams& sp, const double* num, const double* den,
+                        const float* noisy, float* out, cudaStream_t stream);
+
+}  // namespace bmnd

@@ -1,0 +1,183 @@
+"""GPU block matching through the C ABI vs the reference's known answers and the oracle."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from parity import compare_match_sets
+
+pytestmark = pytest.mark.gpu
+
+
+def _mp(counts, radius, max_m, min_m, code, stabilize=True, scale=1.0, pow2=True):
+    from bmnd_gb300 import _abi
+
+    p = _abi.MatchParams()
+    p.ndim = len(counts)
+    for a, (c, r) in enumerate(zip(counts, radius)):
+        p.counts[a] = c
+        p.search_radius[a] = r
+    p.max_matches, p.min_matches = max_m, min_m
+    p.prefer_power_of_two = int(pow2)
+    p.distance = code
+    p.stabilize_ties = int(stabilize)
+    p.count_scale = scale
+    return p
+
+
+def gpu_match_patches(torch, native, patches, counts, refs, radius, max_m, min_m, thr, code,
+                      stabilize=True, scale=1.0, pow2=True):
+    from bmnd_gb300 import _abi
+
+    dev = torch.device("cuda:0")
+    pt = torch.from_numpy(np.ascontiguousarray(patches, dtype=np.float32)).to(dev)
+    rt = torch.from_numpy(np.ascontiguousarray(refs, dtype=np.int32).reshape(-1, len(counts))).to(dev)
+    n = rt.shape[0]
+    tt = torch.full((max(n, 1),), float(np.float32(thr)), dtype=torch.float32, device=dev)
+    sel = torch.full((max(n, 1), max_m), -7, dtype=torch.int32, device=dev)
+    cnt = torch.zeros(max(n, 1), dtype=torch.int32, device=dev)
+    acc = torch.zeros(max(n, 1), dtype=torch.int32, device=dev)
+    p = _mp(counts, radius, max_m, min_m, code, stabilize, scale, pow2)
+    _abi.check(native.bmnd_blockmatch_patches(ctypes.byref(p), pt.data_ptr(), pt.shape[1], rt.data_ptr(),
+                                              n, tt.data_ptr(), sel.data_ptr(), cnt.data_ptr(),
+                                              acc.data_ptr(), 0))
+    torch.cuda.synchronize()
+    return sel.cpu().numpy()[:n], cnt.cpu().numpy()[:n], acc.cpu().numpy()[:n]
+
+
+def selected(sel, cnt, i):
+    return sel[i, : cnt[i]].tolist()
+
+
+SSD, DEV, PEARSON, ANSCOMBE = 0, 1, 2, 3
+
+
+def test_self_only_with_zero_radius(cuda, native):
+    # tests/test_blockmatching_unit.py:11-30
+    patches = np.array([[0.0, 0.0], [1.0, 1.0], [2.0, 2.0]], dtype=np.float32)
+    sel, cnt, _ = gpu_match_patches(cuda, native, patches, (3,), [[0], [1], [2]], (0,), 2, 1, 1.0, SSD,
+                                    stabilize=False, pow2=False)
+    assert [selected(sel, cnt, i) for i in range(3)] == [[0], [1], [2]]
+
+
+def test_includes_self_in_neighbors(cuda, native):
+    # tests/test_blockmatching_unit.py:32-48
+    patches = np.array([[0.0, 0.0], [1.0, 1.0], [2.0, 2.0]], dtype=np.float32)
+    sel, cnt, _ = gpu_match_patches(cuda, native, patches, (3,), [[1]], (1,), 2, 1, 100.0, SSD,
+                                    stabilize=False, pow2=False)
+    assert selected(sel, cnt, 0) == [1, 0]
+
+
+@pytest.mark.parametrize("code", [DEV, PEARSON, ANSCOMBE])
+def test_poisson_distances_account_for_count_dependent_variance(cuda, native, code):
+    # tests/test_blockmatching_unit.py:101-133
+    patches = np.array([[0.0, 2.0], [2.0, 2.0], [1.0, 1.0]], dtype=np.float32)
+    sel, cnt, _ = gpu_match_patches(cuda, native, patches, (3,), [[2]], (2,), 3, 1, 100.0, SSD,
+                                    stabilize=False, pow2=False)
+    assert selected(sel, cnt, 0) == [2, 0, 1]
+    sel, cnt, _ = gpu_match_patches(cuda, native, patches, (3,), [[2]], (2,), 3, 1, 100.0, code,
+                                    stabilize=False, pow2=False)
+    assert selected(sel, cnt, 0) == [2, 1, 0]
+
+
+@pytest.mark.parametrize("code", [DEV, PEARSON, ANSCOMBE])
+def test_poisson_distances_are_invariant_to_representation_scale(cuda, native, code):
+    # tests/test_blockmatching_unit.py:145-181
+    counts_p = np.array([[11.0, 9.0], [10.0, 10.0], [20.0, 20.0]], dtype=np.float32)
+    a, ca, _ = gpu_match_patches(cuda, native, counts_p, (3,), [[1]], (1,), 3, 1, 0.2, code,
+                                 stabilize=False, pow2=False, scale=1.0)
+    b, cb, _ = gpu_match_patches(cuda, native, 7.0 * counts_p, (3,), [[1]], (1,), 3, 1, 0.2, code,
+                                 stabilize=False, pow2=False, scale=7.0)
+    assert selected(a, ca, 0) == [1, 0]
+    assert selected(b, cb, 0) == selected(a, ca, 0)
+
+
+def test_min_stack_fill_from_rejected(cuda, native):
+    # tests/test_blockmatching_internal_unit.py:96-109
+    patches = np.array([[0.0], [10.0], [20.0], [30.0]], dtype=np.float32)
+    sel, cnt, acc = gpu_match_patches(cuda, native, patches, (4,), [[1]], (3,), 4, 3, 1e-8, SSD,
+                                      stabilize=False, pow2=False)
+    assert acc[0] == 1 and cnt[0] == 3
+    assert selected(sel, cnt, 0) == [1, 0, 2]
+
+
+def test_tie_break_by_linear_index_and_reference_first(cuda, native):
+    # ties at equal distance resolve by linear index; the reference leads
+    patches = np.array([[5.0], [5.0], [5.0], [5.0], [5.0]], dtype=np.float32)
+    sel, cnt, acc = gpu_match_patches(cuda, native, patches, (5,), [[3]], (4,), 4, 1, 1.0, DEV,
+                                      stabilize=True, pow2=False)
+    assert selected(sel, cnt, 0) == [3, 0, 1, 2]
+    assert acc[0] == 5
+
+
+def test_power_of_two_truncation(cuda, native):
+    patches = np.arange(7, dtype=np.float32).reshape(7, 1)
+    sel, cnt, _ = gpu_match_patches(cuda, native, patches, (7,), [[3]], (3,), 16, 2, 100.0, SSD,
+                                    stabilize=False, pow2=True)
+    assert cnt[0] == 4
+    assert selected(sel, cnt, 0) == [3, 2, 4, 1]
+
+
+def test_batch_and_order_invariance(cuda, native):
+    rng = np.random.default_rng(3)
+    patches = rng.poisson(8.0, size=(50, 9)).astype(np.float32)
+    refs = np.arange(50).reshape(-1, 1)
+    a = gpu_match_patches(cuda, native, patches, (50,), refs, (6,), 8, 2, 3.0, DEV)
+    b = gpu_match_patches(cuda, native, patches, (50,), refs[::-1], (6,), 8, 2, 3.0, DEV)
+    np.testing.assert_array_equal(a[0], b[0][::-1])
+    np.testing.assert_array_equal(a[1], b[1][::-1])
+
+
+@pytest.mark.parametrize("code", [SSD, DEV, PEARSON, ANSCOMBE])
+def test_patch_table_matches_oracle_2d(cuda, native, oracle_lib, code):
+    rng = np.random.default_rng(100 + code)
+    counts = (23, 31)
+    lam = rng.uniform(0.5, 30.0, size=(counts[0] * counts[1], 1))
+    patches = rng.poisson(lam, size=(counts[0] * counts[1], 16)).astype(np.float32)
+    refs = np.array([(i, j) for i in range(0, counts[0], 2) for j in range(0, counts[1], 3)], dtype=np.int32)
+    thr = 1e9 if code == SSD else 2.5
+    g = gpu_match_patches(cuda, native, patches, counts, refs, (5, 4), 16, 2, thr, code,
+                          stabilize=code != SSD)
+    o = oracle_lib.blockmatch_patches(patches, counts, refs, (5, 4), 16, 2, thr, code,
+                                      stabilize=code != SSD)
+    np.testing.assert_array_equal(g[2], o[2])
+    np.testing.assert_array_equal(g[1], o[1])
+    assert np.mean(np.all(g[0] == o[0], axis=1)) >= 0.98
+
+
+@pytest.mark.parametrize("shape,block,radius,max_m,thr", [
+    ((48, 40), (8, 8), (19, 19), 16, 2.9527),
+    ((48, 40), (8, 8), (19, 19), 32, 0.3937),
+    ((20, 22, 18), (4, 4, 4), (7, 7, 7), 16, 2.9527),
+    ((20, 22, 18), (5, 5, 5), (7, 7, 7), 32, 0.7689),
+])
+def test_volume_matching_vs_oracle(cuda, native, oracle_lib, shape, block, radius, max_m, thr):
+    from bmnd_gb300 import _abi
+
+    rng = np.random.default_rng(sum(shape))
+    base = rng.uniform(1.0, 40.0, size=shape)
+    vol = rng.poisson(base).astype(np.float32)
+    counts = tuple(s - b + 1 for s, b in zip(shape, block))
+    refs = np.stack(np.meshgrid(*[np.arange(0, c, 3) for c in counts], indexing="ij"), -1).reshape(-1, len(shape))
+    refs = refs.astype(np.int32)
+    dev = cuda.device("cuda:0")
+    vt = cuda.from_numpy(vol).to(dev)
+    rt = cuda.from_numpy(refs).to(dev)
+    n = refs.shape[0]
+    tt = cuda.full((n,), float(np.float32(thr)), device=dev)
+    sel = cuda.empty((n, max_m), dtype=cuda.int32, device=dev)
+    cnt = cuda.empty(n, dtype=cuda.int32, device=dev)
+    acc = cuda.empty(n, dtype=cuda.int32, device=dev)
+    p = _mp(counts, radius, max_m, 2, DEV)
+    sh = (ctypes.c_int32 * len(shape))(*shape)
+    bl = (ctypes.c_int32 * len(shape))(*block)
+    _abi.check(native.bmnd_blockmatch_volume(ctypes.byref(p), vt.data_ptr(), sh, bl, rt.data_ptr(), n,
+                                             tt.data_ptr(), sel.data_ptr(), cnt.data_ptr(), acc.data_ptr(), 0))
+    cuda.cuda.synchronize()
+    gs, gc, ga = sel.cpu().numpy(), cnt.cpu().numpy(), acc.cpu().numpy()
+    os_, oc, oa = oracle_lib.blockmatch_volume(vol, block, refs, radius, max_m, 2, thr, DEV)
+    eq, tied, bad = compare_match_sets(oracle_lib, vol, block, refs, gs, gc, os_, oc, DEV, thr)
+    assert not bad, f"unexplained match-set differences in rows {bad[:10]}"
+    assert eq >= 0.98 * n
+    assert np.mean(ga == oa) >= 0.98

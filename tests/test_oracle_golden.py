@@ -1,0 +1,82 @@
+"""The C oracle against the reference's own outputs (golden fixtures), on CPU.
+
+Pins the oracle before it is trusted as the GPU checker: same schedules, same
+match sets (up to near-ties of the reference's key rounding), estimates
+within 1e-3 counts of the reference everywhere outside tie footprints.
+"""
+
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from parity import compare_match_sets, output_parity, tie_footprint
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = sorted(os.path.basename(p)[5:-4] for p in glob.glob(os.path.join(GOLDEN, "pipe_*.npz")))
+UNIT = os.path.join(GOLDEN, "unit_reference.npz")
+
+
+def _profile(kind):
+    import bmnd_gb300 as bg
+
+    cls = bg.BM3DProfile if kind == "bm3d" else bg.BM4DProfile
+    return cls(noise_model=bg.NoiseModel.POISSON)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_pipeline_matches_reference(oracle_lib, case):
+    g = np.load(os.path.join(GOLDEN, f"pipe_{case}.npz"))
+    if g["noisy"].size > 64 * 64 * 2:
+        pytest.skip("large fixture is covered by the GPU tests")
+    kind = str(g["kind"])
+    profile = _profile(kind)
+    out, det = oracle_lib.bmnd(g["noisy"], _profile(kind), return_details=True)
+    shape = g["noisy"].shape
+    foot = np.zeros(shape, dtype=bool)
+    for stage, src in (("ht", g["noisy"]), ("wiener", g["ht"])):
+        d = det[stage]
+        np.testing.assert_array_equal(d["refs"], g[f"{stage}_refs"])
+        block = tuple(getattr(profile, f"{stage}_block_size"))
+        thr = float(np.float32(getattr(profile, f"{stage}_match_threshold")))
+        eq, tied, bad = compare_match_sets(oracle_lib, src, block, d["refs"], d["sel"], d["count"],
+                                           g[f"{stage}_sel"], g[f"{stage}_count"], 1, thr)
+        assert not bad, (case, stage, bad[:8])
+        assert eq >= 0.98 * len(d["count"])
+        foot |= tie_footprint(shape, block, d["sel"], d["count"], g[f"{stage}_sel"], g[f"{stage}_count"])
+    par = output_parity(det["ht"]["estimate"], g["ht"], g["clean"])
+    assert par["frac_within"] >= 0.999 and par["psnr_delta"] < 0.01, par
+    par = output_parity(out, g["wiener"], g["clean"], exclude=foot)
+    assert par["frac_within"] >= 0.999 and par["psnr_delta"] < 0.01, par
+
+
+def test_oracle_distances_match_reference(oracle_lib):
+    u = np.load(UNIT)
+    for pv in (64, 125):
+        ref_p, cand = u[f"dist_p{pv}_ref"], u[f"dist_p{pv}_cand"]
+        for code in range(4):
+            want = u[f"dist_p{pv}_c{code}"]
+            got = np.array([oracle_lib.patch_distance(ref_p[i], cand[i], code) for i in range(len(want))],
+                           dtype=np.float32)
+            rel = np.abs(got.astype(np.float64) - want) / np.maximum(np.abs(want), 1e-6)
+            # float32 sums with different log implementations: a few ulp of the sum
+            assert np.max(rel) < 2e-5, (pv, code, float(np.max(rel)))
+            if code in (0, 2, 3):
+                assert np.mean(got == want) > 0.95, (pv, code)
+
+
+def test_canonical_keys_exact(oracle_lib):
+    u = np.load(UNIT)
+    got = oracle_lib.canonical(u["canon_in"])
+    np.testing.assert_array_equal(got, u["canon_out"])
+
+
+@pytest.mark.parametrize("idx", range(6))
+def test_oracle_schedule_matches_reference(oracle_lib, idx):
+    u = np.load(UNIT)
+    a, sh, sf = oracle_lib.schedule(tuple(u[f"sched{idx}_counts"]), tuple(u[f"sched{idx}_block"]),
+                                    tuple(u[f"sched{idx}_step"]))
+    np.testing.assert_array_equal(a, u[f"sched{idx}_abs"])
+    np.testing.assert_array_equal(sh, u[f"sched{idx}_shifted"])
+    np.testing.assert_array_equal(sf, u[f"sched{idx}_shift"])
