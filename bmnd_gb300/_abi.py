@@ -42,6 +42,8 @@ WEIGHT_VARIANCE = 1
 MATCH_EXACT = 0
 MATCH_FAST = 1
 
+STATIC_SCRATCH_BYTES = 64 << 20
+
 _I32 = ctypes.c_int32
 _I64 = ctypes.c_int64
 _U64 = ctypes.c_uint64
@@ -120,6 +122,11 @@ SIGNATURES = {
         [ctypes.POINTER(StageParams), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _I64,
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
          _U64, _U64],
+    ),
+    "bmnd_stage_noalloc": (
+        _I32,
+        [ctypes.POINTER(StageParams), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _I64,
+         ctypes.c_void_p, _U64],
     ),
     "bmnd_run": (
         _I32,

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <set>
 #include <string>
 #include <vector>
@@ -176,6 +177,31 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
     return launch_finalize(sp, w.num, w.den, noisy, out, stream);
 }
 
+// Fixed scratch array behind bmnd_stage_noalloc.  Host code must not use the
+// symbol itself as a device pointer: its device address is looked up once per
+// device with cudaGetSymbolAddress and cached.
+static __device__ __align__(256) unsigned char g_static_scratch[BMND_STATIC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_scratch_mutex;
+void* g_static_scratch_ptr[kMaxDevices] = {};
+
+int32_t static_scratch_address(void** out) {
+    int dev = 0;
+    BMND_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(BMND_ERR_UNSUPPORTED, "device index out of range");
+    std::lock_guard<std::mutex> guard(g_static_scratch_mutex);
+    if (!g_static_scratch_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t err = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (err != cudaSuccess) return cuda_fail(err, "cudaGetSymbolAddress(static scratch)");
+        if (!p) return fail(BMND_ERR_CUDA, "static scratch has no device address");
+        g_static_scratch_ptr[dev] = p;
+    }
+    *out = g_static_scratch_ptr[dev];
+    return BMND_OK;
+}
+
 }  // namespace
 }  // namespace bmnd
 
@@ -307,6 +333,27 @@ int32_t bmnd_run(const BmndStageParams* ht, const BmndStageParams* wiener, const
     if (rc) return rc;
     return run_stage(*wiener, d_noisy, d_ht_out, d_refs_wiener, n_refs_wiener, d_out, nullptr,
                      nullptr, nullptr, d_workspace, workspace_bytes, s);
+}
+
+int32_t bmnd_stage_noalloc(const BmndStageParams* params, const float* d_noisy,
+                           const float* d_pilot, const int32_t* d_refs, int64_t n_refs,
+                           float* d_out, uint64_t stream) {
+    clear_error();
+    if (!params) return fail(BMND_ERR_INVALID_ARG, "null params");
+    int32_t rc = validate_stage(*params);
+    if (rc) return rc;
+    if (n_refs < 0) return fail(BMND_ERR_INVALID_ARG, "bad reference list");
+    uint64_t need = carve(*params, n_refs, nullptr).bytes;
+    if (need > BMND_STATIC_SCRATCH_BYTES)
+        return fail(BMND_ERR_WORKSPACE,
+                    "stage needs " + std::to_string(need) + " scratch bytes; the static scratch of "
+                    "bmnd_stage_noalloc holds " + std::to_string(BMND_STATIC_SCRATCH_BYTES) +
+                    " (use bmnd_stage with a caller workspace)");
+    void* scratch = nullptr;
+    rc = static_scratch_address(&scratch);
+    if (rc) return rc;
+    return run_stage(*params, d_noisy, d_pilot, d_refs, n_refs, d_out, nullptr, nullptr, nullptr,
+                     scratch, BMND_STATIC_SCRATCH_BYTES, reinterpret_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

@@ -205,6 +205,32 @@ int32_t bmnd_run(const BmndStageParams* ht, const BmndStageParams* wiener,
                  const int32_t* d_refs_wiener, int64_t n_refs_wiener, float* d_ht_out,
                  float* d_out, void* d_workspace, uint64_t workspace_bytes, uint64_t stream);
 
+/*
+ * Allocation-free variant of bmnd_stage().  It has no counterpart in the
+ * reference.  It is meant for callers that may not allocate device memory
+ * after start-up: hosts whose memory pool owns the whole device (acquisition
+ * pipelines that reserve all memory up front), or bindings that have no way
+ * to call into the CUDA allocator.  The caller still passes inputs and
+ * outputs; the stage's scratch space (float64 numerator and denominator,
+ * match table) is a fixed array of BMND_STATIC_SCRATCH_BYTES compiled into
+ * this library, held by every GPU that loads it until the process exits.
+ *   - A stage needing more scratch than that is rejected with
+ *     BMND_ERR_WORKSPACE before any device work (see
+ *     bmnd_stage_workspace_bytes for the requirement).
+ *   - The first call on a device looks up the array's device address (once
+ *     per device, with that device current); make that first call before any
+ *     stream capture.
+ *   - Every call shares the one array and leaves its contents behind; the
+ *     accumulators are cleared at the start of each call.  Calls whose device
+ *     work overlaps (other streams, other host threads) race on the array.
+ * This function performs no cudaMalloc / cudaFree and calls no allocating
+ * library routine.
+ */
+#define BMND_STATIC_SCRATCH_BYTES (64ull << 20)
+int32_t bmnd_stage_noalloc(const BmndStageParams* params, const float* d_noisy,
+                           const float* d_pilot, const int32_t* d_refs, int64_t n_refs,
+                           float* d_out, uint64_t stream);
+
 #ifdef __cplusplus
 }
 #endif
