@@ -210,6 +210,8 @@ def time_kernels(torch, noisy_t, profile, reps: int = 3) -> dict:
             mp.search_radius[a] = p.search_radius[a]
         mp.max_matches, mp.min_matches, mp.prefer_power_of_two = p.max_stack, p.min_stack, 1
         mp.distance, mp.stabilize_ties, mp.count_scale = p.distance, 1, p.count_scale
+        # the pipeline matches the real-valued pilot with the screened path
+        mp.precision = _abi.MATCH_EXACT if stage == "ht" else _abi.MATCH_FAST
         sh = (ctypes.c_int32 * len(shape))(*shape)
         bl = (ctypes.c_int32 * len(shape))(*block)
         src = noisy_t if stage == "ht" else pilot

@@ -99,6 +99,7 @@ struct StageWorkspace {
     int32_t* sel;
     int32_t* count;
     int32_t* accepted;
+    float* st;  // P x P Kronecker table of the patch transforms
     uint64_t bytes;
 };
 
@@ -118,6 +119,8 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
     uint64_t o_sel = take(4ull * n_refs * sp.max_stack);
     uint64_t o_cnt = take(4ull * n_refs);
     uint64_t o_acc = take(4ull * n_refs);
+    const uint64_t P = static_cast<uint64_t>(patch_volume(sp));
+    uint64_t o_st = take(4ull * P * P);
     w.bytes = off;
     if (base) {
         char* b = static_cast<char*>(base);
@@ -126,6 +129,7 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
         w.sel = reinterpret_cast<int32_t*>(b + o_sel);
         w.count = reinterpret_cast<int32_t*>(b + o_cnt);
         w.accepted = reinterpret_cast<int32_t*>(b + o_acc);
+        w.st = reinterpret_cast<float*>(b + o_st);
     }
     return w;
 }
@@ -169,10 +173,12 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
     BMND_CUDA_TRY(cudaMemsetAsync(w.den, 0, 8 * vox, stream));
     BmndMatchParams mp = match_params_of(sp);
     const float* match_src = sp.filter == BMND_FILTER_WIENER ? pilot : noisy;
+    if (sp.filter == BMND_FILTER_WIENER && sp.match_precision == BMND_MATCH_EXACT)
+        mp.precision = BMND_MATCH_REAL_VALUED;
     rc = launch_blockmatch_volume(mp, match_src, sp.shape, sp.block, refs, n_refs, nullptr,
                                   sp.match_threshold, w.sel, w.count, w.accepted, stream);
     if (rc) return rc;
-    rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, stream);
+    rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, w.st, stream);
     if (rc) return rc;
     return launch_finalize(sp, w.num, w.den, noisy, out, stream);
 }

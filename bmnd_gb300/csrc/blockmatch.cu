@@ -23,6 +23,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "bmnd_common.cuh"
 
 namespace bmnd {
@@ -54,7 +56,47 @@ struct MatchArgs {
     int32_t* sel;
     int32_t* count;
     int32_t* accepted;
+    int32_t use_table;  // integer-count lookup of Poisson-deviance terms
+    int32_t fixup;      // only redo references whose count is negative
 };
+
+constexpr int kTable = 64;  // counts 0..63 are tabulated
+
+// 2 * [r ln(2r/s) + c ln(2c/s)] with the reference's float32 operation order
+// (blockmatching.py:347-355); 0 when r + c == 0 (the term is skipped there)
+__device__ __forceinline__ float deviance_term(float r, float c) {
+    float s = add_rn(r, c);
+    if (!(s > 0.0f)) return 0.0f;
+    float contrib = 0.0f;
+    if (r > 0.0f) contrib = add_rn(contrib, mul_rn(r, logf(div_rn(mul_rn(2.0f, r), s))));
+    if (c > 0.0f) contrib = add_rn(contrib, mul_rn(c, logf(div_rn(mul_rn(2.0f, c), s))));
+    return mul_rn(2.0f, contrib);
+}
+
+// Poisson deviance with integer counts looked up in table[r * kTable + c],
+// which holds deviance_term(r, c) for r, c < kTable; other terms are
+// evaluated directly.  Bit-identical to patch_distance<DEV> with inv == 1.
+__device__ __forceinline__ float deviance_tabulated(const float* __restrict__ ref,
+                                                    const int* __restrict__ ref_row,
+                                                    const float* __restrict__ src, int64_t origin,
+                                                    const int32_t* __restrict__ poff, int P,
+                                                    const float* __restrict__ table) {
+    float d = 0.0f;
+    for (int p = 0; p < P; ++p) {
+        float c = __ldg(src + origin + poff[p]);
+        if (c < 0.0f) c = 0.0f;
+        const int rb = ref_row[p];
+        const int ci = __float2int_rz(c);
+        float t;
+        if (rb >= 0 && ci < kTable && __int2float_rn(ci) == c)
+            t = table[rb + ci];
+        else
+            t = deviance_term(ref[p], c);
+        d = add_rn(d, t);
+    }
+    if (d < 0.0f) d = 0.0f;
+    return div_rn(d, static_cast<float>(P));
+}
 
 template <int CODE>
 __device__ __forceinline__ float patch_distance(const float* __restrict__ ref,
@@ -75,13 +117,7 @@ __device__ __forceinline__ float patch_distance(const float* __restrict__ ref,
         float c = mul_rn(__ldg(src + origin + poff[p]), inv);
         if (c < 0.0f) c = 0.0f;
         if (CODE == BMND_DIST_POISSON_DEVIANCE) {
-            float s = add_rn(r, c);
-            if (s > 0.0f) {
-                float contrib = 0.0f;
-                if (r > 0.0f) contrib = add_rn(contrib, mul_rn(r, logf(div_rn(mul_rn(2.0f, r), s))));
-                if (c > 0.0f) contrib = add_rn(contrib, mul_rn(c, logf(div_rn(mul_rn(2.0f, c), s))));
-                d = add_rn(d, mul_rn(2.0f, contrib));
-            }
+            if (add_rn(r, c) > 0.0f) d = add_rn(d, deviance_term(r, c));
         } else if (CODE == BMND_DIST_PEARSON) {
             float s = add_rn(r, c);
             if (s > 0.0f) {
@@ -150,12 +186,12 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int64_t r = static_cast<int64_t>(blockIdx.x) * kWarps + warp;
     const int P = a.P;
     const int K = a.max_m;
     const int R = a.required;
 
-    // per-warp shared layout: lists [K+R][32] u64, merged [K+R] u64, ref patch [P] f32
+    // shared layout: per warp [K+R][32] u64 lists + [K+R] merged; then
+    // poff[P] i32, ref[kWarps][P] f32, ref_row[kWarps][P] i32, table[64*64] f32
     const int list_rows = K + R;
     uint64_t* lists = reinterpret_cast<uint64_t*>(smem_raw) +
                       static_cast<size_t>(warp) * (list_rows * 32 + list_rows);
@@ -165,6 +201,11 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
     int32_t* poff_s = reinterpret_cast<int32_t*>(reinterpret_cast<uint64_t*>(smem_raw) +
                                                  static_cast<size_t>(kWarps) * (list_rows * 32 + list_rows));
     float* ref_s = reinterpret_cast<float*>(poff_s + P) + static_cast<size_t>(warp) * P;
+    int* ref_row = reinterpret_cast<int*>(reinterpret_cast<float*>(poff_s + P) + kWarps * P) +
+                   static_cast<size_t>(warp) * P;
+    float* table = reinterpret_cast<float*>(reinterpret_cast<int*>(reinterpret_cast<float*>(poff_s + P) +
+                                                                   kWarps * P) + kWarps * P);
+    const bool use_table = CODE == BMND_DIST_POISSON_DEVIANCE && a.use_table;
 
     // offsets of the patch elements relative to the patch origin (C order over the block)
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -180,105 +221,580 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
             poff_s[i] = static_cast<int32_t>(off);
         }
     }
+    if (use_table)
+        for (int i = threadIdx.x; i < kTable * kTable; i += blockDim.x)
+            table[i] = deviance_term(static_cast<float>(i / kTable), static_cast<float>(i % kTable));
     __syncthreads();
-    if (r >= a.n_refs) return;
 
-    int center[BMND_MAX_DIMS], lo[BMND_MAX_DIMS], ext[BMND_MAX_DIMS];
-    int64_t center_lin = 0, center_origin = 0;
-    int64_t window = 1;
-    for (int d = 0; d < a.ndim; ++d) {
-        center[d] = a.refs[r * a.ndim + d];
-        center_lin = center_lin * a.counts[d] + center[d];
-        center_origin += static_cast<int64_t>(center[d]) * a.grid_stride[d];
-        int l = center[d] - a.radius[d];
-        if (l < 0) l = 0;
-        int h = center[d] + a.radius[d];
-        if (h > a.counts[d] - 1) h = a.counts[d] - 1;
-        lo[d] = l;
-        ext[d] = h - l + 1;
-        window *= ext[d];
-    }
-    for (int p = lane; p < P; p += 32) ref_s[p] = __ldg(a.src + center_origin + poff_s[p]);
-    __syncwarp();
-
-    const float thr = a.thresholds ? a.thresholds[r] : a.scalar_threshold;
     const bool stab = a.stab && CODE != BMND_DIST_SSD;
-    const float tkey = stab ? canonical_key(thr) : thr;
-
     uint64_t* my_acc = acc_list + lane;
     uint64_t* my_rej = rej_list + lane;
-    int acc_size = 0, rej_size = 0, acc_count = 0;
-    for (int64_t c = lane; c < window; c += 32) {
-        int64_t rem = c;
-        int coord[BMND_MAX_DIMS];
-        for (int d = a.ndim - 1; d >= 0; --d) {
-            coord[d] = lo[d] + static_cast<int>(rem % ext[d]);
-            rem /= ext[d];
-        }
-        int64_t lin = 0, origin = 0;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * kWarps;
+    for (int64_t r = static_cast<int64_t>(blockIdx.x) * kWarps + warp; r < a.n_refs; r += stride) {
+        if (a.fixup && a.count[r] >= 0) continue;
+        int center[BMND_MAX_DIMS], lo[BMND_MAX_DIMS], ext[BMND_MAX_DIMS];
+        int64_t center_lin = 0, center_origin = 0;
+        int64_t window = 1;
         for (int d = 0; d < a.ndim; ++d) {
-            lin = lin * a.counts[d] + coord[d];
-            origin += static_cast<int64_t>(coord[d]) * a.grid_stride[d];
+            center[d] = a.refs[r * a.ndim + d];
+            center_lin = center_lin * a.counts[d] + center[d];
+            center_origin += static_cast<int64_t>(center[d]) * a.grid_stride[d];
+            int l = center[d] - a.radius[d];
+            if (l < 0) l = 0;
+            int h = center[d] + a.radius[d];
+            if (h > a.counts[d] - 1) h = a.counts[d] - 1;
+            lo[d] = l;
+            ext[d] = h - l + 1;
+            window *= ext[d];
         }
-        float dist = patch_distance<CODE>(ref_s, a.src, origin, poff_s, P, a.inv_scale);
-        float key = stab ? canonical_key(dist) : dist;
-        uint64_t ck = composite_key(key, static_cast<int32_t>(lin));
-        if (key < tkey) {
-            ++acc_count;
-            acc_size = list_insert(my_acc, acc_size, K, ck);
-        } else {
-            rej_size = list_insert(my_rej, rej_size, R, ck);
+        __syncwarp();
+        for (int p = lane; p < P; p += 32) {
+            float v = __ldg(a.src + center_origin + poff_s[p]);
+            if (use_table) {
+                float rv = v < 0.0f ? 0.0f : v;
+                int ri = __float2int_rz(rv);
+                ref_s[p] = rv;
+                ref_row[p] = (ri < kTable && __int2float_rn(ri) == rv) ? ri * kTable : -1;
+            } else {
+                ref_s[p] = v;
+            }
         }
-    }
-    __syncwarp();
-    int total_accepted = acc_count;
+        __syncwarp();
+
+        const float thr = a.thresholds ? a.thresholds[r] : a.scalar_threshold;
+        const float tkey = stab ? canonical_key(thr) : thr;
+        int acc_size = 0, rej_size = 0, acc_count = 0;
+        for (int64_t c = lane; c < window; c += 32) {
+            int64_t rem = c;
+            int coord[BMND_MAX_DIMS];
+            for (int d = a.ndim - 1; d >= 0; --d) {
+                coord[d] = lo[d] + static_cast<int>(rem % ext[d]);
+                rem /= ext[d];
+            }
+            int64_t lin = 0, origin = 0;
+            for (int d = 0; d < a.ndim; ++d) {
+                lin = lin * a.counts[d] + coord[d];
+                origin += static_cast<int64_t>(coord[d]) * a.grid_stride[d];
+            }
+            float dist = use_table ? deviance_tabulated(ref_s, ref_row, a.src, origin, poff_s, P, table)
+                                   : patch_distance<CODE>(ref_s, a.src, origin, poff_s, P, a.inv_scale);
+            float key = stab ? canonical_key(dist) : dist;
+            uint64_t ck = composite_key(key, static_cast<int32_t>(lin));
+            if (key < tkey) {
+                ++acc_count;
+                acc_size = list_insert(my_acc, acc_size, K, ck);
+            } else {
+                rej_size = list_insert(my_rej, rej_size, R, ck);
+            }
+        }
+        __syncwarp();
+        int total_accepted = acc_count;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) total_accepted += __shfl_xor_sync(0xffffffffu, total_accepted, o);
+        for (int o = 16; o > 0; o >>= 1) total_accepted += __shfl_xor_sync(0xffffffffu, total_accepted, o);
 
-    int n_acc = warp_merge(my_acc, acc_size, K, merged, lane);
-    int n_rej = warp_merge(my_rej, rej_size, R, merged + K, lane);
-    __syncwarp();
+        int n_acc = warp_merge(my_acc, acc_size, K, merged, lane);
+        int n_rej = warp_merge(my_rej, rej_size, R, merged + K, lane);
+        __syncwarp();
 
-    if (lane == 0) {
-        int32_t out[kMaxList];
-        int n = 0;
-        int selected = n_acc;
-        int take = 0;
-        if (selected < R) {
-            int need = R - selected;
-            take = need < n_rej ? need : n_rej;
+        if (lane == 0) {
+            int32_t* row = a.sel + r * K;
+            int n = 0;
+            int take = 0;
+            if (n_acc < R) {
+                int need = R - n_acc;
+                take = need < n_rej ? need : n_rej;
+            }
+            row[n++] = static_cast<int32_t>(center_lin);
+            for (int t = 0; t < n_acc + take && n < K; ++t) {
+                uint64_t ck = t < n_acc ? merged[t] : merged[K + (t - n_acc)];
+                int32_t l = static_cast<int32_t>(ck & 0xffffffffu);
+                if (l < 0 || l == center_lin) continue;
+                row[n++] = l;
+            }
+            if (a.pow2 && n > 0) {
+                int target = 1;
+                while ((target << 1) <= n) target <<= 1;
+                if (a.min_m > target) target = a.min_m;
+                if (target < n) n = target;
+            }
+            for (int t = n; t < K; ++t) row[t] = -1;
+            a.count[r] = n;
+            a.accepted[r] = total_accepted;
         }
-        out[n++] = static_cast<int32_t>(center_lin);
-        for (int t = 0; t < n_acc + take && n < K; ++t) {
-            uint64_t ck = t < n_acc ? merged[t] : merged[K + (t - n_acc)];
-            int32_t l = static_cast<int32_t>(ck & 0xffffffffu);
-            if (l < 0 || l == center_lin) continue;
-            out[n++] = l;
-        }
-        if (a.pow2 && n > 0) {
-            int target = 1;
-            while ((target << 1) <= n) target <<= 1;
-            if (a.min_m > target) target = a.min_m;
-            if (target < n) n = target;
-        }
-        int32_t* row = a.sel + r * K;
-        for (int t = 0; t < K; ++t) row[t] = t < n ? out[t] : -1;
-        a.count[r] = n;
-        a.accepted[r] = total_accepted;
+        __syncwarp();
     }
 }
 
-size_t match_smem_bytes(int K, int R, int P) {
+// ---------------------------------------------------------------------------
+// Screened Poisson-deviance matching for real-valued sources
+//
+// Exact per-term evaluation (two IEEE divisions and two logf) is needed only
+// where it can change the result.  Pass A scores every candidate with a
+// cancellation-free form of the same deviance term: with s = r + c and
+// u = (r - c) / s,
+//   t = 2 [r ln(2r/s) + c ln(2c/s)] = s u^2 sum_{k>=1} u^(2k-2) / (k (2k - 1)),
+// summed to k = 6 for u^2 <= 0.16 (truncation < 2.2e-7 relative) and with the
+// SFU log2 otherwise.  A rigorous bound D(d) = Dabs + Drel d on the distance to
+// the exact float32 result covers the screening arithmetic, the exact path's
+// own rounding (its division error enters each log absolutely, 2^-21 s per
+// term), both float32 accumulations, times a safety factor 4.  A candidate is
+//   * certainly accepted   if canonical(d + D) < canonical(threshold),
+//   * certainly rejected   if canonical(d - D) >= canonical(threshold);
+// among the certainly accepted a radix select finds V with at least K of them
+// scoring <= V, so no candidate with canonical(d - D) > canonical(V + D(V))
+// can reach the top K.  Everything else (uncertain accept decisions, possible
+// top-K members) is rescored exactly, warp-parallel from a shared queue, and
+// the top K is kept by (canonical key, lin) as in the exact kernel.
+// References that end with fewer than min(min, max) accepted candidates need
+// the best rejected ones too; they are marked (count = -1) and redone by the
+// exact kernel.
+// ---------------------------------------------------------------------------
+
+// Screening of one candidate with the ratio form
+//   t = 2 ln 2 [r log2(2r/s) + c log2(2c/s)],  s = r + c,
+// using the SFU reciprocal and log2.  Near r = c both logs are near zero and
+// carry only the SFU's absolute error, so the form has no cancellation.
+// Per term the screening error is below s (e_lg + 1.45 e_rcp + 2^-22.5 +
+// 1.27 2^-23) in log2 units (r |log2 q_r| + c |log2 q_c| <= 1.27 s), and the
+// exact float32 path's own error below 2^-21 s; the bound uses the sum of s
+// over the patch.  kScreenAbs is that per-unit-s constant in distance units,
+// times a safety factor 2, with the SFU errors e_lg, e_rcp measured on GB300
+// over the argument ranges used here.
+// measured: lg2.approx abs error <= 2^-22.06 max(|log2 x|, 1) (so r e_lg + c e_lg
+// <= 2^-22.06 2.27 s), rcp.approx relative error <= 2^-23.28
+constexpr float kScreenAbs = 2.0f * (1.38629436f * (5.41e-07f + 1.45f * 9.83e-08f + 1.69e-07f + 1.52e-07f) +
+                                     4.77e-07f);
+
+// SFU reciprocal and log2 of normal arguments (callers clamp to FLT_MIN)
+__device__ __forceinline__ float sfu_rcp(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float sfu_lg2(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// r2 = 2 r; returns r log2(2r/s) + c log2(2c/s)
+__device__ __forceinline__ float ratio_term(float r, float r2, float c, float& ss) {
+    const float kMin = 1.17549435e-38f;
+    const float s = r + c;
+    const float rs = sfu_rcp(fmaxf(s, kMin));
+    const float lr = sfu_lg2(fmaxf(r2 * rs, kMin));
+    const float lc = sfu_lg2(fmaxf((c + c) * rs, kMin));
+    ss += s;
+    return fmaf(r, lr, c * lc);
+}
+
+// generic (runtime patch) screening
+__device__ __forceinline__ float2 screen_deviance(const float2* __restrict__ ref,
+                                                  const float* __restrict__ src, int64_t origin,
+                                                  const int32_t* __restrict__ poff, int P, float inv) {
+    float sum_t = 0.0f, ss = 0.0f;
+    for (int p = 0; p < P; ++p) {
+        const float c = fmaxf(__ldg(src + origin + poff[p]) * inv, 0.0f);
+        const float2 rr = ref[p];
+        sum_t += ratio_term(rr.x, rr.y, c, ss);
+    }
+    const float fp = static_cast<float>(P);
+    return make_float2(fmaxf(1.38629436f * sum_t, 0.0f) / fp, kScreenAbs * ss / fp + 1e-30f);
+}
+
+// compile-time patch (volume source, count scale 1): fully unrolled
+template <int ND, int B0, int B1, int B2>
+__device__ __forceinline__ float2 screen_deviance_fixed(const float2* __restrict__ ref,
+                                                        const float* __restrict__ src, int64_t origin,
+                                                        int64_t s0, int64_t s1,
+                                                        const int32_t* __restrict__ poff) {
+    float sum_t = 0.0f, ss = 0.0f;
+    const float* base = src + origin;
+#pragma unroll 1
+    for (int a0 = 0; a0 < B0; ++a0) {
+#pragma unroll
+        for (int a1 = 0; a1 < B1; ++a1) {
+            const float* row = ND == 3 ? base + a0 * s0 + a1 * s1 : base + a0 * s0;
+#pragma unroll
+            for (int a2 = 0; a2 < B2; ++a2) {
+                const int p = (a0 * B1 + a1) * B2 + a2;
+                const float c = fmaxf(__ldg(row + (ND == 3 ? a2 : a1)), 0.0f);
+                const float2 rr = ref[p];
+                sum_t += ratio_term(rr.x, rr.y, c, ss);
+            }
+        }
+    }
+    constexpr int P = B0 * B1 * B2;
+    return make_float2(fmaxf(1.38629436f * sum_t, 0.0f) / static_cast<float>(P),
+                       kScreenAbs * ss / static_cast<float>(P) + 1e-30f);
+}
+
+// exact deviance with the reference patch already scaled and clamped (.x)
+__device__ __forceinline__ float exact_deviance(const float2* __restrict__ ref, const float* __restrict__ src,
+                                                int64_t origin, const int32_t* __restrict__ poff, int P,
+                                                float inv) {
+    float d = 0.0f;
+    for (int p = 0; p < P; ++p) {
+        const float r = ref[p].x;
+        float c = mul_rn(__ldg(src + origin + poff[p]), inv);
+        if (c < 0.0f) c = 0.0f;
+        if (add_rn(r, c) > 0.0f) d = add_rn(d, deviance_term(r, c));
+    }
+    if (d < 0.0f) d = 0.0f;
+    return div_rn(d, static_cast<float>(P));
+}
+
+__device__ __forceinline__ int64_t window_origin(const MatchArgs& a, const int* lo, const int* ext, int64_t c,
+                                                 int64_t* lin_out) {
+    int coord[BMND_MAX_DIMS];
+    int64_t rem = c;
+    for (int d = a.ndim - 1; d >= 0; --d) {
+        coord[d] = lo[d] + static_cast<int>(rem % ext[d]);
+        rem /= ext[d];
+    }
+    int64_t lin = 0, origin = 0;
+    for (int d = 0; d < a.ndim; ++d) {
+        lin = lin * a.counts[d] + coord[d];
+        origin += static_cast<int64_t>(coord[d]) * a.grid_stride[d];
+    }
+    *lin_out = lin;
+    return origin;
+}
+
+constexpr int kSThreads = 128;   // one CTA per reference
+constexpr int kSQueue = 512;     // rescoring queue (overflow -> exact redo)
+
+// per-CTA shared layout of the screened kernel
+struct ScreenSmem {
+    __host__ __device__ static size_t cand(int64_t wmax) { return (static_cast<size_t>(wmax) * 4 + 15) & ~size_t(15); }
+    __host__ __device__ static size_t bytes(int P, int64_t wmax) {
+        return ((static_cast<size_t>(P) * 4 + 15) & ~size_t(15))   // poff
+               + static_cast<size_t>(P) * 8                           // ref (r, 2r)
+               + cand(wmax)                                           // screening distances
+               + 256 * 4                                              // histogram
+               + kSQueue * 4 + kSQueue * 8                            // queue index, exact keys
+               + 64 * 8                                               // scratch (reductions, top list)
+               + 64;
+    }
+};
+
+template <int ND, int B0, int B1, int B2>
+__global__ void __launch_bounds__(kSThreads) blockmatch_screened_kernel(MatchArgs a, int32_t wmax) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int P = a.P;
+    const int K = a.max_m;
+    const int R = a.required;
+    unsigned char* b = smem_raw;
+    int32_t* poff_s = reinterpret_cast<int32_t*>(b);
+    b += (static_cast<size_t>(P) * 4 + 15) & ~size_t(15);
+    float2* ref = reinterpret_cast<float2*>(b);
+    b += static_cast<size_t>(P) * 8;
+    float* cand = reinterpret_cast<float*>(b);
+    b += ScreenSmem::cand(wmax);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(b);
+    b += 256 * 4;
+    int32_t* qidx = reinterpret_cast<int32_t*>(b);
+    b += kSQueue * 4;
+    uint64_t* qkey = reinterpret_cast<uint64_t*>(b);
+    b += kSQueue * 8;
+    uint64_t* top = reinterpret_cast<uint64_t*>(b);  // [32]
+    float* redf = reinterpret_cast<float*>(top + 32);  // [4 warps]
+    int* redi = reinterpret_cast<int*>(redf + 8);      // [8]
+
+    for (int i = tid; i < P; i += blockDim.x) {
+        if (a.table) {
+            poff_s[i] = i;
+        } else {
+            int rem = i;
+            int64_t o = 0;
+            for (int d = a.ndim - 1; d >= 0; --d) {
+                o += static_cast<int64_t>(rem % a.block[d]) * a.vstride[d];
+                rem /= a.block[d];
+            }
+            poff_s[i] = static_cast<int32_t>(o);
+        }
+    }
+    const bool fixed = ND > 0 && !a.table && a.inv_scale == 1.0f;
+    // relative part of the bound: float32 accumulation of both sums (P 2^-24 each)
+    // and the final scalings, x2
+    const float drel = 2.0f * (2.0f * 5.96046448e-08f * static_cast<float>(P) + 4.76837158e-07f);
+
+    for (int64_t r = blockIdx.x; r < a.n_refs; r += gridDim.x) {
+        int lo[BMND_MAX_DIMS], ext[BMND_MAX_DIMS];
+        int64_t center_lin = 0, center_origin = 0, window = 1;
+        for (int d = 0; d < a.ndim; ++d) {
+            const int cd = a.refs[r * a.ndim + d];
+            center_lin = center_lin * a.counts[d] + cd;
+            center_origin += static_cast<int64_t>(cd) * a.grid_stride[d];
+            const int l = max(cd - a.radius[d], 0);
+            const int h = min(cd + a.radius[d], a.counts[d] - 1);
+            lo[d] = l;
+            ext[d] = h - l + 1;
+            window *= ext[d];
+        }
+        __syncthreads();  // previous reference's shared data is no longer read
+        for (int p = tid; p < P; p += blockDim.x) {
+            float rv = mul_rn(__ldg(a.src + center_origin + poff_s[p]), a.inv_scale);
+            if (rv < 0.0f) rv = 0.0f;
+            ref[p] = make_float2(rv, rv + rv);
+        }
+        for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0u;
+        if (tid == 0) redi[0] = 0;  // queue length
+        __syncthreads();
+        const float thr = a.thresholds ? a.thresholds[r] : a.scalar_threshold;
+        const float tkey = canonical_key(thr);
+
+        // pass A: screening distances and the reference-wide absolute bound
+        float dmax = 0.0f;
+        for (int64_t c = tid; c < window; c += blockDim.x) {
+            int64_t lin;
+            const int64_t origin = window_origin(a, lo, ext, c, &lin);
+            const float2 sd = fixed ? screen_deviance_fixed<ND, B0, B1, B2>(ref, a.src, origin, a.vstride[0],
+                                                                           a.vstride[ND > 1 ? 1 : 0], poff_s)
+                                    : screen_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
+            cand[c] = sd.x;
+            dmax = fmaxf(dmax, sd.y);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        if (lane == 0) redf[warp] = dmax;
+        __syncthreads();
+        float Dabs = redf[0];
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) Dabs = fmaxf(Dabs, redf[w]);
+
+        // radix select over the upper bounds d + D of the certainly accepted:
+        // vstar with >= K of them bounded by it
+        float vstar = INFINITY;
+        {
+            uint32_t prefix = 0;
+            int need = K;
+            bool found = true;
+            for (int pass = 0; pass < 3 && found; ++pass) {
+                const int shift = 24 - 8 * pass;
+                if (pass > 0) {
+                    for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0u;
+                    __syncthreads();
+                }
+                for (int64_t c = tid; c < window; c += blockDim.x) {
+                    const float dv = cand[c];
+                    const float up = dv + (Dabs + drel * dv);
+                    if (!(canonical_key(up) < tkey)) continue;
+                    const uint32_t bits = __float_as_uint(up);
+                    if (pass > 0 && (bits >> (32 - 8 * pass)) != prefix) continue;
+                    atomicAdd(hist + ((bits >> shift) & 0xffu), 1u);
+                }
+                __syncthreads();
+                if (warp == 0) {
+                    uint32_t local[8];
+                    uint32_t lsum = 0;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        local[i] = hist[lane * 8 + i];
+                        lsum += local[i];
+                    }
+                    uint32_t incl = lsum;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= o) incl += t;
+                    }
+                    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                    int bin = -1;
+                    uint32_t before = 0;
+                    if (total >= static_cast<uint32_t>(need)) {
+                        uint32_t run = incl - lsum;
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            if (bin < 0 && run + local[i] >= static_cast<uint32_t>(need)) {
+                                bin = lane * 8 + i;
+                                before = run;
+                            }
+                            run += local[i];
+                        }
+                    }
+                    const unsigned has = __ballot_sync(0xffffffffu, bin >= 0);
+                    if (lane == 0) {
+                        if (!has) {
+                            redi[1] = -1;
+                        } else {
+                            const int src_lane = __ffs(has) - 1;
+                            (void)src_lane;
+                        }
+                    }
+                    if (has) {
+                        const int src_lane = __ffs(has) - 1;
+                        const int bsel = __shfl_sync(0xffffffffu, bin, src_lane);
+                        const uint32_t bef = __shfl_sync(0xffffffffu, before, src_lane);
+                        if (lane == 0) {
+                            redi[1] = bsel;
+                            redi[2] = static_cast<int>(bef);
+                        }
+                    }
+                }
+                __syncthreads();
+                const int bsel = redi[1];
+                if (bsel < 0) {
+                    found = false;
+                } else {
+                    need -= redi[2];
+                    prefix = pass == 0 ? static_cast<uint32_t>(bsel) : ((prefix << 8) | static_cast<uint32_t>(bsel));
+                }
+                __syncthreads();
+            }
+            if (found) vstar = __uint_as_float((prefix << 8) | 0xffu);
+        }
+        // at least K certainly accepted candidates have exact distances <= vstar
+        const float vkey = canonical_key(vstar);
+
+        // pass C: classify; queue the uncertain and the possible top-K members
+        int acc_t = 0;
+        for (int64_t c = tid; c < window; c += blockDim.x) {
+            const float dv = cand[c];
+            const float D = Dabs + drel * dv;
+            const float lo_key = canonical_key(fmaxf(dv - D, 0.0f));
+            const bool cert = canonical_key(dv + D) < tkey;
+            const bool poss = lo_key < tkey;
+            if (cert) ++acc_t;
+            if (poss && (!cert || lo_key <= vkey)) {
+                const int slot = atomicAdd(redi, 1);
+                if (slot < kSQueue)
+                    qidx[slot] = static_cast<int32_t>(c) | (cert ? static_cast<int32_t>(0x80000000u) : 0);
+            }
+        }
+        __syncthreads();
+        const int qn_all = redi[0];
+        const bool overflow = qn_all > kSQueue;
+        const int qn = overflow ? 0 : qn_all;
+        // exact rescoring of the queue
+        for (int i = tid; i < qn; i += blockDim.x) {
+            const int32_t q = qidx[i];
+            int64_t lin;
+            const int64_t origin = window_origin(a, lo, ext, q & 0x7fffffff, &lin);
+            const float dist = exact_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
+            const float key = canonical_key(dist);
+            const bool accepted = key < tkey;
+            if (accepted && q >= 0) ++acc_t;
+            qkey[i] = accepted ? composite_key(key, static_cast<int32_t>(lin)) : ~0ull;
+        }
+        // accepted count (block sum)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc_t += __shfl_xor_sync(0xffffffffu, acc_t, o);
+        if (lane == 0) redi[4 + warp] = acc_t;
+        __syncthreads();
+        if (warp == 0) {
+            int total_accepted = 0;
+            for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) total_accepted += redi[4 + w];
+            // top K of the rescored accepted keys (K rounds of warp minimum)
+            int ntop = 0;
+            if (!overflow && total_accepted >= R) {
+                uint64_t taken_mask_lo = 0;  // per lane: which of its items are taken (<= 16 items)
+                for (int t = 0; t < K; ++t) {
+                    uint64_t mine = ~0ull;
+                    int slot = -1;
+                    for (int i = lane, k = 0; i < qn; i += 32, ++k) {
+                        if ((taken_mask_lo >> k) & 1ull) continue;
+                        const uint64_t key = qkey[i];
+                        if (key < mine) {
+                            mine = key;
+                            slot = k;
+                        }
+                    }
+                    const uint64_t best = warp_min_u64(mine);
+                    if (best == ~0ull) break;
+                    if (mine == best && slot >= 0) taken_mask_lo |= 1ull << slot;
+                    if (lane == 0) top[t] = best;
+                    ++ntop;
+                }
+            }
+            __syncwarp();
+            if (lane == 0) {
+                if (overflow || total_accepted < R) {
+                    a.count[r] = -1;  // queue overflow, or the best rejected are needed: exact redo
+                } else {
+                    int32_t* row = a.sel + r * K;
+                    int n = 0;
+                    row[n++] = static_cast<int32_t>(center_lin);
+                    for (int t = 0; t < ntop && n < K; ++t) {
+                        const int32_t l = static_cast<int32_t>(top[t] & 0xffffffffu);
+                        if (l < 0 || l == center_lin) continue;
+                        row[n++] = l;
+                    }
+                    if (a.pow2 && n > 0) {
+                        int target = 1;
+                        while ((target << 1) <= n) target <<= 1;
+                        if (a.min_m > target) target = a.min_m;
+                        if (target < n) n = target;
+                    }
+                    for (int t = n; t < K; ++t) row[t] = -1;
+                    a.count[r] = n;
+                    a.accepted[r] = total_accepted;
+                }
+            }
+        }
+    }
+}
+
+size_t screened_smem_bytes(int K, int P, int64_t wmax) {
+    (void)K;
+    return ScreenSmem::bytes(P, wmax);
+}
+
+size_t match_smem_bytes(int K, int R, int P, bool table) {
     size_t rows = static_cast<size_t>(K + R);
     return static_cast<size_t>(kWarps) * (rows * 32 + rows) * sizeof(uint64_t) +
-           static_cast<size_t>(P) * sizeof(int32_t) + static_cast<size_t>(kWarps) * P * sizeof(float);
+           static_cast<size_t>(P) * sizeof(int32_t) + static_cast<size_t>(kWarps) * P * sizeof(float) +
+           static_cast<size_t>(kWarps) * P * sizeof(int) + (table ? kTable * kTable * sizeof(float) : 0);
 }
 
-int32_t launch(MatchArgs& a, int code, cudaStream_t stream) {
+int32_t launch_exact(MatchArgs& a, int code, cudaStream_t stream);
+
+int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     if (a.n_refs == 0) return BMND_OK;
-    size_t smem = match_smem_bytes(a.max_m, a.required, a.P);
+    int64_t wmax = 1;
+    for (int d = 0; d < a.ndim; ++d) wmax *= std::min<int64_t>(2 * a.radius[d] + 1, a.counts[d]);
+    const bool screened = code == BMND_DIST_POISSON_DEVIANCE && a.stab &&
+                          (precision == BMND_MATCH_FAST || precision == BMND_MATCH_REAL_VALUED) &&
+                          a.max_m <= 32 && screened_smem_bytes(a.max_m, a.P, wmax) <= 200 * 1024;
+    if (!screened) return launch_exact(a, code, stream);
+    size_t smem = screened_smem_bytes(a.max_m, a.P, wmax);
+    int64_t blocks = a.n_refs;
+    const int64_t cap = 152 * 12;
+    if (blocks > cap) blocks = cap;
+    auto run = [&](auto kernel) -> int32_t {
+        BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(smem)));
+        kernel<<<static_cast<unsigned>(blocks), kSThreads, smem, stream>>>(a, static_cast<int32_t>(wmax));
+        BMND_LAUNCH_CHECK("blockmatch_screened_kernel");
+        return BMND_OK;
+    };
+    int32_t rc;
+    const int* bl = a.block;
+    if (!a.table && a.ndim == 2 && bl[0] == 8 && bl[1] == 8)
+        rc = run(blockmatch_screened_kernel<2, 8, 8, 1>);
+    else if (!a.table && a.ndim == 3 && bl[0] == 5 && bl[1] == 5 && bl[2] == 5)
+        rc = run(blockmatch_screened_kernel<3, 5, 5, 5>);
+    else if (!a.table && a.ndim == 3 && bl[0] == 4 && bl[1] == 4 && bl[2] == 4)
+        rc = run(blockmatch_screened_kernel<3, 4, 4, 4>);
+    else
+        rc = run(blockmatch_screened_kernel<0, 1, 1, 1>);
+    if (rc) return rc;
+    // references that need the best rejected candidates are redone exactly
+    MatchArgs fix = a;
+    fix.fixup = 1;
+    fix.use_table = 0;
+    return launch_exact(fix, code, stream);
+}
+
+int32_t launch_exact(MatchArgs& a, int code, cudaStream_t stream) {
+    if (a.n_refs == 0) return BMND_OK;
+    size_t smem = match_smem_bytes(a.max_m, a.required, a.P, a.use_table != 0);
     int64_t blocks = (a.n_refs + kWarps - 1) / kWarps;
-    if (blocks > 0x7fffffff) return fail(BMND_ERR_INVALID_ARG, "too many references");
+    // persistent CTAs: each walks references with a grid stride, so per-CTA
+    // set-up (offset table, deviance table) is paid once per CTA
+    const int64_t cap = 152 * 16;
+    if (blocks > cap) blocks = cap;
     dim3 grid(static_cast<unsigned>(blocks));
     switch (code) {
         case BMND_DIST_SSD:
@@ -339,6 +855,9 @@ void fill_common(MatchArgs& a, const BmndMatchParams& mp) {
     a.stab = mp.stabilize_ties;
     double scale = mp.distance == BMND_DIST_SSD ? 1.0 : mp.count_scale;
     a.inv_scale = static_cast<float>(1.0 / scale);
+    // the tabulated path is exact for any data but pays off only for integer counts
+    a.use_table = (mp.distance == BMND_DIST_POISSON_DEVIANCE && scale == 1.0 &&
+                   mp.precision != BMND_MATCH_REAL_VALUED) ? 1 : 0;
 }
 
 }  // namespace
@@ -379,7 +898,7 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
     a.sel = sel;
     a.count = count;
     a.accepted = accepted;
-    return launch(a, mp.distance, stream);
+    return launch(a, mp.distance, mp.precision, stream);
 }
 
 int32_t launch_blockmatch_patches(const BmndMatchParams& mp, const float* patches,
@@ -407,7 +926,7 @@ int32_t launch_blockmatch_patches(const BmndMatchParams& mp, const float* patche
     a.sel = sel;
     a.count = count;
     a.accepted = accepted;
-    return launch(a, mp.distance, stream);
+    return launch(a, mp.distance, mp.precision, stream);
 }
 
 }  // namespace bmnd

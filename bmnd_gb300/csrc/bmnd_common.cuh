@@ -11,6 +11,10 @@
 
 namespace bmnd {
 
+// internal value of BmndMatchParams.precision: the source is real-valued (a
+// pilot estimate), so integer-count tabulation is skipped
+constexpr int32_t BMND_MATCH_REAL_VALUED = 100;
+
 // ---------------------------------------------------------------------------
 // error reporting (thread-local message behind bmnd_last_error)
 // ---------------------------------------------------------------------------
@@ -158,7 +162,7 @@ int32_t launch_blockmatch_patches(const BmndMatchParams& mp, const float* patche
                                   cudaStream_t stream);
 int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const float* pilot,
                             const int32_t* sel, const int32_t* count, int64_t n_refs, double* num,
-                            double* den, cudaStream_t stream);
+                            double* den, float* st, cudaStream_t stream);
 int32_t launch_finalize(const BmndStageParams& sp, const double* num, const double* den,
                         const float* noisy, float* out, cudaStream_t stream);
 

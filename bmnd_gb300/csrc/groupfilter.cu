@@ -36,10 +36,15 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// Shared-memory plan.  The union region holds the group buffers X (noisy
+// coefficients), R (pilot coefficients, Wiener only), T (transform scratch)
+// and V (variance group, later the attenuation) outside the exact-variance
+// phase, and the occupancy grid plus the union-voxel lists inside it: the
+// phases are ordered so that none of X/R/T/V is live while the lists are.
 struct Layout {
     // byte offsets into dynamic shared memory
-    int64_t g, fw, fi, win, mdiag, pos, shf, x, t, v, s, r, a, ex, grid, lcoord, lmask, lval, scan,
-        plane, wts, misc, total;
+    int64_t g, gt, fw, fi, win, mdiag, pos, shf, s, ex, uni, x, r, t, v, grid, lval, lstart, lent,
+        scan, plane, wts, misc, total;
 };
 
 struct FilterArgs {
@@ -57,45 +62,50 @@ struct FilterArgs {
     int64_t n_refs;
     double* num;
     double* den;
+    const float* st;  // S^T: st[p * P + j] = S[j, p], the Kronecker product of the patch transforms
 };
 
 __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax, int64_t ucells) {
     Layout L{};
     int64_t off = 0;
+    auto round16 = [](int64_t b) { return (b + 15) & ~int64_t(15); };
     auto take = [&](int64_t bytes) {
         int64_t o = off;
-        off += (bytes + 15) & ~int64_t(15);
+        off += round16(bytes);
         return o;
     };
-    int64_t np = static_cast<int64_t>(nmax) * P;
+    const int64_t np = static_cast<int64_t>(nmax) * P;
+    const bool wiener = sp.filter == BMND_FILTER_WIENER;
+    const int kpad = (kmax + 3) / 4 * 4;
     L.g = take(4 * nmax * nmax);
+    L.gt = take(4 * nmax * (kpad > 0 ? kpad : 4));
     L.fw = take(4 * BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE);
     L.fi = take(4 * BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE);
     L.win = take(4 * P);
     L.mdiag = take(8 * P);
     L.pos = take(4 * nmax * BMND_MAX_DIMS);
     L.shf = take(4 * nmax * BMND_MAX_DIMS);
-    L.x = take(4 * np);
-    // t and v are adjacent: the occupancy grid reuses them once both are dead
-    L.t = take(4 * np);
-    L.v = take(4 * np);
     L.s = take(4 * np);
-    L.r = take(sp.filter == BMND_FILTER_WIENER ? 4 * np : 0);
-    L.a = take(4 * np);
     L.ex = take(4 * static_cast<int64_t>(kmax) * P);
-    if (ucells * 4 <= 8 * np && kmax > 0) {
-        L.grid = L.t;
-    } else {
-        L.grid = take(kmax > 0 ? 4 * ucells : 0);
-    }
-    int64_t umax = kmax > 0 ? (np < ucells ? np : ucells) : 0;
-    L.lcoord = take(4 * umax);
-    L.lmask = take(4 * umax);
-    L.lval = take(4 * umax);
-    L.scan = take(4 * (kThreads + 1));
+    L.scan = take(8 * (kThreads + 1));
     L.plane = take(8 * nmax);
     L.wts = take(4 * nmax);
     L.misc = take(64);
+    // union region
+    L.uni = off;
+    int64_t buf = round16(4 * np);
+    L.x = L.uni;
+    L.r = L.x + buf;
+    L.t = L.r + (wiener ? buf : 0);
+    L.v = L.t + buf;
+    int64_t group_bytes = (L.v + buf) - L.uni;
+    int64_t umax = kmax > 0 ? (np < ucells ? np : ucells) : 0;
+    L.grid = L.uni;
+    L.lval = L.grid + round16(kmax > 0 ? 4 * ucells : 0);
+    L.lstart = L.lval + round16(4 * umax);
+    L.lent = L.lstart + round16(4 * (umax + 1));
+    int64_t list_bytes = (L.lent + round16(kmax > 0 ? 4 * np : 0)) - L.uni;
+    off = L.uni + (group_bytes > list_bytes ? group_bytes : list_bytes);
     L.total = off;
     return L;
 }
@@ -105,23 +115,83 @@ __device__ __forceinline__ T* sm(unsigned char* base, int64_t off) {
     return reinterpret_cast<T*>(base + off);
 }
 
-// out = M applied along `axis` of the (nd)-axis tensor `in` (smem), one fused
-// multiply-add per term in k order; `square` uses fl(M*M), `transpose` uses M^T
-__device__ void apply_axis(const float* in, float* out, const int* dims, int nd, int axis,
-                           const float* M, int ld, bool square, bool transpose) {
-    int m = dims[axis];
-    int inner = 1, total = 1;
-    for (int d = axis + 1; d < nd; ++d) inner *= dims[d];
-    for (int d = 0; d < nd; ++d) total *= dims[d];
+// Patch geometry: compile-time for the default shapes (ND > 0), runtime otherwise.
+template <int ND, int B0, int B1, int B2>
+struct Geom {
+    int nd_, b_[BMND_MAX_DIMS], P_;
+    __device__ explicit Geom(const BmndStageParams& sp) {
+        nd_ = sp.ndim;
+        P_ = 1;
+        for (int d = 0; d < BMND_MAX_DIMS; ++d) {
+            b_[d] = d < sp.ndim ? sp.block[d] : 1;
+            P_ *= b_[d];
+        }
+    }
+    __device__ __forceinline__ int nd() const { return ND > 0 ? ND : nd_; }
+    __device__ __forceinline__ int b(int d) const {
+        if (ND > 0) return d == 0 ? B0 : (d == 1 ? B1 : B2);
+        return b_[d];
+    }
+    __device__ __forceinline__ int P() const { return ND > 0 ? B0 * B1 * B2 : P_; }
+    // product of the patch extents after axis d
+    __device__ __forceinline__ int inner(int d) const {
+        int v = 1;
+#pragma unroll
+        for (int e = 0; e < BMND_MAX_DIMS; ++e)
+            if (e > d && e < nd()) v *= b(e);
+        return v;
+    }
+    // voxel offset of element p of the patch whose origin is `org`
+    __device__ __forceinline__ int64_t offset(const int* org, int p, const int64_t* vstride) const {
+        int64_t off = 0;
+#pragma unroll
+        for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+            if (d < nd()) {
+                off += static_cast<int64_t>(org[d] + p % b(d)) * vstride[d];
+                p /= b(d);
+            }
+        }
+        return off;
+    }
+};
+
+// group axis: out[i, p] = sum_g M[i, g] in[g, p] (fused multiply-add per term,
+// g ascending); `square` uses fl(M*M), `transpose` uses M^T
+template <class GM>
+__device__ void apply_group_axis(const GM& geo, const float* in, float* out, int n, const float* M,
+                                 bool square, bool transpose) {
+    const int P = geo.P();
+    const int total = n * P;
     for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        int t = e % inner;
-        int rest = e / inner;
-        int i = rest % m;
-        int o = rest / m;
-        const float* col = in + static_cast<int64_t>(o) * m * inner + t;
+        const int i = e / P;
+        const int p = e - i * P;
+        float acc = 0.0f;
+        for (int k = 0; k < n; ++k) {
+            float mk = transpose ? M[k * n + i] : M[i * n + k];
+            if (square) mk = mul_rn(mk, mk);
+            acc = fmaf(mk, in[k * P + p], acc);
+        }
+        out[e] = acc;
+    }
+    __syncthreads();
+}
+
+// patch axis d (row-major M of edge b(d), stored with leading dimension b(d))
+template <class GM>
+__device__ void apply_space_axis(const GM& geo, int d, const float* in, float* out, int n,
+                                 const float* M, bool square) {
+    const int m = geo.b(d);
+    const int inner = geo.inner(d);
+    const int total = n * geo.P();
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int t = e % inner;
+        const int rest = e / inner;
+        const int i = rest % m;
+        const int o = rest / m;
+        const float* col = in + o * m * inner + t;
         float acc = 0.0f;
         for (int k = 0; k < m; ++k) {
-            float mk = transpose ? M[k * ld + i] : M[i * ld + k];
+            float mk = M[i * m + k];
             if (square) mk = mul_rn(mk, mk);
             acc = fmaf(mk, col[k * inner], acc);
         }
@@ -134,32 +204,29 @@ __device__ void apply_axis(const float* in, float* out, const int* dims, int nd,
 // dst).  The passes alternate between tmp and dst, starting with tmp, so no
 // pass reads and writes the same buffer.  kind: 0 forward, 1 inverse,
 // 2 squared forward.
-__device__ void transform_group(const FilterArgs& a, unsigned char* smem, int n, float* src,
-                                float* dst, float* tmp, int kind) {
-    const BmndStageParams& sp = a.sp;
-    int dims[BMND_MAX_DIMS + 1];
-    dims[0] = n;
-    for (int d = 0; d < sp.ndim; ++d) dims[1 + d] = sp.block[d];
-    const int nd = sp.ndim + 1;
+template <class GM>
+__device__ void transform_group(const GM& geo, const FilterArgs& a, unsigned char* smem, int n,
+                                float* src, float* dst, float* tmp, int kind) {
     const float* G = sm<float>(smem, a.L.g);
-    const float* Fw = sm<float>(smem, a.L.fw);
-    const float* Fi = sm<float>(smem, a.L.fi);
+    const float* F = sm<float>(smem, kind == 1 ? a.L.fi : a.L.fw);
     const float* cur = src;
     float* bufs[2] = {tmp, dst};
     int which = 0;
-    if (sp.group_transform != BMND_GROUP_NONE) {
-        apply_axis(cur, bufs[which], dims, nd, 0, G, n, kind == 2, kind == 1);
+    if (a.sp.group_transform != BMND_GROUP_NONE) {
+        apply_group_axis(geo, cur, bufs[which], n, G, kind == 2, kind == 1);
         cur = bufs[which];
         which ^= 1;
     }
-    for (int d = 0; d < sp.ndim; ++d) {
-        const float* M = (kind == 1 ? Fi : Fw) + d * BMND_MAX_EDGE * BMND_MAX_EDGE;
-        apply_axis(cur, bufs[which], dims, nd, d + 1, M, sp.block[d], kind == 2, false);
-        cur = bufs[which];
-        which ^= 1;
+#pragma unroll
+    for (int d = 0; d < BMND_MAX_DIMS; ++d) {
+        if (d < geo.nd()) {
+            apply_space_axis(geo, d, cur, bufs[which], n, F + d * BMND_MAX_EDGE * BMND_MAX_EDGE, kind == 2);
+            cur = bufs[which];
+            which ^= 1;
+        }
     }
     if (cur != dst) {
-        int total = n * a.P;
+        const int total = n * geo.P();
         for (int e = threadIdx.x; e < total; e += blockDim.x) dst[e] = cur[e];
         __syncthreads();
     }
@@ -180,44 +247,124 @@ __device__ __forceinline__ bool ht_keep(float mag, float thr, double scale) {
     return cc > tc + tol;
 }
 
+// accumulate c[q] += fl(G[i0 + q, g] * S[j, p]) over the entries [e0, e1) of one
+// voxel; an entry packs member g (low byte) and patch element p (upper bits)
+template <int NQ>
+__device__ __forceinline__ void voxel_contrib(const uint32_t* __restrict__ lent, int e0, int e1,
+                                              const float* __restrict__ GT, int kpad, int i0,
+                                              const float* __restrict__ stj, int P, float* c) {
+    for (int e = e0; e < e1; ++e) {
+        const uint32_t ent = lent[e];
+        const float sv = __ldg(stj + (ent >> 8) * P);
+        const float* gt = GT + (ent & 0xffu) * kpad + i0;
+        if (NQ == 4) {
+            const float4 gv = *reinterpret_cast<const float4*>(gt);
+            c[0] = add_rn(c[0], mul_rn(gv.x, sv));
+            c[1] = add_rn(c[1], mul_rn(gv.y, sv));
+            c[2] = add_rn(c[2], mul_rn(gv.z, sv));
+            c[3] = add_rn(c[3], mul_rn(gv.w, sv));
+        } else if (NQ == 2) {
+            const float2 gv = *reinterpret_cast<const float2*>(gt);
+            c[0] = add_rn(c[0], mul_rn(gv.x, sv));
+            c[1] = add_rn(c[1], mul_rn(gv.y, sv));
+        } else {
+            c[0] = add_rn(c[0], mul_rn(gt[0], sv));
+        }
+    }
+}
+
+// exact overlap-aware variance of planes [i0, i0 + NQ) for spatial coefficient j:
+// var[i, j] = sum_v V_v (sum_{e in v} fl(G[i, g_e] * S[j, p_e]))^2, voxels in
+// ascending union order, entries in ascending member order, every operation
+// rounded on its own (the reference's float32 loop, variance.py:950-975).
+// S[j, p] comes from the precomputed S^T, whose entries are the reference's
+// float32 Kronecker products.  Two voxels are expanded at a time (independent
+// chains); their squares are still added to var in voxel order.
+template <int NQ>
+__device__ void exact_planes(const float* __restrict__ lval, const int* __restrict__ lstart,
+                             const uint32_t* __restrict__ lent, int U, const float* __restrict__ GT,
+                             int kpad, const float* __restrict__ st, int P, int j, int i0, int nq,
+                             float* __restrict__ EX) {
+    const float* stj = st + j;
+    float var[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) var[q] = 0.0f;
+    int u = 0;
+    for (; u + 1 < U; u += 2) {
+        float ca[NQ], cb[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            ca[q] = 0.0f;
+            cb[q] = 0.0f;
+        }
+        const int a0 = lstart[u], a1 = lstart[u + 1], b1 = lstart[u + 2];
+        voxel_contrib<NQ>(lent, a0, a1, GT, kpad, i0, stj, P, ca);
+        voxel_contrib<NQ>(lent, a1, b1, GT, kpad, i0, stj, P, cb);
+        const float va = lval[u], vb = lval[u + 1];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            var[q] = add_rn(var[q], mul_rn(mul_rn(va, ca[q]), ca[q]));
+            var[q] = add_rn(var[q], mul_rn(mul_rn(vb, cb[q]), cb[q]));
+        }
+    }
+    if (u < U) {
+        float ca[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) ca[q] = 0.0f;
+        voxel_contrib<NQ>(lent, lstart[u], lstart[u + 1], GT, kpad, i0, stj, P, ca);
+        const float va = lval[u];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) var[q] = add_rn(var[q], mul_rn(mul_rn(va, ca[q]), ca[q]));
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+        if (q < nq) EX[(i0 + q) * P + j] = sqrtf(var[q] > 0.0f ? var[q] : 0.0f);
+}
+
+template <int ND, int B0, int B1, int B2>
 __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
+    using GM = Geom<ND, B0, B1, B2>;
     const BmndStageParams& sp = a.sp;
+    const GM geo(sp);
     const int64_t gid = blockIdx.x;
     const int tid = threadIdx.x;
-    const int P = a.P;
-    const int ndim = sp.ndim;
+    const int P = geo.P();
     const int n = a.count[gid];
     if (n <= 0) return;
     const bool wiener = sp.filter == BMND_FILTER_WIENER;
 
     float* G = sm<float>(smem, a.L.g);
+    float* GT = sm<float>(smem, a.L.gt);
     float* Fw = sm<float>(smem, a.L.fw);
     float* Fi = sm<float>(smem, a.L.fi);
     float* win = sm<float>(smem, a.L.win);
     double* mdiag = sm<double>(smem, a.L.mdiag);
     int* pos = sm<int>(smem, a.L.pos);
     int* shf = sm<int>(smem, a.L.shf);
+    float* S = sm<float>(smem, a.L.s);
+    float* EX = sm<float>(smem, a.L.ex);
     float* X = sm<float>(smem, a.L.x);
+    float* R = sm<float>(smem, a.L.r);
     float* T = sm<float>(smem, a.L.t);
     float* V = sm<float>(smem, a.L.v);
-    float* S = sm<float>(smem, a.L.s);
-    float* R = sm<float>(smem, a.L.r);
-    float* A = sm<float>(smem, a.L.a);
-    float* EX = sm<float>(smem, a.L.ex);
     uint32_t* grid = sm<uint32_t>(smem, a.L.grid);
-    uint32_t* lcoord = sm<uint32_t>(smem, a.L.lcoord);
-    uint32_t* lmask = sm<uint32_t>(smem, a.L.lmask);
     float* lval = sm<float>(smem, a.L.lval);
-    int* scan = sm<int>(smem, a.L.scan);
+    int* lstart = sm<int>(smem, a.L.lstart);
+    uint32_t* lent = sm<uint32_t>(smem, a.L.lent);
+    int2* scan = sm<int2>(smem, a.L.scan);
     double* plane = sm<double>(smem, a.L.plane);
     float* wts = sm<float>(smem, a.L.wts);
     int* misc = sm<int>(smem, a.L.misc);
 
+    const int k = sp.variance_k;
+    const int kk = k < n ? k : n;
+    const int kpad = (a.kmax + 3) / 4 * 4;
+
     // ---- setup: positions, matrices, window ----
     if (tid < n) {
         int64_t rem = a.sel[gid * sp.max_stack + tid];
-        for (int d = ndim - 1; d >= 0; --d) {
+        for (int d = geo.nd() - 1; d >= 0; --d) {
             pos[tid * BMND_MAX_DIMS + d] = static_cast<int>(rem % a.counts[d]);
             rem /= a.counts[d];
         }
@@ -232,173 +379,178 @@ __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
         mdiag[e] = sp.spatial_metric_diag[e];
     }
     __syncthreads();
+    // G^T restricted to the exact planes, padded to 4: GT[g * kpad + i] = G[i, g]
+    for (int e = tid; e < n * kpad; e += blockDim.x) {
+        int g = e / kpad, i = e % kpad;
+        GT[e] = i < kk ? G[i * n + g] : 0.0f;
+    }
     if (tid == 0) {
         // group origin (min over members) and shifted positions
-        for (int d = 0; d < ndim; ++d) {
+        for (int d = 0; d < geo.nd(); ++d) {
             int mn = pos[d];
             for (int g = 1; g < n; ++g) mn = min(mn, pos[g * BMND_MAX_DIMS + d]);
             int mx = 0;
             for (int g = 0; g < n; ++g) {
-                int s = pos[g * BMND_MAX_DIMS + d] - mn;
-                shf[g * BMND_MAX_DIMS + d] = s;
-                mx = g == 0 ? s : max(mx, s);
+                int sh = pos[g * BMND_MAX_DIMS + d] - mn;
+                shf[g * BMND_MAX_DIMS + d] = sh;
+                mx = g == 0 ? sh : max(mx, sh);
             }
             misc[d] = mn;                  // origin
-            misc[4 + d] = mx + sp.block[d];  // union extent
+            misc[4 + d] = mx + geo.b(d);   // union extent
         }
     }
     __syncthreads();
 
-    // ---- gather ----
     const float scale_f = static_cast<float>(sp.count_scale);
     const float floor_f = static_cast<float>(sp.variance_floor);
     const float* varsrc = wiener ? a.pilot : a.noisy;
     const int total = n * P;
-    for (int e = tid; e < total; e += blockDim.x) {
-        int g = e / P, p = e % P;
-        int rem = p;
-        int64_t off = 0;
-        for (int d = ndim - 1; d >= 0; --d) {
-            off += static_cast<int64_t>(pos[g * BMND_MAX_DIMS + d] + rem % sp.block[d]) * a.vstride[d];
-            rem /= sp.block[d];
-        }
-        X[e] = __ldg(a.noisy + off);
-        V[e] = variance_of(__ldg(varsrc + off), scale_f, floor_f);
-        if (wiener) R[e] = __ldg(a.pilot + off);
-    }
-    __syncthreads();
-
-    // ---- forward transforms ----
-    transform_group(a, smem, n, X, X, T, 0);
-    if (wiener) transform_group(a, smem, n, R, R, T, 0);
-
-    // ---- noise standard deviation ----
-    const int k = sp.variance_k;
-    const int kk = k < n ? k : n;
     const bool need_approx = (k <= 0) || (kk < n);
+
+    // ---- approximate sigma from the variance group (squared transforms) ----
     if (need_approx) {
-        transform_group(a, smem, n, V, V, T, 2);
+        for (int e = tid; e < total; e += blockDim.x) {
+            const int g = e / P;
+            V[e] = variance_of(__ldg(varsrc + geo.offset(pos + g * BMND_MAX_DIMS, e - g * P, a.vstride)),
+                               scale_f, floor_f);
+        }
+        __syncthreads();
+        transform_group(geo, a, smem, n, V, V, T, 2);
         for (int e = tid; e < total; e += blockDim.x) {
             float v = V[e];
-            A[e] = sqrtf(v > 0.0f ? v : 0.0f);  // approximate sigma
+            S[e] = sqrtf(v > 0.0f ? v : 0.0f);
         }
         __syncthreads();
     }
+
+    // ---- exact overlap-aware sigma of the first kk planes ----
     if (kk > 0) {
-        int ush[BMND_MAX_DIMS], org[BMND_MAX_DIMS];
-        int64_t ucells = 1;
-        for (int d = 0; d < ndim; ++d) {
+        int ush[BMND_MAX_DIMS] = {1, 1, 1}, org[BMND_MAX_DIMS] = {0, 0, 0};
+        int ucells = 1;
+        for (int d = 0; d < geo.nd(); ++d) {
             ush[d] = misc[4 + d];
             org[d] = misc[d];
             ucells *= ush[d];
         }
-        for (int64_t c = tid; c < ucells; c += blockDim.x) grid[c] = 0u;
+        for (int c = tid; c < ucells; c += blockDim.x) grid[c] = 0u;
         __syncthreads();
         for (int e = tid; e < total; e += blockDim.x) {
-            int g = e / P, p = e % P;
-            int rem = p;
-            int64_t cell = 0, mul = 1;
-            for (int d = ndim - 1; d >= 0; --d) {
-                cell += static_cast<int64_t>(shf[g * BMND_MAX_DIMS + d] + rem % sp.block[d]) * mul;
-                mul *= ush[d];
-                rem /= sp.block[d];
+            const int g = e / P;
+            int p = e - g * P;
+            int cell = 0, mul = 1;
+#pragma unroll
+            for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                if (d < geo.nd()) {
+                    cell += (shf[g * BMND_MAX_DIMS + d] + p % geo.b(d)) * mul;
+                    mul *= ush[d];
+                    p /= geo.b(d);
+                }
             }
             atomicOr(grid + cell, 1u << g);
         }
         __syncthreads();
-        // compact occupied cells in ascending cell order (block-wide scan)
-        int64_t per = (ucells + blockDim.x - 1) / blockDim.x;
-        int64_t c0 = tid * per, c1 = min(ucells, c0 + per);
-        int mine = 0;
-        for (int64_t c = c0; c < c1; ++c) mine += grid[c] != 0u;
-        scan[tid] = mine;
+        // compact occupied cells (ascending) and their entries (ascending member)
+        const int per = (ucells + blockDim.x - 1) / blockDim.x;
+        const int c0 = tid * per, c1 = min(ucells, c0 + per);
+        int nvox = 0, nent = 0;
+        for (int c = c0; c < c1; ++c) {
+            uint32_t m = grid[c];
+            nvox += m != 0u;
+            nent += __popc(m);
+        }
+        scan[tid] = make_int2(nvox, nent);
         __syncthreads();
-        if (tid == 0) {
-            int run = 0;
-            for (int i = 0; i < static_cast<int>(blockDim.x); ++i) {
-                int v = scan[i];
-                scan[i] = run;
-                run += v;
+        if (tid < 32) {
+            // warp-cooperative exclusive scan over blockDim.x partial counts
+            int carry_v = 0, carry_e = 0;
+            for (int base = 0; base < static_cast<int>(blockDim.x); base += 32) {
+                int2 v = scan[base + tid];
+                int iv = v.x, ie = v.y;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    int tv = __shfl_up_sync(0xffffffffu, iv, o);
+                    int te = __shfl_up_sync(0xffffffffu, ie, o);
+                    if (tid >= o) {
+                        iv += tv;
+                        ie += te;
+                    }
+                }
+                scan[base + tid] = make_int2(carry_v + iv - v.x, carry_e + ie - v.y);
+                carry_v += __shfl_sync(0xffffffffu, iv, 31);
+                carry_e += __shfl_sync(0xffffffffu, ie, 31);
             }
-            scan[blockDim.x] = run;
+            if (tid == 0) scan[blockDim.x] = make_int2(carry_v, carry_e);
         }
         __syncthreads();
-        int w = scan[tid];
-        for (int64_t c = c0; c < c1; ++c) {
+        int w = scan[tid].x, we = scan[tid].y;
+        for (int c = c0; c < c1; ++c) {
             uint32_t m = grid[c];
             if (!m) continue;
-            int64_t rem = c;
-            uint32_t packed = 0;
+            int rem = c;
+            int coords[BMND_MAX_DIMS] = {0, 0, 0};
+#pragma unroll
+            for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                if (d < geo.nd()) {
+                    coords[d] = rem % ush[d];
+                    rem /= ush[d];
+                }
+            }
             int64_t vox = 0;
-            int coords[BMND_MAX_DIMS];
-            for (int d = ndim - 1; d >= 0; --d) {
-                coords[d] = static_cast<int>(rem % ush[d]);
-                rem /= ush[d];
-            }
-            for (int d = 0; d < ndim; ++d) {
-                packed |= static_cast<uint32_t>(coords[d]) << (10 * d);
-                vox += static_cast<int64_t>(coords[d] + org[d]) * a.vstride[d];
-            }
-            lcoord[w] = packed;
-            lmask[w] = m;
+#pragma unroll
+            for (int d = 0; d < BMND_MAX_DIMS; ++d)
+                if (d < geo.nd()) vox += static_cast<int64_t>(coords[d] + org[d]) * a.vstride[d];
             lval[w] = variance_of(__ldg(varsrc + vox), scale_f, floor_f);
+            lstart[w] = we;
+            while (m) {
+                const int g = __ffs(m) - 1;
+                m &= m - 1;
+                int pe = 0;
+#pragma unroll
+                for (int d = 0; d < BMND_MAX_DIMS; ++d)
+                    if (d < geo.nd()) pe = pe * geo.b(d) + (coords[d] - shf[g * BMND_MAX_DIMS + d]);
+                lent[we++] = static_cast<uint32_t>(g) | (static_cast<uint32_t>(pe) << 8);
+            }
             ++w;
         }
+        const int U = scan[blockDim.x].x;
+        if (tid == 0) lstart[U] = scan[blockDim.x].y;
         __syncthreads();
-        const int U = scan[blockDim.x];
-        // one coefficient (plane i < kk, spatial j) per thread iteration
-        for (int idx = tid; idx < kk * P; idx += blockDim.x) {
-            int i = idx / P, j = idx % P;
-            int jd[BMND_MAX_DIMS];
-            {
-                int rem = j;
-                for (int d = ndim - 1; d >= 0; --d) {
-                    jd[d] = rem % sp.block[d];
-                    rem /= sp.block[d];
-                }
-            }
-            float accv = 0.0f;
-            for (int u = 0; u < U; ++u) {
-                uint32_t m = lmask[u];
-                uint32_t pc = lcoord[u];
-                float c = 0.0f;
-                while (m) {
-                    int g = __ffs(m) - 1;
-                    m &= m - 1;
-                    // kron entry S[j, p] = fl(fl(F0 * F1) * F2), then fl(G * S)
-                    float s = 1.0f;
-                    for (int d = 0; d < ndim; ++d) {
-                        int pd = static_cast<int>((pc >> (10 * d)) & 1023u) - shf[g * BMND_MAX_DIMS + d];
-                        float f = Fw[d * BMND_MAX_EDGE * BMND_MAX_EDGE + jd[d] * sp.block[d] + pd];
-                        s = d == 0 ? f : mul_rn(s, f);
-                    }
-                    c = add_rn(c, mul_rn(G[i * n + g], s));
-                }
-                accv = add_rn(accv, mul_rn(mul_rn(lval[u], c), c));
-            }
-            EX[idx] = sqrtf(accv > 0.0f ? accv : 0.0f);
+        // work items: (spatial coefficient j, chunk of up to 4 planes)
+        // planes per item: as many as keep ~90% of the threads busy
+        int ppi = 4;
+        while (ppi > 1 && 10 * P * ((kk + ppi - 1) / ppi) < 9 * static_cast<int>(blockDim.x)) ppi >>= 1;
+        const int chunks = (kk + ppi - 1) / ppi;
+        for (int item = tid; item < P * chunks; item += blockDim.x) {
+            const int j = item % P;
+            const int i0 = (item / P) * ppi;
+            const int nq = min(ppi, kk - i0);
+            if (ppi == 4)
+                exact_planes<4>(lval, lstart, lent, U, GT, kpad, a.st, P, j, i0, nq, EX);
+            else if (ppi == 2)
+                exact_planes<2>(lval, lstart, lent, U, GT, kpad, a.st, P, j, i0, nq, EX);
+            else
+                exact_planes<1>(lval, lstart, lent, U, GT, kpad, a.st, P, j, i0, nq, EX);
         }
         __syncthreads();
     }
-    // final sigma into S
-    if (k <= 0) {
-        for (int e = tid; e < total; e += blockDim.x) S[e] = A[e];
-    } else if (kk == n) {
+
+    // ---- final sigma in S (plane limiting, variance.py:1572-1631) ----
+    if (k > 0 && kk == n) {
         for (int e = tid; e < total; e += blockDim.x) S[e] = EX[e];
-    } else {
+    } else if (k > 0) {
         for (int j = tid; j < P; j += blockDim.x) {
             float sum_a = 0.0f, sum_e = 0.0f, rem_a = 0.0f;
             for (int i = 0; i < n; ++i) {
-                float s = fmaxf(A[i * P + j], 0.0f);
-                sum_a = add_rn(sum_a, mul_rn(s, s));
+                float sa = fmaxf(S[i * P + j], 0.0f);
+                sum_a = add_rn(sum_a, mul_rn(sa, sa));
             }
             for (int i = 0; i < kk; ++i) {
-                float s = fmaxf(EX[i * P + j], 0.0f);
-                sum_e = add_rn(sum_e, mul_rn(s, s));
+                float se = fmaxf(EX[i * P + j], 0.0f);
+                sum_e = add_rn(sum_e, mul_rn(se, se));
             }
             for (int i = kk; i < n; ++i) {
-                float s = fmaxf(A[i * P + j], 0.0f);
-                rem_a = add_rn(rem_a, mul_rn(s, s));
+                float sa = fmaxf(S[i * P + j], 0.0f);
+                rem_a = add_rn(rem_a, mul_rn(sa, sa));
             }
             float target = sub_rn(sum_a, sum_e);
             if (target < 0.0f) target = 0.0f;
@@ -406,11 +558,11 @@ __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
             for (int i = 0; i < n; ++i) {
                 float v;
                 if (i < kk) {
-                    float s = fmaxf(EX[i * P + j], 0.0f);
-                    v = mul_rn(s, s);
+                    float se = fmaxf(EX[i * P + j], 0.0f);
+                    v = mul_rn(se, se);
                 } else if (rem_a > 0.0f) {
-                    float s = fmaxf(A[i * P + j], 0.0f);
-                    v = mul_rn(mul_rn(s, s), scl);
+                    float sa = fmaxf(S[i * P + j], 0.0f);
+                    v = mul_rn(mul_rn(sa, sa), scl);
                 } else {
                     v = div_rn(target, static_cast<float>(n - kk));
                 }
@@ -420,7 +572,18 @@ __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
     }
     __syncthreads();
 
-    // ---- shrinkage: attenuation into A, noise variance into S ----
+    // ---- gather and forward-transform the observation (and the pilot) ----
+    for (int e = tid; e < total; e += blockDim.x) {
+        const int g = e / P;
+        const int64_t off = geo.offset(pos + g * BMND_MAX_DIMS, e - g * P, a.vstride);
+        X[e] = __ldg(a.noisy + off);
+        if (wiener) R[e] = __ldg(a.pilot + off);
+    }
+    __syncthreads();
+    transform_group(geo, a, smem, n, X, X, T, 0);
+    if (wiener) transform_group(geo, a, smem, n, R, R, T, 0);
+
+    // ---- shrinkage: coefficients in X, attenuation in V, noise variance in S ----
     const float eps_f = static_cast<float>(sp.eps);
     for (int e = tid; e < total; e += blockDim.x) {
         float sig = S[e];
@@ -439,7 +602,7 @@ __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
             att = fminf(fmaxf(gain, 0.0f), 1.0f);
         }
         X[e] = mul_rn(X[e], att);
-        A[e] = att;
+        V[e] = att;
         S[e] = nv;
     }
     __syncthreads();
@@ -450,7 +613,7 @@ __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
         for (int g = warp; g < n; g += nwarps) {
             double risk = 0.0;
             for (int j = lane; j < P; j += 32) {
-                double at = static_cast<double>(A[g * P + j]);
+                double at = static_cast<double>(V[g * P + j]);
                 double err = at * at;
                 if (sp.weight_model != BMND_WEIGHT_CLASSIC) err *= static_cast<double>(S[g * P + j]);
                 if (sp.windowed_synthesis) err *= mdiag[j];
@@ -473,18 +636,34 @@ __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
     __syncthreads();
 
     // ---- inverse transform and scatter ----
-    transform_group(a, smem, n, X, X, T, 1);
+    transform_group(geo, a, smem, n, X, X, T, 1);
     for (int e = tid; e < total; e += blockDim.x) {
-        int g = e / P, p = e % P;
-        int rem = p;
-        int64_t off = 0;
-        for (int d = ndim - 1; d >= 0; --d) {
-            off += static_cast<int64_t>(pos[g * BMND_MAX_DIMS + d] + rem % sp.block[d]) * a.vstride[d];
-            rem /= sp.block[d];
-        }
+        const int g = e / P;
+        const int p = e - g * P;
+        const int64_t off = geo.offset(pos + g * BMND_MAX_DIMS, p, a.vstride);
         float ww = mul_rn(wts[g], win[p]);
         atomicAdd(a.num + off, static_cast<double>(mul_rn(X[e], ww)));
         atomicAdd(a.den + off, static_cast<double>(ww));
+    }
+}
+
+// S^T[p * P + j] = S[j, p] with S = kron(F_0, ..., F_{nd-1}) built axis by axis in
+// float32 (fl(fl(F0 * F1) * F2)), as the reference builds its spatial matrix
+// (variance.py:744-755)
+__global__ void spatial_kron_kernel(BmndStageParams sp, int P, float* st) {
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < P * P; idx += gridDim.x * blockDim.x) {
+        const int p = idx / P, j = idx % P;
+        int jd[BMND_MAX_DIMS], pd[BMND_MAX_DIMS];
+        int rj = j, rp = p;
+        for (int d = sp.ndim - 1; d >= 0; --d) {
+            jd[d] = rj % sp.block[d];
+            rj /= sp.block[d];
+            pd[d] = rp % sp.block[d];
+            rp /= sp.block[d];
+        }
+        float v = sp.spatial_fwd[0][jd[0] * sp.block[0] + pd[0]];
+        for (int d = 1; d < sp.ndim; ++d) v = mul_rn(v, sp.spatial_fwd[d][jd[d] * sp.block[d] + pd[d]]);
+        st[idx] = v;
     }
 }
 
@@ -520,9 +699,15 @@ int64_t group_filter_smem_bytes(const BmndStageParams& sp) {
 
 int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const float* pilot,
                             const int32_t* sel, const int32_t* count, int64_t n_refs, double* num,
-                            double* den, cudaStream_t stream) {
+                            double* den, float* st, cudaStream_t stream) {
     if (n_refs == 0) return BMND_OK;
+    {
+        const int P = patch_volume(sp);
+        spatial_kron_kernel<<<(P * P + 255) / 256, 256, 0, stream>>>(sp, P, st);
+        BMND_LAUNCH_CHECK("spatial_kron_kernel");
+    }
     FilterArgs a{};
+    a.st = st;
     a.sp = sp;
     a.P = patch_volume(sp);
     a.nmax = sp.max_stack;
@@ -545,11 +730,18 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
     if (a.L.total > 227 * 1024)
         return fail(BMND_ERR_UNSUPPORTED, "group filter shared memory exceeds 227 KB for this profile");
     if (n_refs > 0x7fffffffLL) return fail(BMND_ERR_UNSUPPORTED, "too many groups");
-    BMND_CUDA_TRY(cudaFuncSetAttribute(group_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(a.L.total)));
-    group_filter_kernel<<<static_cast<unsigned>(n_refs), kThreads, a.L.total, stream>>>(a);
-    BMND_LAUNCH_CHECK("group_filter_kernel");
-    return BMND_OK;
+    auto run = [&](auto kernel) -> int32_t {
+        BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(a.L.total)));
+        kernel<<<static_cast<unsigned>(n_refs), kThreads, a.L.total, stream>>>(a);
+        BMND_LAUNCH_CHECK("group_filter_kernel");
+        return BMND_OK;
+    };
+    const int* b = sp.block;
+    if (sp.ndim == 2 && b[0] == 8 && b[1] == 8) return run(group_filter_kernel<2, 8, 8, 1>);
+    if (sp.ndim == 3 && b[0] == 4 && b[1] == 4 && b[2] == 4) return run(group_filter_kernel<3, 4, 4, 4>);
+    if (sp.ndim == 3 && b[0] == 5 && b[1] == 5 && b[2] == 5) return run(group_filter_kernel<3, 5, 5, 5>);
+    return run(group_filter_kernel<0, 0, 0, 0>);
 }
 
 int32_t launch_finalize(const BmndStageParams& sp, const double* num, const double* den,

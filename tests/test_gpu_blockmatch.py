@@ -181,3 +181,74 @@ def test_volume_matching_vs_oracle(cuda, native, oracle_lib, shape, block, radiu
     assert not bad, f"unexplained match-set differences in rows {bad[:10]}"
     assert eq >= 0.98 * n
     assert np.mean(ga == oa) >= 0.98
+
+
+def _match_volume(cuda, native, vol, block, radius, max_m, min_m, thr, precision, refs=None):
+    from bmnd_gb300 import _abi
+
+    shape = vol.shape
+    counts = tuple(s - b + 1 for s, b in zip(shape, block))
+    if refs is None:
+        refs = np.stack(np.meshgrid(*[np.arange(0, c, 2) for c in counts], indexing="ij"), -1)
+        refs = refs.reshape(-1, len(shape)).astype(np.int32)
+    dev = cuda.device("cuda:0")
+    vt = cuda.from_numpy(np.ascontiguousarray(vol, dtype=np.float32)).to(dev)
+    rt = cuda.from_numpy(refs).to(dev)
+    n = refs.shape[0]
+    tt = cuda.full((n,), float(np.float32(thr)), device=dev)
+    sel = cuda.full((n, max_m), -7, dtype=cuda.int32, device=dev)
+    cnt = cuda.full((n,), -7, dtype=cuda.int32, device=dev)
+    acc = cuda.full((n,), -7, dtype=cuda.int32, device=dev)
+    p = _mp(counts, radius, max_m, min_m, DEV)
+    p.precision = precision
+    sh = (ctypes.c_int32 * len(shape))(*shape)
+    bl = (ctypes.c_int32 * len(shape))(*block)
+    _abi.check(native.bmnd_blockmatch_volume(ctypes.byref(p), vt.data_ptr(), sh, bl, rt.data_ptr(), n,
+                                             tt.data_ptr(), sel.data_ptr(), cnt.data_ptr(), acc.data_ptr(), 0))
+    cuda.cuda.synchronize()
+    return sel.cpu().numpy(), cnt.cpu().numpy(), acc.cpu().numpy()
+
+
+@pytest.mark.parametrize("shape,block,radius,max_m,thr", [
+    ((40, 44), (8, 8), (19, 19), 32, 0.3937),
+    ((40, 44), (8, 8), (19, 19), 16, 2.9527),
+    ((22, 20, 24), (5, 5, 5), (7, 7, 7), 32, 0.7689),
+    ((22, 20, 24), (4, 4, 4), (7, 7, 7), 16, 2.9527),
+])
+@pytest.mark.parametrize("kind", ["smooth", "tiny", "sparse", "large", "flat"])
+def test_screened_matching_equals_exact(cuda, native, shape, block, radius, max_m, thr, kind):
+    """The screened deviance path (precision=fast) must give bit-identical match tables."""
+    from bmnd_gb300 import _abi
+
+    rng = np.random.default_rng(hash((shape, kind)) % 2**32)
+    grids = np.meshgrid(*[np.linspace(0, 1, s) for s in shape], indexing="ij")
+    smooth = 5.0 + 20.0 * np.sin(3 * grids[0]) ** 2 + 10.0 * grids[-1]
+    if kind == "smooth":
+        vol = smooth + rng.normal(0, 0.5, size=shape)
+    elif kind == "tiny":
+        vol = rng.uniform(0.0, 0.05, size=shape)
+    elif kind == "sparse":
+        vol = rng.poisson(0.3, size=shape) * rng.uniform(0.5, 1.5, size=shape)
+    elif kind == "large":
+        vol = 500.0 * smooth + rng.normal(0, 30.0, size=shape)
+    else:
+        vol = np.full(shape, 7.25) + (rng.random(shape) < 0.02) * 3.0
+    vol = np.maximum(vol, 0.0).astype(np.float32)
+    ex = _match_volume(cuda, native, vol, block, radius, max_m, 2, thr, _abi.MATCH_EXACT)
+    fa = _match_volume(cuda, native, vol, block, radius, max_m, 2, thr, _abi.MATCH_FAST)
+    np.testing.assert_array_equal(fa[1], ex[1])
+    np.testing.assert_array_equal(fa[2], ex[2])
+    np.testing.assert_array_equal(fa[0], ex[0])
+
+
+def test_screened_fallback_when_threshold_rejects_everything(cuda, native):
+    """Only the reference is accepted: the best rejected fill comes from the exact redo."""
+    from bmnd_gb300 import _abi
+
+    rng = np.random.default_rng(5)
+    vol = rng.uniform(1.0, 50.0, size=(30, 30)).astype(np.float32)
+    ex = _match_volume(cuda, native, vol, (8, 8), (5, 5), 16, 2, 1e-7, _abi.MATCH_EXACT)
+    fa = _match_volume(cuda, native, vol, (8, 8), (5, 5), 16, 2, 1e-7, _abi.MATCH_FAST)
+    assert np.all(ex[1] == 2)
+    for i in range(3):
+        np.testing.assert_array_equal(fa[i], ex[i])
