@@ -43,7 +43,7 @@ constexpr int kThreads = 256;
 // phases are ordered so that none of X/R/T/V is live while the lists are.
 struct Layout {
     // byte offsets into dynamic shared memory
-    int64_t g, gt, fw, fi, win, mdiag, pos, shf, s, ex, uni, x, r, t, v, grid, lval, lstart, lent,
+    int64_t g, ginv, gsq, gt, fw, fi, win, mdiag, pos, shf, s, ex, uni, x, r, t, v, grid, lval, lstart, lent,
         scan, plane, wts, misc, total;
 };
 
@@ -78,6 +78,8 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     const bool wiener = sp.filter == BMND_FILTER_WIENER;
     const int kpad = (kmax + 3) / 4 * 4;
     L.g = take(4 * nmax * nmax);
+    L.ginv = take(4 * nmax * nmax);
+    L.gsq = take(4 * nmax * nmax);
     L.gt = take(4 * nmax * (kpad > 0 ? kpad : 4));
     L.fw = take(4 * BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE);
     L.fi = take(4 * BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE);
@@ -155,28 +157,103 @@ struct Geom {
     }
 };
 
-// group axis: out[i, p] = sum_g M[i, g] in[g, p] (fused multiply-add per term,
-// g ascending); `square` uses fl(M*M), `transpose` uses M^T
+// Register-blocked group-axis product for a compile-time group size N:
+// out[i, p] = sum_k M[i, k] in[k, p], one fused multiply-add per term in k
+// order.  Each work item holds the column in[:, p] in registers and produces a
+// chunk of the N outputs, reading the matrix rows as float4 broadcasts.
+template <int N>
+__device__ void group_axis_reg(const float* in, float* out, int P, const float* M) {
+    constexpr int IC = N >= 16 ? 8 : N;          // outputs per item
+    constexpr int CH = N / IC;                   // chunks per column
+    const int items = P * CH;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        const int p = it % P;
+        const int i0 = (it / P) * IC;
+        float x[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k) x[k] = in[k * P + p];
+#pragma unroll
+        for (int ii = 0; ii < IC; ++ii) {
+            const float* row = M + (i0 + ii) * N;
+            float acc = 0.0f;
+            if (N % 4 == 0) {
+#pragma unroll
+                for (int k = 0; k < N; k += 4) {
+                    const float4 m = *reinterpret_cast<const float4*>(row + k);
+                    acc = fmaf(m.x, x[k], acc);
+                    acc = fmaf(m.y, x[k + 1], acc);
+                    acc = fmaf(m.z, x[k + 2], acc);
+                    acc = fmaf(m.w, x[k + 3], acc);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < N; ++k) acc = fmaf(row[k], x[k], acc);
+            }
+            out[(i0 + ii) * P + p] = acc;
+        }
+    }
+    __syncthreads();
+}
+
+// runtime group size (non power of two): one output per work item
 template <class GM>
-__device__ void apply_group_axis(const GM& geo, const float* in, float* out, int n, const float* M,
-                                 bool square, bool transpose) {
+__device__ void group_axis_generic(const GM& geo, const float* in, float* out, int n, const float* M) {
     const int P = geo.P();
     const int total = n * P;
     for (int e = threadIdx.x; e < total; e += blockDim.x) {
         const int i = e / P;
         const int p = e - i * P;
         float acc = 0.0f;
-        for (int k = 0; k < n; ++k) {
-            float mk = transpose ? M[k * n + i] : M[i * n + k];
-            if (square) mk = mul_rn(mk, mk);
-            acc = fmaf(mk, in[k * P + p], acc);
-        }
+        for (int k = 0; k < n; ++k) acc = fmaf(M[i * n + k], in[k * P + p], acc);
         out[e] = acc;
     }
     __syncthreads();
 }
 
-// patch axis d (row-major M of edge b(d), stored with leading dimension b(d))
+template <class GM>
+__device__ void apply_group_axis(const GM& geo, const float* in, float* out, int n, const float* M) {
+    const int P = geo.P();
+    switch (n) {
+        case 1: group_axis_reg<1>(in, out, P, M); break;
+        case 2: group_axis_reg<2>(in, out, P, M); break;
+        case 4: group_axis_reg<4>(in, out, P, M); break;
+        case 8: group_axis_reg<8>(in, out, P, M); break;
+        case 16: group_axis_reg<16>(in, out, P, M); break;
+        case 32: group_axis_reg<32>(in, out, P, M); break;
+        default: group_axis_generic(geo, in, out, n, M); break;
+    }
+}
+
+// patch axis d with compile-time edge B and stride INNER: each work item
+// transforms one line of B values with the matrix held in registers
+template <int B, int INNER>
+__device__ void space_axis_reg(const float* in, float* out, int total, const float* Msrc, bool square) {
+    float m[B * B];
+#pragma unroll
+    for (int q = 0; q < B * B; ++q) {
+        const float v = Msrc[q];
+        m[q] = square ? mul_rn(v, v) : v;
+    }
+    const int lines = total / B;
+    for (int line = threadIdx.x; line < lines; line += blockDim.x) {
+        const int o = line / INNER;
+        const int t = line - o * INNER;
+        const int base = o * B * INNER + t;
+        float x[B];
+#pragma unroll
+        for (int k = 0; k < B; ++k) x[k] = in[base + k * INNER];
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int k = 0; k < B; ++k) acc = fmaf(m[i * B + k], x[k], acc);
+            out[base + i * INNER] = acc;
+        }
+    }
+    __syncthreads();
+}
+
+// runtime geometry fallback for a patch axis
 template <class GM>
 __device__ void apply_space_axis(const GM& geo, int d, const float* in, float* out, int n,
                                  const float* M, bool square) {
@@ -200,27 +277,50 @@ __device__ void apply_space_axis(const GM& geo, int d, const float* in, float* o
     __syncthreads();
 }
 
+template <int ND, int B0, int B1, int B2, int D>
+__device__ __forceinline__ void space_axis_fixed(const float* in, float* out, int n, const float* M,
+                                                 bool square) {
+    constexpr int B = D == 0 ? B0 : (D == 1 ? B1 : B2);
+    constexpr int INNER = D == 0 ? (ND > 1 ? B1 : 1) * (ND > 2 ? B2 : 1) : (D == 1 ? (ND > 2 ? B2 : 1) : 1);
+    space_axis_reg<B, INNER>(in, out, n * B0 * B1 * B2, M, square);
+}
+
 // separable transform of an (n, block...) group: src -> dst (src may equal
 // dst).  The passes alternate between tmp and dst, starting with tmp, so no
 // pass reads and writes the same buffer.  kind: 0 forward, 1 inverse,
 // 2 squared forward.
-template <class GM>
+template <int ND, int B0, int B1, int B2, class GM>
 __device__ void transform_group(const GM& geo, const FilterArgs& a, unsigned char* smem, int n,
                                 float* src, float* dst, float* tmp, int kind) {
-    const float* G = sm<float>(smem, a.L.g);
+    const float* G = sm<float>(smem, kind == 0 ? a.L.g : (kind == 1 ? a.L.ginv : a.L.gsq));
     const float* F = sm<float>(smem, kind == 1 ? a.L.fi : a.L.fw);
     const float* cur = src;
     float* bufs[2] = {tmp, dst};
     int which = 0;
     if (a.sp.group_transform != BMND_GROUP_NONE) {
-        apply_group_axis(geo, cur, bufs[which], n, G, kind == 2, kind == 1);
+        apply_group_axis(geo, cur, bufs[which], n, G);
         cur = bufs[which];
         which ^= 1;
     }
-#pragma unroll
-    for (int d = 0; d < BMND_MAX_DIMS; ++d) {
-        if (d < geo.nd()) {
-            apply_space_axis(geo, d, cur, bufs[which], n, F + d * BMND_MAX_EDGE * BMND_MAX_EDGE, kind == 2);
+    const bool square = kind == 2;
+    if constexpr (ND > 0) {
+        space_axis_fixed<ND, B0, B1, B2, 0>(cur, bufs[which], n, F, square);
+        cur = bufs[which];
+        which ^= 1;
+        if constexpr (ND > 1) {
+            space_axis_fixed<ND, B0, B1, B2, 1>(cur, bufs[which], n, F + BMND_MAX_EDGE * BMND_MAX_EDGE, square);
+            cur = bufs[which];
+            which ^= 1;
+        }
+        if constexpr (ND > 2) {
+            space_axis_fixed<ND, B0, B1, B2, 2>(cur, bufs[which], n, F + 2 * BMND_MAX_EDGE * BMND_MAX_EDGE,
+                                                square);
+            cur = bufs[which];
+            which ^= 1;
+        }
+    } else {
+        for (int d = 0; d < geo.nd(); ++d) {
+            apply_space_axis(geo, d, cur, bufs[which], n, F + d * BMND_MAX_EDGE * BMND_MAX_EDGE, square);
             cur = bufs[which];
             which ^= 1;
         }
@@ -247,82 +347,113 @@ __device__ __forceinline__ bool ht_keep(float mag, float thr, double scale) {
     return cc > tc + tol;
 }
 
-// accumulate c[q] += fl(G[i0 + q, g] * S[j, p]) over the entries [e0, e1) of one
-// voxel; an entry packs member g (low byte) and patch element p (upper bits)
-template <int NQ>
-__device__ __forceinline__ void voxel_contrib(const uint32_t* __restrict__ lent, int e0, int e1,
-                                              const float* __restrict__ GT, int kpad, int i0,
-                                              const float* __restrict__ stj, int P, float* c) {
-    for (int e = e0; e < e1; ++e) {
-        const uint32_t ent = lent[e];
-        const float sv = __ldg(stj + (ent >> 8) * P);
-        const float* gt = GT + (ent & 0xffu) * kpad + i0;
-        if (NQ == 4) {
-            const float4 gv = *reinterpret_cast<const float4*>(gt);
-            c[0] = add_rn(c[0], mul_rn(gv.x, sv));
-            c[1] = add_rn(c[1], mul_rn(gv.y, sv));
-            c[2] = add_rn(c[2], mul_rn(gv.z, sv));
-            c[3] = add_rn(c[3], mul_rn(gv.w, sv));
-        } else if (NQ == 2) {
-            const float2 gv = *reinterpret_cast<const float2*>(gt);
-            c[0] = add_rn(c[0], mul_rn(gv.x, sv));
-            c[1] = add_rn(c[1], mul_rn(gv.y, sv));
-        } else {
-            c[0] = add_rn(c[0], mul_rn(gt[0], sv));
+// Exact overlap-aware variance of the first kk group planes (variance.py:950-975):
+//   var[i, j] = sum_v V_v (sum_{e in v} fl(G[i, g_e] * S[j, p_e]))^2
+// over the union voxels v, with every float32 operation rounded on its own and
+// each voxel's entries summed in ascending member order.  S[j, p] is read from
+// the precomputed S^T, whose entries are the reference's float32 Kronecker
+// products.
+//
+// Work split: warp w takes the voxels whose entry lists start in its 1/nw share
+// of all entries, and accumulates every (plane, coefficient) pair over them;
+// lane l holds the coefficients j = j0 + l + 32 r (r < JR) of four planes, so
+// one entry (two broadcast shared loads) feeds 8 * JR float32 operations.  The
+// warps' partial sums are then added in warp order, which fixes the result
+// independently of scheduling.  An entry packs member g (low byte) and the row
+// offset p * P of S^T (upper bits).
+template <int JR>
+__device__ void exact_tile(const float* __restrict__ lval, const int* __restrict__ lstart,
+                           const uint32_t* __restrict__ lent, int u_lo, int u_hi,
+                           const float* __restrict__ GT, int kpad, int iq,
+                           const float* __restrict__ st, int P, int j0, float (&var)[JR][4]) {
+    const int lane = threadIdx.x & 31;
+    int jc[JR];
+#pragma unroll
+    for (int r = 0; r < JR; ++r) {
+        const int j = j0 + lane + 32 * r;
+        jc[r] = j < P ? j : P - 1;  // idle lanes read a valid column
+#pragma unroll
+        for (int q = 0; q < 4; ++q) var[r][q] = 0.0f;
+    }
+    const float* gt0 = GT + 4 * iq;
+    for (int u = u_lo; u < u_hi; ++u) {
+        float c[JR][4];
+#pragma unroll
+        for (int r = 0; r < JR; ++r)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) c[r][q] = 0.0f;
+        const int e1 = lstart[u + 1];
+        for (int e = lstart[u]; e < e1; ++e) {
+            const uint32_t ent = lent[e];
+            const float4 gv = *reinterpret_cast<const float4*>(gt0 + (ent & 0xffu) * kpad);
+            const float* srow = st + (ent >> 8);
+#pragma unroll
+            for (int r = 0; r < JR; ++r) {
+                const float sv = __ldg(srow + jc[r]);
+                c[r][0] = add_rn(c[r][0], mul_rn(gv.x, sv));
+                c[r][1] = add_rn(c[r][1], mul_rn(gv.y, sv));
+                c[r][2] = add_rn(c[r][2], mul_rn(gv.z, sv));
+                c[r][3] = add_rn(c[r][3], mul_rn(gv.w, sv));
+            }
         }
+        const float v = lval[u];
+#pragma unroll
+        for (int r = 0; r < JR; ++r)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) var[r][q] = add_rn(var[r][q], mul_rn(mul_rn(v, c[r][q]), c[r][q]));
     }
 }
 
-// exact overlap-aware variance of planes [i0, i0 + NQ) for spatial coefficient j:
-// var[i, j] = sum_v V_v (sum_{e in v} fl(G[i, g_e] * S[j, p_e]))^2, voxels in
-// ascending union order, entries in ascending member order, every operation
-// rounded on its own (the reference's float32 loop, variance.py:950-975).
-// S[j, p] comes from the precomputed S^T, whose entries are the reference's
-// float32 Kronecker products.  Two voxels are expanded at a time (independent
-// chains); their squares are still added to var in voxel order.
-template <int NQ>
+// all tiles of (4 planes) x (32 * JR coefficients); EX[i * P + j] receives the
+// standard deviation sqrt(max(var, 0)) of planes i < kk
+template <int JR>
 __device__ void exact_planes(const float* __restrict__ lval, const int* __restrict__ lstart,
                              const uint32_t* __restrict__ lent, int U, const float* __restrict__ GT,
-                             int kpad, const float* __restrict__ st, int P, int j, int i0, int nq,
+                             int kpad, int kk, const float* __restrict__ st, int P,
                              float* __restrict__ EX) {
-    const float* stj = st + j;
-    float var[NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) var[q] = 0.0f;
-    int u = 0;
-    for (; u + 1 < U; u += 2) {
-        float ca[NQ], cb[NQ];
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-            ca[q] = 0.0f;
-            cb[q] = 0.0f;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nw = blockDim.x >> 5;
+    // voxel range of this warp: voxels whose first entry lies in its entry share
+    const int E = lstart[U];
+    auto first_voxel = [&](int e) {
+        int lo = 0, hi = U;  // first u in [0, U] with lstart[u] >= e
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (lstart[mid] < e) lo = mid + 1;
+            else hi = mid;
         }
-        const int a0 = lstart[u], a1 = lstart[u + 1], b1 = lstart[u + 2];
-        voxel_contrib<NQ>(lent, a0, a1, GT, kpad, i0, stj, P, ca);
-        voxel_contrib<NQ>(lent, a1, b1, GT, kpad, i0, stj, P, cb);
-        const float va = lval[u], vb = lval[u + 1];
+        return lo;
+    };
+    const int u_lo = first_voxel(static_cast<int>(static_cast<int64_t>(E) * warp / nw));
+    const int u_hi = warp == nw - 1 ? U : first_voxel(static_cast<int>(static_cast<int64_t>(E) * (warp + 1) / nw));
+    for (int iq = 0; 4 * iq < kk; ++iq) {
+        for (int j0 = 0; j0 < P; j0 += 32 * JR) {
+            float var[JR][4];
+            exact_tile<JR>(lval, lstart, lent, u_lo, u_hi, GT, kpad, iq, st, P, j0, var);
+            for (int w = 0; w < nw; ++w) {
+                if (warp == w) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-            var[q] = add_rn(var[q], mul_rn(mul_rn(va, ca[q]), ca[q]));
-            var[q] = add_rn(var[q], mul_rn(mul_rn(vb, cb[q]), cb[q]));
+                    for (int r = 0; r < JR; ++r) {
+                        const int j = j0 + lane + 32 * r;
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const int i = 4 * iq + q;
+                            if (j < P && i < kk) {
+                                float t = w == 0 ? var[r][q] : add_rn(EX[i * P + j], var[r][q]);
+                                if (w == nw - 1) t = sqrtf(t > 0.0f ? t : 0.0f);
+                                EX[i * P + j] = t;
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+            }
         }
     }
-    if (u < U) {
-        float ca[NQ];
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) ca[q] = 0.0f;
-        voxel_contrib<NQ>(lent, lstart[u], lstart[u + 1], GT, kpad, i0, stj, P, ca);
-        const float va = lval[u];
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) var[q] = add_rn(var[q], mul_rn(mul_rn(va, ca[q]), ca[q]));
-    }
-#pragma unroll
-    for (int q = 0; q < NQ; ++q)
-        if (q < nq) EX[(i0 + q) * P + j] = sqrtf(var[q] > 0.0f ? var[q] : 0.0f);
 }
 
 template <int ND, int B0, int B1, int B2>
-__global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) group_filter_kernel(FilterArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     using GM = Geom<ND, B0, B1, B2>;
     const BmndStageParams& sp = a.sp;
@@ -369,7 +500,15 @@ __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
             rem /= a.counts[d];
         }
     }
-    for (int e = tid; e < n * n; e += blockDim.x) G[e] = group_entry(sp.group_transform, n, e / n, e % n);
+    float* Ginv = sm<float>(smem, a.L.ginv);
+    float* Gsq = sm<float>(smem, a.L.gsq);
+    for (int e = tid; e < n * n; e += blockDim.x) {
+        const int i = e / n, k = e % n;
+        const float gv = group_entry(sp.group_transform, n, i, k);
+        G[e] = gv;
+        Ginv[k * n + i] = gv;  // inverse = transpose (transforms.py:423, :436)
+        Gsq[e] = mul_rn(gv, gv);
+    }
     for (int e = tid; e < BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE; e += blockDim.x) {
         Fw[e] = sp.spatial_fwd[e / (BMND_MAX_EDGE * BMND_MAX_EDGE)][e % (BMND_MAX_EDGE * BMND_MAX_EDGE)];
         Fi[e] = sp.spatial_inv[e / (BMND_MAX_EDGE * BMND_MAX_EDGE)][e % (BMND_MAX_EDGE * BMND_MAX_EDGE)];
@@ -415,7 +554,7 @@ __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
                                scale_f, floor_f);
         }
         __syncthreads();
-        transform_group(geo, a, smem, n, V, V, T, 2);
+        transform_group<ND, B0, B1, B2>(geo, a, smem, n, V, V, T, 2);
         for (int e = tid; e < total; e += blockDim.x) {
             float v = V[e];
             S[e] = sqrtf(v > 0.0f ? v : 0.0f);
@@ -508,30 +647,20 @@ __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
 #pragma unroll
                 for (int d = 0; d < BMND_MAX_DIMS; ++d)
                     if (d < geo.nd()) pe = pe * geo.b(d) + (coords[d] - shf[g * BMND_MAX_DIMS + d]);
-                lent[we++] = static_cast<uint32_t>(g) | (static_cast<uint32_t>(pe) << 8);
+                lent[we++] = static_cast<uint32_t>(g) | (static_cast<uint32_t>(pe * P) << 8);
             }
             ++w;
         }
         const int U = scan[blockDim.x].x;
         if (tid == 0) lstart[U] = scan[blockDim.x].y;
         __syncthreads();
-        // work items: (spatial coefficient j, chunk of up to 4 planes)
-        // planes per item: as many as keep ~90% of the threads busy
-        int ppi = 4;
-        while (ppi > 1 && 10 * P * ((kk + ppi - 1) / ppi) < 9 * static_cast<int>(blockDim.x)) ppi >>= 1;
-        const int chunks = (kk + ppi - 1) / ppi;
-        for (int item = tid; item < P * chunks; item += blockDim.x) {
-            const int j = item % P;
-            const int i0 = (item / P) * ppi;
-            const int nq = min(ppi, kk - i0);
-            if (ppi == 4)
-                exact_planes<4>(lval, lstart, lent, U, GT, kpad, a.st, P, j, i0, nq, EX);
-            else if (ppi == 2)
-                exact_planes<2>(lval, lstart, lent, U, GT, kpad, a.st, P, j, i0, nq, EX);
-            else
-                exact_planes<1>(lval, lstart, lent, U, GT, kpad, a.st, P, j, i0, nq, EX);
+        if constexpr (ND > 0) {
+            constexpr int PC = B0 * B1 * B2;
+            constexpr int JR = PC <= 32 ? 1 : (PC <= 64 ? 2 : (PC <= 96 ? 3 : 4));
+            exact_planes<JR>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
+        } else {
+            exact_planes<4>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
         }
-        __syncthreads();
     }
 
     // ---- final sigma in S (plane limiting, variance.py:1572-1631) ----
@@ -580,8 +709,8 @@ __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
         if (wiener) R[e] = __ldg(a.pilot + off);
     }
     __syncthreads();
-    transform_group(geo, a, smem, n, X, X, T, 0);
-    if (wiener) transform_group(geo, a, smem, n, R, R, T, 0);
+    transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, X, T, 0);
+    if (wiener) transform_group<ND, B0, B1, B2>(geo, a, smem, n, R, R, T, 0);
 
     // ---- shrinkage: coefficients in X, attenuation in V, noise variance in S ----
     const float eps_f = static_cast<float>(sp.eps);
@@ -636,7 +765,7 @@ __global__ void __launch_bounds__(kThreads) group_filter_kernel(FilterArgs a) {
     __syncthreads();
 
     // ---- inverse transform and scatter ----
-    transform_group(geo, a, smem, n, X, X, T, 1);
+    transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, X, T, 1);
     for (int e = tid; e < total; e += blockDim.x) {
         const int g = e / P;
         const int p = e - g * P;
