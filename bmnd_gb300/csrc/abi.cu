@@ -99,7 +99,7 @@ struct StageWorkspace {
     int32_t* sel;
     int32_t* count;
     int32_t* accepted;
-    float* st;  // P x P Kronecker table of the patch transforms
+    float* st;  // P x kron_stride(P) Kronecker table of the patch transforms
     uint64_t bytes;
 };
 
@@ -120,7 +120,7 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
     uint64_t o_cnt = take(4ull * n_refs);
     uint64_t o_acc = take(4ull * n_refs);
     const uint64_t P = static_cast<uint64_t>(patch_volume(sp));
-    uint64_t o_st = take(4ull * P * P);
+    uint64_t o_st = take(4ull * P * static_cast<uint64_t>(kron_stride(static_cast<int>(P))));
     w.bytes = off;
     if (base) {
         char* b = static_cast<char*>(base);

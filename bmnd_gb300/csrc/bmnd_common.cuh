@@ -151,6 +151,15 @@ inline int patch_volume(const BmndStageParams& p) {
     return n;
 }
 
+// Layout of the Kronecker table S^T used by the exact variance: lane l of a
+// warp owns the KRON_JR(P) consecutive coefficients j = j0 + KRON_JR * l + r,
+// so each table row is padded with zeros to a multiple of 32 * KRON_JR floats
+// and one vector load per lane fetches all of them.
+__host__ __device__ constexpr int kron_jr(int P) { return P <= 32 ? 1 : (P <= 64 ? 2 : 4); }
+__host__ __device__ constexpr int kron_stride(int P) {
+    return (P + 32 * kron_jr(P) - 1) / (32 * kron_jr(P)) * (32 * kron_jr(P));
+}
+
 // launch helpers implemented in the .cu files
 int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume, const int32_t* shape,
                                  const int32_t* block, const int32_t* refs, int64_t n_refs,

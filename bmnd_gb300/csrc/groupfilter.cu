@@ -43,7 +43,7 @@ constexpr int kThreads = 256;
 // phases are ordered so that none of X/R/T/V is live while the lists are.
 struct Layout {
     // byte offsets into dynamic shared memory
-    int64_t g, ginv, gsq, gt, fw, fi, win, mdiag, pos, shf, s, ex, uni, x, r, t, v, grid, lval, lstart, lent,
+    int64_t g, ginv, gsq, gt, fw, fi, win, mdiag, pos, shf, shl, s, ex, uni, x, r, t, v, grid, lval, lstart, lent,
         scan, plane, wts, misc, total;
 };
 
@@ -62,7 +62,7 @@ struct FilterArgs {
     int64_t n_refs;
     double* num;
     double* den;
-    const float* st;  // S^T: st[p * P + j] = S[j, p], the Kronecker product of the patch transforms
+    const float* st;  // S^T: st[p * kron_stride(P) + j] = S[j, p], the Kronecker product of the patch transforms
 };
 
 __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax, int64_t ucells) {
@@ -87,6 +87,7 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     L.mdiag = take(8 * P);
     L.pos = take(4 * nmax * BMND_MAX_DIMS);
     L.shf = take(4 * nmax * BMND_MAX_DIMS);
+    L.shl = take(4 * nmax);
     L.s = take(4 * np);
     L.ex = take(4 * static_cast<int64_t>(kmax) * P);
     L.scan = take(8 * (kThreads + 1));
@@ -338,7 +339,16 @@ __device__ __forceinline__ float variance_of(float x, float scale_f, float floor
     return v > floor_f ? v : floor_f;
 }
 
-__device__ __forceinline__ bool ht_keep(float mag, float thr, double scale) {
+// Tolerance-aware hard-threshold mask of the Poisson path (bmndalgo.py:460-485,
+// poisson.py:30-46): in count units cc = mag / scale and tc = thr / scale, a
+// coefficient is kept iff cc > tc + 128 eps32 max(cc, tc, 1), evaluated in
+// float64.  Multiplying through by scale, the real-arithmetic boundary is
+// A = thr + 2^-16 max(mag, thr, scale).  Its float32 estimate a is within
+// 2^-23 A of it, and the float64 evaluation within ~2^-50 A, so whenever mag
+// lies outside a * (1 -+ 2^-20) the float32 comparison gives the float64
+// decision; only the band around the boundary (and non-finite inputs) takes the
+// float64 path.
+__device__ __forceinline__ bool ht_keep_f64(float mag, float thr, double scale) {
     double cc = static_cast<double>(mag) / scale;
     double tc = static_cast<double>(thr) / scale;
     double cs = cc > tc ? cc : tc;
@@ -347,34 +357,71 @@ __device__ __forceinline__ bool ht_keep(float mag, float thr, double scale) {
     return cc > tc + tol;
 }
 
+__device__ __forceinline__ bool ht_keep(float mag, float thr, double scale, float scale_f) {
+    const float cs = fmaxf(fmaxf(mag, thr), scale_f);
+    if (cs >= 1e-30f && cs <= 1e30f) {
+        const float a = add_rn(thr, mul_rn(1.52587890625e-05f, cs));  // 2^-16
+        if (mag > mul_rn(a, 1.00000095367431640625f)) return true;   // 1 + 2^-20
+        if (mag < mul_rn(a, 0.99999904632568359375f)) return false;  // 1 - 2^-20
+    }
+    return ht_keep_f64(mag, thr, scale);
+}
+
 // Exact overlap-aware variance of the first kk group planes (variance.py:950-975):
-//   var[i, j] = sum_v V_v (sum_{e in v} fl(G[i, g_e] * S[j, p_e]))^2
-// over the union voxels v, with every float32 operation rounded on its own and
-// each voxel's entries summed in ascending member order.  S[j, p] is read from
-// the precomputed S^T, whose entries are the reference's float32 Kronecker
-// products.
+//   var[i, j] = sum_v V_v c_v[i, j]^2,   c_v[i, j] = sum_{e in v} G[i, g_e] S[j, p_e]
+// over the union voxels v, each voxel's entries taken in ascending member order.
+// S[j, p] is read from the precomputed S^T, whose entries are the reference's
+// float32 Kronecker products.  c is accumulated with fused multiply-adds (one
+// rounding per entry instead of the reference's two); V c^2 and the sum over
+// voxels keep one rounding per operation.
 //
 // Work split: warp w takes the voxels whose entry lists start in its 1/nw share
 // of all entries, and accumulates every (plane, coefficient) pair over them;
-// lane l holds the coefficients j = j0 + l + 32 r (r < JR) of four planes, so
-// one entry (two broadcast shared loads) feeds 8 * JR float32 operations.  The
-// warps' partial sums are then added in warp order, which fixes the result
+// lane l holds four planes of the JR consecutive coefficients j0 + JR * l + r,
+// so one entry costs three loads (the entry and the four G values, both warp
+// broadcasts, and one JR-wide vector of S^T) for 4 * JR fused multiply-adds.
+// The warps' partial sums are then added in warp order, which fixes the result
 // independently of scheduling.  An entry packs member g (low byte) and the row
-// offset p * P of S^T (upper bits).
+// offset p * kron_stride(P) of S^T (upper bits).
+template <int JR>
+struct KronVec;
+template <>
+struct KronVec<1> {
+    float v[1];
+    __device__ __forceinline__ void load(const float* p) { v[0] = __ldg(p); }
+};
+template <>
+struct KronVec<2> {
+    float v[2];
+    __device__ __forceinline__ void load(const float* p) {
+        const float2 t = __ldg(reinterpret_cast<const float2*>(p));
+        v[0] = t.x;
+        v[1] = t.y;
+    }
+};
+template <>
+struct KronVec<4> {
+    float v[4];
+    __device__ __forceinline__ void load(const float* p) {
+        const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+        v[0] = t.x;
+        v[1] = t.y;
+        v[2] = t.z;
+        v[3] = t.w;
+    }
+};
+
 template <int JR>
 __device__ void exact_tile(const float* __restrict__ lval, const int* __restrict__ lstart,
                            const uint32_t* __restrict__ lent, int u_lo, int u_hi,
                            const float* __restrict__ GT, int kpad, int iq,
-                           const float* __restrict__ st, int P, int j0, float (&var)[JR][4]) {
+                           const float* __restrict__ st, int j0, float (&var)[JR][4]) {
     const int lane = threadIdx.x & 31;
-    int jc[JR];
+    const float* stl = st + j0 + JR * lane;
 #pragma unroll
-    for (int r = 0; r < JR; ++r) {
-        const int j = j0 + lane + 32 * r;
-        jc[r] = j < P ? j : P - 1;  // idle lanes read a valid column
+    for (int r = 0; r < JR; ++r)
 #pragma unroll
         for (int q = 0; q < 4; ++q) var[r][q] = 0.0f;
-    }
     const float* gt0 = GT + 4 * iq;
     for (int u = u_lo; u < u_hi; ++u) {
         float c[JR][4];
@@ -383,17 +430,18 @@ __device__ void exact_tile(const float* __restrict__ lval, const int* __restrict
 #pragma unroll
             for (int q = 0; q < 4; ++q) c[r][q] = 0.0f;
         const int e1 = lstart[u + 1];
+#pragma unroll 2
         for (int e = lstart[u]; e < e1; ++e) {
             const uint32_t ent = lent[e];
             const float4 gv = *reinterpret_cast<const float4*>(gt0 + (ent & 0xffu) * kpad);
-            const float* srow = st + (ent >> 8);
+            KronVec<JR> sv;
+            sv.load(stl + (ent >> 8));
 #pragma unroll
             for (int r = 0; r < JR; ++r) {
-                const float sv = __ldg(srow + jc[r]);
-                c[r][0] = add_rn(c[r][0], mul_rn(gv.x, sv));
-                c[r][1] = add_rn(c[r][1], mul_rn(gv.y, sv));
-                c[r][2] = add_rn(c[r][2], mul_rn(gv.z, sv));
-                c[r][3] = add_rn(c[r][3], mul_rn(gv.w, sv));
+                c[r][0] = fmaf(gv.x, sv.v[r], c[r][0]);
+                c[r][1] = fmaf(gv.y, sv.v[r], c[r][1]);
+                c[r][2] = fmaf(gv.z, sv.v[r], c[r][2]);
+                c[r][3] = fmaf(gv.w, sv.v[r], c[r][3]);
             }
         }
         const float v = lval[u];
@@ -429,12 +477,12 @@ __device__ void exact_planes(const float* __restrict__ lval, const int* __restri
     for (int iq = 0; 4 * iq < kk; ++iq) {
         for (int j0 = 0; j0 < P; j0 += 32 * JR) {
             float var[JR][4];
-            exact_tile<JR>(lval, lstart, lent, u_lo, u_hi, GT, kpad, iq, st, P, j0, var);
+            exact_tile<JR>(lval, lstart, lent, u_lo, u_hi, GT, kpad, iq, st, j0, var);
             for (int w = 0; w < nw; ++w) {
                 if (warp == w) {
 #pragma unroll
                     for (int r = 0; r < JR; ++r) {
-                        const int j = j0 + lane + 32 * r;
+                        const int j = j0 + JR * lane + r;
 #pragma unroll
                         for (int q = 0; q < 4; ++q) {
                             const int i = 4 * iq + q;
@@ -539,6 +587,13 @@ __global__ void __launch_bounds__(kThreads, 2) group_filter_kernel(FilterArgs a)
         }
     }
     __syncthreads();
+    // patch-linear offset of each member's shift: element p of member g lies in
+    // union cell coords c with p = lin(c) - shl[g], lin(c) = sum_d c_d inner(d)
+    if (tid < n) {
+        int o = 0;
+        for (int d = 0; d < geo.nd(); ++d) o += shf[tid * BMND_MAX_DIMS + d] * geo.inner(d);
+        sm<int>(smem, a.L.shl)[tid] = o;
+    }
 
     const float scale_f = static_cast<float>(sp.count_scale);
     const float floor_f = static_cast<float>(sp.variance_floor);
@@ -621,45 +676,72 @@ __global__ void __launch_bounds__(kThreads, 2) group_filter_kernel(FilterArgs a)
             if (tid == 0) scan[blockDim.x] = make_int2(carry_v, carry_e);
         }
         __syncthreads();
-        int w = scan[tid].x, we = scan[tid].y;
-        for (int c = c0; c < c1; ++c) {
-            uint32_t m = grid[c];
-            if (!m) continue;
-            int rem = c;
-            int coords[BMND_MAX_DIMS] = {0, 0, 0};
+        // compaction: this thread's cells c0..c1 in order, the cell index parked
+        // in lval until the variance pass below
+        {
+            const int* shl = sm<int>(smem, a.L.shl);
+            const int kstride = kron_stride(P);
+            int w = scan[tid].x, we = scan[tid].y;
+            int cc[BMND_MAX_DIMS] = {0, 0, 0};
+            {
+                int rem = c0;
 #pragma unroll
-            for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
-                if (d < geo.nd()) {
-                    coords[d] = rem % ush[d];
-                    rem /= ush[d];
+                for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                    if (d < geo.nd()) {
+                        cc[d] = rem % ush[d];
+                        rem /= ush[d];
+                    }
                 }
             }
-            int64_t vox = 0;
+            for (int c = c0; c < c1; ++c) {
+                uint32_t m = grid[c];
+                if (m) {
+                    int lin = 0;
 #pragma unroll
-            for (int d = 0; d < BMND_MAX_DIMS; ++d)
-                if (d < geo.nd()) vox += static_cast<int64_t>(coords[d] + org[d]) * a.vstride[d];
-            lval[w] = variance_of(__ldg(varsrc + vox), scale_f, floor_f);
-            lstart[w] = we;
-            while (m) {
-                const int g = __ffs(m) - 1;
-                m &= m - 1;
-                int pe = 0;
+                    for (int d = 0; d < BMND_MAX_DIMS; ++d)
+                        if (d < geo.nd()) lin += cc[d] * geo.inner(d);
+                    reinterpret_cast<int*>(lval)[w] = c;
+                    lstart[w] = we;
+                    while (m) {
+                        const int g = __ffs(m) - 1;
+                        m &= m - 1;
+                        lent[we++] = static_cast<uint32_t>(g) | (static_cast<uint32_t>((lin - shl[g]) * kstride) << 8);
+                    }
+                    ++w;
+                }
 #pragma unroll
-                for (int d = 0; d < BMND_MAX_DIMS; ++d)
-                    if (d < geo.nd()) pe = pe * geo.b(d) + (coords[d] - shf[g * BMND_MAX_DIMS + d]);
-                lent[we++] = static_cast<uint32_t>(g) | (static_cast<uint32_t>(pe * P) << 8);
+                for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                    if (d < geo.nd()) {
+                        if (++cc[d] < ush[d]) break;
+                        cc[d] = 0;
+                    }
+                }
             }
-            ++w;
         }
         const int U = scan[blockDim.x].x;
         if (tid == 0) lstart[U] = scan[blockDim.x].y;
         __syncthreads();
+        // variance of every union voxel, all loads in flight together
+        for (int u = tid; u < U; u += blockDim.x) {
+            int rem = reinterpret_cast<const int*>(lval)[u];
+            int64_t vox = 0;
+#pragma unroll
+            for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                if (d < geo.nd()) {
+                    vox += static_cast<int64_t>(rem % ush[d] + org[d]) * a.vstride[d];
+                    rem /= ush[d];
+                }
+            }
+            lval[u] = variance_of(__ldg(varsrc + vox), scale_f, floor_f);
+        }
+        __syncthreads();
         if constexpr (ND > 0) {
-            constexpr int PC = B0 * B1 * B2;
-            constexpr int JR = PC <= 32 ? 1 : (PC <= 64 ? 2 : (PC <= 96 ? 3 : 4));
-            exact_planes<JR>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
+            exact_planes<kron_jr(B0 * B1 * B2)>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
         } else {
-            exact_planes<4>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
+            const int jr = kron_jr(P);
+            if (jr == 1) exact_planes<1>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
+            else if (jr == 2) exact_planes<2>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
+            else exact_planes<4>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
         }
     }
 
@@ -720,7 +802,7 @@ __global__ void __launch_bounds__(kThreads, 2) group_filter_kernel(FilterArgs a)
         float att;
         if (!wiener) {
             float thr = mul_rn(sp.ht_lambda, sig);
-            att = ht_keep(fabsf(X[e]), thr, sp.count_scale) ? 1.0f : 0.0f;
+            att = ht_keep(fabsf(X[e]), thr, sp.count_scale, scale_f) ? 1.0f : 0.0f;
         } else {
             float eff = mul_rn(sp.wiener_scale, nv);
             float pr = fabsf(R[e]);
@@ -776,12 +858,16 @@ __global__ void __launch_bounds__(kThreads, 2) group_filter_kernel(FilterArgs a)
     }
 }
 
-// S^T[p * P + j] = S[j, p] with S = kron(F_0, ..., F_{nd-1}) built axis by axis in
-// float32 (fl(fl(F0 * F1) * F2)), as the reference builds its spatial matrix
-// (variance.py:744-755)
-__global__ void spatial_kron_kernel(BmndStageParams sp, int P, float* st) {
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < P * P; idx += gridDim.x * blockDim.x) {
-        const int p = idx / P, j = idx % P;
+// S^T[p * stride + j] = S[j, p] with S = kron(F_0, ..., F_{nd-1}) built axis by
+// axis in float32 (fl(fl(F0 * F1) * F2)), as the reference builds its spatial
+// matrix (variance.py:744-755); columns j >= P of the padded rows are zero
+__global__ void spatial_kron_kernel(BmndStageParams sp, int P, int stride, float* st) {
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < P * stride; idx += gridDim.x * blockDim.x) {
+        const int p = idx / stride, j = idx % stride;
+        if (j >= P) {
+            st[idx] = 0.0f;
+            continue;
+        }
         int jd[BMND_MAX_DIMS], pd[BMND_MAX_DIMS];
         int rj = j, rp = p;
         for (int d = sp.ndim - 1; d >= 0; --d) {
@@ -832,7 +918,8 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
     if (n_refs == 0) return BMND_OK;
     {
         const int P = patch_volume(sp);
-        spatial_kron_kernel<<<(P * P + 255) / 256, 256, 0, stream>>>(sp, P, st);
+        const int stride = kron_stride(P);
+        spatial_kron_kernel<<<(P * stride + 255) / 256, 256, 0, stream>>>(sp, P, stride, st);
         BMND_LAUNCH_CHECK("spatial_kron_kernel");
     }
     FilterArgs a{};
