@@ -736,6 +736,345 @@ __global__ void __launch_bounds__(kSThreads) blockmatch_screened_kernel(MatchArg
     }
 }
 
+// ---------------------------------------------------------------------------
+// Integer-count Poisson-deviance matching (volume source, count scale 1)
+//
+// One CTA per reference.  For Poisson counts almost every term of the deviance
+// pairs two small integers, so the CTA tabulates, per reference,
+//   trow[p][c] = deviance_term(r_p, c),  c = 0..62,
+// (one row per patch element; rows of integer r_p < 63 are copied from a
+// 64 x 64 table of the same function, others are evaluated directly) and
+// stages the search box of the reference as byte codes 4 * c (c = the clamped
+// count if it is an integer below 63, else 63, whose table entry is NaN).  A
+// term is then one byte load, one table load and one float32 add, in the
+// reference's patch order, so the sum is bit-identical to the per-term
+// evaluation; a candidate whose sum came out NaN (it touched a code-63 voxel)
+// is recomputed term by term from the float source.  Selection keeps one
+// ascending top-K list per thread (accepted and rejected, as the warp kernel
+// does), merged per warp and then across the CTA's warps.
+// ---------------------------------------------------------------------------
+constexpr int kCThreads = 128;
+constexpr int kCWarps = kCThreads / 32;
+constexpr int kCodes = 64;      // row length of trow; code 63 marks "not tabulated"
+constexpr int kCodeMax = 63;    // counts 0..62 are tabulated
+
+__device__ float g_count_table[kCodes * kCodes];  // deviance_term(r, c), r, c < 64
+
+__global__ void count_table_kernel() {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kCodes * kCodes; i += gridDim.x * blockDim.x)
+        g_count_table[i] = deviance_term(static_cast<float>(i / kCodes), static_cast<float>(i % kCodes));
+}
+
+// Shared layout of the count kernel; every section starts on a 16-byte
+// boundary.  trow comes first: its byte offset is a compile-time 0, so a
+// term's table load addresses [code + p * 256].
+struct CountSmem {
+    size_t trow, box, poff, ref, lists, wmerged, fin, total;
+    __host__ __device__ CountSmem(int P, int64_t boxmax, int rows) {
+        auto r16 = [](size_t v) { return (v + 15) & ~size_t(15); };
+        size_t o = 0;
+        trow = o;
+        o += r16(static_cast<size_t>(P) * kCodes * 4);               // per-reference table
+        box = o;
+        o += r16(static_cast<size_t>(boxmax));                       // box codes
+        poff = o;
+        o += r16(static_cast<size_t>(P) * 4);                        // voxel offsets of the patch
+        ref = o;
+        o += r16(static_cast<size_t>(P) * 8);                        // reference values, row index
+        lists = o;
+        o += r16(static_cast<size_t>(rows) * kCThreads * 8);         // per-thread lists
+        wmerged = o;
+        o += r16(static_cast<size_t>(kCWarps) * rows * 8);           // per-warp merged lists
+        fin = o;
+        o += 64 * 8;                                                 // final lists (48), reductions (16 ints)
+        total = o;
+    }
+};
+
+// ascending list of `size` entries (capacity `cap`) at list[i * stride]
+__device__ __forceinline__ int list_insert_s(uint64_t* list, int stride, int size, int cap, uint64_t key) {
+    if (cap == 0) return size;
+    int at;
+    if (size < cap) {
+        at = size;
+        ++size;
+    } else {
+        if (key >= list[(cap - 1) * stride]) return size;
+        at = cap - 1;
+    }
+    while (at > 0) {
+        const uint64_t prev = list[(at - 1) * stride];
+        if (key >= prev) break;
+        list[at * stride] = prev;
+        --at;
+    }
+    list[at * stride] = key;
+    return size;
+}
+
+// warp-wide merge of one ascending list per lane (mine[i * stride], `size`
+// entries) into out[0..cap); returns the merged size
+__device__ int warp_merge_s(const uint64_t* mine_list, int stride, int size, int cap, uint64_t* out, int lane) {
+    int head = 0, n = 0;
+    for (int t = 0; t < cap; ++t) {
+        const uint64_t mine = head < size ? mine_list[head * stride] : ~0ull;
+        const uint64_t best = warp_min_u64(mine);
+        if (best == ~0ull) break;
+        if (mine == best) ++head;
+        if (lane == 0) out[t] = best;
+        ++n;
+    }
+    return n;
+}
+
+template <int ND, int B0, int B1, int B2>
+__device__ __forceinline__ float counts_distance_fixed(const unsigned char* __restrict__ smem,
+                                                       const unsigned char* __restrict__ cand, int S0, int S1) {
+    float d = 0.0f;
+#pragma unroll
+    for (int a0 = 0; a0 < B0; ++a0) {
+#pragma unroll
+        for (int a1 = 0; a1 < B1; ++a1) {
+            const unsigned char* row = cand + a0 * S0 + (ND == 3 ? a1 * S1 : a1);
+#pragma unroll
+            for (int a2 = 0; a2 < B2; ++a2) {
+                constexpr int kRow = kCodes * 4;
+                const int p = (a0 * B1 + a1) * B2 + a2;
+                const unsigned code4 = row[ND == 3 ? a2 : 0];
+                d = add_rn(d, *reinterpret_cast<const float*>(smem + code4 + p * kRow));
+            }
+        }
+    }
+    return d;
+}
+
+template <int ND, int B0, int B1, int B2>
+__global__ void __launch_bounds__(kCThreads) blockmatch_counts_kernel(MatchArgs a, int32_t rows) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int P = a.P;
+    const int K = a.max_m;
+    const int R = a.required;
+    const int nd = a.ndim;
+    int64_t boxmax = 1;
+    for (int d = 0; d < nd; ++d) boxmax *= min(2 * a.radius[d] + 1, a.counts[d]) + a.block[d] - 1;
+    const CountSmem L(P, boxmax, rows);
+    float* trow = reinterpret_cast<float*>(smem + L.trow);
+    unsigned char* box = smem + L.box;
+    int32_t* poff_s = reinterpret_cast<int32_t*>(smem + L.poff);
+    float* refv = reinterpret_cast<float*>(smem + L.ref);
+    int* refi = reinterpret_cast<int*>(refv + P);
+    uint64_t* lists = reinterpret_cast<uint64_t*>(smem + L.lists);      // [rows][kCThreads]
+    uint64_t* wmerged = reinterpret_cast<uint64_t*>(smem + L.wmerged);  // [kCWarps][rows]
+    uint64_t* fin = reinterpret_cast<uint64_t*>(smem + L.fin);          // [K + R <= 48] final merged keys
+    int* redi = reinterpret_cast<int*>(fin + 48);                        // [16]
+
+    for (int i = tid; i < P; i += blockDim.x) {
+        int rem = i;
+        int64_t o = 0;
+        for (int d = nd - 1; d >= 0; --d) {
+            o += static_cast<int64_t>(rem % a.block[d]) * a.vstride[d];
+            rem /= a.block[d];
+        }
+        poff_s[i] = static_cast<int32_t>(o);
+    }
+    uint64_t* acc_list = lists + tid;
+    uint64_t* rej_list = lists + static_cast<size_t>(K) * kCThreads + tid;
+
+    for (int64_t r = blockIdx.x; r < a.n_refs; r += gridDim.x) {
+        int lo[BMND_MAX_DIMS] = {0, 0, 0}, ext[BMND_MAX_DIMS] = {1, 1, 1}, bx[BMND_MAX_DIMS] = {1, 1, 1};
+        int64_t center_lin = 0, center_origin = 0, window = 1, nbox = 1;
+        for (int d = 0; d < nd; ++d) {
+            const int cd = a.refs[r * nd + d];
+            center_lin = center_lin * a.counts[d] + cd;
+            center_origin += static_cast<int64_t>(cd) * a.vstride[d];
+            const int l = max(cd - a.radius[d], 0);
+            const int h = min(cd + a.radius[d], a.counts[d] - 1);
+            lo[d] = l;
+            ext[d] = h - l + 1;
+            bx[d] = ext[d] + a.block[d] - 1;
+            window *= ext[d];
+            nbox *= bx[d];
+        }
+        __syncthreads();  // the previous reference's shared data is no longer read
+        // reference values and their table rows
+        for (int p = tid; p < P; p += blockDim.x) {
+            float v = __ldg(a.src + center_origin + poff_s[p]);
+            if (v < 0.0f) v = 0.0f;
+            const int vi = __float2int_rz(v);
+            refv[p] = v;
+            refi[p] = (vi < kCodeMax && __int2float_rn(vi) == v) ? vi * kCodes : -1;
+        }
+        // search box as byte codes, one box row (last axis) per warp pass
+        {
+            const int inner = bx[nd - 1];
+            const int64_t nrows = nbox / inner;
+            for (int64_t row = warp; row < nrows; row += kCWarps) {
+                int64_t rem = row, vo = 0;
+                for (int d = nd - 2; d >= 0; --d) {
+                    vo += static_cast<int64_t>(lo[d] + static_cast<int>(rem % bx[d])) * a.vstride[d];
+                    rem /= bx[d];
+                }
+                vo += lo[nd - 1];
+                for (int x = lane; x < inner; x += 32) {
+                    float v = __ldg(a.src + vo + x);
+                    if (v < 0.0f) v = 0.0f;
+                    const int vi = __float2int_rz(v);
+                    const int code = (vi < kCodeMax && __int2float_rn(vi) == v) ? vi : kCodeMax;
+                    box[row * inner + x] = static_cast<unsigned char>(code * 4);
+                }
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < P * kCodes; e += blockDim.x) {
+            const int p = e / kCodes, c = e % kCodes;
+            const int ri = refi[p];
+            float t;
+            if (c == kCodeMax) t = __int_as_float(0x7fc00000);
+            else if (ri >= 0) t = g_count_table[ri + c];
+            else t = deviance_term(refv[p], static_cast<float>(c));
+            trow[e] = t;
+        }
+        __syncthreads();
+
+        const float thr = a.thresholds ? a.thresholds[r] : a.scalar_threshold;
+        const float tkey = canonical_key(thr);
+        int acc_size = 0, rej_size = 0, acc_count = 0;
+        const int S0 = nd == 3 ? bx[1] * bx[2] : bx[1];
+        const int S1 = nd == 3 ? bx[2] : 1;
+        for (int64_t c = tid; c < window; c += blockDim.x) {
+            int w[BMND_MAX_DIMS] = {0, 0, 0};
+            int64_t rem = c;
+            for (int d = nd - 1; d >= 0; --d) {
+                w[d] = static_cast<int>(rem % ext[d]);
+                rem /= ext[d];
+            }
+            int64_t lin = 0, boff = 0;
+            for (int d = 0; d < nd; ++d) {
+                lin = lin * a.counts[d] + lo[d] + w[d];
+                boff = boff * bx[d] + w[d];
+            }
+            float dsum;
+            if constexpr (ND > 0) {
+                dsum = counts_distance_fixed<ND, B0, B1, B2>(smem, box + boff, S0, S1);
+            } else {
+                dsum = 0.0f;
+                for (int p = 0; p < P; ++p) {
+                    int rp = p, bo = 0, mul = 1;
+                    for (int d = nd - 1; d >= 0; --d) {
+                        bo += (rp % a.block[d]) * mul;
+                        mul *= bx[d];
+                        rp /= a.block[d];
+                    }
+                    const unsigned code4 = box[boff + bo];
+                    dsum = add_rn(dsum, *reinterpret_cast<const float*>(smem + code4 + p * (kCodes * 4)));
+                }
+            }
+            if (dsum != dsum) {
+                // a voxel outside the table: term-by-term evaluation from the source
+                int64_t origin = 0;
+                for (int d = 0; d < nd; ++d) origin += static_cast<int64_t>(lo[d] + w[d]) * a.vstride[d];
+                dsum = 0.0f;
+                for (int p = 0; p < P; ++p) {
+                    float cv = __ldg(a.src + origin + poff_s[p]);
+                    if (cv < 0.0f) cv = 0.0f;
+                    const float rv = refv[p];
+                    if (add_rn(rv, cv) > 0.0f) dsum = add_rn(dsum, deviance_term(rv, cv));
+                }
+            }
+            if (dsum < 0.0f) dsum = 0.0f;
+            const float key = canonical_key(div_rn(dsum, static_cast<float>(P)));
+            const uint64_t ck = composite_key(key, static_cast<int32_t>(lin));
+            if (key < tkey) {
+                ++acc_count;
+                acc_size = list_insert_s(acc_list, kCThreads, acc_size, K, ck);
+            } else {
+                rej_size = list_insert_s(rej_list, kCThreads, rej_size, R, ck);
+            }
+        }
+        // per-warp merge, then across warps
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc_count += __shfl_xor_sync(0xffffffffu, acc_count, o);
+        uint64_t* wm = wmerged + static_cast<size_t>(warp) * rows;
+        const int n_acc_w = warp_merge_s(acc_list, kCThreads, acc_size, K, wm, lane);
+        const int n_rej_w = warp_merge_s(rej_list, kCThreads, rej_size, R, wm + K, lane);
+        if (lane == 0) {
+            redi[warp] = n_acc_w;
+            redi[kCWarps + warp] = n_rej_w;
+            redi[2 * kCWarps + warp] = acc_count;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            const bool mine = lane < kCWarps;
+            const uint64_t* ml = wmerged + static_cast<size_t>(mine ? lane : 0) * rows;
+            const int n_acc = warp_merge_s(ml, 1, mine ? redi[lane] : 0, K, fin, lane);
+            const int n_rej = warp_merge_s(ml + K, 1, mine ? redi[kCWarps + lane] : 0, R, fin + K, lane);
+            __syncwarp();
+            if (lane == 0) {
+                int total_accepted = 0;
+                for (int w2 = 0; w2 < kCWarps; ++w2) total_accepted += redi[2 * kCWarps + w2];
+                int32_t* row = a.sel + r * K;
+                int n = 0, take = 0;
+                if (n_acc < R) {
+                    const int need = R - n_acc;
+                    take = need < n_rej ? need : n_rej;
+                }
+                row[n++] = static_cast<int32_t>(center_lin);
+                for (int t = 0; t < n_acc + take && n < K; ++t) {
+                    const uint64_t ck = t < n_acc ? fin[t] : fin[K + (t - n_acc)];
+                    const int32_t l = static_cast<int32_t>(ck & 0xffffffffu);
+                    if (l < 0 || l == center_lin) continue;
+                    row[n++] = l;
+                }
+                if (a.pow2 && n > 0) {
+                    int target = 1;
+                    while ((target << 1) <= n) target <<= 1;
+                    if (a.min_m > target) target = a.min_m;
+                    if (target < n) n = target;
+                }
+                for (int t = n; t < K; ++t) row[t] = -1;
+                a.count[r] = n;
+                a.accepted[r] = total_accepted;
+            }
+        }
+    }
+}
+
+size_t counts_smem_bytes(const MatchArgs& a) {
+    int64_t boxmax = 1;
+    for (int d = 0; d < a.ndim; ++d)
+        boxmax *= std::min<int64_t>(2 * a.radius[d] + 1, a.counts[d]) + a.block[d] - 1;
+    return CountSmem(a.P, boxmax, a.max_m + a.required).total;
+}
+
+int32_t launch_counts(MatchArgs& a, cudaStream_t stream) {
+    count_table_kernel<<<(kCodes * kCodes + 255) / 256, 256, 0, stream>>>();
+    BMND_LAUNCH_CHECK("count_table_kernel");
+    const size_t smem = counts_smem_bytes(a);
+    const int32_t rows = a.max_m + a.required;
+    auto run = [&](auto kernel) -> int32_t {
+        BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(smem)));
+        int per_sm = 0;
+        BMND_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kCThreads, smem));
+        if (per_sm < 1) per_sm = 1;
+        int dev = 0, sms = 0;
+        BMND_CUDA_TRY(cudaGetDevice(&dev));
+        BMND_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        int64_t blocks = static_cast<int64_t>(sms) * per_sm;
+        if (blocks > a.n_refs) blocks = a.n_refs;
+        kernel<<<static_cast<unsigned>(blocks), kCThreads, smem, stream>>>(a, rows);
+        BMND_LAUNCH_CHECK("blockmatch_counts_kernel");
+        return BMND_OK;
+    };
+    const int* bl = a.block;
+    if (a.ndim == 2 && bl[0] == 8 && bl[1] == 8) return run(blockmatch_counts_kernel<2, 8, 8, 1>);
+    if (a.ndim == 3 && bl[0] == 4 && bl[1] == 4 && bl[2] == 4) return run(blockmatch_counts_kernel<3, 4, 4, 4>);
+    if (a.ndim == 3 && bl[0] == 5 && bl[1] == 5 && bl[2] == 5) return run(blockmatch_counts_kernel<3, 5, 5, 5>);
+    return run(blockmatch_counts_kernel<0, 1, 1, 1>);
+}
+
 size_t screened_smem_bytes(int K, int P, int64_t wmax) {
     (void)K;
     return ScreenSmem::bytes(P, wmax);
@@ -757,7 +1096,11 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     const bool screened = code == BMND_DIST_POISSON_DEVIANCE && a.stab &&
                           (precision == BMND_MATCH_FAST || precision == BMND_MATCH_REAL_VALUED) &&
                           a.max_m <= 32 && screened_smem_bytes(a.max_m, a.P, wmax) <= 200 * 1024;
-    if (!screened) return launch_exact(a, code, stream);
+    if (!screened) {
+        const bool counts = code == BMND_DIST_POISSON_DEVIANCE && a.use_table && !a.table && !a.fixup &&
+                            a.P <= 128 && a.max_m + a.required <= 48 && counts_smem_bytes(a) <= 96 * 1024;
+        return counts ? launch_counts(a, stream) : launch_exact(a, code, stream);
+    }
     size_t smem = screened_smem_bytes(a.max_m, a.P, wmax);
     int64_t blocks = a.n_refs;
     const int64_t cap = 152 * 12;

@@ -34,7 +34,8 @@
 namespace bmnd {
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;      // threads per group (CTA)
+constexpr int kThreadsWide = 512;  // largest CTA the kernel is written for (scan buffer)
 
 // Shared-memory plan.  The union region holds the group buffers X (noisy
 // coefficients), R (pilot coefficients, Wiener only), T (transform scratch)
@@ -90,7 +91,7 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     L.shl = take(4 * nmax);
     L.s = take(4 * np);
     L.ex = take(4 * static_cast<int64_t>(kmax) * P);
-    L.scan = take(8 * (kThreads + 1));
+    L.scan = take(8 * (kThreadsWide + 1));
     L.plane = take(8 * nmax);
     L.wts = take(4 * nmax);
     L.misc = take(64);
@@ -371,9 +372,8 @@ __device__ __forceinline__ bool ht_keep(float mag, float thr, double scale, floa
 //   var[i, j] = sum_v V_v c_v[i, j]^2,   c_v[i, j] = sum_{e in v} G[i, g_e] S[j, p_e]
 // over the union voxels v, each voxel's entries taken in ascending member order.
 // S[j, p] is read from the precomputed S^T, whose entries are the reference's
-// float32 Kronecker products.  c is accumulated with fused multiply-adds (one
-// rounding per entry instead of the reference's two); V c^2 and the sum over
-// voxels keep one rounding per operation.
+// float32 Kronecker products.  c and the sum over voxels are accumulated with
+// fused multiply-adds (one rounding per term instead of the reference's two).
 //
 // Work split: warp w takes the voxels whose entry lists start in its 1/nw share
 // of all entries, and accumulates every (plane, coefficient) pair over them;
@@ -424,14 +424,25 @@ __device__ void exact_tile(const float* __restrict__ lval, const int* __restrict
         for (int q = 0; q < 4; ++q) var[r][q] = 0.0f;
     const float* gt0 = GT + 4 * iq;
     for (int u = u_lo; u < u_hi; ++u) {
-        float c[JR][4];
-#pragma unroll
-        for (int r = 0; r < JR; ++r)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) c[r][q] = 0.0f;
+        int e = lstart[u];
         const int e1 = lstart[u + 1];
+        float c[JR][4];
+        {
+            // first entry: the product itself (every voxel has at least one)
+            const uint32_t ent = lent[e];
+            const float4 gv = *reinterpret_cast<const float4*>(gt0 + (ent & 0xffu) * kpad);
+            KronVec<JR> sv;
+            sv.load(stl + (ent >> 8));
+#pragma unroll
+            for (int r = 0; r < JR; ++r) {
+                c[r][0] = mul_rn(gv.x, sv.v[r]);
+                c[r][1] = mul_rn(gv.y, sv.v[r]);
+                c[r][2] = mul_rn(gv.z, sv.v[r]);
+                c[r][3] = mul_rn(gv.w, sv.v[r]);
+            }
+        }
 #pragma unroll 2
-        for (int e = lstart[u]; e < e1; ++e) {
+        for (++e; e < e1; ++e) {
             const uint32_t ent = lent[e];
             const float4 gv = *reinterpret_cast<const float4*>(gt0 + (ent & 0xffu) * kpad);
             KronVec<JR> sv;
@@ -448,7 +459,7 @@ __device__ void exact_tile(const float* __restrict__ lval, const int* __restrict
 #pragma unroll
         for (int r = 0; r < JR; ++r)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) var[r][q] = add_rn(var[r][q], mul_rn(mul_rn(v, c[r][q]), c[r][q]));
+            for (int q = 0; q < 4; ++q) var[r][q] = fmaf(mul_rn(v, c[r][q]), c[r][q], var[r][q]);
     }
 }
 
@@ -500,8 +511,8 @@ __device__ void exact_planes(const float* __restrict__ lval, const int* __restri
     }
 }
 
-template <int ND, int B0, int B1, int B2>
-__global__ void __launch_bounds__(kThreads, 2) group_filter_kernel(FilterArgs a) {
+template <int ND, int B0, int B1, int B2, int NT>
+__global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kernel(FilterArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     using GM = Geom<ND, B0, B1, B2>;
     const BmndStageParams& sp = a.sp;
@@ -571,29 +582,27 @@ __global__ void __launch_bounds__(kThreads, 2) group_filter_kernel(FilterArgs a)
         int g = e / kpad, i = e % kpad;
         GT[e] = i < kk ? G[i * n + g] : 0.0f;
     }
-    if (tid == 0) {
-        // group origin (min over members) and shifted positions
+    if (tid < 32) {
+        // group origin (min over members), member shifts, union extent, and the
+        // patch-linear offset of each shift: element p of member g lies in union
+        // cell c with p = lin(c) - shl[g], lin(c) = sum_d c_d inner(d)
+        const bool live = tid < n;
+        int lin = 0;
         for (int d = 0; d < geo.nd(); ++d) {
-            int mn = pos[d];
-            for (int g = 1; g < n; ++g) mn = min(mn, pos[g * BMND_MAX_DIMS + d]);
-            int mx = 0;
-            for (int g = 0; g < n; ++g) {
-                int sh = pos[g * BMND_MAX_DIMS + d] - mn;
-                shf[g * BMND_MAX_DIMS + d] = sh;
-                mx = g == 0 ? sh : max(mx, sh);
+            const int v = live ? pos[tid * BMND_MAX_DIMS + d] : 0x7fffffff;
+            const int mn = __reduce_min_sync(0xffffffffu, v);
+            const int sh = live ? v - mn : 0;
+            const int mx = __reduce_max_sync(0xffffffffu, sh);
+            if (live) shf[tid * BMND_MAX_DIMS + d] = sh;
+            lin += sh * geo.inner(d);
+            if (tid == 0) {
+                misc[d] = mn;                  // origin
+                misc[4 + d] = mx + geo.b(d);   // union extent
             }
-            misc[d] = mn;                  // origin
-            misc[4 + d] = mx + geo.b(d);   // union extent
         }
+        if (live) sm<int>(smem, a.L.shl)[tid] = lin;
     }
     __syncthreads();
-    // patch-linear offset of each member's shift: element p of member g lies in
-    // union cell coords c with p = lin(c) - shl[g], lin(c) = sum_d c_d inner(d)
-    if (tid < n) {
-        int o = 0;
-        for (int d = 0; d < geo.nd(); ++d) o += shf[tid * BMND_MAX_DIMS + d] * geo.inner(d);
-        sm<int>(smem, a.L.shl)[tid] = o;
-    }
 
     const float scale_f = static_cast<float>(sp.count_scale);
     const float floor_f = static_cast<float>(sp.variance_floor);
@@ -946,18 +955,23 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
     if (a.L.total > 227 * 1024)
         return fail(BMND_ERR_UNSUPPORTED, "group filter shared memory exceeds 227 KB for this profile");
     if (n_refs > 0x7fffffffLL) return fail(BMND_ERR_UNSUPPORTED, "too many groups");
-    auto run = [&](auto kernel) -> int32_t {
+    auto run = [&](auto kernel, int threads) -> int32_t {
         BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(a.L.total)));
-        kernel<<<static_cast<unsigned>(n_refs), kThreads, a.L.total, stream>>>(a);
+        kernel<<<static_cast<unsigned>(n_refs), threads, a.L.total, stream>>>(a);
         BMND_LAUNCH_CHECK("group_filter_kernel");
         return BMND_OK;
     };
+    // two 256-thread CTAs per SM: one CTA's barrier and serial phases are
+    // covered by the other's work (a single 512-thread CTA per SM, which
+    // leaves L1 room for the 5x5x5 Kronecker table, measured 16% slower)
     const int* b = sp.block;
-    if (sp.ndim == 2 && b[0] == 8 && b[1] == 8) return run(group_filter_kernel<2, 8, 8, 1>);
-    if (sp.ndim == 3 && b[0] == 4 && b[1] == 4 && b[2] == 4) return run(group_filter_kernel<3, 4, 4, 4>);
-    if (sp.ndim == 3 && b[0] == 5 && b[1] == 5 && b[2] == 5) return run(group_filter_kernel<3, 5, 5, 5>);
-    return run(group_filter_kernel<0, 0, 0, 0>);
+    if (sp.ndim == 2 && b[0] == 8 && b[1] == 8) return run(group_filter_kernel<2, 8, 8, 1, kThreads>, kThreads);
+    if (sp.ndim == 3 && b[0] == 4 && b[1] == 4 && b[2] == 4)
+        return run(group_filter_kernel<3, 4, 4, 4, kThreads>, kThreads);
+    if (sp.ndim == 3 && b[0] == 5 && b[1] == 5 && b[2] == 5)
+        return run(group_filter_kernel<3, 5, 5, 5, kThreads>, kThreads);
+    return run(group_filter_kernel<0, 0, 0, 0, kThreads>, kThreads);
 }
 
 int32_t launch_finalize(const BmndStageParams& sp, const double* num, const double* den,

@@ -252,3 +252,45 @@ def test_screened_fallback_when_threshold_rejects_everything(cuda, native):
     assert np.all(ex[1] == 2)
     for i in range(3):
         np.testing.assert_array_equal(fa[i], ex[i])
+
+
+def _patch_table(vol, block):
+    """patches_flat of a volume: row = patch-grid linear index, column = patch element (C order)."""
+    win = np.lib.stride_tricks.sliding_window_view(vol, block)
+    counts = win.shape[: vol.ndim]
+    return np.ascontiguousarray(win.reshape(int(np.prod(counts)), int(np.prod(block)))), counts
+
+
+@pytest.mark.parametrize("shape,block,radius,max_m,thr", [
+    ((40, 44), (8, 8), (19, 19), 16, 2.9527),
+    ((22, 20, 24), (4, 4, 4), (7, 7, 7), 16, 2.9527),
+    ((20, 22, 18), (5, 5, 5), (7, 7, 7), 32, 0.7689),
+    ((18, 21, 16), (3, 4, 2), (5, 4, 6), 16, 2.9527),
+])
+@pytest.mark.parametrize("kind", ["counts", "mixed", "bright"])
+def test_count_tabulated_volume_matching_equals_patch_table(cuda, native, shape, block, radius, max_m, thr,
+                                                              kind):
+    """The integer-count tabulated volume kernel and the per-term patch-table
+    kernel are independent implementations of the same exact distance: their
+    match tables must be bit-identical, also where voxels fall outside the
+    table (non-integer, negative, or counts >= 63) and the reference patch is
+    itself non-integer."""
+    from bmnd_gb300 import _abi
+
+    rng = np.random.default_rng(hash((shape, kind)) % 2**32)
+    lam = {"counts": 20.0, "mixed": 20.0, "bright": 70.0}[kind]
+    base = rng.uniform(0.2 * lam, 1.5 * lam, size=shape)
+    vol = rng.poisson(base).astype(np.float32)
+    if kind == "mixed":
+        vol[rng.random(shape) < 0.03] += np.float32(0.25)
+        vol[rng.random(shape) < 0.01] = np.float32(-1.0)
+    counts = tuple(s - b + 1 for s, b in zip(shape, block))
+    refs = np.stack(np.meshgrid(*[np.arange(0, c, 2) for c in counts], indexing="ij"), -1)
+    refs = refs.reshape(-1, len(shape)).astype(np.int32)
+    vg = _match_volume(cuda, native, vol, block, radius, max_m, 2, thr, _abi.MATCH_EXACT, refs=refs)
+    patches, pc = _patch_table(vol, block)
+    assert tuple(pc) == counts
+    pg = gpu_match_patches(cuda, native, patches, counts, refs, radius, max_m, 2, thr, DEV)
+    np.testing.assert_array_equal(vg[1], pg[1])
+    np.testing.assert_array_equal(vg[2], pg[2])
+    np.testing.assert_array_equal(vg[0], pg[0])
