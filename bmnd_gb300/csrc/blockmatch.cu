@@ -181,6 +181,45 @@ __device__ int warp_merge(const uint64_t* list, int size, int cap, uint64_t* out
     return n;
 }
 
+// patch-grid linear index and source offset of window candidate c (C order
+// over the clipped window lo + [0, ext)); windows below 2^21 candidates are
+// decoded with float reciprocals (small_div), larger ones with 64-bit division
+__device__ __forceinline__ int64_t window_origin(const MatchArgs& a, const int* lo, const int* ext,
+                                                 const float* inv_ext, bool small_window, int64_t c,
+                                                 int64_t* lin_out) {
+    int coord[BMND_MAX_DIMS] = {0, 0, 0};
+    if (small_window) {
+        int rem = static_cast<int>(c);
+#pragma unroll
+        for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+            if (d < a.ndim) {
+                const int q = d > 0 ? small_div(rem, inv_ext[d]) : 0;
+                coord[d] = lo[d] + rem - q * ext[d];
+                rem = q;
+            }
+        }
+    } else {
+        int64_t rem = c;
+#pragma unroll
+        for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+            if (d < a.ndim) {
+                coord[d] = lo[d] + static_cast<int>(rem % ext[d]);
+                rem /= ext[d];
+            }
+        }
+    }
+    int64_t lin = 0, origin = 0;
+#pragma unroll
+    for (int d = 0; d < BMND_MAX_DIMS; ++d) {
+        if (d < a.ndim) {
+            lin = lin * a.counts[d] + coord[d];
+            origin += static_cast<int64_t>(coord[d]) * a.grid_stride[d];
+        }
+    }
+    *lin_out = lin;
+    return origin;
+}
+
 template <int CODE>
 __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -232,21 +271,25 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
     const int64_t stride = static_cast<int64_t>(gridDim.x) * kWarps;
     for (int64_t r = static_cast<int64_t>(blockIdx.x) * kWarps + warp; r < a.n_refs; r += stride) {
         if (a.fixup && a.count[r] >= 0) continue;
-        int center[BMND_MAX_DIMS], lo[BMND_MAX_DIMS], ext[BMND_MAX_DIMS];
+        int lo[BMND_MAX_DIMS] = {0, 0, 0}, ext[BMND_MAX_DIMS] = {1, 1, 1};
+        float inv_ext[BMND_MAX_DIMS] = {1.0f, 1.0f, 1.0f};
         int64_t center_lin = 0, center_origin = 0;
         int64_t window = 1;
-        for (int d = 0; d < a.ndim; ++d) {
-            center[d] = a.refs[r * a.ndim + d];
-            center_lin = center_lin * a.counts[d] + center[d];
-            center_origin += static_cast<int64_t>(center[d]) * a.grid_stride[d];
-            int l = center[d] - a.radius[d];
-            if (l < 0) l = 0;
-            int h = center[d] + a.radius[d];
-            if (h > a.counts[d] - 1) h = a.counts[d] - 1;
-            lo[d] = l;
-            ext[d] = h - l + 1;
-            window *= ext[d];
+#pragma unroll
+        for (int d = 0; d < BMND_MAX_DIMS; ++d) {
+            if (d < a.ndim) {
+                const int cd = a.refs[r * a.ndim + d];
+                center_lin = center_lin * a.counts[d] + cd;
+                center_origin += static_cast<int64_t>(cd) * a.grid_stride[d];
+                const int l = max(cd - a.radius[d], 0);
+                const int h = min(cd + a.radius[d], a.counts[d] - 1);
+                lo[d] = l;
+                ext[d] = h - l + 1;
+                inv_ext[d] = 1.0f / static_cast<float>(ext[d]);
+                window *= ext[d];
+            }
         }
+        const bool small_window = window < (int64_t(1) << 21);
         __syncwarp();
         for (int p = lane; p < P; p += 32) {
             float v = __ldg(a.src + center_origin + poff_s[p]);
@@ -265,17 +308,8 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
         const float tkey = stab ? canonical_key(thr) : thr;
         int acc_size = 0, rej_size = 0, acc_count = 0;
         for (int64_t c = lane; c < window; c += 32) {
-            int64_t rem = c;
-            int coord[BMND_MAX_DIMS];
-            for (int d = a.ndim - 1; d >= 0; --d) {
-                coord[d] = lo[d] + static_cast<int>(rem % ext[d]);
-                rem /= ext[d];
-            }
-            int64_t lin = 0, origin = 0;
-            for (int d = 0; d < a.ndim; ++d) {
-                lin = lin * a.counts[d] + coord[d];
-                origin += static_cast<int64_t>(coord[d]) * a.grid_stride[d];
-            }
+            int64_t lin;
+            const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
             float dist = use_table ? deviance_tabulated(ref_s, ref_row, a.src, origin, poff_s, P, table)
                                    : patch_distance<CODE>(ref_s, a.src, origin, poff_s, P, a.inv_scale);
             float key = stab ? canonical_key(dist) : dist;
@@ -444,23 +478,6 @@ __device__ __forceinline__ float exact_deviance(const float2* __restrict__ ref, 
     return div_rn(d, static_cast<float>(P));
 }
 
-__device__ __forceinline__ int64_t window_origin(const MatchArgs& a, const int* lo, const int* ext, int64_t c,
-                                                 int64_t* lin_out) {
-    int coord[BMND_MAX_DIMS];
-    int64_t rem = c;
-    for (int d = a.ndim - 1; d >= 0; --d) {
-        coord[d] = lo[d] + static_cast<int>(rem % ext[d]);
-        rem /= ext[d];
-    }
-    int64_t lin = 0, origin = 0;
-    for (int d = 0; d < a.ndim; ++d) {
-        lin = lin * a.counts[d] + coord[d];
-        origin += static_cast<int64_t>(coord[d]) * a.grid_stride[d];
-    }
-    *lin_out = lin;
-    return origin;
-}
-
 constexpr int kSThreads = 128;   // one CTA per reference
 constexpr int kSQueue = 512;     // rescoring queue (overflow -> exact redo)
 
@@ -479,7 +496,7 @@ struct ScreenSmem {
 };
 
 template <int ND, int B0, int B1, int B2>
-__global__ void __launch_bounds__(kSThreads) blockmatch_screened_kernel(MatchArgs a, int32_t wmax) {
+__global__ void __launch_bounds__(kSThreads, 8) blockmatch_screened_kernel(MatchArgs a, int32_t wmax) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
@@ -522,18 +539,24 @@ __global__ void __launch_bounds__(kSThreads) blockmatch_screened_kernel(MatchArg
     const float drel = 2.0f * (2.0f * 5.96046448e-08f * static_cast<float>(P) + 4.76837158e-07f);
 
     for (int64_t r = blockIdx.x; r < a.n_refs; r += gridDim.x) {
-        int lo[BMND_MAX_DIMS], ext[BMND_MAX_DIMS];
+        int lo[BMND_MAX_DIMS] = {0, 0, 0}, ext[BMND_MAX_DIMS] = {1, 1, 1};
+        float inv_ext[BMND_MAX_DIMS] = {1.0f, 1.0f, 1.0f};
         int64_t center_lin = 0, center_origin = 0, window = 1;
-        for (int d = 0; d < a.ndim; ++d) {
-            const int cd = a.refs[r * a.ndim + d];
-            center_lin = center_lin * a.counts[d] + cd;
-            center_origin += static_cast<int64_t>(cd) * a.grid_stride[d];
-            const int l = max(cd - a.radius[d], 0);
-            const int h = min(cd + a.radius[d], a.counts[d] - 1);
-            lo[d] = l;
-            ext[d] = h - l + 1;
-            window *= ext[d];
+#pragma unroll
+        for (int d = 0; d < BMND_MAX_DIMS; ++d) {
+            if (d < a.ndim) {
+                const int cd = a.refs[r * a.ndim + d];
+                center_lin = center_lin * a.counts[d] + cd;
+                center_origin += static_cast<int64_t>(cd) * a.grid_stride[d];
+                const int l = max(cd - a.radius[d], 0);
+                const int h = min(cd + a.radius[d], a.counts[d] - 1);
+                lo[d] = l;
+                ext[d] = h - l + 1;
+                inv_ext[d] = 1.0f / static_cast<float>(ext[d]);
+                window *= ext[d];
+            }
         }
+        const bool small_window = window < (int64_t(1) << 21);
         __syncthreads();  // previous reference's shared data is no longer read
         for (int p = tid; p < P; p += blockDim.x) {
             float rv = mul_rn(__ldg(a.src + center_origin + poff_s[p]), a.inv_scale);
@@ -550,7 +573,7 @@ __global__ void __launch_bounds__(kSThreads) blockmatch_screened_kernel(MatchArg
         float dmax = 0.0f;
         for (int64_t c = tid; c < window; c += blockDim.x) {
             int64_t lin;
-            const int64_t origin = window_origin(a, lo, ext, c, &lin);
+            const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
             const float2 sd = fixed ? screen_deviance_fixed<ND, B0, B1, B2>(ref, a.src, origin, a.vstride[0],
                                                                            a.vstride[ND > 1 ? 1 : 0], poff_s)
                                     : screen_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
@@ -671,7 +694,7 @@ __global__ void __launch_bounds__(kSThreads) blockmatch_screened_kernel(MatchArg
         for (int i = tid; i < qn; i += blockDim.x) {
             const int32_t q = qidx[i];
             int64_t lin;
-            const int64_t origin = window_origin(a, lo, ext, q & 0x7fffffff, &lin);
+            const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, q & 0x7fffffff, &lin);
             const float dist = exact_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
             const float key = canonical_key(dist);
             const bool accepted = key < tkey;
@@ -849,14 +872,14 @@ __device__ __forceinline__ float counts_distance_fixed(const unsigned char* __re
 }
 
 template <int ND, int B0, int B1, int B2>
-__global__ void __launch_bounds__(kCThreads) blockmatch_counts_kernel(MatchArgs a, int32_t rows) {
+__global__ void __launch_bounds__(kCThreads, 4) blockmatch_counts_kernel(MatchArgs a, int32_t rows) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const int P = a.P;
     const int K = a.max_m;
     const int R = a.required;
-    const int nd = a.ndim;
+    const int nd = ND > 0 ? ND : a.ndim;
     int64_t boxmax = 1;
     for (int d = 0; d < nd; ++d) boxmax *= min(2 * a.radius[d] + 1, a.counts[d]) + a.block[d] - 1;
     const CountSmem L(P, boxmax, rows);
@@ -884,19 +907,25 @@ __global__ void __launch_bounds__(kCThreads) blockmatch_counts_kernel(MatchArgs 
 
     for (int64_t r = blockIdx.x; r < a.n_refs; r += gridDim.x) {
         int lo[BMND_MAX_DIMS] = {0, 0, 0}, ext[BMND_MAX_DIMS] = {1, 1, 1}, bx[BMND_MAX_DIMS] = {1, 1, 1};
+        float inv_ext[BMND_MAX_DIMS] = {1.0f, 1.0f, 1.0f};
         int64_t center_lin = 0, center_origin = 0, window = 1, nbox = 1;
-        for (int d = 0; d < nd; ++d) {
-            const int cd = a.refs[r * nd + d];
-            center_lin = center_lin * a.counts[d] + cd;
-            center_origin += static_cast<int64_t>(cd) * a.vstride[d];
-            const int l = max(cd - a.radius[d], 0);
-            const int h = min(cd + a.radius[d], a.counts[d] - 1);
-            lo[d] = l;
-            ext[d] = h - l + 1;
-            bx[d] = ext[d] + a.block[d] - 1;
-            window *= ext[d];
-            nbox *= bx[d];
+#pragma unroll
+        for (int d = 0; d < BMND_MAX_DIMS; ++d) {
+            if (d < nd) {
+                const int cd = a.refs[r * nd + d];
+                center_lin = center_lin * a.counts[d] + cd;
+                center_origin += static_cast<int64_t>(cd) * a.vstride[d];
+                const int l = max(cd - a.radius[d], 0);
+                const int h = min(cd + a.radius[d], a.counts[d] - 1);
+                lo[d] = l;
+                ext[d] = h - l + 1;
+                inv_ext[d] = 1.0f / static_cast<float>(ext[d]);
+                bx[d] = ext[d] + a.block[d] - 1;
+                window *= ext[d];
+                nbox *= bx[d];
+            }
         }
+        const bool small_window = window < (int64_t(1) << 21);
         __syncthreads();  // the previous reference's shared data is no longer read
         // reference values and their table rows
         for (int p = tid; p < P; p += blockDim.x) {
@@ -945,15 +974,34 @@ __global__ void __launch_bounds__(kCThreads) blockmatch_counts_kernel(MatchArgs 
         const int S1 = nd == 3 ? bx[2] : 1;
         for (int64_t c = tid; c < window; c += blockDim.x) {
             int w[BMND_MAX_DIMS] = {0, 0, 0};
-            int64_t rem = c;
-            for (int d = nd - 1; d >= 0; --d) {
-                w[d] = static_cast<int>(rem % ext[d]);
-                rem /= ext[d];
+            if (small_window) {
+                int rem = static_cast<int>(c);
+#pragma unroll
+                for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                    if (d < nd) {
+                        const int q = d > 0 ? small_div(rem, inv_ext[d]) : 0;
+                        w[d] = rem - q * ext[d];
+                        rem = q;
+                    }
+                }
+            } else {
+                int64_t rem = c;
+#pragma unroll
+                for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                    if (d < nd) {
+                        w[d] = static_cast<int>(rem % ext[d]);
+                        rem /= ext[d];
+                    }
+                }
             }
-            int64_t lin = 0, boff = 0;
-            for (int d = 0; d < nd; ++d) {
-                lin = lin * a.counts[d] + lo[d] + w[d];
-                boff = boff * bx[d] + w[d];
+            int64_t lin = 0;
+            int boff = 0;
+#pragma unroll
+            for (int d = 0; d < BMND_MAX_DIMS; ++d) {
+                if (d < nd) {
+                    lin = lin * a.counts[d] + lo[d] + w[d];
+                    boff = boff * bx[d] + w[d];
+                }
             }
             float dsum;
             if constexpr (ND > 0) {
@@ -974,7 +1022,9 @@ __global__ void __launch_bounds__(kCThreads) blockmatch_counts_kernel(MatchArgs 
             if (dsum != dsum) {
                 // a voxel outside the table: term-by-term evaluation from the source
                 int64_t origin = 0;
-                for (int d = 0; d < nd; ++d) origin += static_cast<int64_t>(lo[d] + w[d]) * a.vstride[d];
+#pragma unroll
+                for (int d = 0; d < BMND_MAX_DIMS; ++d)
+                    if (d < nd) origin += static_cast<int64_t>(lo[d] + w[d]) * a.vstride[d];
                 dsum = 0.0f;
                 for (int p = 0; p < P; ++p) {
                     float cv = __ldg(a.src + origin + poff_s[p]);

@@ -46,6 +46,16 @@ int32_t cuda_fail(cudaError_t err, const char* what);
 // computed exactly in float32 here.
 // ---------------------------------------------------------------------------
 __host__ __device__ inline float canonical_key(float d) {
+#ifdef __CUDA_ARCH__
+    // e = floor(log2(max(|d|, 1))) from the exponent field; both scalings are
+    // by exact powers of two (2^(18-e) <= 2^18, 2^(e-18) >= 2^-18, normal)
+    const uint32_t mbits = __float_as_uint(d) & 0x7fffffffu;
+    if (mbits >= 0x7f800000u) return d;  // NaN, +-inf
+    const int e = mbits >= 0x3f800000u ? static_cast<int>(mbits >> 23) - 127 : 0;
+    const float up = __uint_as_float(static_cast<uint32_t>(127 + 18 - e) << 23);
+    const float down = __uint_as_float(static_cast<uint32_t>(127 - 18 + e) << 23);
+    return __fmul_rn(rintf(__fmul_rn(d, up)), down);
+#else
     if (!(d == d) || d == INFINITY || d == -INFINITY) return d;
     float mag = fabsf(d);
     int e = 0;
@@ -56,6 +66,14 @@ __host__ __device__ inline float canonical_key(float d) {
     }
     float scaled = ldexpf(d, 18 - e);
     return ldexpf(rintf(scaled), e - 18);
+#endif
+}
+
+// q = floor(c / e) for 0 <= c < 2^21 and e >= 1, with inv_e = 1.0f / e:
+// (c + 0.5) / e lies at least 0.5 / e away from an integer, and the float32
+// evaluation errs by less than 2^-22 (c + 0.5) / e < 0.5 / e
+__device__ __forceinline__ int small_div(int c, float inv_e) {
+    return __float2int_rz(__fmul_rn(static_cast<float>(c) + 0.5f, inv_e));
 }
 
 // order-preserving uint32 image of a float (total order for non-NaN values)
