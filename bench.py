@@ -452,7 +452,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="bm4d256", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="exact", choices=["exact", "fast"])
+    ap.add_argument("--precision", default="exact", choices=["exact", "fast", "approx"])
     ap.add_argument("--skip-cpu", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))

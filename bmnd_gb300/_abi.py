@@ -41,6 +41,7 @@ WEIGHT_VARIANCE = 1
 
 MATCH_EXACT = 0
 MATCH_FAST = 1
+MATCH_APPROX = 2
 
 STATIC_SCRATCH_BYTES = 64 << 20
 

@@ -150,7 +150,7 @@ def _match_result(schedule: plan.Schedule, counts, sel, cnt, acc) -> BlockMatchR
     return BlockMatchResult(groups=groups)
 
 
-_MATCH_PRECISIONS = {"exact": _abi.MATCH_EXACT, "fast": _abi.MATCH_FAST}
+_MATCH_PRECISIONS = {"exact": _abi.MATCH_EXACT, "fast": _abi.MATCH_FAST, "approx": _abi.MATCH_APPROX}
 
 
 def bmnd_device(noisy, profile, *, resolved=None, match_precision: str = "exact",
@@ -230,8 +230,10 @@ def bmnd(
     ``volume`` may be a NumPy array (the result is a NumPy float32 array of
     the same shape) or a CUDA tensor (the result stays on that device).
     ``match_precision`` selects exact float32 matching for every candidate
-    ("exact") or screening plus exact rescoring near the selection boundary
-    ("fast").
+    ("exact"), screening plus exact rescoring near the selection boundary
+    ("fast", same match sets), or selection by the screening distances with
+    exact rescoring of the selected candidates only ("approx"; the match sets
+    may differ where the screening and exact orders disagree).
     """
     if sigma is not None and sigma_psd is not None:
         raise ValueError("sigma and sigma_psd are mutually exclusive.")
@@ -239,7 +241,7 @@ def bmnd(
         _validate_sigma(sigma)
     _validate_max_cache_bytes(max_cache_bytes)
     if match_precision not in _MATCH_PRECISIONS:
-        raise ValueError(f"match_precision must be 'exact' or 'fast', got {match_precision!r}.")
+        raise ValueError(f"match_precision must be 'exact', 'fast' or 'approx', got {match_precision!r}.")
 
     torch_input = type(volume).__module__.startswith("torch")
     shape = tuple(int(s) for s in volume.shape)

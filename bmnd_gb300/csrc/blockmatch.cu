@@ -58,6 +58,7 @@ struct MatchArgs {
     int32_t* accepted;
     int32_t use_table;  // integer-count lookup of Poisson-deviance terms
     int32_t fixup;      // only redo references whose count is negative
+    int32_t approx;     // screened kernel: zero bound, the screening distances decide
 };
 
 constexpr int kTable = 64;  // counts 0..63 are tabulated
@@ -536,7 +537,7 @@ __global__ void __launch_bounds__(kSThreads, 8) blockmatch_screened_kernel(Match
     const bool fixed = ND > 0 && !a.table && a.inv_scale == 1.0f;
     // relative part of the bound: float32 accumulation of both sums (P 2^-24 each)
     // and the final scalings, x2
-    const float drel = 2.0f * (2.0f * 5.96046448e-08f * static_cast<float>(P) + 4.76837158e-07f);
+    const float drel = a.approx ? 0.0f : 2.0f * (2.0f * 5.96046448e-08f * static_cast<float>(P) + 4.76837158e-07f);
 
     for (int64_t r = blockIdx.x; r < a.n_refs; r += gridDim.x) {
         int lo[BMND_MAX_DIMS] = {0, 0, 0}, ext[BMND_MAX_DIMS] = {1, 1, 1};
@@ -586,6 +587,7 @@ __global__ void __launch_bounds__(kSThreads, 8) blockmatch_screened_kernel(Match
         __syncthreads();
         float Dabs = redf[0];
         for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) Dabs = fmaxf(Dabs, redf[w]);
+        if (a.approx) Dabs = 0.0f;
 
         // radix select over the upper bounds d + D of the certainly accepted:
         // vstar with >= K of them bounded by it
@@ -1143,8 +1145,10 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     if (a.n_refs == 0) return BMND_OK;
     int64_t wmax = 1;
     for (int d = 0; d < a.ndim; ++d) wmax *= std::min<int64_t>(2 * a.radius[d] + 1, a.counts[d]);
+    a.approx = precision == BMND_MATCH_APPROX;
     const bool screened = code == BMND_DIST_POISSON_DEVIANCE && a.stab &&
-                          (precision == BMND_MATCH_FAST || precision == BMND_MATCH_REAL_VALUED) &&
+                          (precision == BMND_MATCH_FAST || precision == BMND_MATCH_APPROX ||
+                           precision == BMND_MATCH_REAL_VALUED) &&
                           a.max_m <= 32 && screened_smem_bytes(a.max_m, a.P, wmax) <= 200 * 1024;
     if (!screened) {
         const bool counts = code == BMND_DIST_POISSON_DEVIANCE && a.use_table && !a.table && !a.fixup &&
@@ -1177,6 +1181,7 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     MatchArgs fix = a;
     fix.fixup = 1;
     fix.use_table = 0;
+    fix.approx = 0;
     return launch_exact(fix, code, stream);
 }
 

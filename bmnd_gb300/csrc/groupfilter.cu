@@ -377,9 +377,10 @@ __device__ __forceinline__ bool ht_keep(float mag, float thr, double scale, floa
 //
 // Work split: warp w takes the voxels whose entry lists start in its 1/nw share
 // of all entries, and accumulates every (plane, coefficient) pair over them;
-// lane l holds four planes of the JR consecutive coefficients j0 + JR * l + r,
-// so one entry costs three loads (the entry and the four G values, both warp
-// broadcasts, and one JR-wide vector of S^T) for 4 * JR fused multiply-adds.
+// lane l holds NQ planes (4, or kk when fewer) of the JR consecutive
+// coefficients j0 + JR * l + r, so one entry costs three loads (the entry and
+// the NQ G values, both warp broadcasts, and one JR-wide vector of S^T) for
+// NQ * JR fused multiply-adds.
 // The warps' partial sums are then added in warp order, which fixes the result
 // independently of scheduling.  An entry packs member g (low byte) and the row
 // offset p * kron_stride(P) of S^T (upper bits).
@@ -411,61 +412,79 @@ struct KronVec<4> {
     }
 };
 
-template <int JR>
+template <int NQ>
+struct PlaneVec {
+    float v[NQ];
+    __device__ __forceinline__ void load(const float* p) {
+        if constexpr (NQ == 4) {
+            const float4 t = *reinterpret_cast<const float4*>(p);
+            v[0] = t.x;
+            v[1] = t.y;
+            v[2] = t.z;
+            v[3] = t.w;
+        } else if constexpr (NQ == 2) {
+            const float2 t = *reinterpret_cast<const float2*>(p);
+            v[0] = t.x;
+            v[1] = t.y;
+        } else {
+            v[0] = *p;
+        }
+    }
+};
+
+// one tile of NQ planes x 32 JR coefficients over the warp's voxels
+template <int JR, int NQ>
 __device__ void exact_tile(const float* __restrict__ lval, const int* __restrict__ lstart,
                            const uint32_t* __restrict__ lent, int u_lo, int u_hi,
-                           const float* __restrict__ GT, int kpad, int iq,
-                           const float* __restrict__ st, int j0, float (&var)[JR][4]) {
+                           const float* __restrict__ GT, int kpad, int i0,
+                           const float* __restrict__ st, int j0, float (&var)[JR][NQ]) {
     const int lane = threadIdx.x & 31;
     const float* stl = st + j0 + JR * lane;
 #pragma unroll
     for (int r = 0; r < JR; ++r)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) var[r][q] = 0.0f;
-    const float* gt0 = GT + 4 * iq;
+        for (int q = 0; q < NQ; ++q) var[r][q] = 0.0f;
+    const float* gt0 = GT + i0;
     for (int u = u_lo; u < u_hi; ++u) {
         int e = lstart[u];
         const int e1 = lstart[u + 1];
-        float c[JR][4];
+        float c[JR][NQ];
         {
             // first entry: the product itself (every voxel has at least one)
             const uint32_t ent = lent[e];
-            const float4 gv = *reinterpret_cast<const float4*>(gt0 + (ent & 0xffu) * kpad);
+            PlaneVec<NQ> gv;
+            gv.load(gt0 + (ent & 0xffu) * kpad);
             KronVec<JR> sv;
             sv.load(stl + (ent >> 8));
 #pragma unroll
-            for (int r = 0; r < JR; ++r) {
-                c[r][0] = mul_rn(gv.x, sv.v[r]);
-                c[r][1] = mul_rn(gv.y, sv.v[r]);
-                c[r][2] = mul_rn(gv.z, sv.v[r]);
-                c[r][3] = mul_rn(gv.w, sv.v[r]);
-            }
+            for (int r = 0; r < JR; ++r)
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) c[r][q] = mul_rn(gv.v[q], sv.v[r]);
         }
 #pragma unroll 2
         for (++e; e < e1; ++e) {
             const uint32_t ent = lent[e];
-            const float4 gv = *reinterpret_cast<const float4*>(gt0 + (ent & 0xffu) * kpad);
+            PlaneVec<NQ> gv;
+            gv.load(gt0 + (ent & 0xffu) * kpad);
             KronVec<JR> sv;
             sv.load(stl + (ent >> 8));
 #pragma unroll
-            for (int r = 0; r < JR; ++r) {
-                c[r][0] = fmaf(gv.x, sv.v[r], c[r][0]);
-                c[r][1] = fmaf(gv.y, sv.v[r], c[r][1]);
-                c[r][2] = fmaf(gv.z, sv.v[r], c[r][2]);
-                c[r][3] = fmaf(gv.w, sv.v[r], c[r][3]);
-            }
+            for (int r = 0; r < JR; ++r)
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) c[r][q] = fmaf(gv.v[q], sv.v[r], c[r][q]);
         }
         const float v = lval[u];
 #pragma unroll
         for (int r = 0; r < JR; ++r)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) var[r][q] = fmaf(mul_rn(v, c[r][q]), c[r][q], var[r][q]);
+            for (int q = 0; q < NQ; ++q) var[r][q] = fmaf(mul_rn(v, c[r][q]), c[r][q], var[r][q]);
     }
 }
 
-// all tiles of (4 planes) x (32 * JR coefficients); EX[i * P + j] receives the
-// standard deviation sqrt(max(var, 0)) of planes i < kk
-template <int JR>
+// all tiles of (NQ planes) x (32 * JR coefficients); EX[i * P + j] receives the
+// standard deviation sqrt(max(var, 0)) of planes i < kk.  NQ = 4 in general;
+// groups with fewer exact planes (k < 4, or fewer members) use NQ = kk.
+template <int JR, int NQ>
 __device__ void exact_planes(const float* __restrict__ lval, const int* __restrict__ lstart,
                              const uint32_t* __restrict__ lent, int U, const float* __restrict__ GT,
                              int kpad, int kk, const float* __restrict__ st, int P,
@@ -485,18 +504,18 @@ __device__ void exact_planes(const float* __restrict__ lval, const int* __restri
     };
     const int u_lo = first_voxel(static_cast<int>(static_cast<int64_t>(E) * warp / nw));
     const int u_hi = warp == nw - 1 ? U : first_voxel(static_cast<int>(static_cast<int64_t>(E) * (warp + 1) / nw));
-    for (int iq = 0; 4 * iq < kk; ++iq) {
+    for (int i0 = 0; i0 < kk; i0 += NQ) {
         for (int j0 = 0; j0 < P; j0 += 32 * JR) {
-            float var[JR][4];
-            exact_tile<JR>(lval, lstart, lent, u_lo, u_hi, GT, kpad, iq, st, j0, var);
+            float var[JR][NQ];
+            exact_tile<JR, NQ>(lval, lstart, lent, u_lo, u_hi, GT, kpad, i0, st, j0, var);
             for (int w = 0; w < nw; ++w) {
                 if (warp == w) {
 #pragma unroll
                     for (int r = 0; r < JR; ++r) {
                         const int j = j0 + JR * lane + r;
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            const int i = 4 * iq + q;
+                        for (int q = 0; q < NQ; ++q) {
+                            const int i = i0 + q;
                             if (j < P && i < kk) {
                                 float t = w == 0 ? var[r][q] : add_rn(EX[i * P + j], var[r][q]);
                                 if (w == nw - 1) t = sqrtf(t > 0.0f ? t : 0.0f);
@@ -509,6 +528,16 @@ __device__ void exact_planes(const float* __restrict__ lval, const int* __restri
             }
         }
     }
+}
+
+template <int JR>
+__device__ void exact_planes_any(const float* __restrict__ lval, const int* __restrict__ lstart,
+                                 const uint32_t* __restrict__ lent, int U, const float* __restrict__ GT,
+                                 int kpad, int kk, const float* __restrict__ st, int P,
+                                 float* __restrict__ EX) {
+    if (kk == 1) exact_planes<JR, 1>(lval, lstart, lent, U, GT, kpad, kk, st, P, EX);
+    else if (kk == 2) exact_planes<JR, 2>(lval, lstart, lent, U, GT, kpad, kk, st, P, EX);
+    else exact_planes<JR, 4>(lval, lstart, lent, U, GT, kpad, kk, st, P, EX);
 }
 
 template <int ND, int B0, int B1, int B2, int NT>
@@ -745,12 +774,12 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         }
         __syncthreads();
         if constexpr (ND > 0) {
-            exact_planes<kron_jr(B0 * B1 * B2)>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
+            exact_planes_any<kron_jr(B0 * B1 * B2)>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
         } else {
             const int jr = kron_jr(P);
-            if (jr == 1) exact_planes<1>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
-            else if (jr == 2) exact_planes<2>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
-            else exact_planes<4>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
+            if (jr == 1) exact_planes_any<1>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
+            else if (jr == 2) exact_planes_any<2>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
+            else exact_planes_any<4>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
         }
     }
 

@@ -68,6 +68,9 @@ extern "C" {
 /* matching precision */
 #define BMND_MATCH_EXACT 0 /* FP32 per-term distances for every candidate */
 #define BMND_MATCH_FAST 1  /* approximate screening pass + exact FP32 rescoring inside a margin */
+#define BMND_MATCH_APPROX 2 /* screening distances select the group; only the selected candidates
+                               are rescored exactly (Poisson deviance only; the match set may
+                               differ from the exact one where the two orders disagree) */
 
 /*
  * Block matching on one patch grid.  Replaces

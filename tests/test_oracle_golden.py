@@ -27,28 +27,43 @@ def _profile(kind):
 
 @pytest.mark.parametrize("case", CASES)
 def test_oracle_pipeline_matches_reference(oracle_lib, case):
+    """Stage 1 on the noisy input, stage 2 on the reference's own pilot (so a
+    near-tie in stage 1 cannot move stage 2's match sets)."""
+    from bmnd_gb300 import plan
+    from bmnd_gb300.validation import resolve_profile
+
     g = np.load(os.path.join(GOLDEN, f"pipe_{case}.npz"))
-    if g["noisy"].size > 64 * 64 * 2:
-        pytest.skip("large fixture is covered by the GPU tests")
     kind = str(g["kind"])
     profile = _profile(kind)
-    out, det = oracle_lib.bmnd(g["noisy"], _profile(kind), return_details=True)
     shape = g["noisy"].shape
-    foot = np.zeros(shape, dtype=bool)
-    for stage, src in (("ht", g["noisy"]), ("wiener", g["ht"])):
-        d = det[stage]
-        np.testing.assert_array_equal(d["refs"], g[f"{stage}_refs"])
+    resolved = resolve_profile(_profile(kind), shape)
+    for stage in ("ht", "wiener"):
+        params = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k)
+        refs = g[f"{stage}_refs"].astype(np.int32)
+        pilot = None if stage == "ht" else g["ht"]
+        est, sel, cnt, _ = oracle_lib.stage(params, g["noisy"], pilot, refs)
+        src = g["noisy"] if stage == "ht" else g["ht"]
         block = tuple(getattr(profile, f"{stage}_block_size"))
         thr = float(np.float32(getattr(profile, f"{stage}_match_threshold")))
-        eq, tied, bad = compare_match_sets(oracle_lib, src, block, d["refs"], d["sel"], d["count"],
+        eq, tied, bad = compare_match_sets(oracle_lib, src, block, refs, sel, cnt,
                                            g[f"{stage}_sel"], g[f"{stage}_count"], 1, thr)
         assert not bad, (case, stage, bad[:8])
-        assert eq >= 0.98 * len(d["count"])
-        foot |= tie_footprint(shape, block, d["sel"], d["count"], g[f"{stage}_sel"], g[f"{stage}_count"])
-    par = output_parity(det["ht"]["estimate"], g["ht"], g["clean"])
-    assert par["frac_within"] >= 0.999 and par["psnr_delta"] < 0.01, par
-    par = output_parity(out, g["wiener"], g["clean"], exclude=foot)
-    assert par["frac_within"] >= 0.999 and par["psnr_delta"] < 0.01, par
+        assert eq >= 0.98 * len(cnt)
+        foot = tie_footprint(shape, block, sel, cnt, g[f"{stage}_sel"], g[f"{stage}_count"])
+        par = output_parity(est, g[stage], g["clean"], exclude=foot)
+        assert par["frac_within"] >= 0.999 and par["psnr_delta"] < 0.01, (stage, par)
+
+
+def test_oracle_schedule_and_full_pipeline(oracle_lib):
+    """The oracle's own two-stage run reproduces the reference's schedules and
+    its final PSNR on the 256 x 256 configuration."""
+    g = np.load(os.path.join(GOLDEN, "pipe_bm3d_256_cfg.npz"))
+    out, det = oracle_lib.bmnd(g["noisy"], _profile("bm3d"), return_details=True)
+    for stage in ("ht", "wiener"):
+        np.testing.assert_array_equal(det[stage]["refs"], g[f"{stage}_refs"])
+    from bmnd_gb300.phantoms import psnr
+
+    assert abs(psnr(out, g["clean"]) - psnr(g["wiener"], g["clean"])) < 0.01
 
 
 def test_oracle_distances_match_reference(oracle_lib):
