@@ -99,6 +99,19 @@ class StageParams(ctypes.Structure):
     ]
 
 
+class PilotNet(ctypes.Structure):
+    _fields_ = [
+        ("ndim", _I32),
+        ("channels", _I32),
+        ("layers", _I32),
+        ("batch", _I32),
+        ("shape", _I32 * MAX_DIMS),
+    ]
+
+
+_PNP = ctypes.POINTER(PilotNet)
+_VP = ctypes.c_void_p
+
 # name -> (restype, argtypes); every symbol include/bmnd_gb300.h declares
 SIGNATURES = {
     "bmnd_abi_version": (_I32, []),
@@ -129,6 +142,16 @@ SIGNATURES = {
         [ctypes.POINTER(StageParams), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _I64,
          ctypes.c_void_p, _U64],
     ),
+    "bmnd_pilotnet_param_count": (_I32, [_PNP, _I64P]),
+    "bmnd_pilotnet_packed_bytes": (_I32, [_PNP, _U64P]),
+    "bmnd_pilotnet_workspace_bytes": (_I32, [_PNP, _I32, _U64P]),
+    "bmnd_pilotnet_pack": (_I32, [_PNP, _VP, _VP, _U64]),
+    "bmnd_pilotnet_forward": (_I32, [_PNP, _VP, _VP, _VP, _VP, _VP, _U64, _U64]),
+    "bmnd_pilotnet_gradient": (_I32, [_PNP, _VP, _VP, _VP, _VP, _VP, _VP, _U64, _U64]),
+    "bmnd_pilotnet_adam": (_I32, [_I64, _VP, _VP, _VP, _VP, _I32, ctypes.c_float, ctypes.c_float,
+                                  ctypes.c_float, ctypes.c_float, _U64]),
+    "bmnd_pilot_tile_deviance": (_I32, [_I32, _I32, _I32P, _I32, _VP, _VP, _VP, _I32, ctypes.c_float,
+                                        ctypes.c_float, _VP, _U64]),
     "bmnd_run": (
         _I32,
         [ctypes.POINTER(StageParams), ctypes.POINTER(StageParams), ctypes.c_void_p,

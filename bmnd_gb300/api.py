@@ -213,6 +213,39 @@ def bmnd_device(noisy, profile, *, resolved=None, match_precision: str = "exact"
     return out
 
 
+def stage_device(noisy, profile, stage: str, pilot=None, *, resolved=None, match_precision: str = "exact",
+                 stream=None):
+    """One filtering stage on a float32 CUDA tensor: "ht" on ``noisy``, or
+    "wiener" on ``noisy`` with ``pilot`` as the stage-1 estimate.  Returns the
+    stage estimate as a new CUDA tensor."""
+    torch = _torch()
+    shape = tuple(int(s) for s in noisy.shape)
+    if resolved is None:
+        resolved = resolve_profile(profile, shape)
+    if stage not in ("ht", "wiener"):
+        raise ValueError(f"stage must be 'ht' or 'wiener', got {stage!r}")
+    if (stage == "wiener") != (pilot is not None):
+        raise ValueError("the Wiener stage needs a pilot and the hard-thresholding stage takes none")
+    precision = _MATCH_PRECISIONS[match_precision]
+    device = noisy.device
+    L = _abi.lib()
+    if stream is None:
+        stream = torch.cuda.current_stream(device)
+    p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k, precision)
+    block = tuple(int(b) for b in getattr(profile, f"{stage}_block_size"))
+    counts = tuple(s - b + 1 for s, b in zip(shape, block))
+    sched = plan.reference_schedule(profile, counts, stage)
+    nbytes = ctypes.c_uint64(0)
+    _abi.check(L.bmnd_stage_workspace_bytes(ctypes.byref(p), len(sched), ctypes.byref(nbytes)))
+    ws = _WORKSPACE.get(device, nbytes.value)
+    out = torch.empty_like(noisy)
+    refs = _device_refs(sched, device)
+    _abi.check(L.bmnd_stage(
+        ctypes.byref(p), noisy.data_ptr(), None if pilot is None else pilot.data_ptr(), refs.data_ptr(),
+        len(sched), out.data_ptr(), None, None, None, ws.data_ptr(), ws.numel(), int(stream.cuda_stream)))
+    return out
+
+
 def bmnd(
     volume,
     profile,

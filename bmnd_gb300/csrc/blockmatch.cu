@@ -59,6 +59,7 @@ struct MatchArgs {
     int32_t use_table;  // integer-count lookup of Poisson-deviance terms
     int32_t fixup;      // only redo references whose count is negative
     int32_t approx;     // screened kernel: zero bound, the screening distances decide
+    const float2* cb;   // approx mode, volume source: (c, c + c log2 c) per voxel, or null
 };
 
 constexpr int kTable = 64;  // counts 0..63 are tabulated
@@ -464,6 +465,43 @@ __device__ __forceinline__ float2 screen_deviance_fixed(const float2* __restrict
                        kScreenAbs * ss / static_cast<float>(P) + 1e-30f);
 }
 
+// Approximate mode (no error bound): with s = r + c the deviance term is
+//   2 ln 2 [r log2(2r/s) + c log2(2c/s)] = 2 ln 2 [A_r + B_c - s log2 s],
+// A_r = r + r log2 r per reference element (ref[p].y), B_c = c + c log2 c per
+// voxel (cb[v].y), so one SFU log2 per term remains.
+__global__ void approx_voxel_kernel(const float* __restrict__ src, float inv, int64_t n, float2* __restrict__ cb) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float c = fmaxf(src[i] * inv, 0.0f);
+        cb[i] = make_float2(c, c > 0.0f ? c + c * log2f(c) : 0.0f);
+    }
+}
+
+template <int ND, int B0, int B1, int B2>
+__device__ __forceinline__ float approx_deviance_fixed(const float2* __restrict__ ref, const float2* __restrict__ cb,
+                                                       int64_t origin, int64_t s0, int64_t s1) {
+    const float kMin = 1.17549435e-38f;
+    float sum = 0.0f;
+    const float2* base = cb + origin;
+#pragma unroll 1
+    for (int a0 = 0; a0 < B0; ++a0) {
+#pragma unroll
+        for (int a1 = 0; a1 < B1; ++a1) {
+            const float2* row = ND == 3 ? base + a0 * s0 + a1 * s1 : base + a0 * s0;
+#pragma unroll
+            for (int a2 = 0; a2 < B2; ++a2) {
+                const int p = (a0 * B1 + a1) * B2 + a2;
+                const float2 cv = __ldg(row + (ND == 3 ? a2 : a1));
+                const float2 rr = ref[p];
+                const float sv = rr.x + cv.x;
+                sum += fmaf(-sv, sfu_lg2(fmaxf(sv, kMin)), rr.y + cv.y);
+            }
+        }
+    }
+    constexpr int P = B0 * B1 * B2;
+    return fmaxf(1.38629436f * sum, 0.0f) / static_cast<float>(P);
+}
+
 // exact deviance with the reference patch already scaled and clamped (.x)
 __device__ __forceinline__ float exact_deviance(const float2* __restrict__ ref, const float* __restrict__ src,
                                                 int64_t origin, const int32_t* __restrict__ poff, int P,
@@ -559,10 +597,11 @@ __global__ void __launch_bounds__(kSThreads, 8) blockmatch_screened_kernel(Match
         }
         const bool small_window = window < (int64_t(1) << 21);
         __syncthreads();  // previous reference's shared data is no longer read
+        const bool cheap = fixed && a.approx && a.cb != nullptr;
         for (int p = tid; p < P; p += blockDim.x) {
             float rv = mul_rn(__ldg(a.src + center_origin + poff_s[p]), a.inv_scale);
             if (rv < 0.0f) rv = 0.0f;
-            ref[p] = make_float2(rv, rv + rv);
+            ref[p] = make_float2(rv, cheap ? (rv > 0.0f ? rv + rv * log2f(rv) : 0.0f) : rv + rv);
         }
         for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0u;
         if (tid == 0) redi[0] = 0;  // queue length
@@ -575,9 +614,17 @@ __global__ void __launch_bounds__(kSThreads, 8) blockmatch_screened_kernel(Match
         for (int64_t c = tid; c < window; c += blockDim.x) {
             int64_t lin;
             const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
-            const float2 sd = fixed ? screen_deviance_fixed<ND, B0, B1, B2>(ref, a.src, origin, a.vstride[0],
-                                                                           a.vstride[ND > 1 ? 1 : 0], poff_s)
-                                    : screen_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
+            float2 sd;
+            if (cheap) {
+                if constexpr (ND > 0)
+                    sd = make_float2(approx_deviance_fixed<ND, B0, B1, B2>(ref, a.cb, origin, a.vstride[0],
+                                                                          a.vstride[ND > 1 ? 1 : 0]),
+                                     0.0f);
+            } else {
+                sd = fixed ? screen_deviance_fixed<ND, B0, B1, B2>(ref, a.src, origin, a.vstride[0],
+                                                                  a.vstride[ND > 1 ? 1 : 0], poff_s)
+                           : screen_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
+            }
             cand[c] = sd.x;
             dmax = fmaxf(dmax, sd.y);
         }
@@ -1156,6 +1203,25 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
         return counts ? launch_counts(a, stream) : launch_exact(a, code, stream);
     }
     size_t smem = screened_smem_bytes(a.max_m, a.P, wmax);
+    // approximate mode on a volume: per-voxel (c, c + c log2 c), stream-ordered
+    // scratch freed after the launch; without it the bounded form is used with
+    // a zero bound
+    float2* cb = nullptr;
+    if (a.approx && !a.table) {
+        int64_t nvox = 1;
+        for (int d = 0; d < a.ndim; ++d) nvox *= a.counts[d] + a.block[d] - 1;
+        if (cudaMallocAsync(reinterpret_cast<void**>(&cb), static_cast<size_t>(nvox) * sizeof(float2), stream) ==
+            cudaSuccess) {
+            int64_t bl = (nvox + 255) / 256;
+            if (bl > 152 * 16) bl = 152 * 16;
+            approx_voxel_kernel<<<static_cast<unsigned>(bl), 256, 0, stream>>>(a.src, a.inv_scale, nvox, cb);
+            BMND_LAUNCH_CHECK("approx_voxel_kernel");
+        } else {
+            (void)cudaGetLastError();
+            cb = nullptr;
+        }
+    }
+    a.cb = cb;
     int64_t blocks = a.n_refs;
     const int64_t cap = 152 * 12;
     if (blocks > cap) blocks = cap;
@@ -1176,6 +1242,8 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
         rc = run(blockmatch_screened_kernel<3, 4, 4, 4>);
     else
         rc = run(blockmatch_screened_kernel<0, 1, 1, 1>);
+    if (cb) BMND_CUDA_TRY(cudaFreeAsync(cb, stream));
+    a.cb = nullptr;
     if (rc) return rc;
     // references that need the best rejected candidates are redone exactly
     MatchArgs fix = a;

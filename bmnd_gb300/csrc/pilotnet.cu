@@ -1,0 +1,960 @@
+// pilotnet.cu -- learned stage-1 pilot: a residual convolution net in the
+// Anscombe domain.  This part has no counterpart in the reference; it stands in
+// for the hard-thresholding basic estimate on the fast path.
+//
+//   a   = 2 sqrt(max(x, 0) + 3/8)                   variance-stabilised input
+//   h_1 = relu(W_0 * a + b_0)                       1 -> C channels
+//   h_l = relu(W_{l-1} * h_{l-1} + b_{l-1})         C -> C, l = 2 .. L-1
+//   y   = a + W_{L-1} * h_{L-1} + b_{L-1}           C -> 1, residual
+//   pilot = max((y / 2)^2 - 3/8, 0)
+//
+// 3x3 (2-D) or 3x3x3 (3-D) kernels with zero padding, over a batch of
+// volumes.  Weights and hidden activations are BF16; every sum accumulates in
+// FP32.  Parameters are kept as an FP32 master copy, flat, layer by layer:
+// W_l[tap][ci][co] then b_l[co].
+//
+// The C -> C layers run on the tensor cores as an implicit GEMM
+// (mma.sync m16n8k16, BF16 in, FP32 accumulate): a persistent CTA keeps the
+// layer's weights in shared memory, pre-arranged in B-fragment order, and
+// walks output tiles of 256 voxels (16 rows of 16 along x).  Each tile's input
+// with its one-voxel halo is staged channels-last with rows padded to C + 8
+// elements, so the ldmatrix reads of the A fragments are bank-conflict free.
+// The same kernel computes a layer's data gradient with the weights flipped
+// and transposed and the layer input's ReLU mask in the epilogue.  The
+// one-channel layers, the weight gradients and the optimiser run on the CUDA
+// cores.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+#include <vector>
+
+#include "bmnd_common.cuh"
+
+namespace bmnd {
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+struct NetGeo {
+    int nb, D, H, W;  // batch, depth (1 in 2-D), height, width
+    __host__ __device__ int64_t voxels() const { return static_cast<int64_t>(nb) * D * H * W; }
+};
+
+template <int ND>
+struct Tile {
+    static constexpr int taps = ND == 3 ? 27 : 9;
+    static constexpr int tx = 16;                    // voxels per row (one m16 fragment)
+    static constexpr int ty = ND == 3 ? 8 : 16;
+    static constexpr int tz = ND == 3 ? 2 : 1;       // ty * tz = 16 rows, 256 voxels
+    static constexpr int hx = tx + 2, hy = ty + 2, hz = ND == 3 ? tz + 2 : 1;
+    static constexpr int halo = hx * hy * hz;
+};
+
+// tap t -> offsets (dz, dy, dx) in {-1, 0, 1} (dz = 0 in 2-D), C order, so
+// tap taps-1-t has the opposite offsets
+template <int ND>
+__host__ __device__ __forceinline__ void tap_offsets(int t, int& dz, int& dy, int& dx) {
+    if (ND == 3) {
+        dz = t / 9 - 1;
+        dy = (t / 3) % 3 - 1;
+        dx = t % 3 - 1;
+    } else {
+        dz = 0;
+        dy = t / 3 - 1;
+        dx = t % 3 - 1;
+    }
+}
+
+__device__ __forceinline__ int64_t vox_index(const NetGeo& g, int b, int z, int y, int x) {
+    return ((static_cast<int64_t>(b) * g.D + z) * g.H + y) * g.W + x;
+}
+
+__device__ __forceinline__ void vox_decode(const NetGeo& g, int64_t v, int& b, int& z, int& y, int& x) {
+    x = static_cast<int>(v % g.W);
+    v /= g.W;
+    y = static_cast<int>(v % g.H);
+    v /= g.H;
+    z = static_cast<int>(v % g.D);
+    b = static_cast<int>(v / g.D);
+}
+
+__device__ __forceinline__ float anscombe(float x) { return 2.0f * sqrtf(fmaxf(x, 0.0f) + 0.375f); }
+
+// ---------------------------------------------------------------------------
+// element-wise and one-channel layers (CUDA cores)
+// ---------------------------------------------------------------------------
+__global__ void anscombe_kernel(const float* __restrict__ x, float* __restrict__ a, int64_t n) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        a[i] = anscombe(x[i]);
+}
+
+// h[v][c] = relu(b[c] + sum_t w[t][c] a[v + off(t)]), C channels, 16-byte stores
+template <int ND, int C>
+__global__ void conv_in_kernel(const float* __restrict__ a, const float* __restrict__ w,
+                               const float* __restrict__ bias, bf16* __restrict__ h, NetGeo g) {
+    constexpr int T = Tile<ND>::taps;
+    __shared__ float ws[T * C], bs[C];
+    for (int i = threadIdx.x; i < T * C; i += blockDim.x) ws[i] = w[i];
+    for (int i = threadIdx.x; i < C; i += blockDim.x) bs[i] = bias[i];
+    __syncthreads();
+    const int64_t n = g.voxels();
+    for (int64_t v = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; v < n;
+         v += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int b, z, y, x;
+        vox_decode(g, v, b, z, y, x);
+        float in[T];
+#pragma unroll
+        for (int t = 0; t < T; ++t) {
+            int dz, dy, dx;
+            tap_offsets<ND>(t, dz, dy, dx);
+            const int zz = z + dz, yy = y + dy, xx = x + dx;
+            const bool inside = zz >= 0 && zz < g.D && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W;
+            in[t] = inside ? a[vox_index(g, b, zz, yy, xx)] : 0.0f;
+        }
+#pragma unroll
+        for (int c0 = 0; c0 < C; c0 += 8) {
+            float acc[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j] = bs[c0 + j];
+#pragma unroll
+            for (int t = 0; t < T; ++t)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[j] = fmaf(ws[t * C + c0 + j], in[t], acc[j]);
+            __align__(16) bf16 o[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) o[j] = __float2bfloat16_rn(fmaxf(acc[j], 0.0f));
+            *reinterpret_cast<uint4*>(h + v * C + c0) = *reinterpret_cast<const uint4*>(o);
+        }
+    }
+}
+
+// y[v] = a[v] + b + sum_t sum_c w[t][c] h[v + off(t)][c]; pilot = inverse Anscombe
+template <int ND, int C>
+__global__ void conv_out_kernel(const bf16* __restrict__ h, const float* __restrict__ w, const float* __restrict__ bias,
+                                const float* __restrict__ a, float* __restrict__ y, float* __restrict__ pilot,
+                                NetGeo g) {
+    constexpr int T = Tile<ND>::taps;
+    __shared__ float ws[T * C];
+    for (int i = threadIdx.x; i < T * C; i += blockDim.x) ws[i] = w[i];
+    __syncthreads();
+    const float b0 = bias[0];
+    const int64_t n = g.voxels();
+    for (int64_t v = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; v < n;
+         v += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int b, z, yy0, x;
+        vox_decode(g, v, b, z, yy0, x);
+        float acc = b0;
+#pragma unroll 1
+        for (int t = 0; t < T; ++t) {
+            int dz, dy, dx;
+            tap_offsets<ND>(t, dz, dy, dx);
+            const int zz = z + dz, yy = yy0 + dy, xx = x + dx;
+            if (!(zz >= 0 && zz < g.D && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W)) continue;
+            const bf16* hv = h + vox_index(g, b, zz, yy, xx) * C;
+#pragma unroll
+            for (int c0 = 0; c0 < C; c0 += 8) {
+                const uint4 raw = *reinterpret_cast<const uint4*>(hv + c0);
+                const bf16* e = reinterpret_cast<const bf16*>(&raw);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc = fmaf(ws[t * C + c0 + j], __bfloat162float(e[j]), acc);
+            }
+        }
+        const float yv = a[v] + acc;
+        if (y) y[v] = yv;
+        if (pilot) {
+            const float hv = 0.5f * yv;
+            pilot[v] = fmaxf(hv * hv - 0.375f, 0.0f);
+        }
+    }
+}
+
+// loss = mean (y - anscombe(target))^2 and its gradient with respect to y
+__global__ void loss_grad_kernel(const float* __restrict__ y, const float* __restrict__ target,
+                                 float* __restrict__ gy, int64_t n, double* __restrict__ loss) {
+    __shared__ double red[32];
+    double local = 0.0;
+    const float scale = 2.0f / static_cast<float>(n);
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float d = y[i] - anscombe(target[i]);
+        gy[i] = scale * d;
+        local += static_cast<double>(d) * d;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < static_cast<int>(blockDim.x >> 5); ++i) s += red[i];
+        atomicAdd(loss, s / static_cast<double>(n));
+    }
+}
+
+// data gradient of the last layer: gh[u][c] = (h[u][c] > 0) sum_t w[t][c] gy[u - off(t)]
+template <int ND, int C>
+__global__ void conv_out_dgrad_kernel(const float* __restrict__ gy, const float* __restrict__ w,
+                                      const bf16* __restrict__ h, bf16* __restrict__ gh, NetGeo g) {
+    constexpr int T = Tile<ND>::taps;
+    __shared__ float ws[T * C];
+    for (int i = threadIdx.x; i < T * C; i += blockDim.x) ws[i] = w[i];
+    __syncthreads();
+    const int64_t n = g.voxels();
+    for (int64_t u = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; u < n;
+         u += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int b, z, y, x;
+        vox_decode(g, u, b, z, y, x);
+        float gv[T];
+#pragma unroll
+        for (int t = 0; t < T; ++t) {
+            int dz, dy, dx;
+            tap_offsets<ND>(t, dz, dy, dx);
+            const int zz = z - dz, yy = y - dy, xx = x - dx;
+            const bool inside = zz >= 0 && zz < g.D && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W;
+            gv[t] = inside ? gy[vox_index(g, b, zz, yy, xx)] : 0.0f;
+        }
+#pragma unroll
+        for (int c0 = 0; c0 < C; c0 += 8) {
+            const uint4 raw = *reinterpret_cast<const uint4*>(h + u * C + c0);
+            const bf16* hm = reinterpret_cast<const bf16*>(&raw);
+            float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+            for (int t = 0; t < T; ++t)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[j] = fmaf(ws[t * C + c0 + j], gv[t], acc[j]);
+            __align__(16) bf16 o[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                o[j] = __float2bfloat16_rn(__bfloat162float(hm[j]) > 0.0f ? acc[j] : 0.0f);
+            *reinterpret_cast<uint4*>(gh + u * C + c0) = *reinterpret_cast<const uint4*>(o);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// C -> C layers on the tensor cores
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void ldmatrix_x4(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2,
+                                            uint32_t& r3) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+        "{%8, %9}, {%0, %1, %2, %3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+template <int ND, int C>
+struct MidSmem {
+    static constexpr int taps = Tile<ND>::taps;
+    static constexpr int kc = C / 16, nt = C / 8, cp = C + 8;
+    static constexpr size_t wfrag = static_cast<size_t>(taps) * kc * nt * 32;  // uint2 per lane
+    static constexpr size_t wbytes = wfrag * 8;
+    static constexpr size_t tbytes = static_cast<size_t>(Tile<ND>::halo) * cp * 2;
+    static constexpr size_t bytes = wbytes + tbytes;
+};
+
+// B fragment of mma.m16n8k16 (k16 x n8, "col"): lane (g = lane / 4, q = lane % 4)
+// holds B[2q][g], B[2q+1][g] in x and B[2q+8][g], B[2q+9][g] in y.  Forward:
+// B[k][n] = W[t][ci = k][co = n]; data gradient: the layer applied backwards,
+// B[k][n] = W[taps-1-t][ci = n][co = k].
+template <int ND, int C>
+__global__ void pack_mid_kernel(const float* __restrict__ W, uint2* __restrict__ out, int backward) {
+    using S = MidSmem<ND, C>;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < static_cast<int64_t>(S::wfrag);
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int lane = static_cast<int>(i % 32);
+        int64_t r = i / 32;
+        const int nt = static_cast<int>(r % S::nt);
+        r /= S::nt;
+        const int kc = static_cast<int>(r % S::kc);
+        const int t = static_cast<int>(r / S::kc);
+        const int n = nt * 8 + lane / 4;
+        const int k0 = kc * 16 + 2 * (lane % 4);
+        auto B = [&](int k) -> float {
+            return backward ? W[(static_cast<int64_t>(S::taps - 1 - t) * C + n) * C + k]
+                            : W[(static_cast<int64_t>(t) * C + k) * C + n];
+        };
+        auto pack2 = [](float lo, float hi) -> uint32_t {
+            const uint16_t l = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
+            const uint16_t h = __bfloat16_as_ushort(__float2bfloat16_rn(hi));
+            return static_cast<uint32_t>(l) | (static_cast<uint32_t>(h) << 16);
+        };
+        out[i] = make_uint2(pack2(B(k0), B(k0 + 1)), pack2(B(k0 + 8), B(k0 + 9)));
+    }
+}
+
+// out[v][co] = epi(sum_t sum_ci in[v + off(t)][ci] B_t[ci][co]) with
+// epi = relu(. + bias) (forward) or (mask[v][co] > 0 ? . : 0) (data gradient)
+template <int ND, int C>
+__global__ void __launch_bounds__(256, 1) conv_mid_kernel(const bf16* __restrict__ in, const uint2* __restrict__ wpk,
+                                                          const float* __restrict__ bias, const bf16* __restrict__ mask,
+                                                          bf16* __restrict__ out, NetGeo g) {
+    using TL = Tile<ND>;
+    using S = MidSmem<ND, C>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint2* wsm = reinterpret_cast<uint2*>(smem);
+    bf16* tile = reinterpret_cast<bf16*>(smem + S::wbytes);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (int i = tid; i < static_cast<int>(S::wfrag); i += blockDim.x) wsm[i] = wpk[i];
+
+    const int tiles_x = (g.W + TL::tx - 1) / TL::tx;
+    const int tiles_y = (g.H + TL::ty - 1) / TL::ty;
+    const int tiles_z = (g.D + TL::tz - 1) / TL::tz;
+    const int64_t ntiles = static_cast<int64_t>(tiles_x) * tiles_y * tiles_z * g.nb;
+    constexpr int chunks = C / 8;  // 16-byte chunks per voxel
+    const uint32_t tile_base = static_cast<uint32_t>(__cvta_generic_to_shared(tile));
+
+    for (int64_t tl = blockIdx.x; tl < ntiles; tl += gridDim.x) {
+        int64_t r = tl;
+        const int x0 = static_cast<int>(r % tiles_x) * TL::tx;
+        r /= tiles_x;
+        const int y0 = static_cast<int>(r % tiles_y) * TL::ty;
+        r /= tiles_y;
+        const int z0 = static_cast<int>(r % tiles_z) * TL::tz;
+        const int b = static_cast<int>(r / tiles_z);
+        __syncthreads();  // the previous tile is no longer read (and the weights are in place)
+        for (int i = tid; i < TL::halo * chunks; i += blockDim.x) {
+            const int vox = i / chunks, ch = i % chunks;
+            const int hxi = vox % TL::hx, hyi = (vox / TL::hx) % TL::hy, hzi = vox / (TL::hx * TL::hy);
+            const int xx = x0 + hxi - 1, yy = y0 + hyi - 1, zz = ND == 3 ? z0 + hzi - 1 : z0;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (xx >= 0 && xx < g.W && yy >= 0 && yy < g.H && zz >= 0 && zz < g.D)
+                v = *reinterpret_cast<const uint4*>(in + vox_index(g, b, zz, yy, xx) * C + ch * 8);
+            *reinterpret_cast<uint4*>(tile + static_cast<size_t>(vox) * S::cp + ch * 8) = v;
+        }
+        __syncthreads();
+
+        float acc[2][S::nt][4];
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int n = 0; n < S::nt; ++n)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[i][n][q] = 0.0f;
+        int rz[2], ry[2];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const int row = 2 * warp + i;
+            rz[i] = row / TL::ty;
+            ry[i] = row % TL::ty;
+        }
+#pragma unroll 1
+        for (int t = 0; t < S::taps; ++t) {
+            int dz, dy, dx;
+            tap_offsets<ND>(t, dz, dy, dx);
+            uint32_t rowaddr[2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int hzi = ND == 3 ? rz[i] + dz + 1 : 0;
+                const int vox = (hzi * TL::hy + ry[i] + dy + 1) * TL::hx + (lane & 15) + dx + 1;
+                rowaddr[i] = tile_base + static_cast<uint32_t>((vox * S::cp + (lane >> 4) * 8) * 2);
+            }
+#pragma unroll
+            for (int kc = 0; kc < S::kc; ++kc) {
+                uint2 bf[S::nt];
+#pragma unroll
+                for (int n = 0; n < S::nt; ++n) bf[n] = wsm[((t * S::kc + kc) * S::nt + n) * 32 + lane];
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    uint32_t a0, a1, a2, a3;
+                    ldmatrix_x4(rowaddr[i] + kc * 32, a0, a1, a2, a3);
+#pragma unroll
+                    for (int n = 0; n < S::nt; ++n) mma_bf16(acc[i][n], a0, a1, a2, a3, bf[n].x, bf[n].y);
+                }
+            }
+        }
+        // epilogue: acc[i][n][q] is (row m = lane/4 + 8 (q/2), channel n*8 + 2 (lane%4) + q%2)
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const int zz = z0 + rz[i], yy = y0 + ry[i];
+            if (zz >= g.D || yy >= g.H) continue;
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+                const int xx = x0 + lane / 4 + 8 * hh;
+                if (xx >= g.W) continue;
+                const int64_t v = vox_index(g, b, zz, yy, xx);
+#pragma unroll
+                for (int n = 0; n < S::nt; ++n) {
+                    const int co = n * 8 + 2 * (lane % 4);
+                    float v0 = acc[i][n][2 * hh], v1 = acc[i][n][2 * hh + 1];
+                    if (mask) {
+                        const __nv_bfloat162 m2 = *reinterpret_cast<const __nv_bfloat162*>(mask + v * C + co);
+                        v0 = __low2float(m2) > 0.0f ? v0 : 0.0f;
+                        v1 = __high2float(m2) > 0.0f ? v1 : 0.0f;
+                    } else {
+                        v0 = fmaxf(v0 + bias[co], 0.0f);
+                        v1 = fmaxf(v1 + bias[co + 1], 0.0f);
+                    }
+                    *reinterpret_cast<__nv_bfloat162*>(out + v * C + co) = __floats2bfloat162_rn(v0, v1);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// weight gradients (CUDA cores): per-CTA partial sums over a tile of 256
+// voxels, summed over CTAs by reduce_partials_kernel
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ float to_f(T v);
+template <>
+__device__ __forceinline__ float to_f<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ float to_f<bf16>(bf16 v) { return __bfloat162float(v); }
+
+template <int ND, int CIN, int COUT, typename TI, typename TG>
+struct WgradSmem {
+    static constexpr size_t in_floats = static_cast<size_t>(Tile<ND>::halo) * CIN;
+    static constexpr size_t g_floats = 256 * static_cast<size_t>(COUT);
+    static constexpr size_t bytes = (in_floats + g_floats) * 4;
+};
+
+// partial[cta][p]: p = (t * CIN + ci) * COUT + co for the weights, then
+// T * CIN * COUT + co for the bias
+template <int ND, int CIN, int COUT, typename TI, typename TG>
+__global__ void __launch_bounds__(256) wgrad_kernel(const TI* __restrict__ in, const TG* __restrict__ gout,
+                                                    float* __restrict__ partial, NetGeo g) {
+    using TL = Tile<ND>;
+    constexpr int T = TL::taps;
+    constexpr int BI = CIN >= 4 ? 4 : 1, BO = COUT >= 4 ? 4 : 1;
+    constexpr int nw_items = T * (CIN / BI) * (COUT / BO);
+    constexpr int nitems = nw_items + COUT / BO;
+    constexpr int nparams = T * CIN * COUT + COUT;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* sin = reinterpret_cast<float*>(smem);
+    float* sg = sin + static_cast<size_t>(TL::halo) * CIN;
+    const int tiles_x = (g.W + TL::tx - 1) / TL::tx;
+    const int tiles_y = (g.H + TL::ty - 1) / TL::ty;
+    const int tiles_z = (g.D + TL::tz - 1) / TL::tz;
+    int64_t r = blockIdx.x;
+    const int x0 = static_cast<int>(r % tiles_x) * TL::tx;
+    r /= tiles_x;
+    const int y0 = static_cast<int>(r % tiles_y) * TL::ty;
+    r /= tiles_y;
+    const int z0 = static_cast<int>(r % tiles_z) * TL::tz;
+    const int b = static_cast<int>(r / tiles_z);
+    for (int i = threadIdx.x; i < TL::halo * CIN; i += blockDim.x) {
+        const int vox = i / CIN, c = i % CIN;
+        const int hxi = vox % TL::hx, hyi = (vox / TL::hx) % TL::hy, hzi = vox / (TL::hx * TL::hy);
+        const int xx = x0 + hxi - 1, yy = y0 + hyi - 1, zz = ND == 3 ? z0 + hzi - 1 : z0;
+        float v = 0.0f;
+        if (xx >= 0 && xx < g.W && yy >= 0 && yy < g.H && zz >= 0 && zz < g.D)
+            v = to_f<TI>(in[vox_index(g, b, zz, yy, xx) * CIN + c]);
+        sin[i] = v;
+    }
+    for (int i = threadIdx.x; i < 256 * COUT; i += blockDim.x) {
+        const int m = i / COUT, c = i % COUT;
+        const int xx = x0 + m % TL::tx, yy = y0 + (m / TL::tx) % TL::ty, zz = z0 + m / (TL::tx * TL::ty);
+        float v = 0.0f;
+        if (xx < g.W && yy < g.H && zz < g.D) v = to_f<TG>(gout[vox_index(g, b, zz, yy, xx) * COUT + c]);
+        sg[i] = v;
+    }
+    __syncthreads();
+    float* out = partial + static_cast<int64_t>(blockIdx.x) * nparams;
+    for (int item = threadIdx.x; item < nitems; item += blockDim.x) {
+        float acc[BI][BO];
+#pragma unroll
+        for (int i = 0; i < BI; ++i)
+#pragma unroll
+            for (int o = 0; o < BO; ++o) acc[i][o] = 0.0f;
+        if (item < nw_items) {
+            const int cob = item % (COUT / BO);
+            const int cib = (item / (COUT / BO)) % (CIN / BI);
+            const int t = item / ((COUT / BO) * (CIN / BI));
+            int dz, dy, dx;
+            tap_offsets<ND>(t, dz, dy, dx);
+            for (int m = 0; m < 256; ++m) {
+                const int mx = m % TL::tx, my = (m / TL::tx) % TL::ty, mz = m / (TL::tx * TL::ty);
+                const int hz = ND == 3 ? mz + dz + 1 : 0;
+                const int vox = (hz * TL::hy + my + dy + 1) * TL::hx + mx + dx + 1;
+                float iv[BI], gv[BO];
+#pragma unroll
+                for (int i = 0; i < BI; ++i) iv[i] = sin[vox * CIN + cib * BI + i];
+#pragma unroll
+                for (int o = 0; o < BO; ++o) gv[o] = sg[m * COUT + cob * BO + o];
+#pragma unroll
+                for (int i = 0; i < BI; ++i)
+#pragma unroll
+                    for (int o = 0; o < BO; ++o) acc[i][o] = fmaf(iv[i], gv[o], acc[i][o]);
+            }
+#pragma unroll
+            for (int i = 0; i < BI; ++i)
+#pragma unroll
+                for (int o = 0; o < BO; ++o)
+                    out[(t * CIN + cib * BI + i) * COUT + cob * BO + o] = acc[i][o];
+        } else {
+            const int cob = item - nw_items;
+            for (int m = 0; m < 256; ++m)
+#pragma unroll
+                for (int o = 0; o < BO; ++o) acc[0][o] += sg[m * COUT + cob * BO + o];
+#pragma unroll
+            for (int o = 0; o < BO; ++o) out[T * CIN * COUT + cob * BO + o] = acc[0][o];
+        }
+    }
+}
+
+__global__ void reduce_partials_kernel(const float* __restrict__ partial, int64_t nparts, int64_t nparams,
+                                       float* __restrict__ grad) {
+    for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < nparams;
+         p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float s = 0.0f;
+        for (int64_t c = 0; c < nparts; ++c) s += partial[c * nparams + p];
+        grad[p] = s;
+    }
+}
+
+__global__ void round_bf16_kernel(const float* __restrict__ src, float* __restrict__ dst, int64_t n) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        dst[i] = __bfloat162float(__float2bfloat16_rn(src[i]));
+}
+
+__global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ grad, float* __restrict__ m,
+                            float* __restrict__ v, int64_t n, float lr, float b1, float b2, float eps, float bc1,
+                            float bc2) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float gi = grad[i];
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// residual check for the per-tile fallback: for each tile of edge `edge`
+// (cubes in 3-D, squares in 2-D) the observed Poisson deviance of the input
+// against the pilot, sum_v 2 [x ln(x / mu) - (x - mu)], and its expectation and
+// variance under Poisson noise of mean mu (interpolated in ln mu from a table
+// of n points starting at ln_mu0 with step d_ln).  out[tile] = (observed,
+// expected, variance) in float64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void table_lookup(const float* __restrict__ table, int n, float ln_mu0, float d_ln,
+                                             float mu, float& e, float& var) {
+    float f = (logf(fmaxf(mu, 1e-30f)) - ln_mu0) / d_ln;
+    f = fminf(fmaxf(f, 0.0f), static_cast<float>(n - 1));
+    const int i = min(static_cast<int>(f), n - 2);
+    const float w = f - static_cast<float>(i);
+    e = (1.0f - w) * table[i] + w * table[i + 1];
+    var = (1.0f - w) * table[n + i] + w * table[n + i + 1];
+}
+
+__global__ void tile_deviance_kernel(const float* __restrict__ x, const float* __restrict__ mu, NetGeo g, int edge,
+                                     const float* __restrict__ table, int n, float ln_mu0, float d_ln,
+                                     double* __restrict__ out, int tiles_x, int tiles_y, int tiles_z) {
+    __shared__ double red[3][32];
+    const int tile = blockIdx.x;
+    int r = tile;
+    const int tx = r % tiles_x;
+    r /= tiles_x;
+    const int ty = r % tiles_y;
+    r /= tiles_y;
+    const int tz = r % tiles_z;
+    const int b = r / tiles_z;
+    const int ez = g.D > 1 ? edge : 1;
+    double obs = 0.0, ex = 0.0, va = 0.0;
+    for (int i = threadIdx.x; i < ez * edge * edge; i += blockDim.x) {
+        const int xx = tx * edge + i % edge, yy = ty * edge + (i / edge) % edge, zz = tz * ez + i / (edge * edge);
+        if (xx >= g.W || yy >= g.H || zz >= g.D) continue;
+        const int64_t v = vox_index(g, b, zz, yy, xx);
+        const float xv = fmaxf(x[v], 0.0f), m = fmaxf(mu[v], 1e-6f);
+        const float d = 2.0f * ((xv > 0.0f ? xv * logf(xv / m) : 0.0f) - (xv - m));
+        float e, vr;
+        table_lookup(table, n, ln_mu0, d_ln, m, e, vr);
+        obs += d;
+        ex += e;
+        va += vr;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        obs += __shfl_xor_sync(0xffffffffu, obs, o);
+        ex += __shfl_xor_sync(0xffffffffu, ex, o);
+        va += __shfl_xor_sync(0xffffffffu, va, o);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        red[0][w] = obs;
+        red[1][w] = ex;
+        red[2][w] = va;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double s = 0.0;
+        for (int i = 0; i < static_cast<int>(blockDim.x >> 5); ++i) s += red[threadIdx.x][i];
+        out[static_cast<int64_t>(tile) * 3 + threadIdx.x] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct NetPlan {
+    int nd, C, L, taps;
+    NetGeo geo;
+    // flat FP32 parameter offsets (floats) of W_l and b_l
+    std::vector<int64_t> w_off, b_off;
+    int64_t nparams;
+    // packed buffer offsets (bytes): bf16-rounded FP32 copies of the
+    // one-channel layers, fragment-packed BF16 of the mid layers (forward and
+    // data gradient), FP32 biases
+    uint64_t p_in_w, packed_bytes;
+    std::vector<uint64_t> p_mid_fwd, p_mid_bwd;
+    uint64_t mid_frag_bytes;
+    int64_t max_layer_params;
+};
+
+int32_t make_plan(const BmndPilotNet* net, NetPlan& P) {
+    if (!net) return fail(BMND_ERR_INVALID_ARG, "null network descriptor");
+    if (net->ndim != 2 && net->ndim != 3) return fail(BMND_ERR_INVALID_ARG, "pilot net ndim must be 2 or 3");
+    if (!(net->channels == 32 || net->channels == 48))
+        return fail(BMND_ERR_UNSUPPORTED, "pilot net channels must be 32 or 48");
+    if (net->layers < 3 || net->layers > 32) return fail(BMND_ERR_INVALID_ARG, "pilot net layers must be in [3, 32]");
+    if (net->batch < 1) return fail(BMND_ERR_INVALID_ARG, "pilot net batch must be positive");
+    P.nd = net->ndim;
+    P.C = net->channels;
+    P.L = net->layers;
+    P.taps = net->ndim == 3 ? 27 : 9;
+    P.geo.nb = net->batch;
+    P.geo.D = net->ndim == 3 ? net->shape[0] : 1;
+    P.geo.H = net->ndim == 3 ? net->shape[1] : net->shape[0];
+    P.geo.W = net->ndim == 3 ? net->shape[2] : net->shape[1];
+    if (P.geo.D < 1 || P.geo.H < 1 || P.geo.W < 1) return fail(BMND_ERR_INVALID_ARG, "pilot net shape must be positive");
+    if (P.geo.voxels() > (int64_t(1) << 40)) return fail(BMND_ERR_UNSUPPORTED, "pilot net volume too large");
+    P.w_off.clear();
+    P.b_off.clear();
+    int64_t off = 0;
+    P.max_layer_params = 0;
+    for (int l = 0; l < P.L; ++l) {
+        const int cin = l == 0 ? 1 : P.C, cout = l == P.L - 1 ? 1 : P.C;
+        P.w_off.push_back(off);
+        off += static_cast<int64_t>(P.taps) * cin * cout;
+        P.b_off.push_back(off);
+        off += cout;
+        const int64_t lp = static_cast<int64_t>(P.taps) * cin * cout + cout;
+        if (lp > P.max_layer_params) P.max_layer_params = lp;
+    }
+    P.nparams = off;
+    // packed layout
+    auto a256 = [](uint64_t v) { return (v + 255) & ~uint64_t(255); };
+    uint64_t po = 0;
+    P.p_in_w = po;  // bf16-rounded copy of the whole FP32 parameter vector
+    po = a256(po + 4ull * static_cast<uint64_t>(P.nparams));
+    P.mid_frag_bytes = static_cast<uint64_t>(P.taps) * (P.C / 16) * (P.C / 8) * 32 * 8;
+    P.p_mid_fwd.clear();
+    P.p_mid_bwd.clear();
+    for (int l = 1; l < P.L - 1; ++l) {
+        P.p_mid_fwd.push_back(po);
+        po = a256(po + P.mid_frag_bytes);
+        P.p_mid_bwd.push_back(po);
+        po = a256(po + P.mid_frag_bytes);
+    }
+    P.packed_bytes = po;
+    return BMND_OK;
+}
+
+int launch_blocks(int64_t n, int threads) {
+    int64_t blocks = (n + threads - 1) / threads;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    if (blocks < 1) blocks = 1;
+    return static_cast<int>(blocks);
+}
+
+struct Bufs {
+    float* a;            // Anscombe input
+    float* y;            // network output (Anscombe domain)
+    float* gy;           // its gradient
+    bf16* act;           // hidden activations, (L - 1) x voxels x C (training) or 2 (inference)
+    bf16* grad[2];       // hidden gradients, ping-pong
+    float* partial;      // weight-gradient partial sums
+    uint64_t bytes;
+};
+
+Bufs carve_ws(const NetPlan& P, bool training, void* base) {
+    Bufs B{};
+    uint64_t off = 0;
+    auto take = [&](uint64_t bytes) {
+        uint64_t o = off;
+        off += (bytes + 255) & ~uint64_t(255);
+        return o;
+    };
+    const uint64_t nv = static_cast<uint64_t>(P.geo.voxels());
+    const uint64_t hbytes = nv * P.C * 2;
+    const uint64_t o_a = take(nv * 4);
+    const uint64_t o_y = take(nv * 4);
+    const uint64_t o_gy = training ? take(nv * 4) : 0;
+    const uint64_t o_act = take(hbytes * (training ? (P.L - 1) : 2));
+    const uint64_t o_g0 = training ? take(hbytes) : 0;
+    const uint64_t o_g1 = training ? take(hbytes) : 0;
+    const int64_t tiles = [&] {
+        const int tx = 16, ty = P.nd == 3 ? 8 : 16, tz = P.nd == 3 ? 2 : 1;
+        return static_cast<int64_t>((P.geo.W + tx - 1) / tx) * ((P.geo.H + ty - 1) / ty) *
+               ((P.geo.D + tz - 1) / tz) * P.geo.nb;
+    }();
+    const uint64_t o_part = training ? take(static_cast<uint64_t>(tiles) * P.max_layer_params * 4) : 0;
+    B.bytes = off;
+    if (base) {
+        char* c = static_cast<char*>(base);
+        B.a = reinterpret_cast<float*>(c + o_a);
+        B.y = reinterpret_cast<float*>(c + o_y);
+        B.gy = training ? reinterpret_cast<float*>(c + o_gy) : nullptr;
+        B.act = reinterpret_cast<bf16*>(c + o_act);
+        B.grad[0] = training ? reinterpret_cast<bf16*>(c + o_g0) : nullptr;
+        B.grad[1] = training ? reinterpret_cast<bf16*>(c + o_g1) : nullptr;
+        B.partial = training ? reinterpret_cast<float*>(c + o_part) : nullptr;
+    }
+    return B;
+}
+
+template <int ND, int C>
+int32_t run_mid(const bf16* in, const uint2* wpk, const float* bias, const bf16* mask, bf16* out, NetGeo g,
+                cudaStream_t stream) {
+    using S = MidSmem<ND, C>;
+    auto kernel = conv_mid_kernel<ND, C>;
+    BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(S::bytes)));
+    int dev = 0, sms = 0, per_sm = 0;
+    BMND_CUDA_TRY(cudaGetDevice(&dev));
+    BMND_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    BMND_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, S::bytes));
+    if (per_sm < 1) return fail(BMND_ERR_UNSUPPORTED, "pilot net layer does not fit on an SM");
+    using TL = Tile<ND>;
+    const int64_t ntiles = static_cast<int64_t>((g.W + TL::tx - 1) / TL::tx) * ((g.H + TL::ty - 1) / TL::ty) *
+                           ((g.D + TL::tz - 1) / TL::tz) * g.nb;
+    int64_t blocks = static_cast<int64_t>(sms) * per_sm;
+    if (blocks > ntiles) blocks = ntiles;
+    kernel<<<static_cast<unsigned>(blocks), 256, S::bytes, stream>>>(in, wpk, bias, mask, out, g);
+    BMND_LAUNCH_CHECK("conv_mid_kernel");
+    return BMND_OK;
+}
+
+template <int ND, int C>
+int32_t forward_impl(const NetPlan& P, const unsigned char* packed, const float* noisy, float* pilot, float* y_out,
+                     Bufs& B, bool keep_all, cudaStream_t stream) {
+    const NetGeo g = P.geo;
+    const int64_t nv = g.voxels();
+    const float* wr = reinterpret_cast<const float*>(packed + P.p_in_w);  // bf16-rounded parameters
+    const int eb = launch_blocks(nv, 256);
+    anscombe_kernel<<<eb, 256, 0, stream>>>(noisy, B.a, nv);
+    BMND_LAUNCH_CHECK("anscombe_kernel");
+    auto act = [&](int l) -> bf16* {  // hidden activation h_{l+1} (output of layer l)
+        const int64_t stride = nv * C;
+        return B.act + (keep_all ? l : (l & 1)) * stride;
+    };
+    conv_in_kernel<ND, C><<<eb, 256, 0, stream>>>(B.a, wr + P.w_off[0], wr + P.b_off[0], act(0), g);
+    BMND_LAUNCH_CHECK("conv_in_kernel");
+    for (int l = 1; l < P.L - 1; ++l) {
+        const uint2* wpk = reinterpret_cast<const uint2*>(packed + P.p_mid_fwd[l - 1]);
+        int32_t rc = run_mid<ND, C>(act(l - 1), wpk, wr + P.b_off[l], nullptr, act(l), g, stream);
+        if (rc) return rc;
+    }
+    conv_out_kernel<ND, C><<<eb, 256, 0, stream>>>(act(P.L - 2), wr + P.w_off[P.L - 1], wr + P.b_off[P.L - 1], B.a,
+                                                   y_out, pilot, g);
+    BMND_LAUNCH_CHECK("conv_out_kernel");
+    return BMND_OK;
+}
+
+template <int ND, int CIN, int COUT, typename TI, typename TG>
+int32_t run_wgrad(const TI* in, const TG* gout, float* partial, float* grad, int64_t tiles, NetGeo g,
+                  cudaStream_t stream) {
+    using S = WgradSmem<ND, CIN, COUT, TI, TG>;
+    auto kernel = wgrad_kernel<ND, CIN, COUT, TI, TG>;
+    BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(S::bytes)));
+    kernel<<<static_cast<unsigned>(tiles), 256, S::bytes, stream>>>(in, gout, partial, g);
+    BMND_LAUNCH_CHECK("wgrad_kernel");
+    constexpr int64_t np = static_cast<int64_t>(Tile<ND>::taps) * CIN * COUT + COUT;
+    reduce_partials_kernel<<<launch_blocks(np, 256), 256, 0, stream>>>(partial, tiles, np, grad);
+    BMND_LAUNCH_CHECK("reduce_partials_kernel");
+    return BMND_OK;
+}
+
+template <int ND, int C>
+int32_t gradient_impl(const NetPlan& P, const unsigned char* packed, const float* noisy, const float* target,
+                      float* grad, double* loss, Bufs& B, cudaStream_t stream) {
+    const NetGeo g = P.geo;
+    const int64_t nv = g.voxels();
+    int32_t rc = forward_impl<ND, C>(P, packed, noisy, nullptr, B.y, B, true, stream);
+    if (rc) return rc;
+    const float* wr = reinterpret_cast<const float*>(packed + P.p_in_w);
+    const int eb = launch_blocks(nv, 256);
+    BMND_CUDA_TRY(cudaMemsetAsync(loss, 0, sizeof(double), stream));
+    loss_grad_kernel<<<eb, 256, 0, stream>>>(B.y, target, B.gy, nv, loss);
+    BMND_LAUNCH_CHECK("loss_grad_kernel");
+    using TL = Tile<ND>;
+    const int64_t tiles = static_cast<int64_t>((g.W + TL::tx - 1) / TL::tx) * ((g.H + TL::ty - 1) / TL::ty) *
+                          ((g.D + TL::tz - 1) / TL::tz) * g.nb;
+    const int64_t stride = nv * C;
+    auto act = [&](int l) -> bf16* { return B.act + l * stride; };
+    const int L = P.L;
+    // last layer: weight gradient from h_{L-1} and gy, data gradient into h_{L-1}
+    rc = run_wgrad<ND, C, 1, bf16, float>(act(L - 2), B.gy, B.partial, grad + P.w_off[L - 1], tiles, g, stream);
+    if (rc) return rc;
+    int cur = 0;
+    conv_out_dgrad_kernel<ND, C><<<eb, 256, 0, stream>>>(B.gy, wr + P.w_off[L - 1], act(L - 2), B.grad[cur], g);
+    BMND_LAUNCH_CHECK("conv_out_dgrad_kernel");
+    // mid layers, last to first: B.grad[cur] is the gradient of layer l's output
+    for (int l = L - 2; l >= 1; --l) {
+        rc = run_wgrad<ND, C, C, bf16, bf16>(act(l - 1), B.grad[cur], B.partial, grad + P.w_off[l], tiles, g, stream);
+        if (rc) return rc;
+        const uint2* wpk = reinterpret_cast<const uint2*>(packed + P.p_mid_bwd[l - 1]);
+        rc = run_mid<ND, C>(B.grad[cur], wpk, nullptr, act(l - 1), B.grad[cur ^ 1], g, stream);
+        if (rc) return rc;
+        cur ^= 1;
+    }
+    // first layer: weight gradient only
+    return run_wgrad<ND, 1, C, float, bf16>(B.a, B.grad[cur], B.partial, grad + P.w_off[0], tiles, g, stream);
+}
+
+template <typename F>
+int32_t dispatch(const NetPlan& P, F&& f) {
+    if (P.nd == 3 && P.C == 48) return f(std::integral_constant<int, 3>{}, std::integral_constant<int, 48>{});
+    if (P.nd == 3 && P.C == 32) return f(std::integral_constant<int, 3>{}, std::integral_constant<int, 32>{});
+    if (P.nd == 2 && P.C == 48) return f(std::integral_constant<int, 2>{}, std::integral_constant<int, 48>{});
+    return f(std::integral_constant<int, 2>{}, std::integral_constant<int, 32>{});
+}
+
+}  // namespace
+}  // namespace bmnd
+
+using namespace bmnd;
+
+extern "C" {
+
+int32_t bmnd_pilotnet_param_count(const BmndPilotNet* net, int64_t* count) {
+    clear_error();
+    NetPlan P;
+    if (int32_t rc = make_plan(net, P)) return rc;
+    if (!count) return fail(BMND_ERR_INVALID_ARG, "null output");
+    *count = P.nparams;
+    return BMND_OK;
+}
+
+int32_t bmnd_pilotnet_packed_bytes(const BmndPilotNet* net, uint64_t* bytes) {
+    clear_error();
+    NetPlan P;
+    if (int32_t rc = make_plan(net, P)) return rc;
+    if (!bytes) return fail(BMND_ERR_INVALID_ARG, "null output");
+    *bytes = P.packed_bytes;
+    return BMND_OK;
+}
+
+int32_t bmnd_pilotnet_workspace_bytes(const BmndPilotNet* net, int32_t training, uint64_t* bytes) {
+    clear_error();
+    NetPlan P;
+    if (int32_t rc = make_plan(net, P)) return rc;
+    if (!bytes) return fail(BMND_ERR_INVALID_ARG, "null output");
+    *bytes = carve_ws(P, training != 0, nullptr).bytes;
+    return BMND_OK;
+}
+
+int32_t bmnd_pilotnet_pack(const BmndPilotNet* net, const float* d_params, void* d_packed, uint64_t stream_u64) {
+    clear_error();
+    NetPlan P;
+    if (int32_t rc = make_plan(net, P)) return rc;
+    if (!d_params || !d_packed) return fail(BMND_ERR_INVALID_ARG, "null buffer");
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_u64);
+    unsigned char* pk = static_cast<unsigned char*>(d_packed);
+    round_bf16_kernel<<<launch_blocks(P.nparams, 256), 256, 0, stream>>>(
+        d_params, reinterpret_cast<float*>(pk + P.p_in_w), P.nparams);
+    BMND_LAUNCH_CHECK("round_bf16_kernel");
+    return dispatch(P, [&](auto nd, auto c) -> int32_t {
+        constexpr int ND = decltype(nd)::value, C = decltype(c)::value;
+        const int64_t nfrag = static_cast<int64_t>(MidSmem<ND, C>::wfrag);
+        for (int l = 1; l < P.L - 1; ++l) {
+            pack_mid_kernel<ND, C><<<launch_blocks(nfrag, 256), 256, 0, stream>>>(
+                d_params + P.w_off[l], reinterpret_cast<uint2*>(pk + P.p_mid_fwd[l - 1]), 0);
+            BMND_LAUNCH_CHECK("pack_mid_kernel");
+            pack_mid_kernel<ND, C><<<launch_blocks(nfrag, 256), 256, 0, stream>>>(
+                d_params + P.w_off[l], reinterpret_cast<uint2*>(pk + P.p_mid_bwd[l - 1]), 1);
+            BMND_LAUNCH_CHECK("pack_mid_kernel");
+        }
+        return BMND_OK;
+    });
+}
+
+int32_t bmnd_pilotnet_forward(const BmndPilotNet* net, const void* d_packed, const float* d_noisy, float* d_pilot,
+                              float* d_y, void* d_ws, uint64_t ws_bytes, uint64_t stream_u64) {
+    clear_error();
+    NetPlan P;
+    if (int32_t rc = make_plan(net, P)) return rc;
+    if (!d_packed || !d_noisy || (!d_pilot && !d_y) || !d_ws) return fail(BMND_ERR_INVALID_ARG, "null buffer");
+    Bufs B = carve_ws(P, false, nullptr);
+    if (ws_bytes < B.bytes) return fail(BMND_ERR_WORKSPACE, "pilot net workspace too small");
+    B = carve_ws(P, false, d_ws);
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_u64);
+    const unsigned char* pk = static_cast<const unsigned char*>(d_packed);
+    return dispatch(P, [&](auto nd, auto c) -> int32_t {
+        return forward_impl<decltype(nd)::value, decltype(c)::value>(P, pk, d_noisy, d_pilot, d_y, B, false, stream);
+    });
+}
+
+int32_t bmnd_pilotnet_gradient(const BmndPilotNet* net, const void* d_packed, const float* d_noisy,
+                               const float* d_target, float* d_grad, double* d_loss, void* d_ws, uint64_t ws_bytes,
+                               uint64_t stream_u64) {
+    clear_error();
+    NetPlan P;
+    if (int32_t rc = make_plan(net, P)) return rc;
+    if (!d_packed || !d_noisy || !d_target || !d_grad || !d_loss || !d_ws)
+        return fail(BMND_ERR_INVALID_ARG, "null buffer");
+    Bufs B = carve_ws(P, true, nullptr);
+    if (ws_bytes < B.bytes) return fail(BMND_ERR_WORKSPACE, "pilot net workspace too small");
+    B = carve_ws(P, true, d_ws);
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_u64);
+    const unsigned char* pk = static_cast<const unsigned char*>(d_packed);
+    return dispatch(P, [&](auto nd, auto c) -> int32_t {
+        return gradient_impl<decltype(nd)::value, decltype(c)::value>(P, pk, d_noisy, d_target, d_grad, d_loss, B,
+                                                                      stream);
+    });
+}
+
+int32_t bmnd_pilot_tile_deviance(int32_t ndim, int32_t batch, const int32_t* shape, int32_t edge,
+                                 const float* d_noisy, const float* d_pilot, const float* d_table, int32_t n_table,
+                                 float ln_mu0, float d_ln, double* d_out, uint64_t stream_u64) {
+    clear_error();
+    if ((ndim != 2 && ndim != 3) || batch < 1 || !shape || edge < 1 || n_table < 2 || !(d_ln > 0.0f))
+        return fail(BMND_ERR_INVALID_ARG, "bad tile-deviance arguments");
+    if (!d_noisy || !d_pilot || !d_table || !d_out) return fail(BMND_ERR_INVALID_ARG, "null buffer");
+    NetGeo g;
+    g.nb = batch;
+    g.D = ndim == 3 ? shape[0] : 1;
+    g.H = ndim == 3 ? shape[1] : shape[0];
+    g.W = ndim == 3 ? shape[2] : shape[1];
+    if (g.D < 1 || g.H < 1 || g.W < 1) return fail(BMND_ERR_INVALID_ARG, "shape must be positive");
+    const int tx = (g.W + edge - 1) / edge, ty = (g.H + edge - 1) / edge;
+    const int tz = ndim == 3 ? (g.D + edge - 1) / edge : 1;
+    const int64_t tiles = static_cast<int64_t>(tx) * ty * tz * batch;
+    if (tiles > 0x7fffffffLL) return fail(BMND_ERR_UNSUPPORTED, "too many tiles");
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_u64);
+    tile_deviance_kernel<<<static_cast<unsigned>(tiles), 256, 0, stream>>>(d_noisy, d_pilot, g, edge, d_table, n_table,
+                                                                          ln_mu0, d_ln, d_out, tx, ty, tz);
+    BMND_LAUNCH_CHECK("tile_deviance_kernel");
+    return BMND_OK;
+}
+
+int32_t bmnd_pilotnet_adam(int64_t n, float* d_params, const float* d_grad, float* d_m, float* d_v, int32_t step,
+                           float lr, float beta1, float beta2, float eps, uint64_t stream_u64) {
+    clear_error();
+    if (n < 0 || !d_params || !d_grad || !d_m || !d_v) return fail(BMND_ERR_INVALID_ARG, "bad Adam arguments");
+    if (step < 1) return fail(BMND_ERR_INVALID_ARG, "Adam step counts from 1");
+    const float bc1 = 1.0f - powf(beta1, static_cast<float>(step));
+    const float bc2 = 1.0f - powf(beta2, static_cast<float>(step));
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_u64);
+    adam_kernel<<<launch_blocks(n, 256), 256, 0, stream>>>(d_params, d_grad, d_m, d_v, n, lr, beta1, beta2, eps, bc1,
+                                                           bc2);
+    BMND_LAUNCH_CHECK("adam_kernel");
+    return BMND_OK;
+}
+
+}  // extern "C"

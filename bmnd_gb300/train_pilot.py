@@ -1,0 +1,110 @@
+"""Train the learned stage-1 pilot on the GPU and evaluate the fast path.
+
+    python -m bmnd_gb300.train_pilot --kind bm4d --out bmnd_gb300/weights/pilot_bm4d.npz
+
+Training pairs are (noisy phantom, plain stage-1 estimate) produced by this
+package's own GPU path on seeded synthetic phantoms (seeds 1000 + i); the
+held-out evaluation volume uses seed 2000, the benchmark seeds 0 .. 7.  The
+net's forward and backward passes are the kernels of ``csrc/pilotnet.cu``.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import time
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--kind", default="bm4d", choices=["bm4d", "bm3d"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--count", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--crop", type=int, default=32)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--lr", type=float, default=3e-4)
+    ap.add_argument("--channels", type=int, default=None)
+    ap.add_argument("--layers", type=int, default=None)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--out", default=None)
+    args = ap.parse_args(argv)
+
+    import numpy as np
+    import torch
+
+    import bmnd_gb300 as bg
+    from bmnd_gb300 import phantoms
+    from bmnd_gb300.api import stage_device
+    from bmnd_gb300.pilot import (PilotNet, bmnd_fast, calibrate_excess_high, default_net_path, fast_profile,
+                                  training_pairs)
+
+    torch.cuda.set_device(0)
+    nd = 3 if args.kind == "bm4d" else 2
+    channels = args.channels or (48 if nd == 3 else 32)
+    layers = args.layers or (8 if nd == 3 else 10)
+    crop = args.crop if nd == 3 else max(args.crop, 64)
+    t0 = time.time()
+    pairs = training_pairs(args.kind, args.size, args.count)
+    torch.cuda.synchronize()
+    t_data = time.time() - t0
+    net = PilotNet(nd, channels, layers, seed=args.seed)
+    t0 = time.time()
+    hist = net.fit(pairs, steps=args.steps, crop=crop, batch=args.batch, lr=args.lr, seed=args.seed,
+                   log_every=max(args.steps // 20, 1), log=lambda m: print(m, flush=True))
+    torch.cuda.synchronize()
+    t_train = time.time() - t0
+    net.excess_high = calibrate_excess_high(pairs)
+    from bmnd_gb300.pilot import tile_excess
+
+    ev = np.concatenate([np.ravel(tile_excess(x, t, 32)[0]) for x, t in pairs])
+    print(f"plain stage-1 tile excess: min {ev.min():.4f} median {np.median(ev):.4f} max {ev.max():.4f}", flush=True)
+    out = args.out or default_net_path(args.kind)
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    net.save(out)
+
+    # held-out evaluation: pilot quality and the fast path against the plain path
+    prof = (bg.BM4DProfile if nd == 3 else bg.BM3DProfile)(noise_model=bg.NoiseModel.POISSON)
+    if nd == 3:
+        clean, noisy = phantoms.ellipsoids_3d(args.size, seed=2000)
+    else:
+        clean, noisy = phantoms.shapes_2d(args.size, seed=2000)
+    x = torch.from_numpy(noisy).cuda()
+    def timed(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            r = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return r, e0.elapsed_time(e1) / reps
+
+    plain_pilot = stage_device(x, prof, "ht")
+    plain, ms_plain = timed(lambda: bg.bmnd_device(x, prof))
+    d = {}
+    fast, ms_fast = timed(lambda: bmnd_fast(x, prof, net, details=d))
+    nocheck, ms_nocheck = timed(lambda: bmnd_fast(x, prof, net, check=False))
+    plainpilot_fast = stage_device(x, fast_profile(prof), "wiener", plain_pilot, match_precision="approx")
+    learned_pilot, ms_net = timed(lambda: net.forward(x))
+    r = dict(
+        data_seconds=t_data, train_seconds=t_train, steps=args.steps, crop=crop, batch=args.batch,
+        loss_first=hist[0][1], loss_last=hist[-1][1],
+        psnr_noisy=phantoms.psnr(noisy, clean),
+        psnr_plain_stage1=phantoms.psnr(plain_pilot.cpu().numpy(), clean),
+        psnr_learned_pilot=phantoms.psnr(learned_pilot.cpu().numpy(), clean),
+        psnr_learned_pilot_vs_plain_stage1=phantoms.psnr(learned_pilot.cpu().numpy(), plain_pilot.cpu().numpy()),
+        psnr_plain=phantoms.psnr(plain.cpu().numpy(), clean),
+        psnr_fast=phantoms.psnr(fast.cpu().numpy(), clean),
+        psnr_fast_no_fallback=phantoms.psnr(nocheck.cpu().numpy(), clean),
+        psnr_plain_pilot_fast_stage2=phantoms.psnr(plainpilot_fast.cpu().numpy(), clean),
+        ms_plain=ms_plain, ms_fast=ms_fast, ms_fast_no_fallback=ms_nocheck, ms_net=ms_net,
+        excess_high=net.excess_high, fallback_tiles=d["fallback_tiles"], tiles=d["tiles"], weights=out,
+    )
+    print(json.dumps(r), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -234,6 +234,55 @@ int32_t bmnd_stage_noalloc(const BmndStageParams* params, const float* d_noisy,
                            const float* d_pilot, const int32_t* d_refs, int64_t n_refs,
                            float* d_out, uint64_t stream);
 
+/* ------------------------------------------------------------------------
+ * Learned stage-1 pilot (fast path).  No counterpart in the reference: a
+ * residual 3x3 (2-D) or 3x3x3 (3-D) convolution net in the Anscombe domain,
+ *   a = 2 sqrt(max(x, 0) + 3/8),  h_1 = relu(W_0 * a + b_0),
+ *   h_l = relu(W_{l-1} * h_{l-1} + b_{l-1}),  y = a + W_{L-1} * h_{L-1} + b_{L-1},
+ *   pilot = max((y / 2)^2 - 3/8, 0),
+ * with BF16 weights and hidden activations and FP32 accumulation; the
+ * C -> C layers run on the tensor cores.  Parameters are one flat FP32
+ * vector, layer by layer: W_l[tap][ci][co] (taps in C order over offsets
+ * -1..1) then b_l[co]; layer 0 has ci = 1, layer L-1 has co = 1.
+ * ------------------------------------------------------------------------ */
+typedef struct {
+    int32_t ndim;     /* 2 or 3 */
+    int32_t channels; /* hidden channels: 32 or 48 */
+    int32_t layers;   /* convolution layers, 3..32 */
+    int32_t batch;    /* volumes (images) in the batch */
+    int32_t shape[3]; /* D, H, W (3-D) or H, W (2-D); the batch is C-ordered before them */
+} BmndPilotNet;
+
+/* Number of FP32 parameters. */
+int32_t bmnd_pilotnet_param_count(const BmndPilotNet* net, int64_t* count);
+/* Bytes of the packed (BF16, fragment-ordered) weights bmnd_pilotnet_pack writes. */
+int32_t bmnd_pilotnet_packed_bytes(const BmndPilotNet* net, uint64_t* bytes);
+/* Workspace bytes for inference (training = 0) or a gradient pass (training = 1). */
+int32_t bmnd_pilotnet_workspace_bytes(const BmndPilotNet* net, int32_t training, uint64_t* bytes);
+/* Round the FP32 parameters to BF16 and lay them out for the kernels. */
+int32_t bmnd_pilotnet_pack(const BmndPilotNet* net, const float* d_params, void* d_packed, uint64_t stream);
+/* Inference: d_pilot (count domain) and/or d_y (Anscombe-domain output), either may be NULL. */
+int32_t bmnd_pilotnet_forward(const BmndPilotNet* net, const void* d_packed, const float* d_noisy,
+                              float* d_pilot, float* d_y, void* d_workspace, uint64_t workspace_bytes,
+                              uint64_t stream);
+/* Loss mean((y - A(target))^2) with A the Anscombe transform, and its gradient
+ * with respect to every parameter (flat, same layout as the parameters). */
+int32_t bmnd_pilotnet_gradient(const BmndPilotNet* net, const void* d_packed, const float* d_noisy,
+                               const float* d_target, float* d_grad, double* d_loss, void* d_workspace,
+                               uint64_t workspace_bytes, uint64_t stream);
+/* Residual check of a pilot, per tile of edge `edge` (cubes in 3-D, squares in
+ * 2-D; shape as in BmndPilotNet): d_out[3 * tile + (0, 1, 2)] = observed Poisson
+ * deviance sum_v 2 [x ln(x / mu) - (x - mu)] of the input x against the pilot
+ * mu, and its expectation and variance under Poisson noise of mean mu, read from
+ * d_table (n_table expectations then n_table variances, at ln mu = ln_mu0 +
+ * i * d_ln).  Tiles are ordered x fastest, then y, z, batch. */
+int32_t bmnd_pilot_tile_deviance(int32_t ndim, int32_t batch, const int32_t* shape, int32_t edge,
+                                 const float* d_noisy, const float* d_pilot, const float* d_table,
+                                 int32_t n_table, float ln_mu0, float d_ln, double* d_out, uint64_t stream);
+/* One Adam step (bias-corrected, step counts from 1). */
+int32_t bmnd_pilotnet_adam(int64_t n, float* d_params, const float* d_grad, float* d_m, float* d_v,
+                           int32_t step, float lr, float beta1, float beta2, float eps, uint64_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,57 @@
+"""What the trained pilot net gains (GPU), on a held-out phantom crop.
+
+The committed weights (bmnd_gb300/weights/pilot_bm4d.npz) were trained by
+``python -m bmnd_gb300.train_pilot`` on seeds 1000-1007; this test uses a
+128^3 crop of the 256^3 phantom with seed 2001 (same structure scale)."""
+
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def case(cuda, native):
+    import bmnd_gb300 as bg
+    from bmnd_gb300 import phantoms
+    from bmnd_gb300.pilot import PilotNet, default_net_path
+
+    path = default_net_path("bm4d")
+    if not os.path.exists(path):
+        pytest.skip("no trained weights")
+    clean, noisy = phantoms.ellipsoids_3d(256, seed=2001)
+    sl = (slice(64, 192),) * 3
+    clean, noisy = np.ascontiguousarray(clean[sl]), np.ascontiguousarray(noisy[sl])
+    x = cuda.from_numpy(noisy).cuda()
+    prof = bg.BM4DProfile(noise_model=bg.NoiseModel.POISSON)
+    return dict(clean=clean, noisy=noisy, x=x, prof=prof, net=PilotNet.load(path))
+
+
+def test_trained_pilot_beats_untrained_and_no_pilot(cuda, case):
+    from bmnd_gb300 import phantoms
+    from bmnd_gb300.api import stage_device
+    from bmnd_gb300.pilot import PilotNet, bmnd_fast, fast_profile
+
+    clean, x, prof, net = case["clean"], case["x"], case["prof"], case["net"]
+    trained = bmnd_fast(x, prof, net, check=False)
+    untrained = bmnd_fast(x, prof, PilotNet(net.ndim, net.channels, net.layers, seed=0), check=False)
+    no_pilot = stage_device(x, fast_profile(prof), "wiener", x, match_precision="approx")
+    p_tr = phantoms.psnr(trained.cpu().numpy(), clean)
+    p_un = phantoms.psnr(untrained.cpu().numpy(), clean)
+    p_np = phantoms.psnr(no_pilot.cpu().numpy(), clean)
+    assert p_tr > p_un + 3.0, (p_tr, p_un)
+    assert p_tr > p_np + 3.0, (p_tr, p_np)
+
+
+def test_trained_pilot_tracks_plain_stage1(cuda, case):
+    from bmnd_gb300 import phantoms
+    from bmnd_gb300.api import stage_device
+
+    clean, x, prof, net = case["clean"], case["x"], case["prof"], case["net"]
+    plain1 = stage_device(x, prof, "ht").cpu().numpy()
+    learned = net.forward(x).cpu().numpy()
+    # the net imitates plain stage 1: close to it, and far better than the input
+    assert phantoms.psnr(learned, plain1) > 38.0
+    assert phantoms.psnr(learned, clean) > phantoms.psnr(case["noisy"], clean) + 12.0
