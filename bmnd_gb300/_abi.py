@@ -137,6 +137,13 @@ SIGNATURES = {
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
          _U64, _U64],
     ),
+    "bmnd_stage_sigma_workspace_bytes": (_I32, [ctypes.POINTER(StageParams), _I64, _U64P]),
+    "bmnd_stage_sigma": (
+        _I32,
+        [ctypes.POINTER(StageParams), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _I64,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_void_p, _U64, _U64],
+    ),
     "bmnd_stage_noalloc": (
         _I32,
         [ctypes.POINTER(StageParams), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _I64,
@@ -149,7 +156,7 @@ SIGNATURES = {
     "bmnd_pilotnet_forward": (_I32, [_PNP, _VP, _VP, _VP, _VP, _VP, _U64, _U64]),
     "bmnd_pilotnet_gradient": (_I32, [_PNP, _VP, _VP, _VP, _VP, _VP, _VP, _U64, _U64]),
     "bmnd_pilotnet_adam": (_I32, [_I64, _VP, _VP, _VP, _VP, _I32, ctypes.c_float, ctypes.c_float,
-                                  ctypes.c_float, ctypes.c_float, _U64]),
+                                  ctypes.c_float, ctypes.c_float, ctypes.c_float, _VP, _U64]),
     "bmnd_pilot_tile_deviance": (_I32, [_I32, _I32, _I32P, _I32, _VP, _VP, _VP, _I32, ctypes.c_float,
                                         ctypes.c_float, _VP, _U64]),
     "bmnd_run": (

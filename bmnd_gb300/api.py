@@ -154,12 +154,15 @@ _MATCH_PRECISIONS = {"exact": _abi.MATCH_EXACT, "fast": _abi.MATCH_FAST, "approx
 
 
 def bmnd_device(noisy, profile, *, resolved=None, match_precision: str = "exact",
-                stage_callback=None, blockmatch_callback=None, stream=None):
+                stage_callback=None, blockmatch_callback=None, stream=None, sigma_maps: dict | None = None,
+                global_sigma: float = 0.0):
     """Run both stages on a float32 CUDA tensor and return the CUDA result tensor.
 
     ``noisy`` must be a C-contiguous float32 CUDA tensor holding a validated,
     non-negative, non-zero volume.  This is the device-resident core of
-    :func:`bmnd` (no host copies unless a callback is given).
+    :func:`bmnd` (no host copies unless a callback is given).  With a
+    ``sigma_maps`` dict, each stage also writes its sigma map (CUDA tensor,
+    keys "ht" and "wiener"; uncovered voxels get ``global_sigma``).
     """
     torch = _torch()
     shape = tuple(int(s) for s in noisy.shape)
@@ -181,7 +184,10 @@ def bmnd_device(noisy, profile, *, resolved=None, match_precision: str = "exact"
         counts = tuple(s - b + 1 for s, b in zip(shape, block))
         sched = plan.reference_schedule(profile, counts, stage)
         nbytes = ctypes.c_uint64(0)
-        _abi.check(L.bmnd_stage_workspace_bytes(ctypes.byref(p), len(sched), ctypes.byref(nbytes)))
+        if sigma_maps is not None:
+            _abi.check(L.bmnd_stage_sigma_workspace_bytes(ctypes.byref(p), len(sched), ctypes.byref(nbytes)))
+        else:
+            _abi.check(L.bmnd_stage_workspace_bytes(ctypes.byref(p), len(sched), ctypes.byref(nbytes)))
         need = max(need, nbytes.value)
         params[stage] = (p, counts)
         schedules[stage] = sched
@@ -199,11 +205,20 @@ def bmnd_device(noisy, profile, *, resolved=None, match_precision: str = "exact"
             sel = torch.empty((n, p.max_stack), dtype=torch.int32, device=device)
             cnt = torch.empty(n, dtype=torch.int32, device=device)
             acc = torch.empty(n, dtype=torch.int32, device=device)
-        _abi.check(L.bmnd_stage(
-            ctypes.byref(p), noisy.data_ptr(), None if pilot is None else pilot.data_ptr(),
-            refs.data_ptr(), len(sched), dst.data_ptr(),
-            None if sel is None else sel.data_ptr(), None if cnt is None else cnt.data_ptr(),
-            None if acc is None else acc.data_ptr(), ws.data_ptr(), ws.numel(), sptr))
+        if sigma_maps is not None:
+            smap = torch.empty_like(noisy)
+            _abi.check(L.bmnd_stage_sigma(
+                ctypes.byref(p), noisy.data_ptr(), None if pilot is None else pilot.data_ptr(),
+                refs.data_ptr(), len(sched), dst.data_ptr(), smap.data_ptr(), float(global_sigma),
+                None if sel is None else sel.data_ptr(), None if cnt is None else cnt.data_ptr(),
+                None if acc is None else acc.data_ptr(), ws.data_ptr(), ws.numel(), sptr))
+            sigma_maps[stage] = smap
+        else:
+            _abi.check(L.bmnd_stage(
+                ctypes.byref(p), noisy.data_ptr(), None if pilot is None else pilot.data_ptr(),
+                refs.data_ptr(), len(sched), dst.data_ptr(),
+                None if sel is None else sel.data_ptr(), None if cnt is None else cnt.data_ptr(),
+                None if acc is None else acc.data_ptr(), ws.data_ptr(), ws.numel(), sptr))
         if blockmatch_callback is not None:
             blockmatch_callback(stage, _match_result(sched, counts, sel.cpu().numpy(),
                                                      cnt.cpu().numpy(), acc.cpu().numpy()))
@@ -211,6 +226,42 @@ def bmnd_device(noisy, profile, *, resolved=None, match_precision: str = "exact"
             stage_callback(stage, dst.cpu().numpy().copy())
         pilot = dst
     return out
+
+
+def estimate_poisson_global_sigma(volume, eps: float = 1e-10) -> float:
+    """Global noise level reported with the sigma maps, as the reference
+    computes it (src/bmnd/sigmaestimation.py:48-93): sqrt of the mean of the
+    positive values (10%-trimmed when fewer than 10% are positive), with IQR
+    and MAD fallbacks."""
+    vol = np.asarray(volume, dtype=np.float32)
+    finite = np.isfinite(vol)
+    nonneg = np.maximum(vol[finite], 0.0) if np.any(finite) else np.array([0.0], dtype=np.float32)
+    positive = nonneg[nonneg > 0.0]
+    if positive.size > 0:
+        frac = positive.size / max(nonneg.size, 1)
+        if frac < 0.1 and positive.size >= 3:
+            sv = np.sort(positive, axis=None)
+            trim = max(int(0.1 * sv.size), 1)
+            mean_val = float(np.mean(sv[trim:-trim] if sv.size - 2 * trim > 0 else sv, dtype=np.float32))
+        else:
+            mean_val = float(np.mean(positive, dtype=np.float32))
+    else:
+        mean_val = float(np.mean(nonneg, dtype=np.float32))
+    g = float(np.sqrt(max(mean_val, eps)))
+    if g <= 0.0 and positive.size > 0:
+        q25, q75 = np.percentile(positive, [25.0, 75.0])
+        if float(q75 - q25) > 0.0:
+            g = float(np.sqrt(max(float(q75 - q25) / 1.349, eps)))
+    if g <= 0.0 and positive.size > 0:
+        med = float(np.median(positive))
+        mad = float(np.median(np.abs(positive - med)))
+        if mad > 0.0:
+            g = float(np.sqrt(max(mad / 0.6745, eps)))
+    if g <= 0.0:
+        g = float(np.sqrt(eps))
+    if not np.isfinite(g) or g < 0.0:
+        return 0.0
+    return g
 
 
 def stage_device(noisy, profile, stage: str, pilot=None, *, resolved=None, match_precision: str = "exact",
@@ -323,8 +374,6 @@ def bmnd(
             "Gaussian noise profiles are not on the GPU path; use noise_model='poisson'"
         )
     plan.check_poisson_options(profile)
-    if return_sigma_map:
-        raise plan.unsupported("return_sigma_map is not on the GPU path")
 
     torch = _torch()
     if not torch.cuda.is_available():
@@ -336,8 +385,26 @@ def bmnd(
     else:
         host = torch.from_numpy(np.ascontiguousarray(vol))
         dev = host.pin_memory().cuda(non_blocking=True)
+    maps = None
+    global_sigma = 0.0
+    if return_sigma_map:
+        maps = {}
+        # on the stage-1 variance volume max(scale * max(x, 0), floor) (variance.py:581-592)
+        host_vol = dev.cpu().numpy() if torch_input else vol
+        floor = float(profile.poisson_variance_floor)
+        vvol = np.maximum(np.float32(profile.poisson_count_scale) * np.maximum(host_vol, np.float32(0.0)),
+                          np.float32(floor)).astype(np.float32)
+        global_sigma = estimate_poisson_global_sigma(vvol, eps=max(floor, 1e-10))
     out = bmnd_device(dev, profile, resolved=resolved, match_precision=match_precision,
-                      stage_callback=stage_callback, blockmatch_callback=blockmatch_callback)
+                      stage_callback=stage_callback, blockmatch_callback=blockmatch_callback,
+                      sigma_maps=maps, global_sigma=global_sigma)
     if torch_input:
-        return out if volume.is_cuda else out.cpu()
-    return out.cpu().numpy()
+        res = out if volume.is_cuda else out.cpu()
+        if maps is None:
+            return res
+        conv = (lambda t: t) if volume.is_cuda else (lambda t: t.cpu())
+        return res, {"global": global_sigma, "ht": conv(maps["ht"]), "wiener": conv(maps["wiener"])}
+    if maps is None:
+        return out.cpu().numpy()
+    return out.cpu().numpy(), {"global": global_sigma, "ht": maps["ht"].cpu().numpy(),
+                               "wiener": maps["wiener"].cpu().numpy()}

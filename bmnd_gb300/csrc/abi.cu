@@ -151,9 +151,15 @@ BmndMatchParams match_params_of(const BmndStageParams& sp) {
     return mp;
 }
 
+// bytes of the stage workspace followed by the float64 sigma-map numerator
+uint64_t sigma_workspace_bytes(const BmndStageParams& sp, int64_t n_refs) {
+    return carve(sp, n_refs, nullptr).bytes + align256(8ull * static_cast<uint64_t>(volume_voxels(sp)));
+}
+
 int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pilot,
                   const int32_t* refs, int64_t n_refs, float* out, int32_t* sel, int32_t* count,
-                  int32_t* accepted, void* ws, uint64_t ws_bytes, cudaStream_t stream) {
+                  int32_t* accepted, void* ws, uint64_t ws_bytes, cudaStream_t stream,
+                  float* sigma_out = nullptr, float global_sigma = 0.0f) {
     int32_t rc = validate_stage(sp);
     if (rc) return rc;
     if (!noisy || !out) return fail(BMND_ERR_INVALID_ARG, "noisy and out are required");
@@ -161,7 +167,8 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
         return fail(BMND_ERR_INVALID_ARG, "the Wiener stage needs the pilot estimate");
     if (n_refs < 0 || (n_refs > 0 && !refs)) return fail(BMND_ERR_INVALID_ARG, "bad reference list");
     StageWorkspace need = carve(sp, n_refs, nullptr);
-    if (!ws || ws_bytes < need.bytes) return fail(BMND_ERR_WORKSPACE, "workspace too small");
+    const uint64_t need_bytes = sigma_out ? sigma_workspace_bytes(sp, n_refs) : need.bytes;
+    if (!ws || ws_bytes < need_bytes) return fail(BMND_ERR_WORKSPACE, "workspace too small");
     if (reinterpret_cast<uintptr_t>(ws) % 256 != 0)
         return fail(BMND_ERR_INVALID_ARG, "workspace must be 256-byte aligned");
     StageWorkspace w = carve(sp, n_refs, ws);
@@ -171,6 +178,11 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
     uint64_t vox = static_cast<uint64_t>(volume_voxels(sp));
     BMND_CUDA_TRY(cudaMemsetAsync(w.num, 0, 8 * vox, stream));
     BMND_CUDA_TRY(cudaMemsetAsync(w.den, 0, 8 * vox, stream));
+    double* sig_num = nullptr;
+    if (sigma_out) {
+        sig_num = reinterpret_cast<double*>(static_cast<char*>(ws) + need.bytes);
+        BMND_CUDA_TRY(cudaMemsetAsync(sig_num, 0, 8 * vox, stream));
+    }
     BmndMatchParams mp = match_params_of(sp);
     const float* match_src = sp.filter == BMND_FILTER_WIENER ? pilot : noisy;
     if (sp.filter == BMND_FILTER_WIENER && sp.match_precision == BMND_MATCH_EXACT)
@@ -178,8 +190,12 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
     rc = launch_blockmatch_volume(mp, match_src, sp.shape, sp.block, refs, n_refs, nullptr,
                                   sp.match_threshold, w.sel, w.count, w.accepted, stream);
     if (rc) return rc;
-    rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, w.st, stream);
+    rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, w.st, sig_num, stream);
     if (rc) return rc;
+    if (sigma_out) {
+        rc = launch_finalize_sigma(sp, sig_num, w.den, global_sigma, sigma_out, stream);
+        if (rc) return rc;
+    }
     return launch_finalize(sp, w.num, w.den, noisy, out, stream);
 }
 
@@ -323,6 +339,26 @@ int32_t bmnd_stage(const BmndStageParams* params, const float* d_noisy, const fl
     if (!params) return fail(BMND_ERR_INVALID_ARG, "null params");
     return run_stage(*params, d_noisy, d_pilot, d_refs, n_refs, d_out, d_sel, d_count, d_accepted,
                      d_workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int32_t bmnd_stage_sigma_workspace_bytes(const BmndStageParams* params, int64_t n_refs, uint64_t* out_bytes) {
+    clear_error();
+    if (!params || !out_bytes) return fail(BMND_ERR_INVALID_ARG, "null argument");
+    if (int32_t rc = validate_stage(*params)) return rc;
+    if (n_refs < 0) return fail(BMND_ERR_INVALID_ARG, "n_refs must be >= 0");
+    *out_bytes = sigma_workspace_bytes(*params, n_refs);
+    return BMND_OK;
+}
+
+int32_t bmnd_stage_sigma(const BmndStageParams* params, const float* d_noisy, const float* d_pilot,
+                         const int32_t* d_refs, int64_t n_refs, float* d_out, float* d_sigma_map,
+                         float global_sigma, int32_t* d_sel, int32_t* d_count, int32_t* d_accepted,
+                         void* d_workspace, uint64_t workspace_bytes, uint64_t stream) {
+    clear_error();
+    if (!params) return fail(BMND_ERR_INVALID_ARG, "null params");
+    if (!d_sigma_map) return fail(BMND_ERR_INVALID_ARG, "d_sigma_map is required");
+    return run_stage(*params, d_noisy, d_pilot, d_refs, n_refs, d_out, d_sel, d_count, d_accepted, d_workspace,
+                     workspace_bytes, reinterpret_cast<cudaStream_t>(stream), d_sigma_map, global_sigma);
 }
 
 int32_t bmnd_run(const BmndStageParams* ht, const BmndStageParams* wiener, const float* d_noisy,

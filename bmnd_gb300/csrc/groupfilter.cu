@@ -35,17 +35,17 @@ namespace bmnd {
 namespace {
 
 constexpr int kThreads = 256;      // threads per group (CTA)
-constexpr int kThreadsWide = 512;  // largest CTA the kernel is written for (scan buffer)
 
-// Shared-memory plan.  The union region holds the group buffers X (noisy
-// coefficients), R (pilot coefficients, Wiener only), T (transform scratch)
-// and V (variance group, later the attenuation) outside the exact-variance
-// phase, and the occupancy grid plus the union-voxel lists inside it: the
-// phases are ordered so that none of X/R/T/V is live while the lists are.
+// Shared-memory plan.  A fixed part holds the group matrix, the transform
+// tables, positions and small per-group arrays.  The union region first holds
+// the exact-variance phase's occupancy grid and union-voxel lists; once that
+// phase is done it holds the group buffers: S (noise sigma), X (noisy
+// coefficients) and R (pilot coefficients, Wiener) or V (attenuation, hard
+// thresholding).  Transforms run in place, so no scratch buffer is needed.
 struct Layout {
     // byte offsets into dynamic shared memory
-    int64_t g, ginv, gsq, gt, fw, fi, win, mdiag, pos, shf, shl, s, ex, uni, x, r, t, v, grid, lval, lstart, lent,
-        scan, plane, wts, misc, total;
+    int64_t g, gt, fw, fi, win, mdiag, pos, shf, shl, sg, ex, uni, s, x, r, v, grid, lval, lstart, lent, scan,
+        plane, wts, misc, total;
 };
 
 struct FilterArgs {
@@ -64,9 +64,10 @@ struct FilterArgs {
     double* num;
     double* den;
     const float* st;  // S^T: st[p * kron_stride(P) + j] = S[j, p], the Kronecker product of the patch transforms
+    double* sig_num;  // optional: sigma-map numerator (sum of sigma x weight x window), else null
 };
 
-__host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax, int64_t ucells) {
+__host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax, int64_t ucells, bool sigma) {
     Layout L{};
     int64_t off = 0;
     auto round16 = [](int64_t b) { return (b + 15) & ~int64_t(15); };
@@ -79,8 +80,6 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     const bool wiener = sp.filter == BMND_FILTER_WIENER;
     const int kpad = (kmax + 3) / 4 * 4;
     L.g = take(4 * nmax * nmax);
-    L.ginv = take(4 * nmax * nmax);
-    L.gsq = take(4 * nmax * nmax);
     L.gt = take(4 * nmax * (kpad > 0 ? kpad : 4));
     L.fw = take(4 * BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE);
     L.fi = take(4 * BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE);
@@ -89,26 +88,27 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     L.pos = take(4 * nmax * BMND_MAX_DIMS);
     L.shf = take(4 * nmax * BMND_MAX_DIMS);
     L.shl = take(4 * nmax);
-    L.s = take(4 * np);
+    // hard thresholding with a sigma map keeps each coefficient's sigma until the scatter
+    L.sg = take(sigma && !wiener ? 4 * np : 16);
     L.ex = take(4 * static_cast<int64_t>(kmax) * P);
-    L.scan = take(8 * (kThreadsWide + 1));
+    L.scan = take(8 * (kThreads + 1));
     L.plane = take(8 * nmax);
     L.wts = take(4 * nmax);
     L.misc = take(64);
     // union region
     L.uni = off;
-    int64_t buf = round16(4 * np);
-    L.x = L.uni;
-    L.r = L.x + buf;
-    L.t = L.r + (wiener ? buf : 0);
-    L.v = L.t + buf;
-    int64_t group_bytes = (L.v + buf) - L.uni;
-    int64_t umax = kmax > 0 ? (np < ucells ? np : ucells) : 0;
+    const int64_t buf = round16(4 * np);
+    L.s = L.uni;
+    L.x = L.s + buf;
+    L.r = L.x + buf;  // Wiener: pilot coefficients, then the attenuation
+    L.v = L.r;        // hard thresholding: the attenuation
+    const int64_t group_bytes = 3 * buf;
+    const int64_t umax = kmax > 0 ? (np < ucells ? np : ucells) : 0;
     L.grid = L.uni;
     L.lval = L.grid + round16(kmax > 0 ? 4 * ucells : 0);
     L.lstart = L.lval + round16(4 * umax);
     L.lent = L.lstart + round16(4 * (umax + 1));
-    int64_t list_bytes = (L.lent + round16(kmax > 0 ? 4 * np : 0)) - L.uni;
+    const int64_t list_bytes = (L.lent + round16(kmax > 0 ? 4 * np : 0)) - L.uni;
     off = L.uni + (group_bytes > list_bytes ? group_bytes : list_bytes);
     L.total = off;
     return L;
@@ -159,77 +159,102 @@ struct Geom {
     }
 };
 
-// Register-blocked group-axis product for a compile-time group size N:
-// out[i, p] = sum_k M[i, k] in[k, p], one fused multiply-add per term in k
-// order.  Each work item holds the column in[:, p] in registers and produces a
-// chunk of the N outputs, reading the matrix rows as float4 broadcasts.
-template <int N>
-__device__ void group_axis_reg(const float* in, float* out, int P, const float* M) {
-    constexpr int IC = N >= 16 ? 8 : N;          // outputs per item
-    constexpr int CH = N / IC;                   // chunks per column
-    const int items = P * CH;
-    for (int it = threadIdx.x; it < items; it += blockDim.x) {
-        const int p = it % P;
-        const int i0 = (it / P) * IC;
+// Transforms work in place on an (n, block...) group held in shared memory.
+// Every axis product accumulates with one fused multiply-add per term in k
+// order, which is how NumPy's sgemm evaluates the reference's products.
+//
+// Group axis, compile-time size N: out[i, p] = sum_k M[i, k] in[k, p] with
+// KIND 0: M = G, KIND 1: M = G^T (the inverse, transforms.py:423, :436),
+// KIND 2: M = G o G with each entry rounded as fl(g * g) (the squared
+// transform of the variance propagation).  Each thread holds one column in
+// registers and produces IC of its N outputs; a round takes whole columns
+// (all their chunks) and reads them completely before any thread writes, so
+// the product can overwrite its input.
+template <int KIND>
+__device__ __forceinline__ float gmat(const float* G, int N, int i, int k) {
+    float m = KIND == 1 ? G[k * N + i] : G[i * N + k];
+    return KIND == 2 ? mul_rn(m, m) : m;
+}
+
+template <int N, int KIND>
+__device__ void group_axis_inplace(float* buf, int P, const float* G) {
+    constexpr int IC = N >= 16 ? 8 : N;  // outputs per thread
+    constexpr int CH = N / IC;           // threads per column
+    const int cols = static_cast<int>(blockDim.x) / CH;
+    for (int c0 = 0; c0 < P; c0 += cols) {
+        const int p = c0 + static_cast<int>(threadIdx.x) / CH;
+        const int i0 = (static_cast<int>(threadIdx.x) % CH) * IC;
+        const bool act = static_cast<int>(threadIdx.x) < cols * CH && p < P;
         float x[N];
+        if (act) {
 #pragma unroll
-        for (int k = 0; k < N; ++k) x[k] = in[k * P + p];
+            for (int k = 0; k < N; ++k) x[k] = buf[k * P + p];
+        }
+        __syncthreads();
+        if (act) {
 #pragma unroll
-        for (int ii = 0; ii < IC; ++ii) {
-            const float* row = M + (i0 + ii) * N;
-            float acc = 0.0f;
-            if (N % 4 == 0) {
+            for (int ii = 0; ii < IC; ++ii) {
+                const int i = i0 + ii;
+                float acc = 0.0f;
+                if (KIND != 1 && N % 4 == 0) {
 #pragma unroll
-                for (int k = 0; k < N; k += 4) {
-                    const float4 m = *reinterpret_cast<const float4*>(row + k);
-                    acc = fmaf(m.x, x[k], acc);
-                    acc = fmaf(m.y, x[k + 1], acc);
-                    acc = fmaf(m.z, x[k + 2], acc);
-                    acc = fmaf(m.w, x[k + 3], acc);
+                    for (int k = 0; k < N; k += 4) {
+                        float4 m = *reinterpret_cast<const float4*>(G + i * N + k);
+                        if (KIND == 2) {
+                            m.x = mul_rn(m.x, m.x);
+                            m.y = mul_rn(m.y, m.y);
+                            m.z = mul_rn(m.z, m.z);
+                            m.w = mul_rn(m.w, m.w);
+                        }
+                        acc = fmaf(m.x, x[k], acc);
+                        acc = fmaf(m.y, x[k + 1], acc);
+                        acc = fmaf(m.z, x[k + 2], acc);
+                        acc = fmaf(m.w, x[k + 3], acc);
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < N; ++k) acc = fmaf(gmat<KIND>(G, N, i, k), x[k], acc);
                 }
-            } else {
-#pragma unroll
-                for (int k = 0; k < N; ++k) acc = fmaf(row[k], x[k], acc);
+                buf[i * P + p] = acc;
             }
-            out[(i0 + ii) * P + p] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+// runtime group size (not a power of two): one thread per column
+template <int KIND>
+__device__ void group_axis_generic(float* buf, int n, int P, const float* G) {
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        float x[BMND_MAX_STACK];
+        for (int k = 0; k < n; ++k) x[k] = buf[k * P + p];
+        for (int i = 0; i < n; ++i) {
+            float acc = 0.0f;
+            for (int k = 0; k < n; ++k) acc = fmaf(gmat<KIND>(G, n, i, k), x[k], acc);
+            buf[i * P + p] = acc;
         }
     }
     __syncthreads();
 }
 
-// runtime group size (non power of two): one output per work item
-template <class GM>
-__device__ void group_axis_generic(const GM& geo, const float* in, float* out, int n, const float* M) {
-    const int P = geo.P();
-    const int total = n * P;
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int i = e / P;
-        const int p = e - i * P;
-        float acc = 0.0f;
-        for (int k = 0; k < n; ++k) acc = fmaf(M[i * n + k], in[k * P + p], acc);
-        out[e] = acc;
-    }
-    __syncthreads();
-}
-
-template <class GM>
-__device__ void apply_group_axis(const GM& geo, const float* in, float* out, int n, const float* M) {
-    const int P = geo.P();
+template <int KIND>
+__device__ void group_axis_any(float* buf, int n, int P, const float* G) {
     switch (n) {
-        case 1: group_axis_reg<1>(in, out, P, M); break;
-        case 2: group_axis_reg<2>(in, out, P, M); break;
-        case 4: group_axis_reg<4>(in, out, P, M); break;
-        case 8: group_axis_reg<8>(in, out, P, M); break;
-        case 16: group_axis_reg<16>(in, out, P, M); break;
-        case 32: group_axis_reg<32>(in, out, P, M); break;
-        default: group_axis_generic(geo, in, out, n, M); break;
+        case 1: group_axis_inplace<1, KIND>(buf, P, G); break;
+        case 2: group_axis_inplace<2, KIND>(buf, P, G); break;
+        case 4: group_axis_inplace<4, KIND>(buf, P, G); break;
+        case 8: group_axis_inplace<8, KIND>(buf, P, G); break;
+        case 16: group_axis_inplace<16, KIND>(buf, P, G); break;
+        case 32: group_axis_inplace<32, KIND>(buf, P, G); break;
+        default: group_axis_generic<KIND>(buf, n, P, G); break;
     }
 }
 
-// patch axis d with compile-time edge B and stride INNER: each work item
-// transforms one line of B values with the matrix held in registers
+// patch axis d with compile-time edge B and stride INNER: each thread
+// transforms whole lines of B values (matrix in registers), so lines never
+// share a thread and the product overwrites its input
 template <int B, int INNER>
-__device__ void space_axis_reg(const float* in, float* out, int total, const float* Msrc, bool square) {
+__device__ void space_axis_reg(float* buf, int total, const float* Msrc, bool square) {
     float m[B * B];
 #pragma unroll
     for (int q = 0; q < B * B; ++q) {
@@ -243,94 +268,72 @@ __device__ void space_axis_reg(const float* in, float* out, int total, const flo
         const int base = o * B * INNER + t;
         float x[B];
 #pragma unroll
-        for (int k = 0; k < B; ++k) x[k] = in[base + k * INNER];
+        for (int k = 0; k < B; ++k) x[k] = buf[base + k * INNER];
 #pragma unroll
         for (int i = 0; i < B; ++i) {
             float acc = 0.0f;
 #pragma unroll
             for (int k = 0; k < B; ++k) acc = fmaf(m[i * B + k], x[k], acc);
-            out[base + i * INNER] = acc;
+            buf[base + i * INNER] = acc;
         }
     }
     __syncthreads();
 }
 
-// runtime geometry fallback for a patch axis
+// runtime geometry: one thread per line of edge m along axis d
 template <class GM>
-__device__ void apply_space_axis(const GM& geo, int d, const float* in, float* out, int n,
-                                 const float* M, bool square) {
+__device__ void space_axis_generic(const GM& geo, int d, float* buf, int n, const float* M, bool square) {
     const int m = geo.b(d);
     const int inner = geo.inner(d);
-    const int total = n * geo.P();
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int t = e % inner;
-        const int rest = e / inner;
-        const int i = rest % m;
-        const int o = rest / m;
-        const float* col = in + o * m * inner + t;
-        float acc = 0.0f;
-        for (int k = 0; k < m; ++k) {
-            float mk = M[i * m + k];
-            if (square) mk = mul_rn(mk, mk);
-            acc = fmaf(mk, col[k * inner], acc);
+    const int lines = n * geo.P() / m;
+    for (int line = threadIdx.x; line < lines; line += blockDim.x) {
+        const int o = line / inner;
+        const int t = line - o * inner;
+        const int base = o * m * inner + t;
+        float x[BMND_MAX_EDGE];
+        for (int k = 0; k < m; ++k) x[k] = buf[base + k * inner];
+        for (int i = 0; i < m; ++i) {
+            float acc = 0.0f;
+            for (int k = 0; k < m; ++k) {
+                float mk = M[i * m + k];
+                if (square) mk = mul_rn(mk, mk);
+                acc = fmaf(mk, x[k], acc);
+            }
+            buf[base + i * inner] = acc;
         }
-        out[e] = acc;
     }
     __syncthreads();
 }
 
 template <int ND, int B0, int B1, int B2, int D>
-__device__ __forceinline__ void space_axis_fixed(const float* in, float* out, int n, const float* M,
-                                                 bool square) {
+__device__ __forceinline__ void space_axis_fixed(float* buf, int n, const float* M, bool square) {
     constexpr int B = D == 0 ? B0 : (D == 1 ? B1 : B2);
     constexpr int INNER = D == 0 ? (ND > 1 ? B1 : 1) * (ND > 2 ? B2 : 1) : (D == 1 ? (ND > 2 ? B2 : 1) : 1);
-    space_axis_reg<B, INNER>(in, out, n * B0 * B1 * B2, M, square);
+    space_axis_reg<B, INNER>(buf, n * B0 * B1 * B2, M, square);
 }
 
-// separable transform of an (n, block...) group: src -> dst (src may equal
-// dst).  The passes alternate between tmp and dst, starting with tmp, so no
-// pass reads and writes the same buffer.  kind: 0 forward, 1 inverse,
-// 2 squared forward.
+// separable transform of an (n, block...) group in place: the group axis
+// first, then the patch axes (transforms.py:209-255).  kind: 0 forward,
+// 1 inverse, 2 squared forward.
 template <int ND, int B0, int B1, int B2, class GM>
-__device__ void transform_group(const GM& geo, const FilterArgs& a, unsigned char* smem, int n,
-                                float* src, float* dst, float* tmp, int kind) {
-    const float* G = sm<float>(smem, kind == 0 ? a.L.g : (kind == 1 ? a.L.ginv : a.L.gsq));
+__device__ void transform_group(const GM& geo, const FilterArgs& a, unsigned char* smem, int n, float* buf,
+                                int kind) {
+    const float* G = sm<float>(smem, a.L.g);
     const float* F = sm<float>(smem, kind == 1 ? a.L.fi : a.L.fw);
-    const float* cur = src;
-    float* bufs[2] = {tmp, dst};
-    int which = 0;
     if (a.sp.group_transform != BMND_GROUP_NONE) {
-        apply_group_axis(geo, cur, bufs[which], n, G);
-        cur = bufs[which];
-        which ^= 1;
+        if (kind == 0) group_axis_any<0>(buf, n, geo.P(), G);
+        else if (kind == 1) group_axis_any<1>(buf, n, geo.P(), G);
+        else group_axis_any<2>(buf, n, geo.P(), G);
     }
     const bool square = kind == 2;
     if constexpr (ND > 0) {
-        space_axis_fixed<ND, B0, B1, B2, 0>(cur, bufs[which], n, F, square);
-        cur = bufs[which];
-        which ^= 1;
-        if constexpr (ND > 1) {
-            space_axis_fixed<ND, B0, B1, B2, 1>(cur, bufs[which], n, F + BMND_MAX_EDGE * BMND_MAX_EDGE, square);
-            cur = bufs[which];
-            which ^= 1;
-        }
-        if constexpr (ND > 2) {
-            space_axis_fixed<ND, B0, B1, B2, 2>(cur, bufs[which], n, F + 2 * BMND_MAX_EDGE * BMND_MAX_EDGE,
-                                                square);
-            cur = bufs[which];
-            which ^= 1;
-        }
+        space_axis_fixed<ND, B0, B1, B2, 0>(buf, n, F, square);
+        if constexpr (ND > 1) space_axis_fixed<ND, B0, B1, B2, 1>(buf, n, F + BMND_MAX_EDGE * BMND_MAX_EDGE, square);
+        if constexpr (ND > 2)
+            space_axis_fixed<ND, B0, B1, B2, 2>(buf, n, F + 2 * BMND_MAX_EDGE * BMND_MAX_EDGE, square);
     } else {
-        for (int d = 0; d < geo.nd(); ++d) {
-            apply_space_axis(geo, d, cur, bufs[which], n, F + d * BMND_MAX_EDGE * BMND_MAX_EDGE, square);
-            cur = bufs[which];
-            which ^= 1;
-        }
-    }
-    if (cur != dst) {
-        const int total = n * geo.P();
-        for (int e = threadIdx.x; e < total; e += blockDim.x) dst[e] = cur[e];
-        __syncthreads();
+        for (int d = 0; d < geo.nd(); ++d)
+            space_axis_generic(geo, d, buf, n, F + d * BMND_MAX_EDGE * BMND_MAX_EDGE, square);
     }
 }
 
@@ -565,8 +568,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
     float* EX = sm<float>(smem, a.L.ex);
     float* X = sm<float>(smem, a.L.x);
     float* R = sm<float>(smem, a.L.r);
-    float* T = sm<float>(smem, a.L.t);
-    float* V = sm<float>(smem, a.L.v);
+    float* V = sm<float>(smem, a.L.v);  // aliases R: the attenuation
     uint32_t* grid = sm<uint32_t>(smem, a.L.grid);
     float* lval = sm<float>(smem, a.L.lval);
     int* lstart = sm<int>(smem, a.L.lstart);
@@ -588,15 +590,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
             rem /= a.counts[d];
         }
     }
-    float* Ginv = sm<float>(smem, a.L.ginv);
-    float* Gsq = sm<float>(smem, a.L.gsq);
-    for (int e = tid; e < n * n; e += blockDim.x) {
-        const int i = e / n, k = e % n;
-        const float gv = group_entry(sp.group_transform, n, i, k);
-        G[e] = gv;
-        Ginv[k * n + i] = gv;  // inverse = transpose (transforms.py:423, :436)
-        Gsq[e] = mul_rn(gv, gv);
-    }
+    for (int e = tid; e < n * n; e += blockDim.x) G[e] = group_entry(sp.group_transform, n, e / n, e % n);
     for (int e = tid; e < BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE; e += blockDim.x) {
         Fw[e] = sp.spatial_fwd[e / (BMND_MAX_EDGE * BMND_MAX_EDGE)][e % (BMND_MAX_EDGE * BMND_MAX_EDGE)];
         Fi[e] = sp.spatial_inv[e / (BMND_MAX_EDGE * BMND_MAX_EDGE)][e % (BMND_MAX_EDGE * BMND_MAX_EDGE)];
@@ -638,22 +632,6 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
     const float* varsrc = wiener ? a.pilot : a.noisy;
     const int total = n * P;
     const bool need_approx = (k <= 0) || (kk < n);
-
-    // ---- approximate sigma from the variance group (squared transforms) ----
-    if (need_approx) {
-        for (int e = tid; e < total; e += blockDim.x) {
-            const int g = e / P;
-            V[e] = variance_of(__ldg(varsrc + geo.offset(pos + g * BMND_MAX_DIMS, e - g * P, a.vstride)),
-                               scale_f, floor_f);
-        }
-        __syncthreads();
-        transform_group<ND, B0, B1, B2>(geo, a, smem, n, V, V, T, 2);
-        for (int e = tid; e < total; e += blockDim.x) {
-            float v = V[e];
-            S[e] = sqrtf(v > 0.0f ? v : 0.0f);
-        }
-        __syncthreads();
-    }
 
     // ---- exact overlap-aware sigma of the first kk planes ----
     if (kk > 0) {
@@ -783,6 +761,23 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         }
     }
 
+    // ---- approximate sigma from the variance group (squared transforms) ----
+    // (after the exact phase: S shares the union region with its lists)
+    if (need_approx) {
+        for (int e = tid; e < total; e += blockDim.x) {
+            const int g = e / P;
+            S[e] = variance_of(__ldg(varsrc + geo.offset(pos + g * BMND_MAX_DIMS, e - g * P, a.vstride)),
+                               scale_f, floor_f);
+        }
+        __syncthreads();
+        transform_group<ND, B0, B1, B2>(geo, a, smem, n, S, 2);
+        for (int e = tid; e < total; e += blockDim.x) {
+            const float v = S[e];
+            S[e] = sqrtf(v > 0.0f ? v : 0.0f);
+        }
+        __syncthreads();
+    }
+
     // ---- final sigma in S (plane limiting, variance.py:1572-1631) ----
     if (k > 0 && kk == n) {
         for (int e = tid; e < total; e += blockDim.x) S[e] = EX[e];
@@ -829,13 +824,19 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         if (wiener) R[e] = __ldg(a.pilot + off);
     }
     __syncthreads();
-    transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, X, T, 0);
-    if (wiener) transform_group<ND, B0, B1, B2>(geo, a, smem, n, R, R, T, 0);
+    transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, 0);
+    if (wiener) transform_group<ND, B0, B1, B2>(geo, a, smem, n, R, 0);
 
     // ---- shrinkage: coefficients in X, attenuation in V, noise variance in S ----
     const float eps_f = static_cast<float>(sp.eps);
+    float* SG = sm<float>(smem, a.L.sg);
+    float sig_sum = 0.0f;  // Wiener sigma map: this thread's share of the group's sigma sum
     for (int e = tid; e < total; e += blockDim.x) {
         float sig = S[e];
+        if (a.sig_num) {
+            if (wiener) sig_sum += sig;
+            else SG[e] = sig;
+        }
         float nv = mul_rn(sig, sig);
         float att;
         if (!wiener) {
@@ -855,6 +856,22 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         S[e] = nv;
     }
     __syncthreads();
+
+    // Wiener sigma map: the group's mean coefficient sigma (bmndalgo.py:874-875),
+    // summed per warp and then over warps in warp order
+    if (a.sig_num && wiener) {
+        float v = sig_sum;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((tid & 31) == 0) sm<float>(smem, a.L.scan)[tid >> 5] = v;
+        __syncthreads();
+        if (tid == 0) {
+            float t = 0.0f;
+            for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) t += sm<float>(smem, a.L.scan)[w];
+            sm<float>(smem, a.L.misc)[12] = t / static_cast<float>(total);
+        }
+        __syncthreads();
+    }
 
     // ---- aggregation weights (float64, aggregationweights.py:213-259) ----
     {
@@ -885,7 +902,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
     __syncthreads();
 
     // ---- inverse transform and scatter ----
-    transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, X, T, 1);
+    transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, 1);
     for (int e = tid; e < total; e += blockDim.x) {
         const int g = e / P;
         const int p = e - g * P;
@@ -893,6 +910,12 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         float ww = mul_rn(wts[g], win[p]);
         atomicAdd(a.num + off, static_cast<double>(mul_rn(X[e], ww)));
         atomicAdd(a.den + off, static_cast<double>(ww));
+        if (a.sig_num) {
+            // sigma map numerator (patchaggregation.py:229-294): per coefficient
+            // (hard thresholding) or the group's mean (Wiener)
+            const float sv = wiener ? sm<float>(smem, a.L.misc)[12] : SG[e];
+            atomicAdd(a.sig_num + off, static_cast<double>(mul_rn(sv, ww)));
+        }
     }
 }
 
@@ -930,6 +953,17 @@ __global__ void finalize_kernel(const double* __restrict__ num, const double* __
     }
 }
 
+// sigma map = sigma_num / den where den > 0, else the global sigma
+// (bmndalgo.py:1048-1057)
+__global__ void finalize_sigma_kernel(const double* __restrict__ sig_num, const double* __restrict__ den,
+                                      float global_sigma, float* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float d = static_cast<float>(den[i]);
+        out[i] = d > 0.0f ? div_rn(static_cast<float>(sig_num[i]), d) : global_sigma;
+    }
+}
+
 }  // namespace
 
 int64_t union_cells_bound(const BmndStageParams& sp) {
@@ -947,12 +981,12 @@ int64_t group_filter_smem_bytes(const BmndStageParams& sp) {
     int P = patch_volume(sp);
     int kmax = sp.variance_k < sp.max_stack ? sp.variance_k : sp.max_stack;
     if (kmax < 0) kmax = 0;
-    return make_layout(sp, P, sp.max_stack, kmax, union_cells_bound(sp)).total;
+    return make_layout(sp, P, sp.max_stack, kmax, union_cells_bound(sp), true).total;
 }
 
 int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const float* pilot,
                             const int32_t* sel, const int32_t* count, int64_t n_refs, double* num,
-                            double* den, float* st, cudaStream_t stream) {
+                            double* den, float* st, double* sig_num, cudaStream_t stream) {
     if (n_refs == 0) return BMND_OK;
     {
         const int P = patch_volume(sp);
@@ -973,7 +1007,8 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
         s *= sp.shape[d];
     }
     for (int d = 0; d < sp.ndim; ++d) a.counts[d] = sp.shape[d] - sp.block[d] + 1;
-    a.L = make_layout(sp, a.P, a.nmax, a.kmax, union_cells_bound(sp));
+    a.sig_num = sig_num;
+    a.L = make_layout(sp, a.P, a.nmax, a.kmax, union_cells_bound(sp), sig_num != nullptr);
     a.noisy = noisy;
     a.pilot = pilot;
     a.sel = sel;
@@ -987,6 +1022,19 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
     auto run = [&](auto kernel, int threads) -> int32_t {
         BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(a.L.total)));
+        // give shared memory only what the resident CTAs need, so the rest of
+        // the unified L1 caches the Kronecker table and the volumes
+        int per_sm = 0, dev = 0, smem_sm = 0;
+        BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        BMND_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, a.L.total));
+        BMND_CUDA_TRY(cudaGetDevice(&dev));
+        BMND_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+        if (per_sm > 0 && smem_sm > 0) {
+            const int64_t want = static_cast<int64_t>(per_sm) * (a.L.total + 1024);
+            int pct = static_cast<int>((want * 100 + smem_sm - 1) / smem_sm);
+            if (pct > 100) pct = 100;
+            BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+        }
         kernel<<<static_cast<unsigned>(n_refs), threads, a.L.total, stream>>>(a);
         BMND_LAUNCH_CHECK("group_filter_kernel");
         return BMND_OK;
@@ -1001,6 +1049,17 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
     if (sp.ndim == 3 && b[0] == 5 && b[1] == 5 && b[2] == 5)
         return run(group_filter_kernel<3, 5, 5, 5, kThreads>, kThreads);
     return run(group_filter_kernel<0, 0, 0, 0, kThreads>, kThreads);
+}
+
+int32_t launch_finalize_sigma(const BmndStageParams& sp, const double* sig_num, const double* den,
+                              float global_sigma, float* out, cudaStream_t stream) {
+    int64_t n = volume_voxels(sp);
+    if (n == 0) return BMND_OK;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    finalize_sigma_kernel<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(sig_num, den, global_sigma, out, n);
+    BMND_LAUNCH_CHECK("finalize_sigma_kernel");
+    return BMND_OK;
 }
 
 int32_t launch_finalize(const BmndStageParams& sp, const double* num, const double* den,

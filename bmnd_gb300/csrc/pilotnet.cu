@@ -521,12 +521,36 @@ __global__ void round_bf16_kernel(const float* __restrict__ src, float* __restri
         dst[i] = __bfloat162float(__float2bfloat16_rn(src[i]));
 }
 
+// squared L2 norm of the gradient (for clipping), accumulated in float64
+__global__ void sumsq_kernel(const float* __restrict__ g, int64_t n, double* __restrict__ out) {
+    __shared__ double red[32];
+    double local = 0.0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        local += static_cast<double>(g[i]) * g[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < static_cast<int>(blockDim.x >> 5); ++i) s += red[i];
+        atomicAdd(out, s);
+    }
+}
+
+// Adam on the gradient scaled by min(1, clip / ||g||) when clip > 0
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ grad, float* __restrict__ m,
                             float* __restrict__ v, int64_t n, float lr, float b1, float b2, float eps, float bc1,
-                            float bc2) {
+                            float bc2, float clip, const double* __restrict__ sumsq) {
+    float scale = 1.0f;
+    if (clip > 0.0f) {
+        const double norm = sqrt(*sumsq);
+        if (norm > static_cast<double>(clip)) scale = static_cast<float>(static_cast<double>(clip) / norm);
+    }
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const float gi = grad[i];
+        const float gi = grad[i] * scale;
         const float mi = b1 * m[i] + (1.0f - b1) * gi;
         const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
         m[i] = mi;
@@ -944,15 +968,22 @@ int32_t bmnd_pilot_tile_deviance(int32_t ndim, int32_t batch, const int32_t* sha
 }
 
 int32_t bmnd_pilotnet_adam(int64_t n, float* d_params, const float* d_grad, float* d_m, float* d_v, int32_t step,
-                           float lr, float beta1, float beta2, float eps, uint64_t stream_u64) {
+                           float lr, float beta1, float beta2, float eps, float clip_norm, double* d_sumsq,
+                           uint64_t stream_u64) {
     clear_error();
     if (n < 0 || !d_params || !d_grad || !d_m || !d_v) return fail(BMND_ERR_INVALID_ARG, "bad Adam arguments");
     if (step < 1) return fail(BMND_ERR_INVALID_ARG, "Adam step counts from 1");
+    if (clip_norm > 0.0f && !d_sumsq) return fail(BMND_ERR_INVALID_ARG, "clipping needs the norm scratch");
     const float bc1 = 1.0f - powf(beta1, static_cast<float>(step));
     const float bc2 = 1.0f - powf(beta2, static_cast<float>(step));
     cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_u64);
+    if (clip_norm > 0.0f) {
+        BMND_CUDA_TRY(cudaMemsetAsync(d_sumsq, 0, sizeof(double), stream));
+        sumsq_kernel<<<launch_blocks(n, 256), 256, 0, stream>>>(d_grad, n, d_sumsq);
+        BMND_LAUNCH_CHECK("sumsq_kernel");
+    }
     adam_kernel<<<launch_blocks(n, 256), 256, 0, stream>>>(d_params, d_grad, d_m, d_v, n, lr, beta1, beta2, eps, bc1,
-                                                           bc2);
+                                                           bc2, clip_norm, d_sumsq);
     BMND_LAUNCH_CHECK("adam_kernel");
     return BMND_OK;
 }

@@ -62,6 +62,7 @@ class PilotNet:
         self._v = torch.zeros_like(self.params)
         self._grad = torch.zeros_like(self.params)
         self._loss = torch.zeros(1, dtype=torch.float64, device=self.device)
+        self._sumsq = torch.zeros(1, dtype=torch.float64, device=self.device)
         self.step = 0
         self._packed = None
         self._packed_version = -1
@@ -145,22 +146,31 @@ class PilotNet:
             self._loss.data_ptr(), ws.data_ptr(), ws.numel(), self._stream()))
         return self._loss, self._grad
 
-    def adam_step(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8):
+    def adam_step(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8,
+                  clip: float = 1.0):
+        """Adam on the last gradient, clipped to an L2 norm of ``clip`` (<= 0: none)."""
         self.step += 1
         _abi.check(_abi.lib().bmnd_pilotnet_adam(
             self.n_params, self.params.data_ptr(), self._grad.data_ptr(), self._m.data_ptr(), self._v.data_ptr(),
-            self.step, float(lr), float(beta1), float(beta2), float(eps), self._stream()))
+            self.step, float(lr), float(beta1), float(beta2), float(eps), float(clip), self._sumsq.data_ptr(),
+            self._stream()))
         self._version += 1
 
     def fit(self, pairs, steps: int = 2000, crop: int = 32, batch: int = 4, lr: float = 3e-4, seed: int = 0,
-            log_every: int = 100, log=None):
-        """Adam on random crops of (noisy, target) CUDA volume pairs; returns the loss history."""
+            log_every: int = 100, log=None, clip: float = 1.0):
+        """Adam on random crops of (noisy, target) CUDA volume pairs; returns the
+        loss history.  The gradient is clipped to an L2 norm of ``clip``; the
+        parameters with the lowest logged loss (a running mean over the last
+        ``log_every`` steps) are kept at the end, which guards against a late
+        divergence."""
         torch = _torch()
         rng = np.random.default_rng(seed)
         shape = tuple(int(s) for s in pairs[0][0].shape)
         cs = tuple(min(crop, s) for s in shape)
         xb = torch.empty((batch,) + cs, dtype=torch.float32, device=self.device)
         tb = torch.empty_like(xb)
+        running = torch.zeros(1, dtype=torch.float64, device=self.device)
+        best, best_params = math.inf, None
         history = []
         for it in range(steps):
             for b in range(batch):
@@ -171,14 +181,23 @@ class PilotNet:
                 xb[b].copy_(x[sl])
                 tb[b].copy_(t[sl])
             loss, _ = self.gradient(xb, tb)
+            running += loss
             frac = it / max(steps - 1, 1)
             rate = lr * (0.5 * (1.0 + math.cos(math.pi * frac)) * 0.9 + 0.1)  # cosine to lr / 10
-            self.adam_step(rate)
+            self.adam_step(rate, clip=clip)
             if (it + 1) % log_every == 0 or it == steps - 1:
-                value = float(loss.item())
+                n = (it % log_every) + 1
+                value = float(running.item()) / n
+                running.zero_()
                 history.append((it + 1, value))
+                if value < best:
+                    best = value
+                    best_params = self.params.clone()
                 if log:
-                    log(f"step {it + 1} loss {value:.6f}")
+                    log(f"step {it + 1} loss {value:.6f} grad_norm {math.sqrt(float(self._sumsq.item())):.4f}")
+        if best_params is not None:
+            self.params.copy_(best_params)
+            self._version += 1
         return history
 
     # -- persistence -------------------------------------------------------

@@ -197,6 +197,22 @@ int32_t bmnd_stage(const BmndStageParams* params, const float* d_noisy, const fl
                    uint64_t workspace_bytes, uint64_t stream);
 
 /*
+ * bmnd_stage() plus the stage's sigma map (the reference's return_sigma_map,
+ * bmndalgo.py:253-256, :576-597, :874-875, :1001-1010, :1048-1062): every
+ * group's noise sigma is aggregated with the weights of its estimate, per
+ * coefficient for hard thresholding and as the group mean for Wiener, and
+ * divided by the aggregated weight; voxels no patch covers get global_sigma.
+ * d_sel/d_count/d_accepted are optional as in bmnd_stage().  The workspace is
+ * bmnd_stage_sigma_workspace_bytes() bytes, 256-byte aligned.
+ */
+int32_t bmnd_stage_sigma_workspace_bytes(const BmndStageParams* params, int64_t n_refs,
+                                         uint64_t* out_bytes);
+int32_t bmnd_stage_sigma(const BmndStageParams* params, const float* d_noisy, const float* d_pilot,
+                         const int32_t* d_refs, int64_t n_refs, float* d_out, float* d_sigma_map,
+                         float global_sigma, int32_t* d_sel, int32_t* d_count, int32_t* d_accepted,
+                         void* d_workspace, uint64_t workspace_bytes, uint64_t stream);
+
+/*
  * Both stages back to back (hard thresholding, then Wiener on the pilot),
  * i.e. the body of bmnd() for a direct-Poisson profile.  ht/wiener are the
  * stage parameters, refs_ht/refs_wiener their schedules; d_ht_out receives
@@ -279,9 +295,12 @@ int32_t bmnd_pilotnet_gradient(const BmndPilotNet* net, const void* d_packed, co
 int32_t bmnd_pilot_tile_deviance(int32_t ndim, int32_t batch, const int32_t* shape, int32_t edge,
                                  const float* d_noisy, const float* d_pilot, const float* d_table,
                                  int32_t n_table, float ln_mu0, float d_ln, double* d_out, uint64_t stream);
-/* One Adam step (bias-corrected, step counts from 1). */
+/* One Adam step (bias-corrected, step counts from 1) on the gradient scaled to
+ * an L2 norm of at most clip_norm (clip_norm <= 0: no clipping); d_sumsq is one
+ * double of scratch that receives the squared gradient norm. */
 int32_t bmnd_pilotnet_adam(int64_t n, float* d_params, const float* d_grad, float* d_m, float* d_v,
-                           int32_t step, float lr, float beta1, float beta2, float eps, uint64_t stream);
+                           int32_t step, float lr, float beta1, float beta2, float eps, float clip_norm,
+                           double* d_sumsq, uint64_t stream);
 
 #ifdef __cplusplus
 }

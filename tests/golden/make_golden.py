@@ -11,6 +11,7 @@ Usage::
 
     python tests/golden/make_golden.py unit
     python tests/golden/make_golden.py pipeline bm3d_32 [bm4d_16 ...]
+    python tests/golden/make_golden.py sigma bm3d_32 [bm4d_12x16x20 ...]
     python tests/golden/make_golden.py list
 
 ``unit`` writes ``unit_*.npz`` (distances, canonical keys, transforms, exact
@@ -120,6 +121,40 @@ def run_pipeline(name: str) -> None:
     path = os.path.join(HERE, f"pipe_{name}.npz")
     np.savez_compressed(path, **payload)
     print(f"{name}: {noisy.shape} in {elapsed:.1f} s -> {path}")
+
+
+def run_sigma(name: str) -> None:
+    """sigma_<case>.npz: the reference's return_sigma_map output (global value and
+    both stages' maps), with the stage estimates and match sets of the same run."""
+    import bmnd as ref
+
+    kind, gen, kwargs, extra = PIPELINE_CASES[name]
+    clean, noisy = _make_input(gen, kwargs)
+    profile_cls = ref.BM3DProfile if kind == "bm3d" else ref.BM4DProfile
+    profile = profile_cls(noise_model=ref.NoiseModel.POISSON, **extra)
+    stages, matches = {}, {}
+
+    def stage_cb(stage, est):
+        stages[stage] = np.asarray(est, dtype=np.float32)
+
+    def bm_cb(stage, result):
+        max_stack = profile.ht_max_stack_size if stage == "ht" else profile.wiener_max_stack_size
+        matches[stage] = _pack_matches(result, max_stack, noisy.ndim)
+
+    t0 = time.time()
+    out, smap = ref.bmnd(noisy, profile, return_sigma_map=True, stage_callback=stage_cb, blockmatch_callback=bm_cb)
+    elapsed = time.time() - t0
+    payload = dict(kind=np.array(kind), clean=clean, noisy=noisy, ht=stages["ht"], wiener=stages["wiener"],
+                   out=np.asarray(out, dtype=np.float32), global_sigma=np.float64(smap["global"]),
+                   sigma_ht=np.asarray(smap["ht"], dtype=np.float32),
+                   sigma_wiener=np.asarray(smap["wiener"], dtype=np.float32), seconds=np.float64(elapsed))
+    for stage, (sel, counts, accepted, refs) in matches.items():
+        payload[f"{stage}_sel"] = sel
+        payload[f"{stage}_count"] = counts
+        payload[f"{stage}_refs"] = refs
+    path = os.path.join(HERE, f"sigma_{name}.npz")
+    np.savez_compressed(path, **payload)
+    print(f"sigma {name}: {noisy.shape} in {elapsed:.1f} s -> {path}")
 
 
 def run_unit() -> None:
@@ -261,6 +296,10 @@ def main(argv: list[str]) -> None:
         return
     if argv[0] == "unit":
         run_unit()
+        return
+    if argv[0] == "sigma":
+        for name in argv[1:]:
+            run_sigma(name)
         return
     if argv[0] == "pipeline":
         for name in argv[1:]:
