@@ -169,7 +169,8 @@ struct Geom {
 // transform of the variance propagation).  Each thread holds one column in
 // registers and produces IC of its N outputs; a round takes whole columns
 // (all their chunks) and reads them completely before any thread writes, so
-// the product can overwrite its input.
+// the product can overwrite its input.  blockDim.x must be a multiple of
+// 32 * CH so that each warp holds a single chunk.
 template <int KIND>
 __device__ __forceinline__ float gmat(const float* G, int N, int i, int k) {
     float m = KIND == 1 ? G[k * N + i] : G[i * N + k];
@@ -180,10 +181,12 @@ template <int N, int KIND>
 __device__ void group_axis_inplace(float* buf, int P, const float* G) {
     constexpr int IC = N >= 16 ? 8 : N;  // outputs per thread
     constexpr int CH = N / IC;           // threads per column
+    // a warp shares one output chunk over 32 consecutive columns: matrix reads
+    // are broadcasts, column reads and writes hit consecutive banks
     const int cols = static_cast<int>(blockDim.x) / CH;
     for (int c0 = 0; c0 < P; c0 += cols) {
-        const int p = c0 + static_cast<int>(threadIdx.x) / CH;
-        const int i0 = (static_cast<int>(threadIdx.x) % CH) * IC;
+        const int p = c0 + static_cast<int>(threadIdx.x) % cols;
+        const int i0 = (static_cast<int>(threadIdx.x) / cols) * IC;
         const bool act = static_cast<int>(threadIdx.x) < cols * CH && p < P;
         float x[N];
         if (act) {
