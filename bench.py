@@ -399,7 +399,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         psnr_fast = psnr(fast["out"].cpu().numpy(), clean)
         fast_block = {
             "path": "learned pilot (BF16 tensor-core residual net) + per-tile deviance fallback + Wiener stage "
-                    "with max stack 16, one exact variance plane, approximate screening",
+                    "with reference step 4, approximate Poisson sigma, approximate screening",
             "value": nvox * world / (fast["ms"] * 1e-3) / 1e6,
             "ms_per_step": fast["ms"],
             "psnr_db": psnr_fast,

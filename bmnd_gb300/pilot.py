@@ -14,8 +14,9 @@ its pilot:
    voxels) and pasted back.  ``excess_high`` is calibrated on the plain
    stage-1 pilots of the training volumes;
 3. the Wiener stage on that pilot, with the stage-2 settings of
-   ``FAST_STAGE2`` (maximum stack 16, one exact variance plane, matching by
-   screening distances with exact rescoring of the selected candidates).
+   ``FAST_STAGE2`` (reference step 4, the approximate Poisson sigma for every
+   plane, matching by screening distances with exact rescoring of the selected
+   candidates).
 
 The net is trained on the GPU by its own forward and backward kernels
 (``PilotNet.fit``) on pairs (noisy volume, plain stage-1 estimate) that the
@@ -35,8 +36,15 @@ from . import _abi, phantoms
 from .api import _torch, stage_device
 from .validation import resolve_profile
 
-# stage-2 settings of the fast path: everything else stays at the profile's values
-FAST_STAGE2 = dict(wiener_max_stack_size=16, k=1)
+# Stage-2 settings of the fast path by dimensionality (everything else stays at
+# the profile's values).  3-D: reference step 4 instead of 3 and the
+# approximate Poisson sigma for every plane (k = 0); chosen by a sweep at
+# 256^3 on three seeds, where the learned pilot plus these settings gained
+# 0.044 to 0.09 dB over the plain path at 7.2x its speed.
+FAST_STAGE2 = {
+    3: dict(wiener_step=(4, 4, 4), k=0),
+    2: dict(wiener_step=(4, 4), k=0),
+}
 FAST_MATCH_PRECISION = "approx"
 
 
@@ -246,6 +254,8 @@ def training_pairs(kind: str = "bm4d", size: int = 128, count: int = 8, seed0: i
     for i in range(count):
         if kind == "bm4d":
             _, noisy = phantoms.ellipsoids_3d(size, seed=seed0 + i)
+        elif size >= 1024:
+            _, noisy = phantoms.blobs_2d(size, seed=seed0 + i)
         else:
             _, noisy = phantoms.shapes_2d(size, seed=seed0 + i)
         x = torch.from_numpy(noisy).cuda()
@@ -365,13 +375,19 @@ DEFAULT_EXCESS_HIGH = 0.5
 # the fast path
 # ---------------------------------------------------------------------------
 def fast_profile(profile):
+    """Copy of ``profile`` with the fast path's stage-2 settings."""
     p = copy.deepcopy(profile)
-    for k, v in FAST_STAGE2.items():
+    for k, v in FAST_STAGE2[len(tuple(profile.wiener_block_size))].items():
         setattr(p, k, v)
     return p
 
 
-def bmnd_fast(noisy, profile, net: PilotNet, *, tile: int = 32, excess_high: float | None = None,
+def default_tile(ndim: int) -> int:
+    """Residual-check tile edge: 32^3 voxels in 3-D, 64^2 pixels in 2-D."""
+    return 32 if ndim == 3 else 64
+
+
+def bmnd_fast(noisy, profile, net: PilotNet, *, tile: int | None = None, excess_high: float | None = None,
               stage2: bool = True, match_precision: str = FAST_MATCH_PRECISION, check: bool = True,
               details: dict | None = None):
     """Learned-pilot fast path on a float32 CUDA volume; returns the CUDA estimate.
@@ -382,6 +398,8 @@ def bmnd_fast(noisy, profile, net: PilotNet, *, tile: int = 32, excess_high: flo
     x = noisy.contiguous().to(torch.float32)
     shape = tuple(int(s) for s in x.shape)
     resolve_profile(profile, shape)
+    if tile is None:
+        tile = default_tile(x.dim())
     pilot = net.forward(x)
     n_fb, excess = 0, None
     if check:
@@ -396,13 +414,13 @@ def bmnd_fast(noisy, profile, net: PilotNet, *, tile: int = 32, excess_high: flo
     return stage_device(x, p2, "wiener", pilot, match_precision=match_precision if stage2 else "exact")
 
 
-def calibrate_excess_high(pairs, tile: int = 32, spread: float = 3.0) -> float:
+def calibrate_excess_high(pairs, tile: int | None = None, spread: float = 3.0) -> float:
     """Upper bound of the per-tile excess deviance: the largest value the plain
     stage-1 pilots (the training targets) reach on the training volumes, plus
     ``spread`` standard deviations of their per-tile values."""
     vals = []
     for x, t in pairs:
-        e, _ = tile_excess(x, t, tile)
+        e, _ = tile_excess(x, t, tile or default_tile(x.dim()))
         vals.append(np.ravel(e))
     v = np.concatenate(vals)
     return float(np.max(v) + spread * np.std(v))

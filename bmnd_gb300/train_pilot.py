@@ -19,7 +19,7 @@ import time
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--kind", default="bm4d", choices=["bm4d", "bm3d"])
-    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--size", type=int, default=None)
     ap.add_argument("--count", type=int, default=8)
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--crop", type=int, default=32)
@@ -45,6 +45,8 @@ def main(argv=None):
     channels = args.channels or (48 if nd == 3 else 32)
     layers = args.layers or (8 if nd == 3 else 10)
     crop = args.crop if nd == 3 else max(args.crop, 64)
+    if args.size is None:
+        args.size = 256 if nd == 3 else 2048
     t0 = time.time()
     pairs = training_pairs(args.kind, args.size, args.count)
     torch.cuda.synchronize()
@@ -58,7 +60,9 @@ def main(argv=None):
     net.excess_high = calibrate_excess_high(pairs)
     from bmnd_gb300.pilot import tile_excess
 
-    ev = np.concatenate([np.ravel(tile_excess(x, t, 32)[0]) for x, t in pairs])
+    from bmnd_gb300.pilot import default_tile
+
+    ev = np.concatenate([np.ravel(tile_excess(x, t, default_tile(nd))[0]) for x, t in pairs])
     print(f"plain stage-1 tile excess: min {ev.min():.4f} median {np.median(ev):.4f} max {ev.max():.4f}", flush=True)
     out = args.out or default_net_path(args.kind)
     os.makedirs(os.path.dirname(out), exist_ok=True)
@@ -68,6 +72,8 @@ def main(argv=None):
     prof = (bg.BM4DProfile if nd == 3 else bg.BM3DProfile)(noise_model=bg.NoiseModel.POISSON)
     if nd == 3:
         clean, noisy = phantoms.ellipsoids_3d(args.size, seed=2000)
+    elif args.size >= 1024:
+        clean, noisy = phantoms.blobs_2d(args.size, seed=2000)
     else:
         clean, noisy = phantoms.shapes_2d(args.size, seed=2000)
     x = torch.from_numpy(noisy).cuda()
