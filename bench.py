@@ -35,7 +35,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "Mvoxel/s at 256^3 BM4D: learned+BF16 vs plain GPU at <=0.05 dB PSNR loss"
+METRIC = "Mvoxel/s at 256\u00b3 BM4D: learned+BF16 vs plain GPU at \u22640.05 dB PSNR loss"
 
 WORKLOADS = {
     "bm4d256": dict(kind="bm4d", size=256, desc="256^3 BM4D-Poisson, 30 ellipsoids"),
@@ -182,8 +182,14 @@ def cpu_baseline(workload: str, seed: int, budget_s: float = 20.0) -> dict:
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def time_kernels(torch, noisy_t, profile, reps: int = 2) -> dict:
-    """CUDA-event times of the block-matching kernels and of each stage."""
+def time_kernels(torch, noisy_t, profile, reps: int = 2, stages=("ht", "wiener"), pilot=None,
+                 precision=None) -> dict:
+    """CUDA-event times of the block-matching kernels and of each stage.
+
+    ``pilot`` (optional) is the Wiener stage's pilot; by default it is the
+    stage-1 output, as in the plain pipeline.  ``precision`` maps a stage to
+    its matching precision (default: exact for stage 1, bounded screening for
+    stage 2, which is what the plain pipeline runs)."""
     import bmnd_gb300 as bg
     from bmnd_gb300 import _abi, plan
     from bmnd_gb300.validation import resolve_profile
@@ -193,9 +199,12 @@ def time_kernels(torch, noisy_t, profile, reps: int = 2) -> dict:
     resolved = resolve_profile(profile, shape)
     stream = torch.cuda.current_stream()
     res = {}
-    pilot = None  # the stage-1 estimate, as in the pipeline
-    for stage in ("ht", "wiener"):
-        p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k)
+    if precision is None:
+        precision = {"ht": _abi.MATCH_EXACT, "wiener": _abi.MATCH_FAST}
+    for stage in stages:
+        stage_prec = precision[stage]
+        p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k,
+                              stage_prec if stage_prec == _abi.MATCH_APPROX else _abi.MATCH_EXACT)
         block = tuple(getattr(profile, f"{stage}_block_size"))
         counts = tuple(s - b + 1 for s, b in zip(shape, block))
         sched = plan.reference_schedule(profile, counts, stage)
@@ -213,7 +222,7 @@ def time_kernels(torch, noisy_t, profile, reps: int = 2) -> dict:
         mp.max_matches, mp.min_matches, mp.prefer_power_of_two = p.max_stack, p.min_stack, 1
         mp.distance, mp.stabilize_ties, mp.count_scale = p.distance, 1, p.count_scale
         # the pipeline matches the real-valued pilot with the screened path
-        mp.precision = _abi.MATCH_EXACT if stage == "ht" else _abi.MATCH_FAST
+        mp.precision = stage_prec
         sh = (ctypes.c_int32 * len(shape))(*shape)
         bl = (ctypes.c_int32 * len(shape))(*block)
         src = noisy_t if stage == "ht" else pilot
@@ -360,38 +369,67 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
 
     kt = time_kernels(torch, x, profile)
     peaks = load_peaks()
-    # dominant kernel: the larger of the two matching launches or group-filter launches
-    cands = []
-    for stage in ("ht", "wiener"):
-        k = kt[stage]
-        cands.append((k["match_ms"], f"blockmatch_{stage}", stage))
-        cands.append((k["stage_ms"] - k["match_ms"], f"groupfilter_{stage}", stage))
-    dom_ms, dom_name, dom_stage = max(cands)
-    k = kt[dom_stage]
-    if dom_name.startswith("blockmatch"):
-        # algorithmic bytes: read the matching source once, write the match table
-        alg_bytes = nvox * 4 + k["groups"] * (int(profile.ht_max_stack_size if dom_stage == "ht" else profile.wiener_max_stack_size) + 2) * 4
-    else:
-        # read noisy (+ pilot) once, write float64 numerator and denominator once
-        alg_bytes = nvox * (4 if dom_stage == "ht" else 8) + nvox * 16
-    achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
-    traffic = profile_traffic(dom_name, args.workload)
-    # the dominant kernels are FP32/SFU compute bound; report that rate too
     sm_mhz = clocks.get("sm_mhz") or 2070.0
     fp32_peak = 152 * 128 * sm_mhz * 1e6  # FP32 instructions per second
-    if dom_name.startswith("groupfilter"):
-        kk = min(4, int(k["mean_group"]))
-        pairs = k["groups"] * k["mean_group"] * k["P"] * kk * k["P"]
-        compute = {
-            "what": "exact overlap-aware variance: entry x coefficient pairs (1 FP32 mul + 1 add each)",
-            "achieved_gpairs_s": pairs / (dom_ms * 1e-3) / 1e9,
-            "fp32_ops_frac_of_peak": 2 * pairs / (dom_ms * 1e-3) / fp32_peak,
-        }
+    from bmnd_gb300 import _abi
+
+    # kernels of the measured path: the fast path when it ran (its Wiener
+    # stage on the learned pilot, and the net), else the plain path
+    cands = []
+    if fast is not None:
+        fprof = pl.fast_profile(profile)
+        kf = time_kernels(torch, x, fprof, stages=("wiener",), pilot=fast["pilot"],
+                          precision={"wiener": _abi.MATCH_APPROX})
+        kt["fast_wiener"] = kf["wiener"]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            fast["net"].forward(x)
+        e1.record(stream)
+        e1.synchronize()
+        kt["pilot_net_ms"] = e0.elapsed_time(e1) / 3
+        k = kf["wiener"]
+        cands.append((k["match_ms"], "blockmatch_wiener_approx", "fast_wiener"))
+        cands.append((k["stage_ms"] - k["match_ms"], "groupfilter_wiener_fast", "fast_wiener"))
+        cands.append((kt["pilot_net_ms"], "pilot_net", None))
     else:
-        compute = {
-            "what": "Poisson-deviance voxel terms",
-            "achieved_gterms_s": k["voxel_terms"] / (dom_ms * 1e-3) / 1e9,
-        }
+        for stage in ("ht", "wiener"):
+            k = kt[stage]
+            cands.append((k["match_ms"], f"blockmatch_{stage}", stage))
+            cands.append((k["stage_ms"] - k["match_ms"], f"groupfilter_{stage}", stage))
+    dom_ms, dom_name, dom_stage = max(cands)
+    if dom_name == "pilot_net":
+        # the C -> C layers: 2 * taps * C * C flops per voxel each
+        nd = noisy.ndim
+        C, L_ = fast["net"].channels, fast["net"].layers
+        flops = 2.0 * nvox * (3 ** nd) * C * C * (L_ - 2)
+        achieved = flops / (dom_ms * 1e-3) / 1e12
+        bound, unit, peak_v, alg_bytes = "tensor", "TFLOP/s", peaks["bf16_tflops"], None
+        compute = {"what": "BF16 multiply-adds of the C->C layers on the tensor cores"}
+    else:
+        k = kt[dom_stage]
+        wiener = "wiener" in dom_stage
+        if dom_name.startswith("blockmatch"):
+            # algorithmic bytes: read the matching source once, write the match table
+            stack = int(profile.wiener_max_stack_size if wiener else profile.ht_max_stack_size)
+            alg_bytes = nvox * 4 + k["groups"] * (stack + 2) * 4
+            compute = {
+                "what": "Poisson-deviance voxel terms",
+                "achieved_gterms_s": k["voxel_terms"] / (dom_ms * 1e-3) / 1e9,
+            }
+        else:
+            # read noisy (+ pilot) once, write float64 numerator and denominator once
+            alg_bytes = nvox * (8 if wiener else 4) + nvox * 16
+            kk = min(int(fprof.k) if dom_stage == "fast_wiener" else 4, int(k["mean_group"]))
+            pairs = k["groups"] * k["mean_group"] * k["P"] * kk * k["P"]
+            compute = {
+                "what": "exact overlap-aware variance: entry x coefficient pairs (one FP32 fused multiply-add each)",
+                "achieved_gpairs_s": pairs / (dom_ms * 1e-3) / 1e9,
+                "fp32_ops_frac_of_peak": 2 * pairs / (dom_ms * 1e-3) / fp32_peak,
+            }
+        achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
+        bound, unit, peak_v = "hbm", "GB/s", peaks["hbm_gbs"]
+    traffic = profile_traffic(dom_name, args.workload)
     launches_per_step = 6  # per stage: blockmatch, group filter, finalize
     plain_value = nvox * world / (ms * 1e-3) / 1e6
     psnr_plain = psnr(out.cpu().numpy(), clean)
@@ -459,11 +497,11 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         "fast": fast_block,
         "roofline": {
             "kernel": dom_name,
-            "bound": "hbm",
+            "bound": bound,
             "achieved": achieved,
-            "peak": peaks["hbm_gbs"],
-            "unit": "GB/s",
-            "frac": achieved / peaks["hbm_gbs"],
+            "peak": peak_v,
+            "unit": unit,
+            "frac": achieved / peak_v,
             "traffic": traffic,
             "peak_source": peaks["source"],
             "ms_per_launch": dom_ms,
