@@ -417,6 +417,11 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
                 "what": "Poisson-deviance voxel terms",
                 "achieved_gterms_s": k["voxel_terms"] / (dom_ms * 1e-3) / 1e9,
             }
+            if dom_name == "blockmatch_wiener_approx":
+                # one lg2 per term on the SFU (16 results per clock per SM)
+                sfu = 152 * 16 * sm_mhz * 1e6
+                compute["sfu_bound_gterms_s"] = sfu / 1e9
+                compute["frac_of_sfu_bound"] = k["voxel_terms"] / (dom_ms * 1e-3) / sfu
         else:
             # read noisy (+ pilot) once, write float64 numerator and denominator once
             alg_bytes = nvox * (8 if wiener else 4) + nvox * 16

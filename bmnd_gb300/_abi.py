@@ -42,6 +42,8 @@ WEIGHT_VARIANCE = 1
 MATCH_EXACT = 0
 MATCH_FAST = 1
 MATCH_APPROX = 2
+CONV_TCGEN05 = 0
+CONV_MMA_SYNC = 1
 
 STATIC_SCRATCH_BYTES = 64 << 20
 
@@ -153,6 +155,9 @@ SIGNATURES = {
     "bmnd_pilotnet_packed_bytes": (_I32, [_PNP, _U64P]),
     "bmnd_pilotnet_workspace_bytes": (_I32, [_PNP, _I32, _U64P]),
     "bmnd_pilotnet_pack": (_I32, [_PNP, _VP, _VP, _U64]),
+    "bmnd_pilotnet_status": (_I32, [_PNP, _VP, _U64]),
+    "bmnd_pilotnet_set_conv_engine": (_I32, [_I32]),
+    "bmnd_pilotnet_get_conv_engine": (_I32, [_I32P]),
     "bmnd_pilotnet_forward": (_I32, [_PNP, _VP, _VP, _VP, _VP, _VP, _U64, _U64]),
     "bmnd_pilotnet_gradient": (_I32, [_PNP, _VP, _VP, _VP, _VP, _VP, _VP, _U64, _U64]),
     "bmnd_pilotnet_adam": (_I32, [_I64, _VP, _VP, _VP, _VP, _I32, ctypes.c_float, ctypes.c_float,

@@ -404,6 +404,273 @@ __global__ void __launch_bounds__(256, 1) conv_mid_kernel(const bf16* __restrict
 }
 
 // ---------------------------------------------------------------------------
+// C -> C layers with tcgen05 (fifth-generation tensor cores, accumulator in
+// tensor memory).
+//
+// Output tile: one z plane of 16 rows x 8 voxels = the M = 128 rows of one
+// tcgen05.mma (kind::f16, BF16 in, FP32 accumulate, N = C, K = 16).  The
+// input halo of the tile is staged chunk-major, [8-channel chunk][halo voxel]
+// [16 bytes], so that for every tap the A operand is a no-swizzle K-major
+// matrix: a core matrix is 8 consecutive voxels of one row (128 contiguous
+// bytes), the next 8 rows of M are the next row of the halo (stride 16 * hx
+// bytes), and the second 8 channels of the K = 16 slice are the next chunk
+// (stride 16 * halo bytes).  The weights sit in shared memory for the whole
+// launch as B = W_t[ci][co] in the same K-major core-matrix layout.  One
+// thread issues the 27 x C/16 MMAs of a tile and commits them to an mbarrier;
+// meanwhile all threads prefetch the next tile's halo with cp.async into the
+// second buffer; the four warps then read the accumulator rows they own
+// (tcgen05.ld 32x32b) and apply the epilogue.  Every mbarrier wait is bounded:
+// on timeout the kernel records an error, stops issuing work and frees its
+// tensor memory.
+// ---------------------------------------------------------------------------
+template <int ND, int C>
+struct TcTile {
+    static constexpr int tx = 8, ty = 16;
+    static constexpr int hx = tx + 2, hy = ty + 2, hz = ND == 3 ? 3 : 1;
+    static constexpr int halo = hx * hy * hz;
+    static constexpr int chunks = C / 8;
+    static constexpr int taps = ND == 3 ? 27 : 9;
+    static constexpr int kc = C / 16;
+    static constexpr size_t wbytes = static_cast<size_t>(taps) * kc * 2 * C * 16;  // B core matrices
+    static constexpr size_t tbytes = static_cast<size_t>(chunks) * halo * 16;      // one A halo tile
+    static constexpr size_t bytes = wbytes + 2 * tbytes;
+    static constexpr uint32_t tmem_cols = C <= 32 ? 32 : 64;
+};
+
+// B for tcgen05: element (t, kc, kk, n, e) = W[t][ci = 16 kc + 8 kk + e][co = n]
+// (forward) or W[taps-1-t][ci = n][co = 16 kc + 8 kk + e] (data gradient), BF16
+template <int ND, int C>
+__global__ void pack_tc_kernel(const float* __restrict__ W, bf16* __restrict__ out, int backward) {
+    constexpr int T = Tile<ND>::taps;
+    const int64_t total = static_cast<int64_t>(T) * (C / 16) * 2 * C * 8;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t r = i;
+        const int e = static_cast<int>(r % 8);
+        r /= 8;
+        const int n = static_cast<int>(r % C);
+        r /= C;
+        const int kk = static_cast<int>(r % 2);
+        r /= 2;
+        const int kc = static_cast<int>(r % (C / 16));
+        const int t = static_cast<int>(r / (C / 16));
+        const int k = 16 * kc + 8 * kk + e;
+        const float v = backward ? W[(static_cast<int64_t>(T - 1 - t) * C + n) * C + k]
+                                 : W[(static_cast<int64_t>(t) * C + k) * C + n];
+        out[i] = __float2bfloat16_rn(v);
+    }
+}
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t smem_addr, uint32_t lbo, uint32_t sbo) {
+    // no-swizzle K-major shared-memory matrix descriptor: start, leading
+    // (K-direction core matrix) and stride (M/N-direction 8-row group) byte
+    // offsets, each >> 4; bits 46-47 = 1 (descriptor version); layout 0
+    return static_cast<uint64_t>((smem_addr >> 4) & 0x3FFFu) |
+           (static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16) |
+           (static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;\n" : "=l"(t));
+    return t;
+}
+
+// wait for the phase of parity `phase` to complete, for at most limit_ns
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, uint64_t limit_ns) {
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (done) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+}
+
+template <int ND, int C>
+__device__ __forceinline__ void tc_load_tile(const bf16* __restrict__ in, const NetGeo& g, int b, int z0, int y0,
+                                             int x0, uint32_t tile_addr) {
+    using TT = TcTile<ND, C>;
+    for (int i = threadIdx.x; i < TT::halo * TT::chunks; i += blockDim.x) {
+        const int vox = i % TT::halo, ch = i / TT::halo;
+        const int hxi = vox % TT::hx, hyi = (vox / TT::hx) % TT::hy, hzi = vox / (TT::hx * TT::hy);
+        const int xx = x0 + hxi - 1, yy = y0 + hyi - 1, zz = ND == 3 ? z0 + hzi - 1 : z0;
+        const bool inside = xx >= 0 && xx < g.W && yy >= 0 && yy < g.H && zz >= 0 && zz < g.D;
+        const bf16* src = inside ? in + vox_index(g, b, zz, yy, xx) * C + ch * 8 : in;
+        const uint32_t dst = tile_addr + static_cast<uint32_t>((ch * TT::halo + vox) * 16);
+        const uint32_t n = inside ? 16u : 0u;  // 0: fill with zeros, read nothing
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+template <int ND, int C>
+__global__ void __launch_bounds__(128, 1) conv_mid_tc_kernel(const bf16* __restrict__ in, const uint4* __restrict__ wtc,
+                                                             const float* __restrict__ bias,
+                                                             const bf16* __restrict__ mask, bf16* __restrict__ out,
+                                                             NetGeo g, int* __restrict__ err) {
+    using TT = TcTile<ND, C>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t w_addr = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+    const uint32_t t_addr0 = w_addr + static_cast<uint32_t>(TT::wbytes);  // halo tile buffers
+    const uint32_t t_addr1 = t_addr0 + static_cast<uint32_t>(TT::tbytes);
+    const uint32_t mbar_addr = static_cast<uint32_t>(__cvta_generic_to_shared(&mbar));
+
+    // weights for the whole launch
+    for (int i = tid; i < static_cast<int>(TT::wbytes / 16); i += blockDim.x)
+        reinterpret_cast<uint4*>(smem)[i] = wtc[i];
+    if (warp == 0) {
+        const uint32_t slot = static_cast<uint32_t>(__cvta_generic_to_shared(&tmem_slot));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(slot),
+                     "r"(TT::tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar_addr) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    const int tiles_x = (g.W + TT::tx - 1) / TT::tx;
+    const int tiles_y = (g.H + TT::ty - 1) / TT::ty;
+    const int tiles_z = g.D;
+    const int64_t ntiles = static_cast<int64_t>(tiles_x) * tiles_y * tiles_z * g.nb;
+    auto decode = [&](int64_t tl, int& b, int& z0, int& y0, int& x0) {
+        int64_t r = tl;
+        x0 = static_cast<int>(r % tiles_x) * TT::tx;
+        r /= tiles_x;
+        y0 = static_cast<int>(r % tiles_y) * TT::ty;
+        r /= tiles_y;
+        z0 = static_cast<int>(r % tiles_z);
+        b = static_cast<int>(r / tiles_z);
+    };
+    // instruction descriptor: FP32 accumulator, BF16 A and B, both K-major,
+    // N = C (bits 17-22: N >> 3), M = 128 (bits 24-28: M >> 4)
+    constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(C >> 3) << 17) |
+                               (static_cast<uint32_t>(128 >> 4) << 24);
+    constexpr uint64_t kWaitLimitNs = 1000000000ull;  // one tile takes microseconds
+
+    int64_t tl = blockIdx.x;
+    int cur = 0;
+    uint32_t phase = 0;
+    bool ok = true;
+    if (tl < ntiles) {
+        int b, z0, y0, x0;
+        decode(tl, b, z0, y0, x0);
+        tc_load_tile<ND, C>(in, g, b, z0, y0, x0, t_addr0);
+    }
+    for (; tl < ntiles && ok; tl += gridDim.x) {
+        int b, z0, y0, x0;
+        decode(tl, b, z0, y0, x0);
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        if (tid == 0) {
+#pragma unroll 1
+            for (int t = 0; t < TT::taps; ++t) {
+                int dz, dy, dx;
+                tap_offsets<ND>(t, dz, dy, dx);
+                const int vox0 = ((ND == 3 ? dz + 1 : 0) * TT::hy + dy + 1) * TT::hx + dx + 1;
+#pragma unroll
+                for (int k = 0; k < TT::kc; ++k) {
+                    const uint64_t ad = umma_desc((cur ? t_addr1 : t_addr0) + static_cast<uint32_t>((2 * k * TT::halo + vox0) * 16),
+                                                  TT::halo * 16, TT::hx * 16);
+                    const uint64_t bd =
+                        umma_desc(w_addr + static_cast<uint32_t>((t * TT::kc + k) * 2 * C * 16), C * 16, 128);
+                    const uint32_t acc = (t | k) != 0 ? 1u : 0u;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                        : "memory");
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             mbar_addr)
+                         : "memory");
+        }
+        // prefetch the next tile into the other buffer (its last readers, the
+        // previous tile's MMAs, completed before the previous epilogue)
+        const int64_t nx = tl + gridDim.x;
+        if (nx < ntiles) {
+            int b2, z2, y2, x2;
+            decode(nx, b2, z2, y2, x2);
+            tc_load_tile<ND, C>(in, g, b2, z2, y2, x2, cur ? t_addr0 : t_addr1);
+        }
+        if (!mbar_wait(mbar_addr, phase, kWaitLimitNs)) {
+            atomicExch(err, 1);
+            ok = false;
+        }
+        ok = __syncthreads_and(ok) != 0;  // uniform, so every barrier below is reached by all threads
+        phase ^= 1;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        if (ok) {
+            // epilogue: this thread owns accumulator row m = 32 * warp + lane
+            const int m = tid;
+            const int xx = x0 + (m % TT::tx), yy = y0 + m / TT::tx;
+            const bool inside = xx < g.W && yy < g.H;
+            const int64_t v = inside ? vox_index(g, b, z0, yy, xx) : 0;
+#pragma unroll
+            for (int c0 = 0; c0 < C; c0 += 16) {
+                uint32_t r[16];
+                const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * warp) << 16) + static_cast<uint32_t>(c0);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                    "%12, %13, %14, %15}, [%16];\n"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                      "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                      "=r"(r[14]), "=r"(r[15])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (inside) {
+                    __align__(16) bf16 o[16];
+                    if (mask) {
+                        __align__(16) bf16 mk[16];
+                        *reinterpret_cast<uint4*>(mk) = *reinterpret_cast<const uint4*>(mask + v * C + c0);
+                        *reinterpret_cast<uint4*>(mk + 8) = *reinterpret_cast<const uint4*>(mask + v * C + c0 + 8);
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            o[j] = __float2bfloat16_rn(__bfloat162float(mk[j]) > 0.0f ? __uint_as_float(r[j]) : 0.0f);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            o[j] = __float2bfloat16_rn(fmaxf(__uint_as_float(r[j]) + bias[c0 + j], 0.0f));
+                    }
+                    *reinterpret_cast<uint4*>(out + v * C + c0) = *reinterpret_cast<const uint4*>(o);
+                    *reinterpret_cast<uint4*>(out + v * C + c0 + 8) = *reinterpret_cast<const uint4*>(o + 8);
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        cur ^= 1;
+    }
+    // outstanding prefetches (a timeout leaves one in flight), then release tensor memory
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TT::tmem_cols)
+                     : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // weight gradients (CUDA cores): per-CTA partial sums over a tile of 256
 // voxels, summed over CTAs by reduce_partials_kernel
 // ---------------------------------------------------------------------------
@@ -638,6 +905,9 @@ struct NetPlan {
     uint64_t p_in_w, packed_bytes;
     std::vector<uint64_t> p_mid_fwd, p_mid_bwd;
     uint64_t mid_frag_bytes;
+    // the same layers as tcgen05 B operands (forward and data gradient)
+    std::vector<uint64_t> p_tc_fwd, p_tc_bwd;
+    uint64_t tc_bytes;
     int64_t max_layer_params;
 };
 
@@ -686,6 +956,15 @@ int32_t make_plan(const BmndPilotNet* net, NetPlan& P) {
         P.p_mid_bwd.push_back(po);
         po = a256(po + P.mid_frag_bytes);
     }
+    P.tc_bytes = static_cast<uint64_t>(P.taps) * (P.C / 16) * 2 * P.C * 16;
+    P.p_tc_fwd.clear();
+    P.p_tc_bwd.clear();
+    for (int l = 1; l < P.L - 1; ++l) {
+        P.p_tc_fwd.push_back(po);
+        po = a256(po + P.tc_bytes);
+        P.p_tc_bwd.push_back(po);
+        po = a256(po + P.tc_bytes);
+    }
     P.packed_bytes = po;
     return BMND_OK;
 }
@@ -698,6 +977,7 @@ int launch_blocks(int64_t n, int threads) {
 }
 
 struct Bufs {
+    int* err;            // set by a kernel whose bounded wait ran out
     float* a;            // Anscombe input
     float* y;            // network output (Anscombe domain)
     float* gy;           // its gradient
@@ -717,6 +997,7 @@ Bufs carve_ws(const NetPlan& P, bool training, void* base) {
     };
     const uint64_t nv = static_cast<uint64_t>(P.geo.voxels());
     const uint64_t hbytes = nv * P.C * 2;
+    const uint64_t o_err = take(sizeof(int));
     const uint64_t o_a = take(nv * 4);
     const uint64_t o_y = take(nv * 4);
     const uint64_t o_gy = training ? take(nv * 4) : 0;
@@ -732,6 +1013,7 @@ Bufs carve_ws(const NetPlan& P, bool training, void* base) {
     B.bytes = off;
     if (base) {
         char* c = static_cast<char*>(base);
+        B.err = reinterpret_cast<int*>(c + o_err);
         B.a = reinterpret_cast<float*>(c + o_a);
         B.y = reinterpret_cast<float*>(c + o_y);
         B.gy = training ? reinterpret_cast<float*>(c + o_gy) : nullptr;
@@ -764,6 +1046,40 @@ int32_t run_mid(const bf16* in, const uint2* wpk, const float* bias, const bf16*
     return BMND_OK;
 }
 
+int g_conv_engine = BMND_CONV_TCGEN05;
+
+template <int ND, int C>
+int32_t run_mid_tc(const bf16* in, const uint4* wtc, const float* bias, const bf16* mask, bf16* out, NetGeo g,
+                   int* err, cudaStream_t stream) {
+    using TT = TcTile<ND, C>;
+    auto kernel = conv_mid_tc_kernel<ND, C>;
+    BMND_CUDA_TRY(
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(TT::bytes)));
+    int dev = 0, sms = 0;
+    BMND_CUDA_TRY(cudaGetDevice(&dev));
+    BMND_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t ntiles = static_cast<int64_t>((g.W + TT::tx - 1) / TT::tx) * ((g.H + TT::ty - 1) / TT::ty) * g.D *
+                           g.nb;
+    // one persistent CTA per SM: the weights fill most of the shared memory
+    int64_t blocks = sms;
+    if (blocks > ntiles) blocks = ntiles;
+    kernel<<<static_cast<unsigned>(blocks), 128, TT::bytes, stream>>>(in, wtc, bias, mask, out, g, err);
+    BMND_LAUNCH_CHECK("conv_mid_tc_kernel");
+    return BMND_OK;
+}
+
+// one C -> C layer with the selected engine; l is the layer (1 .. L-2)
+template <int ND, int C>
+int32_t run_layer(const NetPlan& P, const unsigned char* packed, int l, bool backward, const bf16* in,
+                  const float* bias, const bf16* mask, bf16* out, const Bufs& B, cudaStream_t stream) {
+    if (g_conv_engine == BMND_CONV_TCGEN05) {
+        const uint4* w = reinterpret_cast<const uint4*>(packed + (backward ? P.p_tc_bwd : P.p_tc_fwd)[l - 1]);
+        return run_mid_tc<ND, C>(in, w, bias, mask, out, P.geo, B.err, stream);
+    }
+    const uint2* w = reinterpret_cast<const uint2*>(packed + (backward ? P.p_mid_bwd : P.p_mid_fwd)[l - 1]);
+    return run_mid<ND, C>(in, w, bias, mask, out, P.geo, stream);
+}
+
 template <int ND, int C>
 int32_t forward_impl(const NetPlan& P, const unsigned char* packed, const float* noisy, float* pilot, float* y_out,
                      Bufs& B, bool keep_all, cudaStream_t stream) {
@@ -780,8 +1096,7 @@ int32_t forward_impl(const NetPlan& P, const unsigned char* packed, const float*
     conv_in_kernel<ND, C><<<eb, 256, 0, stream>>>(B.a, wr + P.w_off[0], wr + P.b_off[0], act(0), g);
     BMND_LAUNCH_CHECK("conv_in_kernel");
     for (int l = 1; l < P.L - 1; ++l) {
-        const uint2* wpk = reinterpret_cast<const uint2*>(packed + P.p_mid_fwd[l - 1]);
-        int32_t rc = run_mid<ND, C>(act(l - 1), wpk, wr + P.b_off[l], nullptr, act(l), g, stream);
+        int32_t rc = run_layer<ND, C>(P, packed, l, false, act(l - 1), wr + P.b_off[l], nullptr, act(l), B, stream);
         if (rc) return rc;
     }
     conv_out_kernel<ND, C><<<eb, 256, 0, stream>>>(act(P.L - 2), wr + P.w_off[P.L - 1], wr + P.b_off[P.L - 1], B.a,
@@ -832,8 +1147,7 @@ int32_t gradient_impl(const NetPlan& P, const unsigned char* packed, const float
     for (int l = L - 2; l >= 1; --l) {
         rc = run_wgrad<ND, C, C, bf16, bf16>(act(l - 1), B.grad[cur], B.partial, grad + P.w_off[l], tiles, g, stream);
         if (rc) return rc;
-        const uint2* wpk = reinterpret_cast<const uint2*>(packed + P.p_mid_bwd[l - 1]);
-        rc = run_mid<ND, C>(B.grad[cur], wpk, nullptr, act(l - 1), B.grad[cur ^ 1], g, stream);
+        rc = run_layer<ND, C>(P, packed, l, true, B.grad[cur], nullptr, act(l - 1), B.grad[cur ^ 1], B, stream);
         if (rc) return rc;
         cur ^= 1;
     }
@@ -883,6 +1197,35 @@ int32_t bmnd_pilotnet_workspace_bytes(const BmndPilotNet* net, int32_t training,
     return BMND_OK;
 }
 
+int32_t bmnd_pilotnet_set_conv_engine(int32_t engine) {
+    clear_error();
+    if (engine != BMND_CONV_TCGEN05 && engine != BMND_CONV_MMA_SYNC)
+        return fail(BMND_ERR_INVALID_ARG, "unknown convolution engine");
+    g_conv_engine = engine;
+    return BMND_OK;
+}
+
+int32_t bmnd_pilotnet_get_conv_engine(int32_t* engine) {
+    clear_error();
+    if (!engine) return fail(BMND_ERR_INVALID_ARG, "null output");
+    *engine = g_conv_engine;
+    return BMND_OK;
+}
+
+int32_t bmnd_pilotnet_status(const BmndPilotNet* net, const void* d_ws, uint64_t stream_u64) {
+    clear_error();
+    NetPlan P;
+    if (int32_t rc = make_plan(net, P)) return rc;
+    if (!d_ws) return fail(BMND_ERR_INVALID_ARG, "null workspace");
+    Bufs B = carve_ws(P, false, const_cast<void*>(d_ws));
+    int flag = 0;
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_u64);
+    BMND_CUDA_TRY(cudaMemcpyAsync(&flag, B.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    BMND_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (flag) return fail(BMND_ERR_TIMEOUT, "a pilot net tensor-core wait ran out of time");
+    return BMND_OK;
+}
+
 int32_t bmnd_pilotnet_pack(const BmndPilotNet* net, const float* d_params, void* d_packed, uint64_t stream_u64) {
     clear_error();
     NetPlan P;
@@ -903,6 +1246,12 @@ int32_t bmnd_pilotnet_pack(const BmndPilotNet* net, const float* d_params, void*
             pack_mid_kernel<ND, C><<<launch_blocks(nfrag, 256), 256, 0, stream>>>(
                 d_params + P.w_off[l], reinterpret_cast<uint2*>(pk + P.p_mid_bwd[l - 1]), 1);
             BMND_LAUNCH_CHECK("pack_mid_kernel");
+            const int64_t ntc = static_cast<int64_t>(P.tc_bytes / 2);
+            for (int dir = 0; dir < 2; ++dir) {
+                pack_tc_kernel<ND, C><<<launch_blocks(ntc, 256), 256, 0, stream>>>(
+                    d_params + P.w_off[l], reinterpret_cast<bf16*>(pk + (dir ? P.p_tc_bwd : P.p_tc_fwd)[l - 1]), dir);
+                BMND_LAUNCH_CHECK("pack_tc_kernel");
+            }
         }
         return BMND_OK;
     });
@@ -918,6 +1267,7 @@ int32_t bmnd_pilotnet_forward(const BmndPilotNet* net, const void* d_packed, con
     if (ws_bytes < B.bytes) return fail(BMND_ERR_WORKSPACE, "pilot net workspace too small");
     B = carve_ws(P, false, d_ws);
     cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_u64);
+    BMND_CUDA_TRY(cudaMemsetAsync(B.err, 0, sizeof(int), stream));
     const unsigned char* pk = static_cast<const unsigned char*>(d_packed);
     return dispatch(P, [&](auto nd, auto c) -> int32_t {
         return forward_impl<decltype(nd)::value, decltype(c)::value>(P, pk, d_noisy, d_pilot, d_y, B, false, stream);
@@ -936,6 +1286,7 @@ int32_t bmnd_pilotnet_gradient(const BmndPilotNet* net, const void* d_packed, co
     if (ws_bytes < B.bytes) return fail(BMND_ERR_WORKSPACE, "pilot net workspace too small");
     B = carve_ws(P, true, d_ws);
     cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_u64);
+    BMND_CUDA_TRY(cudaMemsetAsync(B.err, 0, sizeof(int), stream));
     const unsigned char* pk = static_cast<const unsigned char*>(d_packed);
     return dispatch(P, [&](auto nd, auto c) -> int32_t {
         return gradient_impl<decltype(nd)::value, decltype(c)::value>(P, pk, d_noisy, d_target, d_grad, d_loss, B,

@@ -76,6 +76,7 @@ class PilotNet:
         self._packed_version = -1
         self._version = 0
         self._ws = {}
+        self._last_desc = {}
         self.excess_high = DEFAULT_EXCESS_HIGH
 
     # -- plumbing ----------------------------------------------------------
@@ -109,6 +110,7 @@ class PilotNet:
         nb = ctypes.c_uint64(0)
         _abi.check(_abi.lib().bmnd_pilotnet_workspace_bytes(ctypes.byref(desc), int(training), ctypes.byref(nb)))
         key = bool(training)
+        self._last_desc[key] = desc
         ws = self._ws.get(key)
         if ws is None or ws.numel() < nb.value:
             ws = torch.empty(nb.value, dtype=torch.uint8, device=self.device)
@@ -139,6 +141,15 @@ class PilotNet:
             pilot = pilot[0]
             y = None if y is None else y[0]
         return (pilot, y) if want_y else pilot
+
+    def check_status(self, training: bool = False) -> None:
+        """Raise if a bounded tensor-core wait of the last forward (or, with
+        ``training``, gradient) call ran out; synchronises the stream."""
+        ws = self._ws.get(bool(training))
+        if ws is None:
+            return
+        desc = self._last_desc.get(bool(training))
+        _abi.check(_abi.lib().bmnd_pilotnet_status(ctypes.byref(desc), ws.data_ptr(), self._stream()))
 
     # -- training ----------------------------------------------------------
     def gradient(self, noisy, target):
@@ -201,6 +212,7 @@ class PilotNet:
                 if value < best:
                     best = value
                     best_params = self.params.clone()
+                self.check_status(training=True)
                 if log:
                     log(f"step {it + 1} loss {value:.6f} grad_norm {math.sqrt(float(self._sumsq.item())):.4f}")
         if best_params is not None:
@@ -382,6 +394,23 @@ def fast_profile(profile):
     return p
 
 
+_CONV_ENGINES = {"tcgen05": _abi.CONV_TCGEN05, "mma_sync": _abi.CONV_MMA_SYNC}
+
+
+def set_conv_engine(name: str) -> None:
+    """Engine of the pilot net's C -> C layers, process-wide: "tcgen05"
+    (default; accumulator in tensor memory) or "mma_sync" (warp-level MMA)."""
+    if name not in _CONV_ENGINES:
+        raise ValueError(f"conv engine must be one of {sorted(_CONV_ENGINES)}")
+    _abi.check(_abi.lib().bmnd_pilotnet_set_conv_engine(_CONV_ENGINES[name]))
+
+
+def get_conv_engine() -> str:
+    v = ctypes.c_int32(0)
+    _abi.check(_abi.lib().bmnd_pilotnet_get_conv_engine(ctypes.byref(v)))
+    return {c: n for n, c in _CONV_ENGINES.items()}[v.value]
+
+
 def default_tile(ndim: int) -> int:
     """Residual-check tile edge: 32^3 voxels in 3-D, 64^2 pixels in 2-D."""
     return 32 if ndim == 3 else 64
@@ -405,6 +434,7 @@ def bmnd_fast(noisy, profile, net: PilotNet, *, tile: int | None = None, excess_
     if check:
         hi = excess_high if excess_high is not None else net.excess_high
         excess, _ = tile_excess(x, pilot, tile)
+        net.check_status()
         fail = (excess > hi) | (excess < EXCESS_LOW)
         n_fb = apply_fallback(x, pilot, profile, fail, tile)
     if details is not None:

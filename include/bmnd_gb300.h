@@ -286,6 +286,17 @@ int32_t bmnd_pilotnet_forward(const BmndPilotNet* net, const void* d_packed, con
 int32_t bmnd_pilotnet_gradient(const BmndPilotNet* net, const void* d_packed, const float* d_noisy,
                                const float* d_target, float* d_grad, double* d_loss, void* d_workspace,
                                uint64_t workspace_bytes, uint64_t stream);
+/* Status of the most recent forward or gradient call that used d_workspace:
+ * synchronises the stream, then BMND_OK, or BMND_ERR_TIMEOUT when a bounded
+ * wait of a tensor-core layer ran out (the outputs are then incomplete). */
+int32_t bmnd_pilotnet_status(const BmndPilotNet* net, const void* d_workspace, uint64_t stream);
+/* Engine of the C -> C layers, process-wide: BMND_CONV_TCGEN05 (default: one
+ * tcgen05.mma per 128-voxel tile and K = 16 slice, accumulator in tensor
+ * memory) or BMND_CONV_MMA_SYNC (warp-level mma.sync, kept for comparison). */
+#define BMND_CONV_TCGEN05 0
+#define BMND_CONV_MMA_SYNC 1
+int32_t bmnd_pilotnet_set_conv_engine(int32_t engine);
+int32_t bmnd_pilotnet_get_conv_engine(int32_t* engine);
 /* Residual check of a pilot, per tile of edge `edge` (cubes in 3-D, squares in
  * 2-D; shape as in BmndPilotNet): d_out[3 * tile + (0, 1, 2)] = observed Poisson
  * deviance sum_v 2 [x ln(x / mu) - (x - mu)] of the input x against the pilot

@@ -9,6 +9,16 @@ from oracle import pilotnet_ref as R
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=["tcgen05", "mma_sync"])
+def engine(request, native):
+    from bmnd_gb300.pilot import get_conv_engine, set_conv_engine
+
+    old = get_conv_engine()
+    set_conv_engine(request.param)
+    yield request.param
+    set_conv_engine(old)
+
+
 def _net(cuda, ndim, channels, layers, seed):
     from bmnd_gb300.pilot import PilotNet
 
@@ -22,7 +32,7 @@ def _net(cuda, ndim, channels, layers, seed):
     (2, 32, 4, (2, 20, 36)),
     (2, 48, 5, (1, 33, 17)),
 ])
-def test_forward_and_gradient_match_oracle(cuda, native, ndim, channels, layers, shape):
+def test_forward_and_gradient_match_oracle(cuda, engine, ndim, channels, layers, shape):
     rng = np.random.default_rng(sum(shape))
     x = rng.poisson(rng.uniform(1, 30, size=shape)).astype(np.float32)
     t = (0.7 * x + 2.0).astype(np.float32)
@@ -31,12 +41,14 @@ def test_forward_and_gradient_match_oracle(cuda, native, ndim, channels, layers,
     tg = cuda.from_numpy(t).cuda()
     # forward (inference path, ping-pong activations) vs the oracle's BF16 mirror
     pilot_g, y_g = net.forward(xg, want_y=True)
+    net.check_status()
     pilot_o, y_o, _ = R.forward(params, x, ndim, channels, layers, bf16=True)
     y_g = y_g.cpu().numpy()
     assert np.max(np.abs(y_g - y_o)) <= 2e-2 * max(1.0, np.max(np.abs(y_o))), np.max(np.abs(y_g - y_o))
     assert np.corrcoef(y_g.ravel(), y_o.ravel())[0, 1] > 0.9999
     # gradient pass (keeps every activation) vs the oracle
     loss_g, grad_g = net.gradient(xg, tg)
+    net.check_status(training=True)
     loss_o, grad_o, _ = R.loss_and_gradient(params, x, t, ndim, channels, layers, bf16=True)
     assert abs(float(loss_g.item()) - loss_o) <= 1e-3 * loss_o + 1e-7
     grad_g = grad_g.cpu().numpy().astype(np.float64)
@@ -47,6 +59,41 @@ def test_forward_and_gradient_match_oracle(cuda, native, ndim, channels, layers,
         rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
         assert rel < 3e-2, (l, rel)
         off += n
+
+
+@pytest.mark.parametrize("ndim,channels,layers,shape", [
+    (3, 48, 6, (2, 40, 70, 66)),    # thousands of tiles per launch, ragged x and y edges
+    (2, 32, 5, (3, 300, 129)),
+])
+def test_tensor_memory_engine_matches_warp_mma(cuda, native, ndim, channels, layers, shape):
+    """The tcgen05 layers (persistent CTAs, double-buffered halo tiles) against
+    the mma.sync layers on volumes too large for the oracle: same BF16 inputs,
+    FP32 accumulation in a different order."""
+    from bmnd_gb300.pilot import get_conv_engine, set_conv_engine
+
+    rng = np.random.default_rng(3)
+    x = rng.poisson(rng.uniform(1, 30, size=shape)).astype(np.float32)
+    t = (0.7 * x + 2.0).astype(np.float32)
+    net, _ = _net(cuda, ndim, channels, layers, seed=4)
+    xg, tg = cuda.from_numpy(x).cuda(), cuda.from_numpy(t).cuda()
+    old = get_conv_engine()
+    res = {}
+    try:
+        for eng in ("mma_sync", "tcgen05"):
+            set_conv_engine(eng)
+            _, y = net.forward(xg, want_y=True)
+            net.check_status()
+            loss, grad = net.gradient(xg, tg)
+            net.check_status(training=True)
+            res[eng] = (y.cpu().numpy(), float(loss.item()), grad.cpu().numpy().astype(np.float64))
+    finally:
+        set_conv_engine(old)
+    (ya, la, ga), (yb, lb, gb) = res["mma_sync"], res["tcgen05"]
+    scale = max(1.0, float(np.max(np.abs(ya))))
+    assert np.max(np.abs(ya - yb)) <= 2e-2 * scale, np.max(np.abs(ya - yb))
+    assert np.corrcoef(ya.ravel(), yb.ravel())[0, 1] > 0.99999
+    assert abs(la - lb) <= 1e-3 * abs(la) + 1e-7
+    assert np.linalg.norm(ga - gb) / np.linalg.norm(ga) < 2e-2
 
 
 def test_tile_deviance_matches_numpy(cuda, native):
