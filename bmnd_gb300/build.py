@@ -69,7 +69,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     with concurrent.futures.ThreadPoolExecutor(max_workers=workers) as pool:
         objs = list(pool.map(lambda s: _compile(s, extra), sources))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcuda"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

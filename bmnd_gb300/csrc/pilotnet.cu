@@ -23,9 +23,12 @@
 // and transposed and the layer input's ReLU mask in the epilogue.  The
 // one-channel layers, the weight gradients and the optimiser run on the CUDA
 // cores.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include <type_traits>
 #include <vector>
@@ -405,36 +408,50 @@ __global__ void __launch_bounds__(256, 1) conv_mid_kernel(const bf16* __restrict
 
 // ---------------------------------------------------------------------------
 // C -> C layers with tcgen05 (fifth-generation tensor cores, accumulator in
-// tensor memory).
+// tensor memory), fed by TMA.
 //
 // Output tile: one z plane of 16 rows x 8 voxels = the M = 128 rows of one
 // tcgen05.mma (kind::f16, BF16 in, FP32 accumulate, N = C, K = 16).  The
-// input halo of the tile is staged chunk-major, [8-channel chunk][halo voxel]
-// [16 bytes], so that for every tap the A operand is a no-swizzle K-major
-// matrix: a core matrix is 8 consecutive voxels of one row (128 contiguous
-// bytes), the next 8 rows of M are the next row of the halo (stride 16 * hx
-// bytes), and the second 8 channels of the K = 16 slice are the next chunk
-// (stride 16 * halo bytes).  The weights sit in shared memory for the whole
-// launch as B = W_t[ci][co] in the same K-major core-matrix layout.  One
-// thread issues the 27 x C/16 MMAs of a tile and commits them to an mbarrier;
-// meanwhile all threads prefetch the next tile's halo with cp.async into the
-// second buffer; the four warps then read the accumulator rows they own
-// (tcgen05.ld 32x32b) and apply the epilogue.  Every mbarrier wait is bounded:
-// on timeout the kernel records an error, stops issuing work and frees its
-// tensor memory.
+// input halo of the tile (10 x 18 voxels, x 3 planes in 3-D) arrives by TMA,
+// one 4-D box per 8-channel chunk, so shared memory holds it chunk-major:
+// [chunk][halo voxel][16 bytes], chunks 128-byte aligned.  For every tap the A
+// operand is then a no-swizzle K-major matrix: a core matrix is 8 consecutive
+// voxels of one row (128 contiguous bytes), the next 8 rows of M are the next
+// halo row (16 * hx bytes on), the second 8 channels of the K = 16 slice are
+// the next chunk.  TMA fills the out-of-volume halo with zeros, which is the
+// convolution's zero padding.  The weights stay in shared memory for the whole
+// launch as B = W_t[ci][co] in the same K-major core-matrix layout.
+//
+// Warp roles (192 threads, one CTA per SM): warp 0 issues the TMA loads into
+// two halo stages; one thread of warp 1 issues the 27 x C/16 MMAs of a tile
+// into one of two accumulators in tensor memory and commits them to mbarriers
+// (stage free, accumulator full); warps 2-5 read the accumulator rows they may
+// access (tcgen05.ld 32x32b), release it, and apply the epilogue.  Loads, MMAs
+// and epilogues of neighbouring tiles overlap.  Every mbarrier wait is
+// bounded: on timeout the kernel records an error, stops issuing work, waits
+// (bounded) for its copies and MMAs in flight, and frees its tensor memory.
 // ---------------------------------------------------------------------------
 template <int ND, int C>
 struct TcTile {
     static constexpr int tx = 8, ty = 16;
     static constexpr int hx = tx + 2, hy = ty + 2, hz = ND == 3 ? 3 : 1;
     static constexpr int halo = hx * hy * hz;
+    static constexpr int halo_pad = (halo + 7) / 8 * 8;  // chunk stride: 128-byte multiple
     static constexpr int chunks = C / 8;
     static constexpr int taps = ND == 3 ? 27 : 9;
     static constexpr int kc = C / 16;
-    static constexpr size_t wbytes = static_cast<size_t>(taps) * kc * 2 * C * 16;  // B core matrices
-    static constexpr size_t tbytes = static_cast<size_t>(chunks) * halo * 16;      // one A halo tile
-    static constexpr size_t bytes = wbytes + 2 * tbytes;
-    static constexpr uint32_t tmem_cols = C <= 32 ? 32 : 64;
+    static constexpr uint32_t cbytes = static_cast<uint32_t>(halo_pad) * 16;           // one chunk in shared memory
+    static constexpr uint32_t box_bytes = static_cast<uint32_t>(halo) * 16;            // one chunk by TMA
+    static constexpr uint32_t tbytes = chunks * cbytes;                                 // one halo stage
+    static constexpr uint32_t wbytes = static_cast<uint32_t>(taps) * kc * 2 * C * 16;  // B core matrices
+    static constexpr uint32_t bytes = 2 * tbytes + wbytes;
+    static constexpr uint32_t acc_cols = C <= 32 ? 32 : 64;
+    static constexpr uint32_t tmem_cols = 2 * acc_cols;
+    static constexpr int threads = 192;
+};
+
+struct TcMaps {
+    CUtensorMap m[6];  // one per 8-channel chunk of the input
 };
 
 // B for tcgen05: element (t, kc, kk, n, e) = W[t][ci = 16 kc + 8 kk + e][co = n]
@@ -476,196 +493,296 @@ __device__ __forceinline__ uint64_t global_ns() {
     return t;
 }
 
-// wait for the phase of parity `phase` to complete, for at most limit_ns
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, uint64_t limit_ns) {
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// wait until the phase of parity `parity` has completed, for at most limit_ns
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint64_t limit_ns) {
+    if (mbar_try(mbar, parity)) return true;
     const uint64_t t0 = global_ns();
     for (;;) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}\n"
-            : "=r"(done)
-            : "r"(mbar), "r"(phase)
-            : "memory");
-        if (done) return true;
+        if (mbar_try(mbar, parity)) return true;
         if (global_ns() - t0 > limit_ns) return false;
     }
 }
 
-template <int ND, int C>
-__device__ __forceinline__ void tc_load_tile(const bf16* __restrict__ in, const NetGeo& g, int b, int z0, int y0,
-                                             int x0, uint32_t tile_addr) {
-    using TT = TcTile<ND, C>;
-    for (int i = threadIdx.x; i < TT::halo * TT::chunks; i += blockDim.x) {
-        const int vox = i % TT::halo, ch = i / TT::halo;
-        const int hxi = vox % TT::hx, hyi = (vox / TT::hx) % TT::hy, hzi = vox / (TT::hx * TT::hy);
-        const int xx = x0 + hxi - 1, yy = y0 + hyi - 1, zz = ND == 3 ? z0 + hzi - 1 : z0;
-        const bool inside = xx >= 0 && xx < g.W && yy >= 0 && yy < g.H && zz >= 0 && zz < g.D;
-        const bf16* src = inside ? in + vox_index(g, b, zz, yy, xx) * C + ch * 8 : in;
-        const uint32_t dst = tile_addr + static_cast<uint32_t>((ch * TT::halo + vox) * 16);
-        const uint32_t n = inside ? 16u : 0u;  // 0: fill with zeros, read nothing
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n) : "memory");
-    }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];\n" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(mbar)
+        : "memory");
 }
 
 template <int ND, int C>
-__global__ void __launch_bounds__(128, 1) conv_mid_tc_kernel(const bf16* __restrict__ in, const uint4* __restrict__ wtc,
+__global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_constant__ TcMaps maps,
+                                                             const bf16* __restrict__ wtc,
                                                              const float* __restrict__ bias,
                                                              const bf16* __restrict__ mask, bf16* __restrict__ out,
                                                              NetGeo g, int* __restrict__ err) {
     using TT = TcTile<ND, C>;
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar;
+    extern __shared__ __align__(128) unsigned char tc_smem[];
+    // full[2] (halo stage landed), empty[2] (stage read by the MMAs), afull[2]
+    // (accumulator complete), aempty[2] (accumulator read out), weights
+    __shared__ __align__(8) uint64_t bars[9];
     __shared__ uint32_t tmem_slot;
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t w_addr = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
-    const uint32_t t_addr0 = w_addr + static_cast<uint32_t>(TT::wbytes);  // halo tile buffers
-    const uint32_t t_addr1 = t_addr0 + static_cast<uint32_t>(TT::tbytes);
-    const uint32_t mbar_addr = static_cast<uint32_t>(__cvta_generic_to_shared(&mbar));
+    __shared__ int abort_flag;
+    volatile int* abort_v = &abort_flag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(tc_smem));
+    const uint32_t wsm = sbase + 2 * TT::tbytes;
+    const uint32_t bar0 = static_cast<uint32_t>(__cvta_generic_to_shared(bars));
+    auto full = [&](int s) { return bar0 + 8u * s; };
+    auto empty = [&](int s) { return bar0 + 16u + 8u * s; };
+    auto afull = [&](int s) { return bar0 + 32u + 8u * s; };
+    auto aempty = [&](int s) { return bar0 + 48u + 8u * s; };
+    const uint32_t wbar = bar0 + 64u;
+    constexpr uint64_t kWaitNs = 1000000000ull;  // one tile takes microseconds
 
-    // weights for the whole launch
-    for (int i = tid; i < static_cast<int>(TT::wbytes / 16); i += blockDim.x)
-        reinterpret_cast<uint4*>(smem)[i] = wtc[i];
-    if (warp == 0) {
+    if (tid == 0) {
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(full(s), 1);
+            mbar_init(empty(s), 1);
+            mbar_init(afull(s), 1);
+            mbar_init(aempty(s), 4);  // one arrival per epilogue warp
+        }
+        mbar_init(wbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        abort_flag = (sbase & 127u) != 0u ? 1 : 0;  // TMA destinations need 128-byte alignment
+        if (abort_flag) atomicExch(err, 2);
+    }
+    if (warp == 1) {
         const uint32_t slot = static_cast<uint32_t>(__cvta_generic_to_shared(&tmem_slot));
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(slot),
                      "r"(TT::tmem_cols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar_addr) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    tc_fence_before();
     __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    tc_fence_after();
     const uint32_t tmem = tmem_slot;
 
     const int tiles_x = (g.W + TT::tx - 1) / TT::tx;
     const int tiles_y = (g.H + TT::ty - 1) / TT::ty;
-    const int tiles_z = g.D;
-    const int64_t ntiles = static_cast<int64_t>(tiles_x) * tiles_y * tiles_z * g.nb;
+    const int64_t ntiles = static_cast<int64_t>(tiles_x) * tiles_y * g.D * g.nb;
     auto decode = [&](int64_t tl, int& b, int& z0, int& y0, int& x0) {
         int64_t r = tl;
         x0 = static_cast<int>(r % tiles_x) * TT::tx;
         r /= tiles_x;
         y0 = static_cast<int>(r % tiles_y) * TT::ty;
         r /= tiles_y;
-        z0 = static_cast<int>(r % tiles_z);
-        b = static_cast<int>(r / tiles_z);
+        z0 = static_cast<int>(r % g.D);
+        b = static_cast<int>(r / g.D);
     };
-    // instruction descriptor: FP32 accumulator, BF16 A and B, both K-major,
-    // N = C (bits 17-22: N >> 3), M = 128 (bits 24-28: M >> 4)
-    constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(C >> 3) << 17) |
-                               (static_cast<uint32_t>(128 >> 4) << 24);
-    constexpr uint64_t kWaitLimitNs = 1000000000ull;  // one tile takes microseconds
+    auto fail = [&](int code) {
+        *abort_v = 1;
+        atomicExch(err, code);
+    };
 
-    int64_t tl = blockIdx.x;
-    int cur = 0;
-    uint32_t phase = 0;
-    bool ok = true;
-    if (tl < ntiles) {
-        int b, z0, y0, x0;
-        decode(tl, b, z0, y0, x0);
-        tc_load_tile<ND, C>(in, g, b, z0, y0, x0, t_addr0);
-    }
-    for (; tl < ntiles && ok; tl += gridDim.x) {
-        int b, z0, y0, x0;
-        decode(tl, b, z0, y0, x0);
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        if (tid == 0) {
-#pragma unroll 1
-            for (int t = 0; t < TT::taps; ++t) {
-                int dz, dy, dx;
-                tap_offsets<ND>(t, dz, dy, dx);
-                const int vox0 = ((ND == 3 ? dz + 1 : 0) * TT::hy + dy + 1) * TT::hx + dx + 1;
-#pragma unroll
-                for (int k = 0; k < TT::kc; ++k) {
-                    const uint64_t ad = umma_desc((cur ? t_addr1 : t_addr0) + static_cast<uint32_t>((2 * k * TT::halo + vox0) * 16),
-                                                  TT::halo * 16, TT::hx * 16);
-                    const uint64_t bd =
-                        umma_desc(w_addr + static_cast<uint32_t>((t * TT::kc + k) * 2 * C * 16), C * 16, 128);
-                    const uint32_t acc = (t | k) != 0 ? 1u : 0u;
-                    asm volatile(
-                        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-                        : "memory");
+    if (warp == 0) {
+        // ---- producer: weights once, then one halo stage per tile ----
+        int issued = 0;
+        if (lane == 0 && !*abort_v) {
+            mbar_expect_tx(wbar, TT::wbytes);
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                    wsm),
+                "l"(reinterpret_cast<uint64_t>(wtc)), "r"(TT::wbytes), "r"(wbar)
+                : "memory");
+            int it = 0;
+            for (int64_t tl = blockIdx.x; tl < ntiles; tl += gridDim.x, ++it) {
+                const int s = it & 1;
+                if (!mbar_wait(empty(s), ((it >> 1) & 1) ^ 1, kWaitNs)) {
+                    fail(1);
+                    break;
                 }
+                if (*abort_v) break;
+                int b, z0, y0, x0;
+                decode(tl, b, z0, y0, x0);
+                const int zc = ND == 3 ? b * g.D + z0 - 1 : b;
+                mbar_expect_tx(full(s), TT::chunks * TT::box_bytes);
+                const uint32_t dst = sbase + static_cast<uint32_t>(s) * TT::tbytes;
+#pragma unroll
+                for (int ch = 0; ch < TT::chunks; ++ch)
+                    tma_load_4d(dst + ch * TT::cbytes, &maps.m[ch], 0, x0 - 1, y0 - 1, zc, full(s));
+                issued = it + 1;
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                             mbar_addr)
-                         : "memory");
+            if (*abort_v) {
+                // copies in flight: wait (bounded) for the last two stages
+                for (int j = issued - 2; j < issued; ++j)
+                    if (j >= 0) (void)mbar_wait(full(j & 1), (j >> 1) & 1, kWaitNs);
+                (void)mbar_wait(wbar, 0, kWaitNs);
+            }
         }
-        // prefetch the next tile into the other buffer (its last readers, the
-        // previous tile's MMAs, completed before the previous epilogue)
-        const int64_t nx = tl + gridDim.x;
-        if (nx < ntiles) {
-            int b2, z2, y2, x2;
-            decode(nx, b2, z2, y2, x2);
-            tc_load_tile<ND, C>(in, g, b2, z2, y2, x2, cur ? t_addr0 : t_addr1);
-        }
-        if (!mbar_wait(mbar_addr, phase, kWaitLimitNs)) {
-            atomicExch(err, 1);
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---- MMA issuer (lane 0); the warp zeroes batch-boundary planes ----
+        constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(C >> 3) << 17) |
+                                   (static_cast<uint32_t>(128 >> 4) << 24);
+        int committed = 0;
+        bool ok = !*abort_v;
+        if (ok && !mbar_wait(wbar, 0, kWaitNs)) {
+            fail(1);
             ok = false;
         }
-        ok = __syncthreads_and(ok) != 0;  // uniform, so every barrier below is reached by all threads
-        phase ^= 1;
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        if (ok) {
-            // epilogue: this thread owns accumulator row m = 32 * warp + lane
-            const int m = tid;
-            const int xx = x0 + (m % TT::tx), yy = y0 + m / TT::tx;
-            const bool inside = xx < g.W && yy < g.H;
-            const int64_t v = inside ? vox_index(g, b, z0, yy, xx) : 0;
+        int it = 0;
+        for (int64_t tl = blockIdx.x; ok && tl < ntiles; tl += gridDim.x, ++it) {
+            const int s = it & 1;
+            const uint32_t ph = (it >> 1) & 1;
+            bool got = true;
+            if (lane == 0) got = mbar_wait(full(s), ph, kWaitNs) && mbar_wait(aempty(s), ph ^ 1, kWaitNs);
+            got = __shfl_sync(0xffffffffu, got ? 1 : 0, 0) != 0;
+            if (!got || *abort_v) {
+                if (lane == 0 && !got) fail(1);
+                break;
+            }
+            const uint32_t stage = sbase + static_cast<uint32_t>(s) * TT::tbytes;
+            if (ND == 3 && g.nb > 1) {
+                // planes of the neighbouring volume in the batch read as zero padding
+                int b, z0, y0, x0;
+                decode(tl, b, z0, y0, x0);
+                const bool below = z0 == 0 && b > 0, above = z0 == g.D - 1 && b < g.nb - 1;
+                if (below || above) {
+                    constexpr int pv = TT::hx * TT::hy;
+                    for (int plane = 0; plane < 3; plane += 2) {
+                        if (plane == 0 ? !below : !above) continue;
+                        for (int i = lane; i < TT::chunks * pv; i += 32) {
+                            const int ch = i / pv, v = plane * pv + i % pv;
+                            const uint32_t a = stage + ch * TT::cbytes + static_cast<uint32_t>(v) * 16u;
+                            asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};\n" ::"r"(a), "r"(0) : "memory");
+                        }
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                    __syncwarp();
+                }
+            }
+            tc_fence_after();
+            if (lane == 0) {
+                const uint64_t a_base = umma_desc(stage, TT::cbytes, TT::hx * 16);
+                const uint64_t b_base = umma_desc(wsm, C * 16, 128);
+                const uint32_t d_tmem = tmem + static_cast<uint32_t>(s) * TT::acc_cols;
+#pragma unroll
+                for (int t = 0; t < TT::taps; ++t) {
+                    const int dz = ND == 3 ? t / 9 : 0;
+                    const int dy = ND == 3 ? (t / 3) % 3 : t / 3;
+                    const int dx = t % 3;
+                    const int vox0 = (dz * TT::hy + dy) * TT::hx + dx;
+#pragma unroll
+                    for (int k = 0; k < TT::kc; ++k) {
+                        // start-address field += offset / 16 (stays below 2^14: no carry)
+                        const uint64_t ad = a_base + static_cast<uint64_t>(2 * k * TT::halo_pad + vox0);
+                        const uint64_t bd = b_base + static_cast<uint64_t>((t * TT::kc + k) * 2 * C);
+                        const uint32_t acc = (t | k) != 0 ? 1u : 0u;
+                        asm volatile(
+                            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+                            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                            : "memory");
+                    }
+                }
+                asm volatile(
+                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(empty(s))
+                    : "memory");
+                asm volatile(
+                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(afull(s))
+                    : "memory");
+            }
+            committed = it + 1;
+            __syncwarp();
+        }
+        if (lane == 0 && *abort_v && committed > 0) {
+            const int j = committed - 1;  // MMAs in flight: wait (bounded) for the last commit
+            (void)mbar_wait(afull(j & 1), (j >> 1) & 1, kWaitNs);
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31 ----
+        const int q = warp & 3;
+        const int m = 32 * q + lane;  // accumulator row = voxel of the tile
+        int it = 0;
+        for (int64_t tl = blockIdx.x; tl < ntiles; tl += gridDim.x, ++it) {
+            const int s = it & 1;
+            bool got = true;
+            if (lane == 0) got = mbar_wait(afull(s), (it >> 1) & 1, kWaitNs);
+            got = __shfl_sync(0xffffffffu, got ? 1 : 0, 0) != 0;
+            if (!got || *abort_v) {
+                if (lane == 0 && !got) fail(1);
+                break;
+            }
+            tc_fence_after();
+            uint32_t r[C];
 #pragma unroll
             for (int c0 = 0; c0 < C; c0 += 16) {
-                uint32_t r[16];
-                const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * warp) << 16) + static_cast<uint32_t>(c0);
+                const uint32_t taddr =
+                    tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(s) * TT::acc_cols + c0;
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
                     "%12, %13, %14, %15}, [%16];\n"
-                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                      "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                      "=r"(r[14]), "=r"(r[15])
+                    : "=r"(r[c0 + 0]), "=r"(r[c0 + 1]), "=r"(r[c0 + 2]), "=r"(r[c0 + 3]), "=r"(r[c0 + 4]),
+                      "=r"(r[c0 + 5]), "=r"(r[c0 + 6]), "=r"(r[c0 + 7]), "=r"(r[c0 + 8]), "=r"(r[c0 + 9]),
+                      "=r"(r[c0 + 10]), "=r"(r[c0 + 11]), "=r"(r[c0 + 12]), "=r"(r[c0 + 13]), "=r"(r[c0 + 14]),
+                      "=r"(r[c0 + 15])
                     : "r"(taddr));
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                if (inside) {
-                    __align__(16) bf16 o[16];
-                    if (mask) {
-                        __align__(16) bf16 mk[16];
-                        *reinterpret_cast<uint4*>(mk) = *reinterpret_cast<const uint4*>(mask + v * C + c0);
-                        *reinterpret_cast<uint4*>(mk + 8) = *reinterpret_cast<const uint4*>(mask + v * C + c0 + 8);
+            }
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(aempty(s));
+            int b, z0, y0, x0;
+            decode(tl, b, z0, y0, x0);
+            const int xx = x0 + (m % TT::tx), yy = y0 + m / TT::tx;
+            if (xx < g.W && yy < g.H) {
+                const int64_t v = vox_index(g, b, z0, yy, xx);
 #pragma unroll
-                        for (int j = 0; j < 16; ++j)
-                            o[j] = __float2bfloat16_rn(__bfloat162float(mk[j]) > 0.0f ? __uint_as_float(r[j]) : 0.0f);
+                for (int c0 = 0; c0 < C; c0 += 8) {
+                    __align__(16) bf16 o[8];
+                    if (mask) {
+                        __align__(16) bf16 mk[8];
+                        *reinterpret_cast<uint4*>(mk) = *reinterpret_cast<const uint4*>(mask + v * C + c0);
+#pragma unroll
+                        for (int j = 0; j < 8; ++j)
+                            o[j] = __float2bfloat16_rn(__bfloat162float(mk[j]) > 0.0f ? __uint_as_float(r[c0 + j])
+                                                                                     : 0.0f);
                     } else {
 #pragma unroll
-                        for (int j = 0; j < 16; ++j)
-                            o[j] = __float2bfloat16_rn(fmaxf(__uint_as_float(r[j]) + bias[c0 + j], 0.0f));
+                        for (int j = 0; j < 8; ++j)
+                            o[j] = __float2bfloat16_rn(fmaxf(__uint_as_float(r[c0 + j]) + __ldg(bias + c0 + j), 0.0f));
                     }
                     *reinterpret_cast<uint4*>(out + v * C + c0) = *reinterpret_cast<const uint4*>(o);
-                    *reinterpret_cast<uint4*>(out + v * C + c0 + 8) = *reinterpret_cast<const uint4*>(o + 8);
                 }
             }
         }
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();
-        cur ^= 1;
     }
-    // outstanding prefetches (a timeout leaves one in flight), then release tensor memory
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    tc_fence_before();
     __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (warp == 0)
+    tc_fence_after();
+    if (warp == 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TT::tmem_cols)
                      : "memory");
 }
@@ -1049,12 +1166,40 @@ int32_t run_mid(const bf16* in, const uint2* wpk, const float* bias, const bf16*
 int g_conv_engine = BMND_CONV_TCGEN05;
 
 template <int ND, int C>
-int32_t run_mid_tc(const bf16* in, const uint4* wtc, const float* bias, const bf16* mask, bf16* out, NetGeo g,
+int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf16* mask, bf16* out, NetGeo g,
                    int* err, cudaStream_t stream) {
     using TT = TcTile<ND, C>;
     auto kernel = conv_mid_tc_kernel<ND, C>;
     BMND_CUDA_TRY(
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(TT::bytes)));
+    if ((reinterpret_cast<uintptr_t>(in) & 15u) != 0 || (reinterpret_cast<uintptr_t>(wtc) & 15u) != 0)
+        return fail(BMND_ERR_INVALID_ARG, "pilot net buffers must be 16-byte aligned");
+    // one 4-D map per 8-channel chunk: (8 channels, x, y, z * batch), a box of
+    // (8, hx, hy, hz) voxels; out-of-range elements read as zero
+    TcMaps maps;
+    memset(&maps, 0, sizeof(maps));
+    const cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(g.W), static_cast<cuuint64_t>(g.H),
+                                static_cast<cuuint64_t>(g.D) * static_cast<cuuint64_t>(g.nb)};
+    const cuuint64_t strides[3] = {static_cast<cuuint64_t>(C) * 2, static_cast<cuuint64_t>(g.W) * C * 2,
+                                   static_cast<cuuint64_t>(g.H) * g.W * C * 2};
+    const cuuint32_t box[4] = {8, TT::hx, TT::hy, TT::hz};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    // the driver's encoder, fetched through the runtime (no link-time dependency on the driver library)
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        void* fn = nullptr;
+        BMND_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !fn) return fail(BMND_ERR_CUDA, "cuTensorMapEncodeTiled not available");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    for (int ch = 0; ch < TT::chunks; ++ch) {
+        const CUresult rc = encode(
+            &maps.m[ch], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(in) + ch * 8, dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (rc != CUDA_SUCCESS) return fail(BMND_ERR_CUDA, "cuTensorMapEncodeTiled failed for the pilot net input");
+    }
     int dev = 0, sms = 0;
     BMND_CUDA_TRY(cudaGetDevice(&dev));
     BMND_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1063,7 +1208,7 @@ int32_t run_mid_tc(const bf16* in, const uint4* wtc, const float* bias, const bf
     // one persistent CTA per SM: the weights fill most of the shared memory
     int64_t blocks = sms;
     if (blocks > ntiles) blocks = ntiles;
-    kernel<<<static_cast<unsigned>(blocks), 128, TT::bytes, stream>>>(in, wtc, bias, mask, out, g, err);
+    kernel<<<static_cast<unsigned>(blocks), TT::threads, TT::bytes, stream>>>(maps, wtc, bias, mask, out, g, err);
     BMND_LAUNCH_CHECK("conv_mid_tc_kernel");
     return BMND_OK;
 }
@@ -1073,7 +1218,7 @@ template <int ND, int C>
 int32_t run_layer(const NetPlan& P, const unsigned char* packed, int l, bool backward, const bf16* in,
                   const float* bias, const bf16* mask, bf16* out, const Bufs& B, cudaStream_t stream) {
     if (g_conv_engine == BMND_CONV_TCGEN05) {
-        const uint4* w = reinterpret_cast<const uint4*>(packed + (backward ? P.p_tc_bwd : P.p_tc_fwd)[l - 1]);
+        const bf16* w = reinterpret_cast<const bf16*>(packed + (backward ? P.p_tc_bwd : P.p_tc_fwd)[l - 1]);
         return run_mid_tc<ND, C>(in, w, bias, mask, out, P.geo, B.err, stream);
     }
     const uint2* w = reinterpret_cast<const uint2*>(packed + (backward ? P.p_mid_bwd : P.p_mid_fwd)[l - 1]);

@@ -31,6 +31,7 @@ def _net(cuda, ndim, channels, layers, seed):
     (3, 32, 3, (1, 9, 17, 18)),
     (2, 32, 4, (2, 20, 36)),
     (2, 48, 5, (1, 33, 17)),
+    (3, 48, 3, (3, 1, 19, 9)),   # one-plane volumes in a batch: both z-halo planes belong to neighbours
 ])
 def test_forward_and_gradient_match_oracle(cuda, engine, ndim, channels, layers, shape):
     rng = np.random.default_rng(sum(shape))
