@@ -59,7 +59,10 @@ struct MatchArgs {
     int32_t use_table;  // integer-count lookup of Poisson-deviance terms
     int32_t fixup;      // only redo references whose count is negative
     int32_t approx;     // screened kernel: zero bound, the screening distances decide
-    const float2* cb;   // approx mode, volume source: (c, c + c log2 c) per voxel, or null
+    // approx mode, volume source (or null): c = max(x * inv_scale, 0) per
+    // voxel, and the sum of B(c) = c + c log2 c over the patch at each origin
+    const float* cv;
+    const float* boxb;
 };
 
 constexpr int kTable = 64;  // counts 0..63 are tabulated
@@ -467,39 +470,78 @@ __device__ __forceinline__ float2 screen_deviance_fixed(const float2* __restrict
 
 // Approximate mode (no error bound): with s = r + c the deviance term is
 //   2 ln 2 [r log2(2r/s) + c log2(2c/s)] = 2 ln 2 [A_r + B_c - s log2 s],
-// A_r = r + r log2 r per reference element (ref[p].y), B_c = c + c log2 c per
-// voxel (cb[v].y), so one SFU log2 per term remains.
-__global__ void approx_voxel_kernel(const float* __restrict__ src, float inv, int64_t n, float2* __restrict__ cb) {
+// A_r = r + r log2 r, B_c = c + c log2 c.  Summed over a patch, the A part is
+// one number per reference and the B part one number per candidate origin
+// (a box sum over the patch, prepared once per volume), so only
+// -sum_p s_p log2 s_p remains per candidate: one SFU log2 and two FP32
+// operations per term.  A thread scores XR candidates that are neighbours
+// along x, so one row of XR + BX - 1 voxels serves XR x BX terms.
+__global__ void approx_voxel_kernel(const float* __restrict__ src, float inv, int64_t n, float* __restrict__ cv,
+                                    float* __restrict__ bv) {
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const float c = fmaxf(src[i] * inv, 0.0f);
-        cb[i] = make_float2(c, c > 0.0f ? c + c * log2f(c) : 0.0f);
+        cv[i] = c;
+        bv[i] = c > 0.0f ? c + c * log2f(c) : 0.0f;
     }
 }
 
+// boxb[o] = sum over the patch at origin o of bv (0 where no patch starts)
 template <int ND, int B0, int B1, int B2>
-__device__ __forceinline__ float approx_deviance_fixed(const float2* __restrict__ ref, const float2* __restrict__ cb,
-                                                       int64_t origin, int64_t s0, int64_t s1) {
-    const float kMin = 1.17549435e-38f;
-    float sum = 0.0f;
-    const float2* base = cb + origin;
+__global__ void approx_box_kernel(const float* __restrict__ bv, int n0, int n1, int n2, float* __restrict__ boxb) {
+    const int64_t n = static_cast<int64_t>(n0) * n1 * n2;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int x = static_cast<int>(i % n2);
+        const int y = static_cast<int>((i / n2) % n1);
+        const int z = static_cast<int>(i / (static_cast<int64_t>(n1) * n2));
+        float sum = 0.0f;
+        if (ND == 3 ? (z <= n0 - B0 && y <= n1 - B1 && x <= n2 - B2) : (y <= n1 - B0 && x <= n2 - B1)) {
+#pragma unroll 1
+            for (int a0 = 0; a0 < B0; ++a0) {
+#pragma unroll
+                for (int a1 = 0; a1 < (ND == 3 ? B1 : 1); ++a1) {
+                    const float* row = ND == 3 ? bv + i + (static_cast<int64_t>(a0) * n1 + a1) * n2
+                                               : bv + i + static_cast<int64_t>(a0) * n2;
+#pragma unroll
+                    for (int a2 = 0; a2 < (ND == 3 ? B2 : B1); ++a2) sum += __ldg(row + a2);
+                }
+            }
+        }
+        boxb[i] = sum;
+    }
+}
+
+// -sum_p s_p log2 s_p for the XR candidates at origin + j (j < XR) along x;
+// ref[p].y holds max(r, 2^-100), so s > 0; xroom voxels of the row exist
+template <int ND, int B0, int B1, int B2, int XR>
+__device__ __forceinline__ void approx_unit(const float2* __restrict__ ref, const float* __restrict__ cv,
+                                            int64_t origin, int64_t s0, int64_t s1, int xroom, float (&acc)[XR]) {
+    constexpr int BX = ND == 3 ? B2 : B1;  // patch extent along x
+    constexpr int BR = ND == 3 ? B1 : 1;   // rows per step of axis 0
+    constexpr int NL = XR + BX - 1;
+#pragma unroll
+    for (int j = 0; j < XR; ++j) acc[j] = 0.0f;
+    const float* base = cv + origin;
 #pragma unroll 1
     for (int a0 = 0; a0 < B0; ++a0) {
 #pragma unroll
-        for (int a1 = 0; a1 < B1; ++a1) {
-            const float2* row = ND == 3 ? base + a0 * s0 + a1 * s1 : base + a0 * s0;
+        for (int a1 = 0; a1 < BR; ++a1) {
+            const float* row = base + a0 * s0 + (ND == 3 ? a1 * s1 : 0);
+            float xv[NL];
 #pragma unroll
-            for (int a2 = 0; a2 < B2; ++a2) {
-                const int p = (a0 * B1 + a1) * B2 + a2;
-                const float2 cv = __ldg(row + (ND == 3 ? a2 : a1));
-                const float2 rr = ref[p];
-                const float sv = rr.x + cv.x;
-                sum += fmaf(-sv, sfu_lg2(fmaxf(sv, kMin)), rr.y + cv.y);
+            for (int i = 0; i < NL; ++i) xv[i] = i < xroom ? __ldg(row + i) : 0.0f;
+#pragma unroll
+            for (int ax = 0; ax < BX; ++ax) {
+                const float r = ref[(a0 * BR + a1) * BX + ax].y;
+#pragma unroll
+                for (int j = 0; j < XR; ++j) {
+                    const float sv = r + xv[ax + j];
+                    acc[j] = fmaf(-sv, sfu_lg2(sv), acc[j]);
+                }
             }
         }
     }
-    constexpr int P = B0 * B1 * B2;
-    return fmaxf(1.38629436f * sum, 0.0f) / static_cast<float>(P);
 }
 
 // exact deviance with the reference patch already scaled and clamped (.x)
@@ -597,36 +639,80 @@ __global__ void __launch_bounds__(kSThreads, 8) blockmatch_screened_kernel(Match
         }
         const bool small_window = window < (int64_t(1) << 21);
         __syncthreads();  // previous reference's shared data is no longer read
-        const bool cheap = fixed && a.approx && a.cb != nullptr;
+        const bool cheap = fixed && a.approx && a.cv != nullptr;
+        float sa = 0.0f;  // cheap mode: sum_p A_r
         for (int p = tid; p < P; p += blockDim.x) {
             float rv = mul_rn(__ldg(a.src + center_origin + poff_s[p]), a.inv_scale);
             if (rv < 0.0f) rv = 0.0f;
-            ref[p] = make_float2(rv, cheap ? (rv > 0.0f ? rv + rv * log2f(rv) : 0.0f) : rv + rv);
+            if (cheap) sa += rv > 0.0f ? rv + rv * log2f(rv) : 0.0f;
+            ref[p] = make_float2(rv, cheap ? fmaxf(rv, 7.88860905e-31f) : rv + rv);
+        }
+        if (cheap) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sa += __shfl_xor_sync(0xffffffffu, sa, o);
+            if (lane == 0) redf[4 + warp] = sa;
         }
         for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0u;
-        if (tid == 0) redi[0] = 0;  // queue length
+        if (tid == 0) {
+            redi[0] = 0;  // queue length
+            redi[3] = 0;  // accepted keys in the queue
+        }
         __syncthreads();
         const float thr = a.thresholds ? a.thresholds[r] : a.scalar_threshold;
         const float tkey = canonical_key(thr);
 
         // pass A: screening distances and the reference-wide absolute bound
         float dmax = 0.0f;
-        for (int64_t c = tid; c < window; c += blockDim.x) {
-            int64_t lin;
-            const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
-            float2 sd;
-            if (cheap) {
-                if constexpr (ND > 0)
-                    sd = make_float2(approx_deviance_fixed<ND, B0, B1, B2>(ref, a.cb, origin, a.vstride[0],
-                                                                          a.vstride[ND > 1 ? 1 : 0]),
-                                     0.0f);
-            } else {
-                sd = fixed ? screen_deviance_fixed<ND, B0, B1, B2>(ref, a.src, origin, a.vstride[0],
-                                                                  a.vstride[ND > 1 ? 1 : 0], poff_s)
-                           : screen_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
+        if (cheap) {
+            if constexpr (ND > 0) {
+                constexpr int XR = 3;
+                constexpr int BX = ND == 3 ? B2 : B1;
+                const float sum_a = redf[4] + redf[5] + redf[6] + redf[7];
+                const int ex = ext[ND - 1];
+                const int nu = (ex + XR - 1) / XR;
+                const float inv_nu = 1.0f / static_cast<float>(nu);
+                const int nx = a.counts[ND - 1] + BX - 1;  // voxels along x
+                const int64_t units = window / ex * nu;
+                for (int64_t u = tid; u < units; u += blockDim.x) {
+                    // unit -> (row of the window, x run); rows are C-ordered over the outer axes
+                    const int ui = static_cast<int>(u);
+                    const int rowi = small_div(ui, inv_nu);
+                    const int k = ui - rowi * nu;
+                    int64_t origin = 0;
+                    if (ND == 3) {
+                        const int i0 = small_div(rowi, inv_ext[1]);
+                        const int i1 = rowi - i0 * ext[1];
+                        origin = static_cast<int64_t>(lo[0] + i0) * a.grid_stride[0] +
+                                 static_cast<int64_t>(lo[1] + i1) * a.grid_stride[1];
+                    } else {
+                        origin = static_cast<int64_t>(lo[0] + rowi) * a.grid_stride[0];
+                    }
+                    const int x0 = lo[ND - 1] + k * XR;
+                    origin += x0;
+                    float acc[XR];
+                    approx_unit<ND, B0, B1, B2, XR>(ref, a.cv, origin, a.vstride[0], a.vstride[ND > 1 ? 1 : 0],
+                                                    nx - x0, acc);
+                    const int64_t c0 = static_cast<int64_t>(rowi) * ex + k * XR;
+                    const int nvalid = min(XR, ex - k * XR);
+#pragma unroll
+                    for (int j = 0; j < XR; ++j) {
+                        if (j < nvalid) {
+                            const float d = 1.38629436f * (sum_a + __ldg(a.boxb + origin + j) + acc[j]);
+                            cand[c0 + j] = fmaxf(d, 0.0f) / static_cast<float>(P);
+                        }
+                    }
+                }
             }
-            cand[c] = sd.x;
-            dmax = fmaxf(dmax, sd.y);
+        } else {
+            for (int64_t c = tid; c < window; c += blockDim.x) {
+                int64_t lin;
+                const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
+                const float2 sd = fixed ? screen_deviance_fixed<ND, B0, B1, B2>(ref, a.src, origin, a.vstride[0],
+                                                                                a.vstride[ND > 1 ? 1 : 0], poff_s)
+                                        : screen_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
+                cand[c] = sd.x;
+                dmax = fmaxf(dmax, sd.y);
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
@@ -649,13 +735,28 @@ __global__ void __launch_bounds__(kSThreads, 8) blockmatch_screened_kernel(Match
                     for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0u;
                     __syncthreads();
                 }
-                for (int64_t c = tid; c < window; c += blockDim.x) {
-                    const float dv = cand[c];
-                    const float up = dv + (Dabs + drel * dv);
-                    if (!(canonical_key(up) < tkey)) continue;
-                    const uint32_t bits = __float_as_uint(up);
-                    if (pass > 0 && (bits >> (32 - 8 * pass)) != prefix) continue;
-                    atomicAdd(hist + ((bits >> shift) & 0xffu), 1u);
+                // warp-uniform sweep; lanes that share a bin add once (most
+                // candidates share the leading bits, so plain atomics serialise)
+                for (int64_t base = static_cast<int64_t>(warp) * 32; base < window; base += blockDim.x) {
+                    const int64_t c = base + lane;
+                    bool take = false;
+                    uint32_t bin = 0;
+                    if (c < window) {
+                        const float dv = cand[c];
+                        const float up = dv + (Dabs + drel * dv);
+                        if (canonical_key(up) < tkey) {
+                            const uint32_t bits = __float_as_uint(up);
+                            if (pass == 0 || (bits >> (32 - 8 * pass)) == prefix) {
+                                take = true;
+                                bin = (bits >> shift) & 0xffu;
+                            }
+                        }
+                    }
+                    const unsigned tm = __ballot_sync(0xffffffffu, take);
+                    if (take) {
+                        const unsigned peers = __match_any_sync(tm, bin);
+                        if (lane == __ffs(peers) - 1) atomicAdd(hist + bin, static_cast<uint32_t>(__popc(peers)));
+                    }
                 }
                 __syncthreads();
                 if (warp == 0) {
@@ -739,70 +840,86 @@ __global__ void __launch_bounds__(kSThreads, 8) blockmatch_screened_kernel(Match
         const int qn_all = redi[0];
         const bool overflow = qn_all > kSQueue;
         const int qn = overflow ? 0 : qn_all;
-        // exact rescoring of the queue
-        for (int i = tid; i < qn; i += blockDim.x) {
-            const int32_t q = qidx[i];
-            int64_t lin;
-            const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, q & 0x7fffffff, &lin);
-            const float dist = exact_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
-            const float key = canonical_key(dist);
-            const bool accepted = key < tkey;
-            if (accepted && q >= 0) ++acc_t;
-            qkey[i] = accepted ? composite_key(key, static_cast<int32_t>(lin)) : ~0ull;
+        // rescoring of the queue.  Fast mode: the exact float32 distance, one
+        // thread per candidate, bit-identical to the exact kernel.  Approx mode:
+        // the same terms, one warp per candidate (lanes over patch elements,
+        // tree-ordered sum), so the whole CTA works on the queue.
+        if (a.approx) {
+            const int nwarps = static_cast<int>(blockDim.x >> 5);
+            for (int i = warp; i < qn; i += nwarps) {
+                const int32_t q = qidx[i];
+                int64_t lin;
+                const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, q & 0x7fffffff, &lin);
+                float d = 0.0f;
+                for (int p = lane; p < P; p += 32) {
+                    float c = mul_rn(__ldg(a.src + origin + poff_s[p]), a.inv_scale);
+                    if (c < 0.0f) c = 0.0f;
+                    d += deviance_term(ref[p].x, c);
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+                if (lane == 0) {
+                    const float key = canonical_key(div_rn(fmaxf(d, 0.0f), static_cast<float>(P)));
+                    const bool accepted = key < tkey;
+                    if (accepted && q >= 0) ++acc_t;
+                    qkey[i] = accepted ? composite_key(key, static_cast<int32_t>(lin)) : ~0ull;
+                }
+            }
+        } else {
+            for (int i = tid; i < qn; i += blockDim.x) {
+                const int32_t q = qidx[i];
+                int64_t lin;
+                const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, q & 0x7fffffff, &lin);
+                const float dist = exact_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
+                const float key = canonical_key(dist);
+                const bool accepted = key < tkey;
+                if (accepted && q >= 0) ++acc_t;
+                qkey[i] = accepted ? composite_key(key, static_cast<int32_t>(lin)) : ~0ull;
+            }
         }
         // accepted count (block sum)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc_t += __shfl_xor_sync(0xffffffffu, acc_t, o);
         if (lane == 0) redi[4 + warp] = acc_t;
         __syncthreads();
-        if (warp == 0) {
-            int total_accepted = 0;
-            for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) total_accepted += redi[4 + w];
-            // top K of the rescored accepted keys (K rounds of warp minimum)
-            int ntop = 0;
-            if (!overflow && total_accepted >= R) {
-                uint64_t taken_mask_lo = 0;  // per lane: which of its items are taken (<= 16 items)
-                for (int t = 0; t < K; ++t) {
-                    uint64_t mine = ~0ull;
-                    int slot = -1;
-                    for (int i = lane, k = 0; i < qn; i += 32, ++k) {
-                        if ((taken_mask_lo >> k) & 1ull) continue;
-                        const uint64_t key = qkey[i];
-                        if (key < mine) {
-                            mine = key;
-                            slot = k;
-                        }
-                    }
-                    const uint64_t best = warp_min_u64(mine);
-                    if (best == ~0ull) break;
-                    if (mine == best && slot >= 0) taken_mask_lo |= 1ull << slot;
-                    if (lane == 0) top[t] = best;
-                    ++ntop;
-                }
+        int total_accepted = 0;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) total_accepted += redi[4 + w];
+        const bool complete = !overflow && total_accepted >= R;
+        // top K of the rescored accepted keys: each key's rank among the queue
+        // (composite keys are unique), in parallel
+        if (complete) {
+            for (int i = tid; i < qn; i += blockDim.x) {
+                const uint64_t k = qkey[i];
+                if (k == ~0ull) continue;
+                int rank = 0;
+                for (int j = 0; j < qn; ++j) rank += qkey[j] < k ? 1 : 0;
+                if (rank < K) top[rank] = k;
+                atomicAdd(redi + 3, 1);
             }
-            __syncwarp();
-            if (lane == 0) {
-                if (overflow || total_accepted < R) {
-                    a.count[r] = -1;  // queue overflow, or the best rejected are needed: exact redo
-                } else {
-                    int32_t* row = a.sel + r * K;
-                    int n = 0;
-                    row[n++] = static_cast<int32_t>(center_lin);
-                    for (int t = 0; t < ntop && n < K; ++t) {
-                        const int32_t l = static_cast<int32_t>(top[t] & 0xffffffffu);
-                        if (l < 0 || l == center_lin) continue;
-                        row[n++] = l;
-                    }
-                    if (a.pow2 && n > 0) {
-                        int target = 1;
-                        while ((target << 1) <= n) target <<= 1;
-                        if (a.min_m > target) target = a.min_m;
-                        if (target < n) n = target;
-                    }
-                    for (int t = n; t < K; ++t) row[t] = -1;
-                    a.count[r] = n;
-                    a.accepted[r] = total_accepted;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            if (!complete) {
+                a.count[r] = -1;  // queue overflow, or the best rejected are needed: exact redo
+            } else {
+                const int ntop = min(redi[3], K);
+                int32_t* row = a.sel + r * K;
+                int n = 0;
+                row[n++] = static_cast<int32_t>(center_lin);
+                for (int t = 0; t < ntop && n < K; ++t) {
+                    const int32_t l = static_cast<int32_t>(top[t] & 0xffffffffu);
+                    if (l < 0 || l == center_lin) continue;
+                    row[n++] = l;
                 }
+                if (a.pow2 && n > 0) {
+                    int target = 1;
+                    while ((target << 1) <= n) target <<= 1;
+                    if (a.min_m > target) target = a.min_m;
+                    if (target < n) n = target;
+                }
+                for (int t = n; t < K; ++t) row[t] = -1;
+                a.count[r] = n;
+                a.accepted[r] = total_accepted;
             }
         }
     }
@@ -1203,25 +1320,44 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
         return counts ? launch_counts(a, stream) : launch_exact(a, code, stream);
     }
     size_t smem = screened_smem_bytes(a.max_m, a.P, wmax);
-    // approximate mode on a volume: per-voxel (c, c + c log2 c), stream-ordered
-    // scratch freed after the launch; without it the bounded form is used with
-    // a zero bound
-    float2* cb = nullptr;
-    if (a.approx && !a.table) {
+    // approximate mode on a volume: per-voxel c and per-origin box sums of
+    // c + c log2 c, in stream-ordered scratch freed after the launch; without
+    // it the bounded form runs with a zero bound
+    float* aux = nullptr;
+    const int* bl = a.block;
+    const bool box_ok = (a.ndim == 2 && bl[0] == 8 && bl[1] == 8) ||
+                        (a.ndim == 3 && bl[0] == 5 && bl[1] == 5 && bl[2] == 5) ||
+                        (a.ndim == 3 && bl[0] == 4 && bl[1] == 4 && bl[2] == 4);
+    if (a.approx && !a.table && box_ok && a.inv_scale == 1.0f && a.grid_stride[a.ndim - 1] == 1) {
+        int n[3] = {1, 1, 1};
         int64_t nvox = 1;
-        for (int d = 0; d < a.ndim; ++d) nvox *= a.counts[d] + a.block[d] - 1;
-        if (cudaMallocAsync(reinterpret_cast<void**>(&cb), static_cast<size_t>(nvox) * sizeof(float2), stream) ==
+        for (int d = 0; d < a.ndim; ++d) {
+            n[3 - a.ndim + d] = a.counts[d] + a.block[d] - 1;
+            nvox *= n[3 - a.ndim + d];
+        }
+        if (cudaMallocAsync(reinterpret_cast<void**>(&aux), static_cast<size_t>(nvox) * 3 * sizeof(float), stream) ==
             cudaSuccess) {
-            int64_t bl = (nvox + 255) / 256;
-            if (bl > 152 * 16) bl = 152 * 16;
-            approx_voxel_kernel<<<static_cast<unsigned>(bl), 256, 0, stream>>>(a.src, a.inv_scale, nvox, cb);
+            float* cv = aux;
+            float* bv = aux + nvox;
+            float* boxb = aux + 2 * nvox;
+            int64_t nb = (nvox + 255) / 256;
+            if (nb > 152 * 16) nb = 152 * 16;
+            approx_voxel_kernel<<<static_cast<unsigned>(nb), 256, 0, stream>>>(a.src, a.inv_scale, nvox, cv, bv);
             BMND_LAUNCH_CHECK("approx_voxel_kernel");
+            if (a.ndim == 2)
+                approx_box_kernel<2, 8, 8, 1><<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, 1, n[1], n[2], boxb);
+            else if (bl[0] == 5)
+                approx_box_kernel<3, 5, 5, 5><<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, n[0], n[1], n[2], boxb);
+            else
+                approx_box_kernel<3, 4, 4, 4><<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, n[0], n[1], n[2], boxb);
+            BMND_LAUNCH_CHECK("approx_box_kernel");
+            a.cv = cv;
+            a.boxb = boxb;
         } else {
             (void)cudaGetLastError();
-            cb = nullptr;
+            aux = nullptr;
         }
     }
-    a.cb = cb;
     int64_t blocks = a.n_refs;
     const int64_t cap = 152 * 12;
     if (blocks > cap) blocks = cap;
@@ -1233,7 +1369,6 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
         return BMND_OK;
     };
     int32_t rc;
-    const int* bl = a.block;
     if (!a.table && a.ndim == 2 && bl[0] == 8 && bl[1] == 8)
         rc = run(blockmatch_screened_kernel<2, 8, 8, 1>);
     else if (!a.table && a.ndim == 3 && bl[0] == 5 && bl[1] == 5 && bl[2] == 5)
@@ -1242,8 +1377,9 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
         rc = run(blockmatch_screened_kernel<3, 4, 4, 4>);
     else
         rc = run(blockmatch_screened_kernel<0, 1, 1, 1>);
-    if (cb) BMND_CUDA_TRY(cudaFreeAsync(cb, stream));
-    a.cb = nullptr;
+    if (aux) BMND_CUDA_TRY(cudaFreeAsync(aux, stream));
+    a.cv = nullptr;
+    a.boxb = nullptr;
     if (rc) return rc;
     // references that need the best rejected candidates are redone exactly
     MatchArgs fix = a;

@@ -254,6 +254,63 @@ def test_screened_fallback_when_threshold_rejects_everything(cuda, native):
         np.testing.assert_array_equal(fa[i], ex[i])
 
 
+def _exact_deviance(vol, block, counts, ref_lin, cand_lin):
+    """Mean Poisson-deviance term (float64) between the patches at two patch-grid linear indices."""
+    ra = np.array(np.unravel_index(ref_lin, counts))
+    ca = np.array(np.unravel_index(np.asarray(cand_lin), counts))
+    r = vol[tuple(slice(int(o), int(o) + b) for o, b in zip(ra, block))].astype(np.float64).ravel()
+    out = []
+    for k in range(ca.shape[1]):
+        c = vol[tuple(slice(int(o), int(o) + b) for o, b in zip(ca[:, k], block))].astype(np.float64).ravel()
+        s = r + c
+        with np.errstate(divide="ignore", invalid="ignore"):
+            t = np.where(r > 0, r * np.log(2 * r / s), 0.0) + np.where(c > 0, c * np.log(2 * c / s), 0.0)
+        out.append(2.0 * t.sum() / r.size)
+    return np.array(out)
+
+
+@pytest.mark.parametrize("shape,block,radius,max_m,thr", [
+    ((22, 20, 24), (5, 5, 5), (7, 7, 7), 16, 2.9527),
+    ((21, 23, 19), (4, 4, 4), (6, 7, 5), 16, 2.9527),
+    ((46, 41), (8, 8), (19, 19), 16, 2.9527),
+])
+@pytest.mark.parametrize("kind", ["smooth", "counts"])
+def test_approx_matching_selects_near_optimal_groups(cuda, native, shape, block, radius, max_m, thr, kind):
+    """precision=approx ranks candidates by the box-sum screening form without
+    a bound.  Its groups must match the exact groups in size for almost every
+    reference, and their summed exact distances may exceed the exact optimum
+    only by rounding-level amounts."""
+    from bmnd_gb300 import _abi
+
+    rng = np.random.default_rng(17 + len(shape))
+    grids = np.meshgrid(*[np.linspace(0, 1, s) for s in shape], indexing="ij")
+    smooth = 5.0 + 20.0 * np.sin(3 * grids[0]) ** 2 + 10.0 * grids[-1]
+    if kind == "smooth":
+        vol = smooth + rng.normal(0, 0.5, size=shape)
+    else:
+        vol = rng.poisson(smooth).astype(np.float64)
+    vol = np.maximum(vol, 0.0).astype(np.float32)
+    counts = tuple(s - b + 1 for s, b in zip(shape, block))
+    refs = np.stack(np.meshgrid(*[np.arange(0, c, 3) for c in counts], indexing="ij"), -1)
+    refs = refs.reshape(-1, len(shape)).astype(np.int32)
+    ex = _match_volume(cuda, native, vol, block, radius, max_m, 2, thr, _abi.MATCH_EXACT, refs)
+    ap = _match_volume(cuda, native, vol, block, radius, max_m, 2, thr, _abi.MATCH_APPROX, refs)
+    same = ap[1] == ex[1]
+    assert same.mean() >= 0.97, same.mean()
+    worse, tot_a, tot_e = 0, 0.0, 0.0
+    for i in np.flatnonzero(same):
+        rl = int(np.ravel_multi_index(tuple(refs[i]), counts))
+        assert ap[0][i, 0] == rl  # the reference leads its group
+        da = _exact_deviance(vol, block, counts, rl, ap[0][i, : ap[1][i]]).sum()
+        de = _exact_deviance(vol, block, counts, rl, ex[0][i, : ex[1][i]]).sum()
+        tot_a += da
+        tot_e += de
+        if da > de * (1 + 1e-3) + 1e-6:
+            worse += 1
+    assert worse <= 0.02 * same.sum(), (worse, same.sum())
+    assert tot_a <= tot_e * (1 + 1e-4) + 1e-6, (tot_a, tot_e)
+
+
 def _patch_table(vol, block):
     """patches_flat of a volume: row = patch-grid linear index, column = patch element (C order)."""
     win = np.lib.stride_tricks.sliding_window_view(vol, block)
