@@ -11,7 +11,7 @@ import ctypes
 import os
 import threading
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_DIMS = 3
 MAX_EDGE = 8
 MAX_PATCH = 512
@@ -38,6 +38,9 @@ GROUP_NONE = 2
 
 WEIGHT_CLASSIC = 0
 WEIGHT_VARIANCE = 1
+
+NOISE_POISSON = 0
+NOISE_GAUSSIAN = 1
 
 MATCH_EXACT = 0
 MATCH_FAST = 1
@@ -98,6 +101,13 @@ class StageParams(ctypes.Structure):
         ("spatial_inv", (ctypes.c_float * (MAX_EDGE * MAX_EDGE)) * MAX_DIMS),
         ("window", ctypes.c_float * MAX_PATCH),
         ("spatial_metric_diag", ctypes.c_double * MAX_PATCH),
+        ("noise_model", _I32),
+        ("cov_domain", _I32 * MAX_DIMS),
+        ("cov_maps", ctypes.c_void_p),
+        ("match_noise_ssd", ctypes.c_void_p),
+        ("ssd_gamma", ctypes.c_float),
+        ("reserved1", _I32),
+        ("ssd_threshold", ctypes.c_double),
     ]
 
 

@@ -9,8 +9,10 @@ device buffers and the stream.  There is no CPU fallback: without a CUDA
 device, or without the built library, the call raises.
 
 Scope of the GPU path: direct-Poisson profiles (``noise_model="poisson"``)
-with the default Poisson options, 1-3 dimensional volumes, patch edges up to
-8 and stacks up to 32.  Anything else raises ``NotImplementedError`` after
+with the default Poisson options, and stationary Gaussian noise
+(``noise_model="gaussian"``, with ``sigma``, a ``sigma_psd`` or neither, in
+which case sigma is estimated), on 1-3 dimensional volumes with patch edges up
+to 8 and stacks up to 32.  Anything else raises ``NotImplementedError`` after
 validation.
 """
 
@@ -23,8 +25,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import _abi, plan
-from .enums import CacheMode, coerce_enum
+from . import _abi, gaussian, plan
+from .enums import BlockMatchDistance, CacheMode, coerce_enum
 from .validation import resolve_profile
 
 __all__ = ["bmnd", "BlockMatchGroup", "BlockMatchResult", "bmnd_device"]
@@ -153,16 +155,40 @@ def _match_result(schedule: plan.Schedule, counts, sel, cnt, acc) -> BlockMatchR
 _MATCH_PRECISIONS = {"exact": _abi.MATCH_EXACT, "fast": _abi.MATCH_FAST, "approx": _abi.MATCH_APPROX}
 
 
+def gaussian_tables(model: gaussian.GaussianModel, profile, shape, resolved, device) -> dict:
+    """Device tables of both stages for stationary Gaussian noise: the
+    covariance maps of each stage's transformed patches ([lag][coefficient])
+    and, for hard thresholding with gamma != 0, the SSD noise bias over the
+    search window (bmndalgo.py:291-303)."""
+    torch = _torch()
+    out = {}
+    for stage in ("ht", "wiener"):
+        block = tuple(int(b) for b in getattr(profile, f"{stage}_block_size"))
+        maps = gaussian.covariance_maps(model, block, plan.spatial_forward(profile, len(shape), stage))
+        cov = torch.from_numpy(np.ascontiguousarray(maps.reshape(maps.shape[0], -1).T)).to(device)
+        entry = {"cov": cov, "domain": model.domain, "ssd": None, "gamma": 0.0}
+        if stage == "ht" and resolved.blockmatch_distance is BlockMatchDistance.SSD:
+            gamma = 0.0 if resolved.conventional_nf else float(profile.gamma)
+            if gamma != 0.0:
+                radius = tuple(int(r) for r in profile.ht_search_window)
+                table = gaussian.blockmatch_noise_ssd(model, block, radius)
+                entry["ssd"] = torch.from_numpy(np.ascontiguousarray(table.reshape(-1))).to(device)
+                entry["gamma"] = float(np.float32(gamma))
+        out[stage] = entry
+    return out
+
+
 def bmnd_device(noisy, profile, *, resolved=None, match_precision: str = "exact",
                 stage_callback=None, blockmatch_callback=None, stream=None, sigma_maps: dict | None = None,
-                global_sigma: float = 0.0):
+                global_sigma: float = 0.0, gauss: dict | None = None):
     """Run both stages on a float32 CUDA tensor and return the CUDA result tensor.
 
     ``noisy`` must be a C-contiguous float32 CUDA tensor holding a validated,
     non-negative, non-zero volume.  This is the device-resident core of
     :func:`bmnd` (no host copies unless a callback is given).  With a
     ``sigma_maps`` dict, each stage also writes its sigma map (CUDA tensor,
-    keys "ht" and "wiener"; uncovered voxels get ``global_sigma``).
+    keys "ht" and "wiener"; uncovered voxels get ``global_sigma``).  ``gauss``
+    (from :func:`gaussian_tables`) selects stationary Gaussian noise.
     """
     torch = _torch()
     shape = tuple(int(s) for s in noisy.shape)
@@ -179,7 +205,7 @@ def bmnd_device(noisy, profile, *, resolved=None, match_precision: str = "exact"
     need = 0
     for stage in ("ht", "wiener"):
         p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance,
-                              resolved.variance_k, precision)
+                              resolved.variance_k, precision, None if gauss is None else gauss[stage])
         block = tuple(int(b) for b in getattr(profile, f"{stage}_block_size"))
         counts = tuple(s - b + 1 for s, b in zip(shape, block))
         sched = plan.reference_schedule(profile, counts, stage)
@@ -265,7 +291,7 @@ def estimate_poisson_global_sigma(volume, eps: float = 1e-10) -> float:
 
 
 def stage_device(noisy, profile, stage: str, pilot=None, *, resolved=None, match_precision: str = "exact",
-                 stream=None):
+                 stream=None, gauss: dict | None = None):
     """One filtering stage on a float32 CUDA tensor: "ht" on ``noisy``, or
     "wiener" on ``noisy`` with ``pilot`` as the stage-1 estimate.  Returns the
     stage estimate as a new CUDA tensor."""
@@ -282,7 +308,8 @@ def stage_device(noisy, profile, stage: str, pilot=None, *, resolved=None, match
     L = _abi.lib()
     if stream is None:
         stream = torch.cuda.current_stream(device)
-    p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k, precision)
+    p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k, precision,
+                          None if gauss is None else gauss[stage])
     block = tuple(int(b) for b in getattr(profile, f"{stage}_block_size"))
     counts = tuple(s - b + 1 for s, b in zip(shape, block))
     sched = plan.reference_schedule(profile, counts, stage)
@@ -358,6 +385,9 @@ def bmnd(
             raise ValueError("Direct Poisson input must contain only non-negative values.")
         all_zero = not np.any(vol != 0.0)
 
+    if sigma_psd is not None:
+        gaussian.validate_sigma_psd(shape, sigma_psd)
+
     if all_zero:
         zero = volume if torch_input else vol
         if stage_callback is not None:
@@ -369,11 +399,10 @@ def bmnd(
             return zero, {"ht": smap, "wiener": smap}
         return zero
 
-    if not resolved.is_poisson:
-        raise plan.unsupported(
-            "Gaussian noise profiles are not on the GPU path; use noise_model='poisson'"
-        )
-    plan.check_poisson_options(profile)
+    if resolved.is_poisson:
+        plan.check_poisson_options(profile)
+    else:
+        plan.check_gaussian_options(profile)
 
     torch = _torch()
     if not torch.cuda.is_available():
@@ -387,7 +416,17 @@ def bmnd(
         dev = host.pin_memory().cuda(non_blocking=True)
     maps = None
     global_sigma = 0.0
-    if return_sigma_map:
+    gauss = None
+    if not resolved.is_poisson:
+        host_vol = None
+        if sigma is None and sigma_psd is None:
+            host_vol = dev.cpu().numpy() if torch_input else vol
+        model = gaussian.build_model(shape, profile.nf, sigma=sigma, sigma_psd=sigma_psd, volume=host_vol)
+        gauss = gaussian_tables(model, profile, shape, resolved, dev.device)
+        if return_sigma_map:
+            maps = {}
+            global_sigma = model.global_sigma
+    elif return_sigma_map:
         maps = {}
         # on the stage-1 variance volume max(scale * max(x, 0), floor) (variance.py:581-592)
         host_vol = dev.cpu().numpy() if torch_input else vol
@@ -397,7 +436,7 @@ def bmnd(
         global_sigma = estimate_poisson_global_sigma(vvol, eps=max(floor, 1e-10))
     out = bmnd_device(dev, profile, resolved=resolved, match_precision=match_precision,
                       stage_callback=stage_callback, blockmatch_callback=blockmatch_callback,
-                      sigma_maps=maps, global_sigma=global_sigma)
+                      sigma_maps=maps, global_sigma=global_sigma, gauss=gauss)
     if torch_input:
         res = out if volume.is_cuda else out.cpu()
         if maps is None:

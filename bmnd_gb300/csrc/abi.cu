@@ -88,6 +88,17 @@ int32_t validate_stage(const BmndStageParams& sp) {
     if (!(sp.eps > 0.0)) return fail(BMND_ERR_INVALID_ARG, "eps must be positive");
     if (!(sp.match_threshold >= 0.0f) || !std::isfinite(sp.match_threshold))
         return fail(BMND_ERR_INVALID_ARG, "match threshold must be finite and >= 0");
+    if (sp.noise_model != BMND_NOISE_POISSON && sp.noise_model != BMND_NOISE_GAUSSIAN)
+        return fail(BMND_ERR_INVALID_ARG, "unknown noise model");
+    if (sp.noise_model == BMND_NOISE_GAUSSIAN) {
+        if (!sp.cov_maps) return fail(BMND_ERR_INVALID_ARG, "Gaussian noise needs the covariance maps");
+        for (int d = 0; d < sp.ndim; ++d)
+            if (sp.cov_domain[d] < 1) return fail(BMND_ERR_INVALID_ARG, "covariance domain must be positive");
+    }
+    if (sp.match_noise_ssd && sp.distance != BMND_DIST_SSD)
+        return fail(BMND_ERR_INVALID_ARG, "the noise-bias correction applies to SSD matching only");
+    if (sp.distance == BMND_DIST_SSD && (!(sp.ssd_threshold >= 0.0) || !std::isfinite(sp.ssd_threshold)))
+        return fail(BMND_ERR_INVALID_ARG, "SSD threshold multiplier must be finite and >= 0");
     if (group_filter_smem_bytes(sp) > 227 * 1024)
         return fail(BMND_ERR_UNSUPPORTED, "profile needs more than 227 KB of shared memory per group");
     return BMND_OK;
@@ -100,6 +111,8 @@ struct StageWorkspace {
     int32_t* count;
     int32_t* accepted;
     float* st;  // P x kron_stride(P) Kronecker table of the patch transforms
+    uint32_t* mm;  // SSD threshold: order bits of the matched volume's min and max
+    float* thr;    // SSD threshold, computed on the device
     uint64_t bytes;
 };
 
@@ -121,6 +134,7 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
     uint64_t o_acc = take(4ull * n_refs);
     const uint64_t P = static_cast<uint64_t>(patch_volume(sp));
     uint64_t o_st = take(4ull * P * static_cast<uint64_t>(kron_stride(static_cast<int>(P))));
+    uint64_t o_mm = take(16);
     w.bytes = off;
     if (base) {
         char* b = static_cast<char*>(base);
@@ -130,6 +144,8 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
         w.count = reinterpret_cast<int32_t*>(b + o_cnt);
         w.accepted = reinterpret_cast<int32_t*>(b + o_acc);
         w.st = reinterpret_cast<float*>(b + o_st);
+        w.mm = reinterpret_cast<uint32_t*>(b + o_mm);
+        w.thr = reinterpret_cast<float*>(b + o_mm + 8);
     }
     return w;
 }
@@ -159,7 +175,7 @@ uint64_t sigma_workspace_bytes(const BmndStageParams& sp, int64_t n_refs) {
 int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pilot,
                   const int32_t* refs, int64_t n_refs, float* out, int32_t* sel, int32_t* count,
                   int32_t* accepted, void* ws, uint64_t ws_bytes, cudaStream_t stream,
-                  float* sigma_out = nullptr, float global_sigma = 0.0f) {
+                  float* sigma_out = nullptr, float global_sigma = 0.0f, bool allow_alloc = true) {
     int32_t rc = validate_stage(sp);
     if (rc) return rc;
     if (!noisy || !out) return fail(BMND_ERR_INVALID_ARG, "noisy and out are required");
@@ -187,8 +203,15 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
     const float* match_src = sp.filter == BMND_FILTER_WIENER ? pilot : noisy;
     if (sp.filter == BMND_FILTER_WIENER && sp.match_precision == BMND_MATCH_EXACT)
         mp.precision = BMND_MATCH_REAL_VALUED;
+    const float* thr_dev = nullptr;
+    if (sp.distance == BMND_DIST_SSD) {
+        rc = launch_ssd_threshold(match_src, static_cast<int64_t>(vox), sp.ssd_threshold, w.mm, w.thr, stream);
+        if (rc) return rc;
+        thr_dev = w.thr;
+    }
     rc = launch_blockmatch_volume(mp, match_src, sp.shape, sp.block, refs, n_refs, nullptr,
-                                  sp.match_threshold, w.sel, w.count, w.accepted, stream);
+                                  sp.match_threshold, w.sel, w.count, w.accepted, stream, thr_dev,
+                                  sp.match_noise_ssd, sp.ssd_gamma, allow_alloc);
     if (rc) return rc;
     rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, w.st, sig_num, stream);
     if (rc) return rc;
@@ -395,7 +418,8 @@ int32_t bmnd_stage_noalloc(const BmndStageParams* params, const float* d_noisy,
     rc = static_scratch_address(&scratch);
     if (rc) return rc;
     return run_stage(*params, d_noisy, d_pilot, d_refs, n_refs, d_out, nullptr, nullptr, nullptr,
-                     scratch, BMND_STATIC_SCRATCH_BYTES, reinterpret_cast<cudaStream_t>(stream));
+                     scratch, BMND_STATIC_SCRATCH_BYTES, reinterpret_cast<cudaStream_t>(stream), nullptr, 0.0f,
+                     false);
 }
 
 }  // extern "C"

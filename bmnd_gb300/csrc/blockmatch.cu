@@ -63,6 +63,13 @@ struct MatchArgs {
     // voxel, and the sum of B(c) = c + c log2 c over the patch at each origin
     const float* cv;
     const float* boxb;
+    // SSD noise-bias correction (blockmatching.py:1133-1139): distance -=
+    // gamma * noise_ssd[offset of the candidate from the reference], or null
+    const float* noise_ssd;
+    float gamma;
+    // threshold computed on the device (one float), overrides the scalar one
+    const float* thr_dev;
+    int32_t no_alloc;  // 1: no stream-ordered scratch (approx mode then runs the bounded form)
 };
 
 constexpr int kTable = 64;  // counts 0..63 are tabulated
@@ -309,7 +316,7 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
         }
         __syncwarp();
 
-        const float thr = a.thresholds ? a.thresholds[r] : a.scalar_threshold;
+        const float thr = a.thresholds ? a.thresholds[r] : (a.thr_dev ? *a.thr_dev : a.scalar_threshold);
         const float tkey = stab ? canonical_key(thr) : thr;
         int acc_size = 0, rej_size = 0, acc_count = 0;
         for (int64_t c = lane; c < window; c += 32) {
@@ -317,6 +324,20 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
             const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
             float dist = use_table ? deviance_tabulated(ref_s, ref_row, a.src, origin, poff_s, P, table)
                                    : patch_distance<CODE>(ref_s, a.src, origin, poff_s, P, a.inv_scale);
+            if (CODE == BMND_DIST_SSD && a.noise_ssd) {
+                // offset of the candidate from the reference, C order over 2 r + 1 per axis
+                int64_t rem = c, gidx = 0, mul = 1;
+#pragma unroll
+                for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                    if (d < a.ndim) {
+                        const int cd = lo[d] + static_cast<int>(rem % ext[d]);
+                        rem /= ext[d];
+                        gidx += (cd - a.refs[r * a.ndim + d] + a.radius[d]) * mul;
+                        mul *= 2 * a.radius[d] + 1;
+                    }
+                }
+                dist = sub_rn(dist, mul_rn(a.gamma, __ldg(a.noise_ssd + gidx)));
+            }
             float key = stab ? canonical_key(dist) : dist;
             uint64_t ck = composite_key(key, static_cast<int32_t>(lin));
             if (key < tkey) {
@@ -658,7 +679,7 @@ __global__ void __launch_bounds__(kSThreads, 8) blockmatch_screened_kernel(Match
             redi[3] = 0;  // accepted keys in the queue
         }
         __syncthreads();
-        const float thr = a.thresholds ? a.thresholds[r] : a.scalar_threshold;
+        const float thr = a.thresholds ? a.thresholds[r] : (a.thr_dev ? *a.thr_dev : a.scalar_threshold);
         const float tkey = canonical_key(thr);
 
         // pass A: screening distances and the reference-wide absolute bound
@@ -1133,7 +1154,7 @@ __global__ void __launch_bounds__(kCThreads, 4) blockmatch_counts_kernel(MatchAr
         }
         __syncthreads();
 
-        const float thr = a.thresholds ? a.thresholds[r] : a.scalar_threshold;
+        const float thr = a.thresholds ? a.thresholds[r] : (a.thr_dev ? *a.thr_dev : a.scalar_threshold);
         const float tkey = canonical_key(thr);
         int acc_size = 0, rej_size = 0, acc_count = 0;
         const int S0 = nd == 3 ? bx[1] * bx[2] : bx[1];
@@ -1328,7 +1349,7 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     const bool box_ok = (a.ndim == 2 && bl[0] == 8 && bl[1] == 8) ||
                         (a.ndim == 3 && bl[0] == 5 && bl[1] == 5 && bl[2] == 5) ||
                         (a.ndim == 3 && bl[0] == 4 && bl[1] == 4 && bl[2] == 4);
-    if (a.approx && !a.table && box_ok && a.inv_scale == 1.0f && a.grid_stride[a.ndim - 1] == 1) {
+    if (a.approx && !a.table && !a.no_alloc && box_ok && a.inv_scale == 1.0f && a.grid_stride[a.ndim - 1] == 1) {
         int n[3] = {1, 1, 1};
         int64_t nvox = 1;
         for (int d = 0; d < a.ndim; ++d) {
@@ -1468,11 +1489,18 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
                                  const int32_t* shape, const int32_t* block, const int32_t* refs,
                                  int64_t n_refs, const float* thresholds, float scalar_threshold,
                                  int32_t* sel, int32_t* count, int32_t* accepted,
-                                 cudaStream_t stream) {
+                                 cudaStream_t stream, const float* thr_dev, const float* noise_ssd,
+                                 float gamma, bool allow_alloc) {
     int32_t rc = validate_match(mp);
     if (rc) return rc;
+    if (noise_ssd && mp.distance != BMND_DIST_SSD)
+        return fail(BMND_ERR_INVALID_ARG, "the noise-bias correction applies to SSD matching only");
     MatchArgs a{};
     fill_common(a, mp);
+    a.thr_dev = thr_dev;
+    a.noise_ssd = noise_ssd;
+    a.gamma = gamma;
+    a.no_alloc = allow_alloc ? 0 : 1;
     int P = 1;
     int64_t vstride[BMND_MAX_DIMS];
     int64_t s = 1;
@@ -1501,6 +1529,53 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
     a.count = count;
     a.accepted = accepted;
     return launch(a, mp.distance, mp.precision, stream);
+}
+
+namespace {
+// order-preserving min / max of a volume, then the SSD threshold
+// float32(t * d * d), d = max - min (1 when d <= 0) (blockmatching.py:168-184)
+__global__ void minmax_kernel(const float* __restrict__ x, int64_t n, uint32_t* __restrict__ mm) {
+    uint32_t lo = 0xffffffffu, hi = 0u;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const uint32_t b = order_bits(__ldg(x + i));
+        lo = min(lo, b);
+        hi = max(hi, b);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(mm, lo);
+        atomicMax(mm + 1, hi);
+    }
+}
+
+__device__ __forceinline__ float from_order_bits(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__global__ void ssd_threshold_kernel(const uint32_t* __restrict__ mm, double t, float* __restrict__ thr) {
+    float d = from_order_bits(mm[1]) - from_order_bits(mm[0]);
+    double ds = d > 0.0f ? static_cast<double>(d) : 1.0;
+    *thr = static_cast<float>(t * ds * ds);
+}
+}  // namespace
+
+int32_t launch_ssd_threshold(const float* volume, int64_t n, double t, uint32_t* mm, float* thr,
+                             cudaStream_t stream) {
+    BMND_CUDA_TRY(cudaMemsetAsync(mm, 0xff, sizeof(uint32_t), stream));
+    BMND_CUDA_TRY(cudaMemsetAsync(mm + 1, 0, sizeof(uint32_t), stream));
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks < 1) blocks = 1;
+    minmax_kernel<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(volume, n, mm);
+    BMND_LAUNCH_CHECK("minmax_kernel");
+    ssd_threshold_kernel<<<1, 1, 0, stream>>>(mm, t, thr);
+    BMND_LAUNCH_CHECK("ssd_threshold_kernel");
+    return BMND_OK;
 }
 
 int32_t launch_blockmatch_patches(const BmndMatchParams& mp, const float* patches,

@@ -182,7 +182,12 @@ __host__ __device__ constexpr int kron_stride(int P) {
 int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume, const int32_t* shape,
                                  const int32_t* block, const int32_t* refs, int64_t n_refs,
                                  const float* thresholds, float scalar_threshold, int32_t* sel,
-                                 int32_t* count, int32_t* accepted, cudaStream_t stream);
+                                 int32_t* count, int32_t* accepted, cudaStream_t stream,
+                                 const float* thr_dev = nullptr, const float* noise_ssd = nullptr,
+                                 float gamma = 0.0f, bool allow_alloc = true);
+// mm: two uint32 of device scratch; thr: one device float
+int32_t launch_ssd_threshold(const float* volume, int64_t n, double t, uint32_t* mm, float* thr,
+                             cudaStream_t stream);
 int32_t launch_blockmatch_patches(const BmndMatchParams& mp, const float* patches, int32_t patch_vol,
                                   const int32_t* refs, int64_t n_refs, const float* thresholds,
                                   int32_t* sel, int32_t* count, int32_t* accepted,

@@ -44,8 +44,8 @@ constexpr int kThreads = 256;      // threads per group (CTA)
 // thresholding).  Transforms run in place, so no scratch buffer is needed.
 struct Layout {
     // byte offsets into dynamic shared memory
-    int64_t g, gt, fw, fi, win, mdiag, pos, shf, shl, sg, ex, uni, s, x, r, v, grid, lval, lstart, lent, scan,
-        plane, wts, misc, total;
+    int64_t g, gt, fw, fi, win, mdiag, pos, shf, shl, sg, ex, lag, uni, s, x, r, v, grid, lval, lstart, lent,
+        scan, plane, wts, misc, total;
 };
 
 struct FilterArgs {
@@ -91,6 +91,9 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     // hard thresholding with a sigma map keeps each coefficient's sigma until the scatter
     L.sg = take(sigma && !wiener ? 4 * np : 16);
     L.ex = take(4 * static_cast<int64_t>(kmax) * P);
+    // Gaussian noise: lag index of every member pair (i >= j)
+    const bool gauss = sp.noise_model == BMND_NOISE_GAUSSIAN;
+    L.lag = take(gauss && kmax > 0 ? 4 * static_cast<int64_t>(nmax) * (nmax + 1) / 2 : 16);
     L.scan = take(8 * (kThreads + 1));
     L.plane = take(8 * nmax);
     L.wts = take(4 * nmax);
@@ -103,12 +106,14 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     L.r = L.x + buf;  // Wiener: pilot coefficients, then the attenuation
     L.v = L.r;        // hard thresholding: the attenuation
     const int64_t group_bytes = 3 * buf;
-    const int64_t umax = kmax > 0 ? (np < ucells ? np : ucells) : 0;
+    // union-voxel lists of the exact Poisson phase (none for Gaussian noise)
+    const int kl = gauss ? 0 : kmax;
+    const int64_t umax = kl > 0 ? (np < ucells ? np : ucells) : 0;
     L.grid = L.uni;
-    L.lval = L.grid + round16(kmax > 0 ? 4 * ucells : 0);
+    L.lval = L.grid + round16(kl > 0 ? 4 * ucells : 0);
     L.lstart = L.lval + round16(4 * umax);
     L.lent = L.lstart + round16(4 * (umax + 1));
-    const int64_t list_bytes = (L.lent + round16(kmax > 0 ? 4 * np : 0)) - L.uni;
+    const int64_t list_bytes = (L.lent + round16(kl > 0 ? 4 * np : 0)) - L.uni;
     off = L.uni + (group_bytes > list_bytes ? group_bytes : list_bytes);
     L.total = off;
     return L;
@@ -636,8 +641,69 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
     const int total = n * P;
     const bool need_approx = (k <= 0) || (kk < n);
 
+    const bool gauss = sp.noise_model == BMND_NOISE_GAUSSIAN;
+    if (gauss) {
+        // ---- stationary Gaussian noise (variance.py:2036-2106) ----
+        // exact planes g < kk: sum_{i,j} G[g,i] G[g,j] C_c((x_i - x_j) mod domain),
+        // C_c the covariance map of spatial coefficient c; the other planes
+        // share what is left of n times the patch variance C_c(0)
+        int* lag = sm<int>(smem, a.L.lag);
+        const int npair = n * (n + 1) / 2;
+        if (kk > 0) {
+            for (int q = tid; q < npair; q += blockDim.x) {
+                int i = static_cast<int>((sqrtf(8.0f * static_cast<float>(q) + 1.0f) - 1.0f) * 0.5f);
+                while (i * (i + 1) / 2 > q) --i;
+                while ((i + 1) * (i + 2) / 2 <= q) ++i;
+                const int j = q - i * (i + 1) / 2;
+                int flat = 0;
+                for (int d = 0; d < geo.nd(); ++d) {
+                    const int D = sp.cov_domain[d];
+                    int l = (pos[i * BMND_MAX_DIMS + d] - pos[j * BMND_MAX_DIMS + d]) % D;
+                    if (l < 0) l += D;
+                    flat = flat * D + l;
+                }
+                lag[q] = flat;
+            }
+            __syncthreads();
+        }
+        const float* cm = sp.cov_maps;
+        for (int c = tid; c < P; c += blockDim.x) {
+            const float pv = __ldg(cm + c);  // lag 0: the patch variance of coefficient c
+            float ex_sum = 0.0f;
+            for (int g = 0; g < kk; ++g) {
+                const float* Gr = G + g * n;
+                float value = 0.0f;
+                for (int i = 0; i < n; ++i) {
+                    const float wi = Gr[i];
+                    if (wi == 0.0f) continue;
+                    value = add_rn(value, mul_rn(mul_rn(wi, pv), wi));
+                    const int* lrow = lag + i * (i + 1) / 2;
+                    for (int j = 0; j < i; ++j) {
+                        const float wj = Gr[j];
+                        if (wj == 0.0f) continue;
+                        const float cv = __ldg(cm + static_cast<int64_t>(lrow[j]) * P + c);
+                        value = add_rn(value, mul_rn(mul_rn(wi, wj), add_rn(cv, cv)));
+                    }
+                }
+                value = fmaxf(value, 0.0f);
+                EX[g * P + c] = value;
+                ex_sum = add_rn(ex_sum, value);
+            }
+            float rest = pv;
+            if (kk > 0 && kk < n) {
+                rest = div_rn(sub_rn(mul_rn(static_cast<float>(n), pv), ex_sum), static_cast<float>(n - kk));
+                rest = fmaxf(rest, 0.0f);
+            }
+            for (int g = 0; g < n; ++g) {
+                const float v = g < kk ? EX[g * P + c] : rest;
+                S[g * P + c] = sqrtf(fmaxf(v, 0.0f));
+            }
+        }
+        __syncthreads();
+    }
+
     // ---- exact overlap-aware sigma of the first kk planes ----
-    if (kk > 0) {
+    if (!gauss && kk > 0) {
         int ush[BMND_MAX_DIMS] = {1, 1, 1}, org[BMND_MAX_DIMS] = {0, 0, 0};
         int ucells = 1;
         for (int d = 0; d < geo.nd(); ++d) {
@@ -766,7 +832,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
 
     // ---- approximate sigma from the variance group (squared transforms) ----
     // (after the exact phase: S shares the union region with its lists)
-    if (need_approx) {
+    if (!gauss && need_approx) {
         for (int e = tid; e < total; e += blockDim.x) {
             const int g = e / P;
             S[e] = variance_of(__ldg(varsrc + geo.offset(pos + g * BMND_MAX_DIMS, e - g * P, a.vstride)),
@@ -782,7 +848,9 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
     }
 
     // ---- final sigma in S (plane limiting, variance.py:1572-1631) ----
-    if (k > 0 && kk == n) {
+    if (gauss) {
+        // done above
+    } else if (k > 0 && kk == n) {
         for (int e = tid; e < total; e += blockDim.x) S[e] = EX[e];
     } else if (k > 0) {
         for (int j = tid; j < P; j += blockDim.x) {
@@ -842,9 +910,21 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         }
         float nv = mul_rn(sig, sig);
         float att;
-        if (!wiener) {
+        if (!wiener && gauss) {
+            // |c| >= lambda sigma, the group DC always kept (bmndalgo.py:462-475)
+            float thr = mul_rn(sp.ht_lambda, sig);
+            att = (fabsf(X[e]) >= thr || e == 0) ? 1.0f : 0.0f;
+        } else if (!wiener) {
             float thr = mul_rn(sp.ht_lambda, sig);
             att = ht_keep(fabsf(X[e]), thr, sp.count_scale, scale_f) ? 1.0f : 0.0f;
+        } else if (gauss) {
+            // |R|^2 / (|R|^2 + mu^2 max(sigma^2, 1e-8)) (wiener.py:50-69)
+            float eff = mul_rn(sp.wiener_scale, fmaxf(nv, fmaxf(eps_f, 1e-8f)));
+            float pr = fabsf(R[e]);
+            pr = mul_rn(pr, pr);
+            float den = add_rn(pr, eff);
+            float gain = den > 0.0f ? div_rn(pr, den) : 0.0f;
+            att = fminf(fmaxf(gain, 0.0f), 1.0f);
         } else {
             float eff = mul_rn(sp.wiener_scale, nv);
             float pr = fabsf(R[e]);

@@ -60,9 +60,22 @@ def unsupported(reason: str) -> NotImplementedError:
     return NotImplementedError(f"bmnd_gb300: {reason}")
 
 
+def spatial_forward(profile, ndim: int, stage: str) -> list:
+    """Per-axis forward spatial matrices of ``stage`` (None: identity)."""
+    block = tuple(int(b) for b in getattr(profile, f"{stage}_block_size"))
+    _, spatial = resolve_axes(getattr(profile, f"{stage}_transform"), ndim)
+    return [None if kind is None else axis_matrices(kind, block[a])[0] for a, kind in enumerate(spatial)]
+
+
 def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMatchDistance,
-                 variance_k: int, match_precision: int = _abi.MATCH_EXACT) -> _abi.StageParams:
-    """Fill the ``StageParams`` of ``stage`` ("ht" or "wiener") for a Poisson profile."""
+                 variance_k: int, match_precision: int = _abi.MATCH_EXACT, gauss: dict | None = None
+                 ) -> _abi.StageParams:
+    """Fill the ``StageParams`` of ``stage`` ("ht" or "wiener").
+
+    ``gauss`` (stationary Gaussian noise) holds the device tables of the stage:
+    ``cov`` (float32 CUDA tensor [lag][coefficient]), ``domain`` (its lag
+    domain), ``ssd`` (SSD noise bias over the search offsets, or None) and
+    ``gamma``; without it the stage models direct Poisson noise."""
     ndim = len(shape)
     if ndim < 1 or ndim > _abi.MAX_DIMS:
         raise unsupported(f"{ndim}-D volumes are not supported (1 to {_abi.MAX_DIMS} dimensions)")
@@ -92,7 +105,7 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     p.max_stack = max_stack
     p.min_stack = min_stack
     p.distance = _DISTANCE_CODES[distance]
-    p.stabilize_ties = 1
+    p.stabilize_ties = 0 if gauss is not None else 1
     p.match_precision = match_precision
     p.filter = _abi.FILTER_HARD_THRESHOLD if stage == "ht" else _abi.FILTER_WIENER
     p.group_transform = _GROUP_CODES[group_kind]
@@ -104,9 +117,22 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     p.match_threshold = float(np.float32(getattr(profile, f"{stage}_match_threshold")))
     p.ht_lambda = float(profile.ht_lambda_threshold)
     p.wiener_scale = float(profile.wiener_variance_scale)
-    p.count_scale = float(profile.poisson_count_scale)
-    p.variance_floor = float(profile.poisson_variance_floor)
     p.eps = EPS
+    p.ssd_threshold = float(getattr(profile, f"{stage}_match_threshold"))
+    if gauss is None:
+        p.noise_model = _abi.NOISE_POISSON
+        p.count_scale = float(profile.poisson_count_scale)
+        p.variance_floor = float(profile.poisson_variance_floor)
+    else:
+        p.noise_model = _abi.NOISE_GAUSSIAN
+        p.count_scale = 1.0
+        p.variance_floor = 0.0
+        for a, n in enumerate(gauss["domain"]):
+            p.cov_domain[a] = int(n)
+        p.cov_maps = gauss["cov"].data_ptr()
+        if gauss.get("ssd") is not None:
+            p.match_noise_ssd = gauss["ssd"].data_ptr()
+            p.ssd_gamma = float(gauss["gamma"])
     inverse = []
     for a in range(ndim):
         kind = spatial[a]
@@ -135,6 +161,19 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     return p
 
 
+def check_gaussian_options(profile) -> None:
+    """Reject the Gaussian options that are not on the GPU path."""
+    if profile.ht_use_soft_thresholding:
+        raise unsupported("soft thresholding is not on the GPU path")
+    if profile.reference_schedule_mode not in (
+        ReferenceScheduleMode.GENERATED,
+        ReferenceScheduleMode.OFF,
+    ):
+        raise unsupported(
+            f"reference schedule {profile.reference_schedule_mode.value!r} is not on the GPU path"
+        )
+
+
 def check_poisson_options(profile) -> None:
     """Reject the non-default Poisson options that are not on the GPU path."""
     if profile.poisson_ht_match_policy is not PoissonHTMatchPolicy.FIXED:
@@ -149,6 +188,8 @@ def check_poisson_options(profile) -> None:
         raise unsupported("only pilot Wiener matching is on the GPU path")
     if profile.ht_use_soft_thresholding:
         raise unsupported("soft thresholding is not on the GPU path")
+    if profile.blockmatch_distance is BlockMatchDistance.SSD and float(profile.gamma) != 0.0:
+        raise unsupported("the Poisson SSD noise-bias correction (gamma != 0) is not on the GPU path")
     if profile.reference_schedule_mode not in (
         ReferenceScheduleMode.GENERATED,
         ReferenceScheduleMode.OFF,

@@ -3,9 +3,9 @@
 Restates resolve_profile (src/bmnd/profilevalidation.py:33-456): the same
 checks in the same order, the same ``ValueError`` texts, and the same in-place
 enum coercion of the caller's profile (profilevalidation.py:133-134, :219,
-:250-252).  The noise-PSD resolution of the Gaussian branch (psd.resolve_nf)
-is not part of the GPU path; Gaussian profiles are validated up to that point
-and then rejected by :func:`bmnd_gb300.bmnd`.
+:250-252).  The Gaussian branch resolves the local-variance domain ``nf``
+(psd.py:57-98, restated in ``gaussian.resolve_nf``); conventional mode (a
+zero ``nf``) sets ``k`` to 0, as the reference does (profilevalidation.py:445-448).
 """
 
 from __future__ import annotations
@@ -27,6 +27,7 @@ from .enums import (
     ReferenceScheduleMode,
     coerce_enum,
 )
+from .gaussian import resolve_nf
 from .transforms import Transform, TransformMode, TransformType
 
 _OPERATOR_TYPES = {
@@ -294,6 +295,10 @@ def resolve_profile(profile, volume_shape: tuple[int, ...]) -> ResolvedProfile:
                 if not np.isfinite(value) or value < 0.0 or (positive and value == 0.0):
                     qualifier = "positive" if positive else "non-negative"
                     raise ValueError(f"{name} must be finite and {qualifier}, got {value}.")
+    else:
+        effective_nf, conventional_nf = resolve_nf(profile.nf, tuple(int(s) for s in volume_shape))
+        if conventional_nf:
+            variance_k = 0
 
     return ResolvedProfile(
         is_poisson=is_poisson,

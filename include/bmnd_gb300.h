@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define BMND_ABI_VERSION 1
+#define BMND_ABI_VERSION 2
 #define BMND_MAX_DIMS 3
 #define BMND_MAX_EDGE 8       /* largest patch edge per axis */
 #define BMND_MAX_PATCH 512    /* largest patch volume */
@@ -64,6 +64,10 @@ extern "C" {
 /* aggregation weight model (src/bmnd/enums.py:30-33); scope is always "patch" */
 #define BMND_WEIGHT_CLASSIC 0
 #define BMND_WEIGHT_VARIANCE 1
+
+/* noise model of a stage */
+#define BMND_NOISE_POISSON 0  /* variance volume max(count_scale * max(x, 0), floor) */
+#define BMND_NOISE_GAUSSIAN 1 /* stationary noise given by cov_maps (bmndalgo.py:404-454, :826-870) */
 
 /* matching precision */
 #define BMND_MATCH_EXACT 0 /* FP32 per-term distances for every candidate */
@@ -123,6 +127,23 @@ typedef struct BmndStageParams {
     float window[BMND_MAX_PATCH];
     /* diag(S_inv^T diag(w^2) S_inv), float64; used only for windowed_synthesis */
     double spatial_metric_diag[BMND_MAX_PATCH];
+    /* ---- noise model (ABI version 2) ---- */
+    int32_t noise_model;                     /* BMND_NOISE_POISSON or BMND_NOISE_GAUSSIAN */
+    int32_t cov_domain[BMND_MAX_DIMS];       /* Gaussian: lag domain of cov_maps (nf) */
+    /* Gaussian: device table [lag][coefficient], lag C-ordered over cov_domain:
+     * covariance of transformed patch coefficient c between two patches whose
+     * origins differ by lag (mod cov_domain) (variance.py:1791-1886) */
+    const float* cov_maps;
+    /* SSD matching: device table over the search offsets (C order over
+     * 2 r + 1 per axis) subtracted times ssd_gamma from every distance
+     * (blockmatching.py:1133-1139), or NULL */
+    const float* match_noise_ssd;
+    float ssd_gamma;
+    int32_t reserved1;
+    /* SSD matching threshold multiplier: the threshold is
+     * float32(ssd_threshold * (max - min)^2) over the matched volume
+     * (blockmatching.py:168-184), evaluated on the device */
+    double ssd_threshold;
 } BmndStageParams;
 
 /* ABI version this library was built with (BMND_ABI_VERSION). */

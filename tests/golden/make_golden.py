@@ -12,6 +12,7 @@ Usage::
     python tests/golden/make_golden.py unit
     python tests/golden/make_golden.py pipeline bm3d_32 [bm4d_16 ...]
     python tests/golden/make_golden.py sigma bm3d_32 [bm4d_12x16x20 ...]
+    python tests/golden/make_golden.py gauss [bm3d_32 ...]
     python tests/golden/make_golden.py list
 
 ``unit`` writes ``unit_*.npz`` (distances, canonical keys, transforms, exact
@@ -290,6 +291,102 @@ def run_unit() -> None:
     print(f"unit fixtures -> {path} ({len(out)} arrays)")
 
 
+# Gaussian cases: name -> (profile kind, clean generator, kwargs, sigma, call options, profile fields)
+GAUSS_CASES = {
+    "bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=11), 3.0, {}, {}),
+    "bm3d_40x24": ("bm3d", "ragged2d", dict(shape=(40, 24), seed=12), 2.0, {}, {}),
+    "bm3d_est_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=13), 4.0, dict(estimate=True), {}),
+    "bm3d_psd_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=14), 2.5, dict(psd=True), {}),
+    "bm3d_conv_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=15), 3.0, {}, dict(nf=0)),
+    "bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=16), 1.5, {}, {}),
+}
+
+
+def _gauss_input(gen, kwargs, sigma):
+    if gen in ("ragged2d", "ragged3d"):
+        clean, _ = _make_input(gen, kwargs)
+    else:
+        clean, _ = gen(**kwargs)
+    rng = np.random.default_rng(1000 + kwargs["seed"])
+    noisy = (clean + sigma * rng.standard_normal(clean.shape)).astype(np.float32)
+    return clean.astype(np.float32), noisy
+
+
+def _colored_psd(shape, sigma):
+    """A smooth, strictly positive PSD of mean N sigma^2 (low frequencies stronger)."""
+    grids = np.meshgrid(*[np.fft.fftfreq(n) for n in shape], indexing="ij")
+    r2 = sum(g * g for g in grids)
+    psd = 1.0 + 3.0 * np.exp(-r2 / 0.02)
+    psd *= float(np.prod(shape)) * sigma * sigma / psd.mean()
+    return psd.astype(np.float32)
+
+
+def run_gauss(name: str) -> None:
+    """gauss_<case>.npz: the reference on stationary Gaussian noise (both stage
+    estimates, both match sets, the sigma maps and the noise model's tables)."""
+    import bmnd as ref
+    from bmnd import variance as refvar
+
+    kind, gen, kwargs, sigma, opts, extra = GAUSS_CASES[name]
+    clean, noisy = _gauss_input(gen, kwargs, sigma)
+    profile_cls = ref.BM3DProfile if kind == "bm3d" else ref.BM4DProfile
+    profile = profile_cls(**extra)
+    call = {}
+    psd = None
+    if opts.get("psd"):
+        psd = _colored_psd(noisy.shape, sigma)
+        call["sigma_psd"] = psd
+    elif not opts.get("estimate"):
+        call["sigma"] = sigma
+    stages, matches = {}, {}
+
+    def stage_cb(stage, est):
+        stages[stage] = np.asarray(est, dtype=np.float32)
+
+    def bm_cb(stage, result):
+        max_stack = profile.ht_max_stack_size if stage == "ht" else profile.wiener_max_stack_size
+        matches[stage] = _pack_matches(result, max_stack, noisy.ndim)
+
+    t0 = time.time()
+    out, smap = ref.bmnd(noisy, profile, return_sigma_map=True, stage_callback=stage_cb,
+                         blockmatch_callback=bm_cb, **call)
+    elapsed = time.time() - t0
+    payload = dict(kind=np.array(kind), clean=clean, noisy=noisy, ht=stages["ht"], wiener=stages["wiener"],
+                   out=np.asarray(out, dtype=np.float32), global_sigma=np.float64(smap["global"]),
+                   sigma_ht=np.asarray(smap["ht"], dtype=np.float32),
+                   sigma_wiener=np.asarray(smap["wiener"], dtype=np.float32), seconds=np.float64(elapsed),
+                   sigma=np.float64(-1.0 if "sigma" not in call else sigma),
+                   nf=np.array(-1 if "nf" not in extra else extra["nf"]))
+    if psd is not None:
+        payload["sigma_psd"] = psd
+    for stage, (sel, counts, accepted, refs) in matches.items():
+        payload[f"{stage}_sel"] = sel
+        payload[f"{stage}_count"] = counts
+        payload[f"{stage}_accepted"] = accepted
+        payload[f"{stage}_refs"] = refs
+    # the noise model's tables, for the host-side restatement
+    from bmnd.profilevalidation import resolve_profile as ref_resolve
+
+    res = ref_resolve(profile, tuple(noisy.shape))
+    model = refvar.build_variance_model(noisy, sigma=call.get("sigma"), sigma_psd=call.get("sigma_psd"),
+                                       nf=res.effective_nf)
+    payload["model_global_sigma"] = np.float64(model.global_sigma)
+    payload["model_domain"] = np.array(model.variance_domain_shape, dtype=np.int64)
+    from bmnd.transforms import get_transform_matrix
+
+    for stage in ("ht", "wiener"):
+        block = tuple(getattr(profile, f"{stage}_block_size"))
+        fwd, _ = get_transform_matrix((2,) + block, getattr(profile, f"{stage}_transform"))
+        payload[f"{stage}_cov_maps"] = np.asarray(
+            refvar._get_cached_transformed_patch_cross_covariance(model, block, list(fwd[1:])), dtype=np.float32)
+    payload["ht_noise_ssd"] = np.asarray(
+        refvar.get_gaussian_blockmatch_noise_ssd(model, tuple(profile.ht_block_size),
+                                                 tuple(profile.ht_search_window)), dtype=np.float32)
+    path = os.path.join(HERE, f"gauss_{name}.npz")
+    np.savez_compressed(path, **payload)
+    print(f"gauss {name}: {noisy.shape} in {elapsed:.1f} s -> {path}")
+
+
 def main(argv: list[str]) -> None:
     if not argv or argv[0] == "list":
         print("\n".join(PIPELINE_CASES))
@@ -300,6 +397,10 @@ def main(argv: list[str]) -> None:
     if argv[0] == "sigma":
         for name in argv[1:]:
             run_sigma(name)
+        return
+    if argv[0] == "gauss":
+        for name in argv[1:] or list(GAUSS_CASES):
+            run_gauss(name)
         return
     if argv[0] == "pipeline":
         for name in argv[1:]:
