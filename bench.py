@@ -42,7 +42,16 @@ WORKLOADS = {
     "bm4d128": dict(kind="bm4d", size=128, desc="128^3 BM4D-Poisson, 30 ellipsoids"),
     "bm3d2048": dict(kind="bm3d", size=2048, desc="2048^2 BM3D-Poisson, 40 blobs + 60 rectangles"),
     "bm3d256": dict(kind="bm3d", size=256, desc="256^2 BM3D-Poisson, 12 rectangles/discs"),
+    # stationary Gaussian noise (default profiles, sigma given)
+    "gauss2048": dict(kind="bm3d", size=2048, noise="gaussian", sigma=5.0,
+                      desc="2048^2 BM3D-Gaussian sigma=5, 40 blobs + 60 rectangles"),
+    "gauss256": dict(kind="bm4d", size=256, noise="gaussian", sigma=2.0,
+                     desc="256^3 BM4D-Gaussian sigma=2, 30 ellipsoids"),
 }
+
+
+def is_gaussian(name: str) -> bool:
+    return WORKLOADS[name].get("noise") == "gaussian"
 
 
 def make_input(name: str, seed: int):
@@ -50,16 +59,23 @@ def make_input(name: str, seed: int):
 
     w = WORKLOADS[name]
     if w["kind"] == "bm4d":
-        return phantoms.ellipsoids_3d(w["size"], seed=seed)
-    if w["size"] == 2048:
-        return phantoms.blobs_2d(2048, seed=seed)
-    return phantoms.shapes_2d(w["size"], seed=seed)
+        clean, noisy = phantoms.ellipsoids_3d(w["size"], seed=seed)
+    elif w["size"] == 2048:
+        clean, noisy = phantoms.blobs_2d(2048, seed=seed)
+    else:
+        clean, noisy = phantoms.shapes_2d(w["size"], seed=seed)
+    if is_gaussian(name):
+        rng = np.random.default_rng(7000 + seed)
+        noisy = (clean + w["sigma"] * rng.standard_normal(clean.shape)).astype(np.float32)
+    return clean, noisy
 
 
 def make_profile(name: str):
     import bmnd_gb300 as bg
 
     cls = bg.BM4DProfile if WORKLOADS[name]["kind"] == "bm4d" else bg.BM3DProfile
+    if is_gaussian(name):
+        return cls()
     return cls(noise_model=bg.NoiseModel.POISSON)
 
 
@@ -147,7 +163,24 @@ def profile_traffic(kernel: str, workload: str):
 # ---------------------------------------------------------------------------
 # CPU baseline (the C oracle on a bounded sample)
 # ---------------------------------------------------------------------------
+def data_desc(workload: str) -> str:
+    if is_gaussian(workload):
+        return f"synthetic (seeded phantom, additive Gaussian noise sigma={WORKLOADS[workload]['sigma']})"
+    return "synthetic (seeded phantom, Poisson counts)"
+
+
+def profile_desc(workload: str) -> str:
+    name = "BM4DProfile" if WORKLOADS[workload]["kind"] == "bm4d" else "BM3DProfile"
+    if is_gaussian(workload):
+        return f"{name}() defaults (Gaussian), sigma={WORKLOADS[workload]['sigma']}"
+    return f"{name}(noise_model=poisson) defaults"
+
+
 def cpu_baseline(workload: str, seed: int, budget_s: float = 20.0) -> dict:
+    if is_gaussian(workload):
+        return {"value": None, "unit": "Mvoxel/s", "cores": 0, "kind": "none",
+                "sample": "the CPU oracle restates the Poisson path only; the Gaussian path is pinned on the "
+                          "reference's own outputs (tests/golden/gauss_*.npz)"}
     import oracle
 
     _, noisy = make_input(workload, seed) if WORKLOADS[workload]["size"] <= 256 else make_input("bm3d256", seed)
@@ -183,7 +216,7 @@ def cpu_baseline(workload: str, seed: int, budget_s: float = 20.0) -> dict:
 # GPU arm
 # ---------------------------------------------------------------------------
 def time_kernels(torch, noisy_t, profile, reps: int = 2, stages=("ht", "wiener"), pilot=None,
-                 precision=None) -> dict:
+                 precision=None, gauss=None) -> dict:
     """CUDA-event times of the block-matching kernels and of each stage.
 
     ``pilot`` (optional) is the Wiener stage's pilot; by default it is the
@@ -204,13 +237,20 @@ def time_kernels(torch, noisy_t, profile, reps: int = 2, stages=("ht", "wiener")
     for stage in stages:
         stage_prec = precision[stage]
         p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k,
-                              stage_prec if stage_prec == _abi.MATCH_APPROX else _abi.MATCH_EXACT)
+                              stage_prec if stage_prec == _abi.MATCH_APPROX else _abi.MATCH_EXACT,
+                              None if gauss is None else gauss[stage])
         block = tuple(getattr(profile, f"{stage}_block_size"))
         counts = tuple(s - b + 1 for s, b in zip(shape, block))
         sched = plan.reference_schedule(profile, counts, stage)
         n = len(sched)
         refs = torch.from_numpy(np.array(sched.reference_abs, dtype=np.int32)).cuda()
-        thr = torch.full((n,), float(p.match_threshold), device="cuda")
+        src = noisy_t if stage == "ht" else pilot
+        thr_v = float(p.match_threshold)
+        if gauss is not None:
+            # SSD threshold: t (max - min)^2 of the matched volume
+            span = float(src.max().item() - src.min().item())
+            thr_v = float(np.float32(p.ssd_threshold * (span if span > 0 else 1.0) ** 2))
+        thr = torch.full((n,), thr_v, device="cuda")
         sel = torch.empty((n, p.max_stack), dtype=torch.int32, device="cuda")
         cnt = torch.empty(n, dtype=torch.int32, device="cuda")
         acc = torch.empty(n, dtype=torch.int32, device="cuda")
@@ -220,19 +260,25 @@ def time_kernels(torch, noisy_t, profile, reps: int = 2, stages=("ht", "wiener")
             mp.counts[a] = counts[a]
             mp.search_radius[a] = p.search_radius[a]
         mp.max_matches, mp.min_matches, mp.prefer_power_of_two = p.max_stack, p.min_stack, 1
-        mp.distance, mp.stabilize_ties, mp.count_scale = p.distance, 1, p.count_scale
+        mp.distance, mp.stabilize_ties, mp.count_scale = p.distance, p.stabilize_ties, p.count_scale
         # the pipeline matches the real-valued pilot with the screened path
         mp.precision = stage_prec
         sh = (ctypes.c_int32 * len(shape))(*shape)
         bl = (ctypes.c_int32 * len(shape))(*block)
-        src = noisy_t if stage == "ht" else pilot
+        ssd_bias = None if gauss is None else gauss[stage].get("ssd")
         times = []
         for _ in range(reps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            _abi.check(L.bmnd_blockmatch_volume(ctypes.byref(mp), src.data_ptr(), sh, bl, refs.data_ptr(), n,
-                                                thr.data_ptr(), sel.data_ptr(), cnt.data_ptr(), acc.data_ptr(),
-                                                int(stream.cuda_stream)))
+            if ssd_bias is not None:
+                _abi.check(L.bmnd_blockmatch_volume_biased(
+                    ctypes.byref(mp), src.data_ptr(), sh, bl, refs.data_ptr(), n, thr.data_ptr(),
+                    ssd_bias.data_ptr(), float(gauss[stage]["gamma"]), sel.data_ptr(), cnt.data_ptr(),
+                    acc.data_ptr(), int(stream.cuda_stream)))
+            else:
+                _abi.check(L.bmnd_blockmatch_volume(ctypes.byref(mp), src.data_ptr(), sh, bl, refs.data_ptr(),
+                                                    n, thr.data_ptr(), sel.data_ptr(), cnt.data_ptr(),
+                                                    acc.data_ptr(), int(stream.cuda_stream)))
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
@@ -320,9 +366,19 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
             t = float(tt.item())
         return t, res
 
+    gauss = None
+    sigma = None
+    if is_gaussian(args.workload):
+        from bmnd_gb300 import api, gaussian
+        from bmnd_gb300.validation import resolve_profile
+
+        sigma = WORKLOADS[args.workload]["sigma"]
+        model = gaussian.build_model(noisy.shape, profile.nf, sigma=sigma)
+        gauss = api.gaussian_tables(model, profile, noisy.shape, resolve_profile(profile, noisy.shape), x.device)
+
     sampler = ClockSampler(torch.cuda.current_device())
     sampler.start()
-    ms, out = timed_loop(lambda: bg.bmnd_device(x, profile, match_precision=args.precision))
+    ms, out = timed_loop(lambda: bg.bmnd_device(x, profile, match_precision=args.precision, gauss=gauss))
 
     # learned-pilot fast path (network trained by bmnd_gb300.train_pilot)
     from bmnd_gb300 import pilot as pl
@@ -330,7 +386,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     kind = WORKLOADS[args.workload]["kind"]
     wpath = pl.default_net_path(kind)
     fast = None
-    if os.path.exists(wpath):
+    if os.path.exists(wpath) and gauss is None:
         net = pl.PilotNet.load(wpath)
         fdet = {}
         ms_fast, out_fast = timed_loop(lambda: pl.bmnd_fast(x, profile, net, details=fdet))
@@ -346,7 +402,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        host_out = bg.bmnd(noisy, profile, match_precision=args.precision)
+        host_out = bg.bmnd(noisy, profile, match_precision=args.precision, sigma=sigma)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_fast_s = None
     if fast is not None:
@@ -367,7 +423,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
 
     from bmnd_gb300.phantoms import psnr
 
-    kt = time_kernels(torch, x, profile)
+    kt = time_kernels(torch, x, profile, gauss=gauss)
     peaks = load_peaks()
     sm_mhz = clocks.get("sm_mhz") or 2070.0
     fp32_peak = 152 * 128 * sm_mhz * 1e6  # FP32 instructions per second
@@ -414,7 +470,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
             stack = int(profile.wiener_max_stack_size if wiener else profile.ht_max_stack_size)
             alg_bytes = nvox * 4 + k["groups"] * (stack + 2) * 4
             compute = {
-                "what": "Poisson-deviance voxel terms",
+                "what": "SSD voxel terms" if gauss is not None else "Poisson-deviance voxel terms",
                 "achieved_gterms_s": k["voxel_terms"] / (dom_ms * 1e-3) / 1e9,
             }
             if dom_name == "blockmatch_wiener_approx":
@@ -426,12 +482,22 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
             # read noisy (+ pilot) once, write float64 numerator and denominator once
             alg_bytes = nvox * (8 if wiener else 4) + nvox * 16
             kk = min(int(fprof.k) if dom_stage == "fast_wiener" else 4, int(k["mean_group"]))
-            pairs = k["groups"] * k["mean_group"] * k["P"] * kk * k["P"]
-            compute = {
-                "what": "exact overlap-aware variance: entry x coefficient pairs (one FP32 fused multiply-add each)",
-                "achieved_gpairs_s": pairs / (dom_ms * 1e-3) / 1e9,
-                "fp32_ops_frac_of_peak": 2 * pairs / (dom_ms * 1e-3) / fp32_peak,
-            }
+            if gauss is not None:
+                n_ = k["mean_group"]
+                terms = k["groups"] * (n_ * (n_ + 1) / 2) * k["P"] * kk
+                compute = {
+                    "what": "Gaussian exact planes: member pairs x coefficients x planes (one covariance-map "
+                            "load and two FP32 multiply-adds each)",
+                    "achieved_gterms_s": terms / (dom_ms * 1e-3) / 1e9,
+                }
+            else:
+                pairs = k["groups"] * k["mean_group"] * k["P"] * kk * k["P"]
+                compute = {
+                    "what": "exact overlap-aware variance: entry x coefficient pairs (one FP32 fused multiply-add "
+                            "each)",
+                    "achieved_gpairs_s": pairs / (dom_ms * 1e-3) / 1e9,
+                    "fp32_ops_frac_of_peak": 2 * pairs / (dom_ms * 1e-3) / fp32_peak,
+                }
         achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
         bound, unit, peak_v = "hbm", "GB/s", peaks["hbm_gbs"]
     traffic = profile_traffic(dom_name, args.workload)
@@ -461,6 +527,9 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         }
         value = fast_block["value"]
         launches_per_step = 16  # net: 9, residual check: 1, Wiener stage: 6
+    elif gauss is not None:
+        fast_block = {"unavailable": "the learned pilot is trained for Poisson counts only"}
+        value = plain_value
     else:
         fast_block = {"unavailable": f"no trained pilot weights at {os.path.relpath(wpath, ROOT)}"}
         value = plain_value
@@ -476,12 +545,11 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded phantom, Poisson counts)",
+        "data": data_desc(args.workload),
         "config": {
             "workload": WORKLOADS[args.workload]["desc"],
             "shape": list(noisy.shape),
-            "profile": "BM4DProfile(noise_model=poisson) defaults" if WORKLOADS[args.workload]["kind"] == "bm4d"
-            else "BM3DProfile(noise_model=poisson) defaults",
+            "profile": profile_desc(args.workload),
             "match_precision": args.precision,
             "parallelism": f"replicas{world}",
             "l2": "flushed between timed steps (256 MiB write)",
@@ -528,6 +596,8 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
 def run_reference(args, rank: int, world: int) -> dict | None:
     if rank != 0:
         return None
+    if is_gaussian(args.workload):
+        return {"impl": "reference", "unavailable": "the CPU oracle restates the Poisson path only"}
     per = []
     for _ in range(args.warmup):
         cpu_baseline(args.workload, seed=0, budget_s=5.0)

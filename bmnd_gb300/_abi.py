@@ -142,6 +142,12 @@ SIGNATURES = {
         [ctypes.POINTER(MatchParams), ctypes.c_void_p, _I32P, _I32P, ctypes.c_void_p, _I64,
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _U64],
     ),
+    "bmnd_blockmatch_volume_biased": (
+        _I32,
+        [ctypes.POINTER(MatchParams), ctypes.c_void_p, _I32P, _I32P, ctypes.c_void_p, _I64,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+         _U64],
+    ),
     "bmnd_stage_workspace_bytes": (_I32, [ctypes.POINTER(StageParams), _I64, _U64P]),
     "bmnd_stage": (
         _I32,

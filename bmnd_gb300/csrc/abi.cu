@@ -331,6 +331,20 @@ int32_t bmnd_blockmatch_patches(const BmndMatchParams* params, const float* d_pa
                                      d_sel, d_count, d_accepted, reinterpret_cast<cudaStream_t>(stream));
 }
 
+int32_t bmnd_blockmatch_volume_biased(const BmndMatchParams* params, const float* d_volume,
+                                      const int32_t* shape, const int32_t* block, const int32_t* d_refs,
+                                      int64_t n_refs, const float* d_thresholds, const float* d_noise_ssd,
+                                      float gamma, int32_t* d_sel, int32_t* d_count, int32_t* d_accepted,
+                                      uint64_t stream) {
+    clear_error();
+    if (!params || !d_volume || !shape || !block || !d_thresholds || !d_noise_ssd || !d_sel || !d_count ||
+        !d_accepted || (n_refs > 0 && !d_refs))
+        return fail(BMND_ERR_INVALID_ARG, "null argument");
+    return launch_blockmatch_volume(*params, d_volume, shape, block, d_refs, n_refs, d_thresholds, 0.0f, d_sel,
+                                    d_count, d_accepted, reinterpret_cast<cudaStream_t>(stream), nullptr,
+                                    d_noise_ssd, gamma);
+}
+
 int32_t bmnd_blockmatch_volume(const BmndMatchParams* params, const float* d_volume,
                                const int32_t* shape, const int32_t* block, const int32_t* d_refs,
                                int64_t n_refs, const float* d_thresholds, int32_t* d_sel,

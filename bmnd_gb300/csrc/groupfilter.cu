@@ -667,28 +667,31 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
             __syncthreads();
         }
         const float* cm = sp.cov_maps;
-        for (int c = tid; c < P; c += blockDim.x) {
+        // one thread per (plane, coefficient): the planes' sums are independent
+        for (int t = tid; t < kk * P; t += blockDim.x) {
+            const int g = t / P, c = t - g * P;
             const float pv = __ldg(cm + c);  // lag 0: the patch variance of coefficient c
-            float ex_sum = 0.0f;
-            for (int g = 0; g < kk; ++g) {
-                const float* Gr = G + g * n;
-                float value = 0.0f;
-                for (int i = 0; i < n; ++i) {
-                    const float wi = Gr[i];
-                    if (wi == 0.0f) continue;
-                    value = add_rn(value, mul_rn(mul_rn(wi, pv), wi));
-                    const int* lrow = lag + i * (i + 1) / 2;
-                    for (int j = 0; j < i; ++j) {
-                        const float wj = Gr[j];
-                        if (wj == 0.0f) continue;
-                        const float cv = __ldg(cm + static_cast<int64_t>(lrow[j]) * P + c);
-                        value = add_rn(value, mul_rn(mul_rn(wi, wj), add_rn(cv, cv)));
-                    }
+            const float* Gr = G + g * n;
+            float value = 0.0f;
+            for (int i = 0; i < n; ++i) {
+                const float wi = Gr[i];
+                if (wi == 0.0f) continue;
+                value = add_rn(value, mul_rn(mul_rn(wi, pv), wi));
+                const int* lrow = lag + i * (i + 1) / 2;
+                for (int j = 0; j < i; ++j) {
+                    const float wj = Gr[j];
+                    if (wj == 0.0f) continue;
+                    const float cv = __ldg(cm + static_cast<int64_t>(lrow[j]) * P + c);
+                    value = add_rn(value, mul_rn(mul_rn(wi, wj), add_rn(cv, cv)));
                 }
-                value = fmaxf(value, 0.0f);
-                EX[g * P + c] = value;
-                ex_sum = add_rn(ex_sum, value);
             }
+            EX[g * P + c] = fmaxf(value, 0.0f);
+        }
+        __syncthreads();
+        for (int c = tid; c < P; c += blockDim.x) {
+            const float pv = __ldg(cm + c);
+            float ex_sum = 0.0f;
+            for (int g = 0; g < kk; ++g) ex_sum = add_rn(ex_sum, EX[g * P + c]);
             float rest = pv;
             if (kk > 0 && kk < n) {
                 rest = div_rn(sub_rn(mul_rn(static_cast<float>(n), pv), ex_sum), static_cast<float>(n - kk));

@@ -193,6 +193,20 @@ int32_t bmnd_blockmatch_volume(const BmndMatchParams* params, const float* d_vol
                                int32_t* d_accepted, uint64_t stream);
 
 /*
+ * bmnd_blockmatch_volume with the SSD noise-bias correction of
+ * blockmatch_groups(gaussian_noise_ssd=..., gamma=...) (blockmatching.py:1133-1139):
+ * every SSD distance minus gamma * d_noise_ssd[offset], the offset of the
+ * candidate from the reference in C order over 2 * search_radius + 1 per axis.
+ * params->distance must be BMND_DIST_SSD.
+ */
+int32_t bmnd_blockmatch_volume_biased(const BmndMatchParams* params, const float* d_volume,
+                                      const int32_t* shape, const int32_t* block,
+                                      const int32_t* d_refs, int64_t n_refs,
+                                      const float* d_thresholds, const float* d_noise_ssd, float gamma,
+                                      int32_t* d_sel, int32_t* d_count, int32_t* d_accepted,
+                                      uint64_t stream);
+
+/*
  * Workspace bytes bmnd_stage() needs for `params` and n_refs references.
  */
 int32_t bmnd_stage_workspace_bytes(const BmndStageParams* params, int64_t n_refs,
