@@ -597,8 +597,18 @@ struct ScreenSmem {
     }
 };
 
+// resident CTAs per SM the screened kernel is compiled for, and the x-run of
+// candidates one thread scores in approximate mode (compile-time tunables)
+#ifndef BMND_SCREEN_MIN_BLOCKS
+#define BMND_SCREEN_MIN_BLOCKS 6
+#endif
+#ifndef BMND_APPROX_XR
+#define BMND_APPROX_XR 2
+#endif
+
 template <int ND, int B0, int B1, int B2>
-__global__ void __launch_bounds__(kSThreads, 8) blockmatch_screened_kernel(MatchArgs a, int32_t wmax) {
+__global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_screened_kernel(MatchArgs a,
+                                                                                              int32_t wmax) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
@@ -686,7 +696,7 @@ __global__ void __launch_bounds__(kSThreads, 8) blockmatch_screened_kernel(Match
         float dmax = 0.0f;
         if (cheap) {
             if constexpr (ND > 0) {
-                constexpr int XR = 3;
+                constexpr int XR = BMND_APPROX_XR;
                 constexpr int BX = ND == 3 ? B2 : B1;
                 const float sum_a = redf[4] + redf[5] + redf[6] + redf[7];
                 const int ex = ext[ND - 1];
