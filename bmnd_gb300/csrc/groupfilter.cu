@@ -959,31 +959,35 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         __syncthreads();
     }
 
-    // ---- aggregation weights (float64, aggregationweights.py:213-259) ----
+    // ---- aggregation weights (aggregationweights.py:213-259) ----
+    // The reference sums the plane risks in float64.  Here the per-coefficient
+    // products and sums are float32 (relative error ~P 2^-24 in a weight, far
+    // inside the output tolerance): float64 arithmetic runs at a small
+    // fraction of the FP32 rate on this GPU and dominated the filter's time.
     {
         const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
         for (int g = warp; g < n; g += nwarps) {
-            double risk = 0.0;
+            float risk = 0.0f;
             for (int j = lane; j < P; j += 32) {
-                double at = static_cast<double>(V[g * P + j]);
-                double err = at * at;
-                if (sp.weight_model != BMND_WEIGHT_CLASSIC) err *= static_cast<double>(S[g * P + j]);
-                if (sp.windowed_synthesis) err *= mdiag[j];
+                const float at = V[g * P + j];
+                float err = at * at;
+                if (sp.weight_model != BMND_WEIGHT_CLASSIC) err *= S[g * P + j];
+                if (sp.windowed_synthesis) err *= static_cast<float>(mdiag[j]);
                 risk += err;
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) risk += __shfl_xor_sync(0xffffffffu, risk, o);
-            if (lane == 0) plane[g] = risk;
+            if (lane == 0) plane[g] = static_cast<double>(risk);
         }
     }
     __syncthreads();
     if (tid < n) {
-        double risk = 0.0;
+        float risk = 0.0f;
         for (int g = 0; g < n; ++g) {
-            double gi = static_cast<double>(G[g * n + tid]);  // Ginv[o, g] = G[g, o]
-            risk += (gi * gi) * plane[g];
+            const float gi = G[g * n + tid];  // Ginv[o, g] = G[g, o]
+            risk = fmaf(gi * gi, static_cast<float>(plane[g]), risk);
         }
-        wts[tid] = (isfinite(risk) && risk >= 0.0) ? static_cast<float>(1.0 / (risk + sp.eps)) : 0.0f;
+        wts[tid] = (isfinite(risk) && risk >= 0.0f) ? 1.0f / (risk + static_cast<float>(sp.eps)) : 0.0f;
     }
     __syncthreads();
 
