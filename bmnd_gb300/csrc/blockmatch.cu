@@ -600,7 +600,7 @@ struct ScreenSmem {
 // resident CTAs per SM the screened kernel is compiled for, and the x-run of
 // candidates one thread scores in approximate mode (compile-time tunables)
 #ifndef BMND_SCREEN_MIN_BLOCKS
-#define BMND_SCREEN_MIN_BLOCKS 6
+#define BMND_SCREEN_MIN_BLOCKS 8
 #endif
 #ifndef BMND_APPROX_XR
 #define BMND_APPROX_XR 2
@@ -1389,12 +1389,17 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
             aux = nullptr;
         }
     }
-    int64_t blocks = a.n_refs;
-    const int64_t cap = 152 * 12;
-    if (blocks > cap) blocks = cap;
     auto run = [&](auto kernel) -> int32_t {
         BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(smem)));
+        // persistent CTAs, exactly one resident wave (a partial second wave
+        // leaves most SMs idle at the end)
+        int dev = 0, sms = 0, per_sm = 0;
+        BMND_CUDA_TRY(cudaGetDevice(&dev));
+        BMND_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        BMND_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kSThreads, smem));
+        int64_t blocks = static_cast<int64_t>(sms) * (per_sm > 0 ? per_sm : 1);
+        if (blocks > a.n_refs) blocks = a.n_refs;
         kernel<<<static_cast<unsigned>(blocks), kSThreads, smem, stream>>>(a, static_cast<int32_t>(wmax));
         BMND_LAUNCH_CHECK("blockmatch_screened_kernel");
         return BMND_OK;

@@ -345,6 +345,21 @@ __device__ void transform_group(const GM& geo, const FilterArgs& a, unsigned cha
     }
 }
 
+// exact float -> double widening on the integer pipe (IEEE 754 binary32 to
+// binary64: rebias the exponent by 1023 - 127, shift the fraction by 29);
+// zeros keep their sign, subnormals, infinities and NaNs take the hardware
+// conversion.  The scatter widens two or three values per entry, and the
+// float64 pipe is a small fraction of the FP32 rate on this GPU.
+__device__ __forceinline__ double widen_f64(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xffu;
+    const uint64_t sign = static_cast<uint64_t>(u & 0x80000000u) << 32;
+    if ((u & 0x7fffffffu) == 0u) return __longlong_as_double(static_cast<long long>(sign));
+    if (e == 0u || e == 0xffu) return static_cast<double>(f);
+    const uint64_t bits = sign | (static_cast<uint64_t>(e + 896u) << 52) | (static_cast<uint64_t>(u & 0x7fffffu) << 29);
+    return __longlong_as_double(static_cast<long long>(bits));
+}
+
 __device__ __forceinline__ float variance_of(float x, float scale_f, float floor_f) {
     float nn = x > 0.0f ? x : 0.0f;
     float v = mul_rn(scale_f, nn);
@@ -998,13 +1013,13 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         const int p = e - g * P;
         const int64_t off = geo.offset(pos + g * BMND_MAX_DIMS, p, a.vstride);
         float ww = mul_rn(wts[g], win[p]);
-        atomicAdd(a.num + off, static_cast<double>(mul_rn(X[e], ww)));
-        atomicAdd(a.den + off, static_cast<double>(ww));
+        atomicAdd(a.num + off, widen_f64(mul_rn(X[e], ww)));
+        atomicAdd(a.den + off, widen_f64(ww));
         if (a.sig_num) {
             // sigma map numerator (patchaggregation.py:229-294): per coefficient
             // (hard thresholding) or the group's mean (Wiener)
             const float sv = wiener ? sm<float>(smem, a.L.misc)[12] : SG[e];
-            atomicAdd(a.sig_num + off, static_cast<double>(mul_rn(sv, ww)));
+            atomicAdd(a.sig_num + off, widen_f64(mul_rn(sv, ww)));
         }
     }
 }
