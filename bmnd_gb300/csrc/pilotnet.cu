@@ -94,84 +94,173 @@ __global__ void anscombe_kernel(const float* __restrict__ x, float* __restrict__
         a[i] = anscombe(x[i]);
 }
 
-// h[v][c] = relu(b[c] + sum_t w[t][c] a[v + off(t)]), C channels, 16-byte stores
+// h[v][c] = relu(b[c] + sum_t w[t][c] a[v + off(t)]), C channels, 16-byte stores.
+// A thread computes two voxels (x and x + 1) so each pair of 16-byte weight
+// loads from shared memory feeds 16 multiply-adds.
 template <int ND, int C>
 __global__ void conv_in_kernel(const float* __restrict__ a, const float* __restrict__ w,
                                const float* __restrict__ bias, bf16* __restrict__ h, NetGeo g) {
     constexpr int T = Tile<ND>::taps;
-    __shared__ float ws[T * C], bs[C];
+    __shared__ __align__(16) float ws[T * C];
+    __shared__ __align__(16) float bs[C];
     for (int i = threadIdx.x; i < T * C; i += blockDim.x) ws[i] = w[i];
     for (int i = threadIdx.x; i < C; i += blockDim.x) bs[i] = bias[i];
     __syncthreads();
-    const int64_t n = g.voxels();
-    for (int64_t v = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; v < n;
-         v += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        int b, z, y, x;
-        vox_decode(g, v, b, z, y, x);
-        float in[T];
+    const int wp = (g.W + 1) / 2;  // voxel pairs per row
+    const int64_t npair = static_cast<int64_t>(g.nb) * g.D * g.H * wp;
+    for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; q < npair;
+         q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t r = q;
+        const int x = static_cast<int>(r % wp) * 2;
+        r /= wp;
+        const int y = static_cast<int>(r % g.H);
+        r /= g.H;
+        const int z = static_cast<int>(r % g.D);
+        const int b = static_cast<int>(r / g.D);
+        const bool two = x + 1 < g.W;
+        float in0[T], in1[T];
 #pragma unroll
         for (int t = 0; t < T; ++t) {
             int dz, dy, dx;
             tap_offsets<ND>(t, dz, dy, dx);
-            const int zz = z + dz, yy = y + dy, xx = x + dx;
-            const bool inside = zz >= 0 && zz < g.D && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W;
-            in[t] = inside ? a[vox_index(g, b, zz, yy, xx)] : 0.0f;
+            const int zz = z + dz, yy = y + dy, xa = x + dx, xb = x + 1 + dx;
+            const bool row = zz >= 0 && zz < g.D && yy >= 0 && yy < g.H;
+            in0[t] = (row && xa >= 0 && xa < g.W) ? a[vox_index(g, b, zz, yy, xa)] : 0.0f;
+            in1[t] = (row && xb >= 0 && xb < g.W) ? a[vox_index(g, b, zz, yy, xb)] : 0.0f;
         }
+        const int64_t v0 = vox_index(g, b, z, y, x);
 #pragma unroll
         for (int c0 = 0; c0 < C; c0 += 8) {
-            float acc[8];
+            float acc0[8], acc1[8];
+            {
+                const float4 b0 = *reinterpret_cast<const float4*>(bs + c0);
+                const float4 b1 = *reinterpret_cast<const float4*>(bs + c0 + 4);
+                const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
-            for (int j = 0; j < 8; ++j) acc[j] = bs[c0 + j];
+                for (int j = 0; j < 8; ++j) acc0[j] = acc1[j] = bb[j];
+            }
 #pragma unroll
-            for (int t = 0; t < T; ++t)
+            for (int t = 0; t < T; ++t) {
+                const float4 w0 = *reinterpret_cast<const float4*>(ws + t * C + c0);
+                const float4 w1 = *reinterpret_cast<const float4*>(ws + t * C + c0 + 4);
+                const float ww[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
-                for (int j = 0; j < 8; ++j) acc[j] = fmaf(ws[t * C + c0 + j], in[t], acc[j]);
+                for (int j = 0; j < 8; ++j) {
+                    acc0[j] = fmaf(ww[j], in0[t], acc0[j]);
+                    acc1[j] = fmaf(ww[j], in1[t], acc1[j]);
+                }
+            }
             __align__(16) bf16 o[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) o[j] = __float2bfloat16_rn(fmaxf(acc[j], 0.0f));
-            *reinterpret_cast<uint4*>(h + v * C + c0) = *reinterpret_cast<const uint4*>(o);
+            for (int j = 0; j < 8; ++j) o[j] = __float2bfloat16_rn(fmaxf(acc0[j], 0.0f));
+            *reinterpret_cast<uint4*>(h + v0 * C + c0) = *reinterpret_cast<const uint4*>(o);
+            if (two) {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) o[j] = __float2bfloat16_rn(fmaxf(acc1[j], 0.0f));
+                *reinterpret_cast<uint4*>(h + (v0 + 1) * C + c0) = *reinterpret_cast<const uint4*>(o);
+            }
         }
     }
 }
 
-// y[v] = a[v] + b + sum_t sum_c w[t][c] h[v + off(t)][c]; pilot = inverse Anscombe
+// y[v] = a[v] + b + sum_t sum_c w[t][c] h[v + off(t)][c]; pilot = inverse
+// Anscombe.  A CTA of 16 x 8 threads walks OutZ planes of a 16 x 8 tile; the
+// three input planes it needs (tile plus one-voxel halo, channels padded to
+// C + 8 so the 16-byte reads are free of bank conflicts) rotate through
+// shared memory, so every input voxel is read from global memory about once.
+template <int ND>
+struct OutTile {
+    static constexpr int tx = 16, ty = 8, hx = tx + 2, hy = ty + 2;
+    static constexpr int planes = ND == 3 ? 3 : 1;
+    static constexpr int zb = ND == 3 ? 8 : 1;  // output planes per CTA
+};
+
 template <int ND, int C>
-__global__ void conv_out_kernel(const bf16* __restrict__ h, const float* __restrict__ w, const float* __restrict__ bias,
-                                const float* __restrict__ a, float* __restrict__ y, float* __restrict__ pilot,
-                                NetGeo g) {
+__global__ void __launch_bounds__(128) conv_out_kernel(const bf16* __restrict__ h, const float* __restrict__ w,
+                                                       const float* __restrict__ bias, const float* __restrict__ a,
+                                                       float* __restrict__ y, float* __restrict__ pilot, NetGeo g) {
+    using OT = OutTile<ND>;
     constexpr int T = Tile<ND>::taps;
-    __shared__ float ws[T * C];
+    constexpr int CP = C + 8;
+    constexpr int HV = OT::hx * OT::hy;
+    constexpr int CH = C / 8;
+    extern __shared__ __align__(16) unsigned char out_smem[];
+    float* ws = reinterpret_cast<float*>(out_smem);
+    bf16* ring = reinterpret_cast<bf16*>(out_smem + static_cast<size_t>(T) * C * 4);
     for (int i = threadIdx.x; i < T * C; i += blockDim.x) ws[i] = w[i];
-    __syncthreads();
     const float b0 = bias[0];
-    const int64_t n = g.voxels();
-    for (int64_t v = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; v < n;
-         v += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        int b, z, yy0, x;
-        vox_decode(g, v, b, z, yy0, x);
-        float acc = b0;
+    const int tiles_x = (g.W + OT::tx - 1) / OT::tx;
+    const int tiles_y = (g.H + OT::ty - 1) / OT::ty;
+    const int zblocks = (g.D + OT::zb - 1) / OT::zb;
+    int64_t r = blockIdx.x;
+    const int x0 = static_cast<int>(r % tiles_x) * OT::tx;
+    r /= tiles_x;
+    const int y0 = static_cast<int>(r % tiles_y) * OT::ty;
+    r /= tiles_y;
+    const int zs = static_cast<int>(r % zblocks) * OT::zb;
+    const int b = static_cast<int>(r / zblocks);
+    const int ze = min(zs + OT::zb, g.D);
+    auto load_plane = [&](int zz, int slot) {
+        bf16* dst = ring + static_cast<size_t>(slot) * HV * CP;
+        for (int i = threadIdx.x; i < HV * CH; i += blockDim.x) {
+            const int hv = i / CH, ch = i - hv * CH;
+            const int xx = x0 - 1 + hv % OT::hx, yy = y0 - 1 + hv / OT::hx;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (zz >= 0 && zz < g.D && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W)
+                v = *reinterpret_cast<const uint4*>(h + vox_index(g, b, zz, yy, xx) * C + ch * 8);
+            *reinterpret_cast<uint4*>(dst + static_cast<size_t>(hv) * CP + ch * 8) = v;
+        }
+    };
+    const int tx = threadIdx.x % OT::tx, ty = threadIdx.x / OT::tx;
+    if (ND == 3) {
+        load_plane(zs - 1, (zs + 2) % 3);
+        load_plane(zs, zs % 3);
+    }
+    for (int z = zs; z < ze; ++z) {
+        if (ND == 3) load_plane(z + 1, (z + 1) % 3);
+        else load_plane(z, 0);
+        __syncthreads();
+        const int xx = x0 + tx, yy = y0 + ty;
+        if (xx < g.W && yy < g.H) {
+            float acc = b0;
 #pragma unroll 1
-        for (int t = 0; t < T; ++t) {
-            int dz, dy, dx;
-            tap_offsets<ND>(t, dz, dy, dx);
-            const int zz = z + dz, yy = yy0 + dy, xx = x + dx;
-            if (!(zz >= 0 && zz < g.D && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W)) continue;
-            const bf16* hv = h + vox_index(g, b, zz, yy, xx) * C;
+            for (int t = 0; t < T; ++t) {
+                int dz, dy, dx;
+                tap_offsets<ND>(t, dz, dy, dx);
+                const int slot = ND == 3 ? (z + dz + 3) % 3 : 0;
+                const bf16* hv = ring + (static_cast<size_t>(slot) * HV + (ty + 1 + dy) * OT::hx + (tx + 1 + dx)) * CP;
 #pragma unroll
-            for (int c0 = 0; c0 < C; c0 += 8) {
-                const uint4 raw = *reinterpret_cast<const uint4*>(hv + c0);
-                const bf16* e = reinterpret_cast<const bf16*>(&raw);
-#pragma unroll
-                for (int j = 0; j < 8; ++j) acc = fmaf(ws[t * C + c0 + j], __bfloat162float(e[j]), acc);
+                for (int c0 = 0; c0 < C; c0 += 8) {
+                    const uint4 raw = *reinterpret_cast<const uint4*>(hv + c0);
+                    const bf16* e = reinterpret_cast<const bf16*>(&raw);
+                    const float4 w0 = *reinterpret_cast<const float4*>(ws + t * C + c0);
+                    const float4 w1 = *reinterpret_cast<const float4*>(ws + t * C + c0 + 4);
+                    acc = fmaf(w0.x, __bfloat162float(e[0]), acc);
+                    acc = fmaf(w0.y, __bfloat162float(e[1]), acc);
+                    acc = fmaf(w0.z, __bfloat162float(e[2]), acc);
+                    acc = fmaf(w0.w, __bfloat162float(e[3]), acc);
+                    acc = fmaf(w1.x, __bfloat162float(e[4]), acc);
+                    acc = fmaf(w1.y, __bfloat162float(e[5]), acc);
+                    acc = fmaf(w1.z, __bfloat162float(e[6]), acc);
+                    acc = fmaf(w1.w, __bfloat162float(e[7]), acc);
+                }
+            }
+            const int64_t v = vox_index(g, b, z, yy, xx);
+            const float yv = a[v] + acc;
+            if (y) y[v] = yv;
+            if (pilot) {
+                const float hh = 0.5f * yv;
+                pilot[v] = fmaxf(hh * hh - 0.375f, 0.0f);
             }
         }
-        const float yv = a[v] + acc;
-        if (y) y[v] = yv;
-        if (pilot) {
-            const float hv = 0.5f * yv;
-            pilot[v] = fmaxf(hv * hv - 0.375f, 0.0f);
-        }
+        __syncthreads();
     }
+}
+
+template <int ND, int C>
+constexpr size_t out_smem_bytes() {
+    return static_cast<size_t>(Tile<ND>::taps) * C * 4 +
+           static_cast<size_t>(OutTile<ND>::planes) * OutTile<ND>::hx * OutTile<ND>::hy * (C + 8) * 2;
 }
 
 // loss = mean (y - anscombe(target))^2 and its gradient with respect to y
@@ -1238,14 +1327,23 @@ int32_t forward_impl(const NetPlan& P, const unsigned char* packed, const float*
         const int64_t stride = nv * C;
         return B.act + (keep_all ? l : (l & 1)) * stride;
     };
-    conv_in_kernel<ND, C><<<eb, 256, 0, stream>>>(B.a, wr + P.w_off[0], wr + P.b_off[0], act(0), g);
+    conv_in_kernel<ND, C><<<launch_blocks((nv + 1) / 2, 256), 256, 0, stream>>>(B.a, wr + P.w_off[0],
+                                                                              wr + P.b_off[0], act(0), g);
     BMND_LAUNCH_CHECK("conv_in_kernel");
     for (int l = 1; l < P.L - 1; ++l) {
         int32_t rc = run_layer<ND, C>(P, packed, l, false, act(l - 1), wr + P.b_off[l], nullptr, act(l), B, stream);
         if (rc) return rc;
     }
-    conv_out_kernel<ND, C><<<eb, 256, 0, stream>>>(act(P.L - 2), wr + P.w_off[P.L - 1], wr + P.b_off[P.L - 1], B.a,
-                                                   y_out, pilot, g);
+    {
+        using OT = OutTile<ND>;
+        constexpr size_t smem = out_smem_bytes<ND, C>();
+        BMND_CUDA_TRY(cudaFuncSetAttribute(conv_out_kernel<ND, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(smem)));
+        const int64_t blocks = static_cast<int64_t>((g.W + OT::tx - 1) / OT::tx) * ((g.H + OT::ty - 1) / OT::ty) *
+                               ((g.D + OT::zb - 1) / OT::zb) * g.nb;
+        conv_out_kernel<ND, C><<<static_cast<unsigned>(blocks), OT::tx * OT::ty, smem, stream>>>(
+            act(P.L - 2), wr + P.w_off[P.L - 1], wr + P.b_off[P.L - 1], B.a, y_out, pilot, g);
+    }
     BMND_LAUNCH_CHECK("conv_out_kernel");
     return BMND_OK;
 }
