@@ -753,13 +753,14 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
         for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) Dabs = fmaxf(Dabs, redf[w]);
         if (a.approx) Dabs = 0.0f;
 
-        // radix select over the upper bounds d + D of the certainly accepted:
-        // vstar with >= K of them bounded by it
-        float vstar = INFINITY;
-        {
+        // radix select over the upper bounds d + D of the certainly accepted
+        // (of every candidate with `all`): the smallest v with >= need of them
+        // bounded by it, or infinity when there are fewer
+        auto select_kth = [&](int need, bool all) -> float {
             uint32_t prefix = 0;
-            int need = K;
             bool found = true;
+            for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0u;
+            __syncthreads();
             for (int pass = 0; pass < 3 && found; ++pass) {
                 const int shift = 24 - 8 * pass;
                 if (pass > 0) {
@@ -775,7 +776,7 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                     if (c < window) {
                         const float dv = cand[c];
                         const float up = dv + (Dabs + drel * dv);
-                        if (canonical_key(up) < tkey) {
+                        if (all || canonical_key(up) < tkey) {
                             const uint32_t bits = __float_as_uint(up);
                             if (pass == 0 || (bits >> (32 - 8 * pass)) == prefix) {
                                 take = true;
@@ -847,8 +848,9 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                 }
                 __syncthreads();
             }
-            if (found) vstar = __uint_as_float((prefix << 8) | 0xffu);
-        }
+            return found ? __uint_as_float((prefix << 8) | 0xffu) : INFINITY;
+        };
+        const float vstar = select_kth(K, false);
         // at least K certainly accepted candidates have exact distances <= vstar
         const float vkey = canonical_key(vstar);
 
@@ -915,7 +917,8 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
         __syncthreads();
         int total_accepted = 0;
         for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) total_accepted += redi[4 + w];
-        const bool complete = !overflow && total_accepted >= R;
+        bool complete = !overflow && total_accepted >= R;
+        int limit = K;  // entries of top[] the group takes
         // top K of the rescored accepted keys: each key's rank among the queue
         // (composite keys are unique), in parallel
         if (complete) {
@@ -927,13 +930,50 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                 if (rank < K) top[rank] = k;
                 atomicAdd(redi + 3, 1);
             }
+        } else if (a.approx && !overflow) {
+            // approximate mode, fewer than `required` accepted: the group is the
+            // R smallest screening distances overall, the accepted (below the
+            // threshold) first, then the best rejected, as the reference fills it
+            __syncthreads();
+            const float v2 = select_kth(R, true);
+            const float v2key = canonical_key(v2);
+            if (tid == 0) {
+                redi[0] = 0;
+                redi[3] = 0;
+            }
+            __syncthreads();
+            for (int64_t c = tid; c < window; c += blockDim.x) {
+                if (canonical_key(cand[c]) <= v2key) {
+                    const int slot = atomicAdd(redi, 1);
+                    if (slot < kSQueue) qidx[slot] = static_cast<int32_t>(c);
+                }
+            }
+            __syncthreads();
+            const int qn2 = redi[0];
+            if (qn2 <= kSQueue) {
+                for (int i = tid; i < qn2; i += blockDim.x) {
+                    int64_t lin;
+                    (void)window_origin(a, lo, ext, inv_ext, small_window, qidx[i], &lin);
+                    qkey[i] = composite_key(canonical_key(cand[qidx[i]]), static_cast<int32_t>(lin));
+                }
+                __syncthreads();
+                for (int i = tid; i < qn2; i += blockDim.x) {
+                    const uint64_t k = qkey[i];
+                    int rank = 0;
+                    for (int j = 0; j < qn2; ++j) rank += qkey[j] < k ? 1 : 0;
+                    if (rank < R) top[rank] = k;
+                    atomicAdd(redi + 3, 1);
+                }
+                complete = true;
+                limit = R;
+            }
         }
         __syncthreads();
         if (tid == 0) {
             if (!complete) {
                 a.count[r] = -1;  // queue overflow, or the best rejected are needed: exact redo
             } else {
-                const int ntop = min(redi[3], K);
+                const int ntop = min(redi[3], limit);
                 int32_t* row = a.sel + r * K;
                 int n = 0;
                 row[n++] = static_cast<int32_t>(center_lin);

@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(128) conv_out_kernel(const bf16* __restrict__ 
         __syncthreads();
         const int xx = x0 + tx, yy = y0 + ty;
         if (xx < g.W && yy < g.H) {
-            float acc = b0;
+            float acc[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // eight independent chains
 #pragma unroll 1
             for (int t = 0; t < T; ++t) {
                 int dz, dy, dx;
@@ -235,18 +235,19 @@ __global__ void __launch_bounds__(128) conv_out_kernel(const bf16* __restrict__ 
                     const bf16* e = reinterpret_cast<const bf16*>(&raw);
                     const float4 w0 = *reinterpret_cast<const float4*>(ws + t * C + c0);
                     const float4 w1 = *reinterpret_cast<const float4*>(ws + t * C + c0 + 4);
-                    acc = fmaf(w0.x, __bfloat162float(e[0]), acc);
-                    acc = fmaf(w0.y, __bfloat162float(e[1]), acc);
-                    acc = fmaf(w0.z, __bfloat162float(e[2]), acc);
-                    acc = fmaf(w0.w, __bfloat162float(e[3]), acc);
-                    acc = fmaf(w1.x, __bfloat162float(e[4]), acc);
-                    acc = fmaf(w1.y, __bfloat162float(e[5]), acc);
-                    acc = fmaf(w1.z, __bfloat162float(e[6]), acc);
-                    acc = fmaf(w1.w, __bfloat162float(e[7]), acc);
+                    acc[0] = fmaf(w0.x, __bfloat162float(e[0]), acc[0]);
+                    acc[1] = fmaf(w0.y, __bfloat162float(e[1]), acc[1]);
+                    acc[2] = fmaf(w0.z, __bfloat162float(e[2]), acc[2]);
+                    acc[3] = fmaf(w0.w, __bfloat162float(e[3]), acc[3]);
+                    acc[4] = fmaf(w1.x, __bfloat162float(e[4]), acc[4]);
+                    acc[5] = fmaf(w1.y, __bfloat162float(e[5]), acc[5]);
+                    acc[6] = fmaf(w1.z, __bfloat162float(e[6]), acc[6]);
+                    acc[7] = fmaf(w1.w, __bfloat162float(e[7]), acc[7]);
                 }
             }
+            const float sum = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
             const int64_t v = vox_index(g, b, z, yy, xx);
-            const float yv = a[v] + acc;
+            const float yv = a[v] + (b0 + sum);
             if (y) y[v] = yv;
             if (pilot) {
                 const float hh = 0.5f * yv;
