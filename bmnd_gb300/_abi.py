@@ -108,6 +108,8 @@ class StageParams(ctypes.Structure):
         ("ssd_gamma", ctypes.c_float),
         ("reserved1", _I32),
         ("ssd_threshold", ctypes.c_double),
+        ("mass_conserve", _I32),
+        ("reserved2", _I32),
     ]
 
 

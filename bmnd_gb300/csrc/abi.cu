@@ -215,6 +215,14 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
     if (rc) return rc;
     rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, w.st, sig_num, stream);
     if (rc) return rc;
+    if (sp.mass_conserve) {
+        // group-mass conservation: re-aggregate the numerator against the
+        // first pass's denominator (poisson.py:231-265)
+        BMND_CUDA_TRY(cudaMemsetAsync(w.num, 0, 8 * vox, stream));
+        rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, w.st, nullptr, stream,
+                                 w.den);
+        if (rc) return rc;
+    }
     if (sigma_out) {
         rc = launch_finalize_sigma(sp, sig_num, w.den, global_sigma, sigma_out, stream);
         if (rc) return rc;

@@ -194,7 +194,8 @@ int32_t launch_blockmatch_patches(const BmndMatchParams& mp, const float* patche
                                   cudaStream_t stream);
 int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const float* pilot,
                             const int32_t* sel, const int32_t* count, int64_t n_refs, double* num,
-                            double* den, float* st, double* sig_num, cudaStream_t stream);
+                            double* den, float* st, double* sig_num, cudaStream_t stream,
+                            const double* den_ro = nullptr, int* err = nullptr);
 int32_t launch_finalize_sigma(const BmndStageParams& sp, const double* sig_num, const double* den,
                               float global_sigma, float* out, cudaStream_t stream);
 int32_t launch_finalize(const BmndStageParams& sp, const double* num, const double* den,

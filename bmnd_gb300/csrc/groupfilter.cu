@@ -44,8 +44,8 @@ constexpr int kThreads = 256;      // threads per group (CTA)
 // thresholding).  Transforms run in place, so no scratch buffer is needed.
 struct Layout {
     // byte offsets into dynamic shared memory
-    int64_t g, gt, fw, fi, win, mdiag, pos, shf, shl, sg, ex, lag, uni, s, x, r, v, grid, lval, lstart, lent,
-        scan, plane, wts, misc, total;
+    int64_t g, gt, fw, fi, fit, dir, win, mdiag, pos, shf, shl, sg, ex, lag, uni, s, x, r, v, grid, lval, lstart,
+        lent, scan, plane, wts, misc, total;
 };
 
 struct FilterArgs {
@@ -65,6 +65,10 @@ struct FilterArgs {
     double* den;
     const float* st;  // S^T: st[p * kron_stride(P) + j] = S[j, p], the Kronecker product of the patch transforms
     double* sig_num;  // optional: sigma-map numerator (sum of sigma x weight x window), else null
+    // group-mass conservation, second pass: the first pass's denominator
+    // (read only); the kernel then re-aggregates the numerator alone
+    const double* den_ro;
+    int* err;  // set when a group's mass correction is undefined
 };
 
 __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax, int64_t ucells, bool sigma) {
@@ -83,6 +87,11 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     L.gt = take(4 * nmax * (kpad > 0 ? kpad : 4));
     L.fw = take(4 * BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE);
     L.fi = take(4 * BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE);
+    // group-mass conservation: transposed inverse spatial matrices, and the
+    // per-axis factors of the constant synthesis direction (group axis, patch axes)
+    const bool mass = sp.mass_conserve != 0;
+    L.fit = take(mass ? 4 * BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE : 16);
+    L.dir = take(mass ? 4 * (BMND_MAX_STACK + BMND_MAX_DIMS * BMND_MAX_EDGE) : 16);
     L.win = take(4 * P);
     L.mdiag = take(8 * P);
     L.pos = take(4 * nmax * BMND_MAX_DIMS);
@@ -95,7 +104,7 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     const bool gauss = sp.noise_model == BMND_NOISE_GAUSSIAN;
     L.lag = take(gauss && kmax > 0 ? 4 * static_cast<int64_t>(nmax) * (nmax + 1) / 2 : 16);
     L.scan = take(8 * (kThreads + 1));
-    L.plane = take(8 * nmax);
+    L.plane = take(8 * (nmax > 40 ? nmax : 40));  // also the mass phase's 8 warps x 5 sums
     L.wts = take(4 * nmax);
     L.misc = take(64);
     // union region
@@ -322,14 +331,16 @@ __device__ __forceinline__ void space_axis_fixed(float* buf, int n, const float*
 
 // separable transform of an (n, block...) group in place: the group axis
 // first, then the patch axes (transforms.py:209-255).  kind: 0 forward,
-// 1 inverse, 2 squared forward.
+// 1 inverse, 2 squared forward, 3 transposed inverse (poisson.py:84-114).
 template <int ND, int B0, int B1, int B2, class GM>
 __device__ void transform_group(const GM& geo, const FilterArgs& a, unsigned char* smem, int n, float* buf,
                                 int kind) {
     const float* G = sm<float>(smem, a.L.g);
-    const float* F = sm<float>(smem, kind == 1 ? a.L.fi : a.L.fw);
+    const float* F = sm<float>(smem, kind == 1 ? a.L.fi : (kind == 3 ? a.L.fit : a.L.fw));
     if (a.sp.group_transform != BMND_GROUP_NONE) {
-        if (kind == 0) group_axis_any<0>(buf, n, geo.P(), G);
+        // kind 3 (transposed inverse): the group transforms are orthonormal, so
+        // the transposed inverse of the group axis is the forward transform
+        if (kind == 0 || kind == 3) group_axis_any<0>(buf, n, geo.P(), G);
         else if (kind == 1) group_axis_any<1>(buf, n, geo.P(), G);
         else group_axis_any<2>(buf, n, geo.P(), G);
     }
@@ -621,6 +632,17 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
     for (int e = tid; e < P; e += blockDim.x) {
         win[e] = sp.window[e];
         mdiag[e] = sp.spatial_metric_diag[e];
+    }
+    if (a.den_ro) {
+        // matrices are stored densely, b x b row-major, per axis
+        float* Fit = sm<float>(smem, a.L.fit);
+        constexpr int EE = BMND_MAX_EDGE * BMND_MAX_EDGE;
+        for (int e = tid; e < BMND_MAX_DIMS * EE; e += blockDim.x) {
+            const int d = e / EE, q = e % EE;
+            const int b = d < geo.nd() ? geo.b(d) : 1;
+            const int i = q / b, k = q % b;
+            Fit[e] = q < b * b ? sp.spatial_inv[d][k * b + i] : 0.0f;
+        }
     }
     __syncthreads();
     // G^T restricted to the exact planes, padded to 4: GT[g * kpad + i] = G[i, g]
@@ -1006,6 +1028,121 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
     }
     __syncthreads();
 
+    // ---- group-mass conservation, second pass (poisson.py:161-265) ----
+    if (a.den_ro) {
+        float* dirv = sm<float>(smem, a.L.dir);  // [n] group axis, then [MAX_DIMS][MAX_EDGE] patch axes
+        double* red = sm<double>(smem, a.L.plane);  // reduction scratch: 5 sums per warp
+        // constant synthesis direction: per axis solve(inverse, 1) = forward 1
+        // (G on the group axis, the forward spatial matrix on each patch axis)
+        if (tid < n) {
+            float sgv = 0.0f;
+            for (int j = 0; j < n; ++j) sgv += G[tid * n + j];
+            dirv[tid] = a.sp.group_transform == BMND_GROUP_NONE ? 1.0f : sgv;
+        }
+        if (tid >= 64 && tid < 64 + BMND_MAX_DIMS * BMND_MAX_EDGE) {
+            const int d = (tid - 64) / BMND_MAX_EDGE, k = (tid - 64) % BMND_MAX_EDGE;
+            float v = 0.0f;
+            if (d < geo.nd() && k < geo.b(d))
+                for (int m = 0; m < geo.b(d); ++m) v += Fw[d * BMND_MAX_EDGE * BMND_MAX_EDGE + k * geo.b(d) + m];
+            dirv[BMND_MAX_STACK + d * BMND_MAX_EDGE + k] = v;
+        }
+        // output functional O = w_g win[p] / den (float32 arithmetic, as the
+        // reference's gather), into S; the target sum(O x noisy) in float64
+        double t_target = 0.0;
+        for (int e = tid; e < total; e += blockDim.x) {
+            const int g = e / P, p = e - g * P;
+            const int64_t off = geo.offset(pos + g * BMND_MAX_DIMS, p, a.vstride);
+            const float o = (wts[g] * win[p]) / static_cast<float>(a.den_ro[off]);
+            S[e] = o;
+            t_target += static_cast<double>(o) * static_cast<double>(__ldg(a.noisy + off));
+        }
+        __syncthreads();
+        transform_group<ND, B0, B1, B2>(geo, a, smem, n, S, 3);  // coefficient functional F
+        __syncthreads();
+        float dmax_g = 0.0f, dmax_s = 1.0f;
+        for (int g = 0; g < n; ++g) dmax_g = fmaxf(dmax_g, fabsf(dirv[g]));
+        for (int d = 0; d < geo.nd(); ++d) {
+            float m = 0.0f;
+            for (int k = 0; k < geo.b(d); ++k) m = fmaxf(m, fabsf(dirv[BMND_MAX_STACK + d * BMND_MAX_EDGE + k]));
+            dmax_s *= m;
+        }
+        const float dmax = dmax_g * dmax_s;
+        auto dir_of = [&](int e) -> float {
+            const int g = e / P;
+            int p = e - g * P;
+            float v = dirv[g];
+#pragma unroll
+            for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                if (d < geo.nd()) {
+                    v *= dirv[BMND_MAX_STACK + d * BMND_MAX_EDGE + p % geo.b(d)];
+                    p /= geo.b(d);
+                }
+            }
+            return v / dmax;
+        };
+        double t_cur = 0.0, t_den = 0.0, t_resp = 0.0;
+        float t_max = 0.0f;
+        for (int e = tid; e < total; e += blockDim.x) {
+            const double f = static_cast<double>(S[e]);
+            t_cur += f * static_cast<double>(X[e]);
+            t_den += f * f;
+            t_resp += f * static_cast<double>(dir_of(e));
+            t_max = fmaxf(t_max, fabsf(S[e]));
+        }
+        const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            t_target += __shfl_xor_sync(0xffffffffu, t_target, o);
+            t_cur += __shfl_xor_sync(0xffffffffu, t_cur, o);
+            t_den += __shfl_xor_sync(0xffffffffu, t_den, o);
+            t_resp += __shfl_xor_sync(0xffffffffu, t_resp, o);
+            t_max = fmaxf(t_max, __shfl_xor_sync(0xffffffffu, t_max, o));
+        }
+        __syncthreads();  // red aliases plane[], last read by the weights
+        if (lane == 0) {
+            red[warp * 5 + 0] = t_target;
+            red[warp * 5 + 1] = t_cur;
+            red[warp * 5 + 2] = t_den;
+            red[warp * 5 + 3] = t_resp;
+            red[warp * 5 + 4] = static_cast<double>(t_max);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double target = 0.0, cur = 0.0, fden = 0.0, resp = 0.0, fmx = 0.0;
+            for (int w = 0; w < nwarps; ++w) {
+                target += red[w * 5 + 0];
+                cur += red[w * 5 + 1];
+                fden += red[w * 5 + 2];
+                resp += red[w * 5 + 3];
+                fmx = fmax(fmx, red[w * 5 + 4]);
+            }
+            double corr = 0.0;
+            bool ok = true;
+            if (fden <= sp.eps) {
+                // rescale a vanishing functional by its largest entry
+                if (!(fmx > 0.0) || !isfinite(fmx)) ok = false;
+                else {
+                    target /= fmx;
+                    cur /= fmx;
+                    resp /= fmx;
+                }
+            }
+            const double residual = target - cur;
+            if (ok && residual != 0.0) {
+                if (!(resp != 0.0) || !isfinite(resp)) ok = false;
+                else corr = residual / resp;
+            }
+            if (!ok && a.err) atomicExch(a.err, 1);
+            red[0] = ok ? corr : 0.0;
+        }
+        __syncthreads();
+        const double corr = red[0];
+        if (corr != 0.0)
+            for (int e = tid; e < total; e += blockDim.x)
+                X[e] = static_cast<float>(static_cast<double>(X[e]) + corr * static_cast<double>(dir_of(e)));
+        __syncthreads();
+    }
+
     // ---- inverse transform and scatter ----
     transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, 1);
     for (int e = tid; e < total; e += blockDim.x) {
@@ -1014,6 +1151,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         const int64_t off = geo.offset(pos + g * BMND_MAX_DIMS, p, a.vstride);
         float ww = mul_rn(wts[g], win[p]);
         atomicAdd(a.num + off, widen_f64(mul_rn(X[e], ww)));
+        if (a.den_ro) continue;  // the re-aggregation pass adds to the numerator only
         atomicAdd(a.den + off, widen_f64(ww));
         if (a.sig_num) {
             // sigma map numerator (patchaggregation.py:229-294): per coefficient
@@ -1050,11 +1188,12 @@ __global__ void spatial_kron_kernel(BmndStageParams sp, int P, int stride, float
 
 __global__ void finalize_kernel(const double* __restrict__ num, const double* __restrict__ den,
                                 const float* __restrict__ noisy, float* __restrict__ out,
-                                int64_t n, float eps_f) {
+                                int64_t n, float eps_f, int no_eps) {
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         float d = static_cast<float>(den[i]);
-        out[i] = d > 0.0f ? div_rn(static_cast<float>(num[i]), add_rn(d, eps_f)) : noisy[i];
+        // mass conservation divides without eps (bmndalgo.py:617-624)
+        out[i] = d > 0.0f ? div_rn(static_cast<float>(num[i]), no_eps ? d : add_rn(d, eps_f)) : noisy[i];
     }
 }
 
@@ -1091,7 +1230,8 @@ int64_t group_filter_smem_bytes(const BmndStageParams& sp) {
 
 int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const float* pilot,
                             const int32_t* sel, const int32_t* count, int64_t n_refs, double* num,
-                            double* den, float* st, double* sig_num, cudaStream_t stream) {
+                            double* den, float* st, double* sig_num, cudaStream_t stream, const double* den_ro,
+                            int* err) {
     if (n_refs == 0) return BMND_OK;
     {
         const int P = patch_volume(sp);
@@ -1121,6 +1261,8 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
     a.n_refs = n_refs;
     a.num = num;
     a.den = den;
+    a.den_ro = den_ro;
+    a.err = err;
     if (a.L.total > 227 * 1024)
         return fail(BMND_ERR_UNSUPPORTED, "group filter shared memory exceeds 227 KB for this profile");
     if (n_refs > 0x7fffffffLL) return fail(BMND_ERR_UNSUPPORTED, "too many groups");
@@ -1175,7 +1317,8 @@ int32_t launch_finalize(const BmndStageParams& sp, const double* num, const doub
     int64_t blocks = (n + threads - 1) / threads;
     if (blocks > 152 * 16) blocks = 152 * 16;
     finalize_kernel<<<static_cast<unsigned>(blocks), threads, 0, stream>>>(num, den, noisy, out, n,
-                                                                            static_cast<float>(sp.eps));
+                                                                            static_cast<float>(sp.eps),
+                                                                            sp.mass_conserve ? 1 : 0);
     BMND_LAUNCH_CHECK("finalize_kernel");
     return BMND_OK;
 }

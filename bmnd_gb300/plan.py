@@ -123,6 +123,10 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
         p.noise_model = _abi.NOISE_POISSON
         p.count_scale = float(profile.poisson_count_scale)
         p.variance_floor = float(profile.poisson_variance_floor)
+        mass = profile.poisson_group_mass_conservation
+        p.mass_conserve = int(mass is PoissonGroupMassConservation.BOTH
+                              or (mass is PoissonGroupMassConservation.HT and stage == "ht")
+                              or (mass is PoissonGroupMassConservation.WIENER and stage == "wiener"))
     else:
         p.noise_model = _abi.NOISE_GAUSSIAN
         p.count_scale = 1.0
@@ -178,8 +182,6 @@ def check_poisson_options(profile) -> None:
     """Reject the non-default Poisson options that are not on the GPU path."""
     if profile.poisson_ht_match_policy is not PoissonHTMatchPolicy.FIXED:
         raise unsupported("only the 'fixed' Poisson HT match policy is on the GPU path")
-    if profile.poisson_group_mass_conservation is not PoissonGroupMassConservation.NONE:
-        raise unsupported("Poisson group-mass conservation is not on the GPU path")
     if profile.poisson_wiener_gain_mode is not PoissonWienerGainMode.VARIANCE_SCALED:
         raise unsupported("only the 'variance-scaled' Poisson Wiener gain is on the GPU path")
     if profile.poisson_variance_source_wiener is not PoissonVarianceSource.PILOT:

@@ -144,6 +144,14 @@ typedef struct BmndStageParams {
      * float32(ssd_threshold * (max - min)^2) over the matched volume
      * (blockmatching.py:168-184), evaluated on the device */
     double ssd_threshold;
+    /* Poisson group-mass conservation of this stage (poisson.py:161-265,
+     * bmndalgo.py:610-625 / :1023-1038): after the usual aggregation, every
+     * group's coefficients are corrected along the group's constant synthesis
+     * direction so that its normalised-occurrence-weighted output matches the
+     * same functional of its noisy patches, the numerator is re-aggregated and
+     * the estimate is numerator / denominator (no eps) */
+    int32_t mass_conserve;
+    int32_t reserved2;
 } BmndStageParams;
 
 /* ABI version this library was built with (BMND_ABI_VERSION). */

@@ -13,6 +13,7 @@ Usage::
     python tests/golden/make_golden.py pipeline bm3d_32 [bm4d_16 ...]
     python tests/golden/make_golden.py sigma bm3d_32 [bm4d_12x16x20 ...]
     python tests/golden/make_golden.py gauss [bm3d_32 ...]
+    python tests/golden/make_golden.py option [mass_bm3d_32 ...]
     python tests/golden/make_golden.py list
 
 ``unit`` writes ``unit_*.npz`` (distances, canonical keys, transforms, exact
@@ -291,6 +292,52 @@ def run_unit() -> None:
     print(f"unit fixtures -> {path} ({len(out)} arrays)")
 
 
+# Poisson cases with non-default profile fields: name -> (kind, generator, kwargs, profile fields)
+OPTION_CASES = {
+    "mass_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=21), dict(poisson_group_mass_conservation="both")),
+    "mass_ht_bm3d_40x24": ("bm3d", "ragged2d", dict(shape=(40, 24), seed=22),
+                           dict(poisson_group_mass_conservation="ht")),
+    "mass_bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=23),
+                           dict(poisson_group_mass_conservation="both")),
+}
+
+
+def run_option(name: str) -> None:
+    """opt_<case>.npz: like pipe_<case>.npz for a Poisson profile with the
+    listed fields changed (stored as ``extra_json``)."""
+    import json
+
+    import bmnd as ref
+
+    kind, gen, kwargs, extra = OPTION_CASES[name]
+    clean, noisy = _make_input(gen, kwargs)
+    profile_cls = ref.BM3DProfile if kind == "bm3d" else ref.BM4DProfile
+    profile = profile_cls(noise_model=ref.NoiseModel.POISSON, **extra)
+    stages, matches = {}, {}
+
+    def stage_cb(stage, est):
+        stages[stage] = np.asarray(est, dtype=np.float32)
+
+    def bm_cb(stage, result):
+        max_stack = profile.ht_max_stack_size if stage == "ht" else profile.wiener_max_stack_size
+        matches[stage] = _pack_matches(result, max_stack, noisy.ndim)
+
+    t0 = time.time()
+    out = ref.bmnd(noisy, profile, stage_callback=stage_cb, blockmatch_callback=bm_cb)
+    elapsed = time.time() - t0
+    payload = dict(kind=np.array(kind), extra_json=np.array(json.dumps(extra)), clean=clean, noisy=noisy,
+                   ht=stages["ht"], wiener=stages["wiener"], out=np.asarray(out, dtype=np.float32),
+                   seconds=np.float64(elapsed))
+    for stage, (sel, counts, accepted, refs) in matches.items():
+        payload[f"{stage}_sel"] = sel
+        payload[f"{stage}_count"] = counts
+        payload[f"{stage}_accepted"] = accepted
+        payload[f"{stage}_refs"] = refs
+    path = os.path.join(HERE, f"opt_{name}.npz")
+    np.savez_compressed(path, **payload)
+    print(f"option {name}: {noisy.shape} in {elapsed:.1f} s -> {path}")
+
+
 # Gaussian cases: name -> (profile kind, clean generator, kwargs, sigma, call options, profile fields)
 GAUSS_CASES = {
     "bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=11), 3.0, {}, {}),
@@ -397,6 +444,10 @@ def main(argv: list[str]) -> None:
     if argv[0] == "sigma":
         for name in argv[1:]:
             run_sigma(name)
+        return
+    if argv[0] == "option":
+        for name in argv[1:] or list(OPTION_CASES):
+            run_option(name)
         return
     if argv[0] == "gauss":
         for name in argv[1:] or list(GAUSS_CASES):

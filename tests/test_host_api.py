@@ -169,7 +169,7 @@ def test_unsupported_options_raise_not_implemented():
     with pytest.raises(NotImplementedError):
         bg.bmnd(vol, bg.BM3DProfile(ht_use_soft_thresholding=True), sigma=1.0)
     with pytest.raises(NotImplementedError):
-        bg.bmnd(vol, _poisson(poisson_group_mass_conservation="both"))
+        bg.bmnd(vol, _poisson(poisson_ht_match_policy="candidate_standardized"))
 
 
 def test_stage_params_defaults():
