@@ -39,6 +39,12 @@ GROUP_NONE = 2
 WEIGHT_CLASSIC = 0
 WEIGHT_VARIANCE = 1
 
+GAIN_VARIANCE_SCALED = 0
+GAIN_CLASSIC = 1
+GAIN_NOISE_FLOOR = 2
+SOURCE_PILOT = 0
+SOURCE_OBSERVATION = 1
+
 NOISE_POISSON = 0
 NOISE_GAUSSIAN = 1
 
@@ -109,7 +115,10 @@ class StageParams(ctypes.Structure):
         ("reserved1", _I32),
         ("ssd_threshold", ctypes.c_double),
         ("mass_conserve", _I32),
-        ("reserved2", _I32),
+        ("wiener_gain_mode", _I32),
+        ("wiener_variance_source", _I32),
+        ("wiener_match_source", _I32),
+        ("soft_threshold", _I32),
     ]
 
 

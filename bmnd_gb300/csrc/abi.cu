@@ -88,6 +88,10 @@ int32_t validate_stage(const BmndStageParams& sp) {
     if (!(sp.eps > 0.0)) return fail(BMND_ERR_INVALID_ARG, "eps must be positive");
     if (!(sp.match_threshold >= 0.0f) || !std::isfinite(sp.match_threshold))
         return fail(BMND_ERR_INVALID_ARG, "match threshold must be finite and >= 0");
+    if (sp.wiener_gain_mode < 0 || sp.wiener_gain_mode > 2) return fail(BMND_ERR_INVALID_ARG, "unknown gain mode");
+    if ((sp.wiener_variance_source != 0 && sp.wiener_variance_source != 1) ||
+        (sp.wiener_match_source != 0 && sp.wiener_match_source != 1))
+        return fail(BMND_ERR_INVALID_ARG, "unknown Wiener source");
     if (sp.noise_model != BMND_NOISE_POISSON && sp.noise_model != BMND_NOISE_GAUSSIAN)
         return fail(BMND_ERR_INVALID_ARG, "unknown noise model");
     if (sp.noise_model == BMND_NOISE_GAUSSIAN) {
@@ -200,9 +204,9 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
         BMND_CUDA_TRY(cudaMemsetAsync(sig_num, 0, 8 * vox, stream));
     }
     BmndMatchParams mp = match_params_of(sp);
-    const float* match_src = sp.filter == BMND_FILTER_WIENER ? pilot : noisy;
-    if (sp.filter == BMND_FILTER_WIENER && sp.match_precision == BMND_MATCH_EXACT)
-        mp.precision = BMND_MATCH_REAL_VALUED;
+    const bool on_pilot = sp.filter == BMND_FILTER_WIENER && sp.wiener_match_source == BMND_SOURCE_PILOT;
+    const float* match_src = on_pilot ? pilot : noisy;
+    if (on_pilot && sp.match_precision == BMND_MATCH_EXACT) mp.precision = BMND_MATCH_REAL_VALUED;
     const float* thr_dev = nullptr;
     if (sp.distance == BMND_DIST_SSD) {
         rc = launch_ssd_threshold(match_src, static_cast<int64_t>(vox), sp.ssd_threshold, w.mm, w.thr, stream);

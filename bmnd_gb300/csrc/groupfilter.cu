@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
 
     const float scale_f = static_cast<float>(sp.count_scale);
     const float floor_f = static_cast<float>(sp.variance_floor);
-    const float* varsrc = wiener ? a.pilot : a.noisy;
+    const float* varsrc = (wiener && sp.wiener_variance_source == BMND_SOURCE_PILOT) ? a.pilot : a.noisy;
     const int total = n * P;
     const bool need_approx = (k <= 0) || (kk < n);
 
@@ -950,7 +950,17 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         }
         float nv = mul_rn(sig, sig);
         float att;
-        if (!wiener && gauss) {
+        if (!wiener && sp.soft_threshold) {
+            // soft thresholding (bmndalgo.py:476-486): sign(c) max(|c| - lambda sigma, 0)
+            const float thr = mul_rn(sp.ht_lambda, sig);
+            const float mag = fabsf(X[e]);
+            const float shr = fmaxf(sub_rn(mag, thr), 0.0f);
+            att = mag > 0.0f ? div_rn(shr, mag) : 0.0f;
+            X[e] = copysignf(shr, X[e]);
+            V[e] = att;
+            S[e] = nv;
+            continue;
+        } else if (!wiener && gauss) {
             // |c| >= lambda sigma, the group DC always kept (bmndalgo.py:462-475)
             float thr = mul_rn(sp.ht_lambda, sig);
             att = (fabsf(X[e]) >= thr || e == 0) ? 1.0f : 0.0f;
@@ -966,11 +976,15 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
             float gain = den > 0.0f ? div_rn(pr, den) : 0.0f;
             att = fminf(fmaxf(gain, 0.0f), 1.0f);
         } else {
+            // signal power by gain mode (wiener.py:24-47)
             float eff = mul_rn(sp.wiener_scale, nv);
             float pr = fabsf(R[e]);
             pr = mul_rn(pr, pr);
-            float spow = sub_rn(pr, eff);
-            if (spow < 0.0f) spow = 0.0f;
+            float spow = pr;
+            if (sp.wiener_gain_mode != BMND_GAIN_CLASSIC) {
+                spow = sub_rn(pr, sp.wiener_gain_mode == BMND_GAIN_NOISE_FLOOR ? nv : eff);
+                if (spow < 0.0f) spow = 0.0f;
+            }
             float gain = div_rn(spow, add_rn(add_rn(spow, eff), eps_f));
             att = fminf(fmaxf(gain, 0.0f), 1.0f);
         }

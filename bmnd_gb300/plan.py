@@ -119,10 +119,20 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     p.wiener_scale = float(profile.wiener_variance_scale)
     p.eps = EPS
     p.ssd_threshold = float(getattr(profile, f"{stage}_match_threshold"))
+    p.soft_threshold = int(stage == "ht" and bool(profile.ht_use_soft_thresholding))
     if gauss is None:
         p.noise_model = _abi.NOISE_POISSON
         p.count_scale = float(profile.poisson_count_scale)
         p.variance_floor = float(profile.poisson_variance_floor)
+        gain = profile.poisson_wiener_gain_mode
+        p.wiener_gain_mode = {PoissonWienerGainMode.VARIANCE_SCALED: _abi.GAIN_VARIANCE_SCALED,
+                              PoissonWienerGainMode.CLASSIC: _abi.GAIN_CLASSIC,
+                              PoissonWienerGainMode.NOISE_FLOOR: _abi.GAIN_NOISE_FLOOR}[gain]
+        obs = PoissonVarianceSource.OBSERVATION
+        p.wiener_variance_source = _abi.SOURCE_OBSERVATION if profile.poisson_variance_source_wiener is obs \
+            else _abi.SOURCE_PILOT
+        p.wiener_match_source = _abi.SOURCE_OBSERVATION if profile.poisson_wiener_match_source is obs \
+            else _abi.SOURCE_PILOT
         mass = profile.poisson_group_mass_conservation
         p.mass_conserve = int(mass is PoissonGroupMassConservation.BOTH
                               or (mass is PoissonGroupMassConservation.HT and stage == "ht")
@@ -167,8 +177,6 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
 
 def check_gaussian_options(profile) -> None:
     """Reject the Gaussian options that are not on the GPU path."""
-    if profile.ht_use_soft_thresholding:
-        raise unsupported("soft thresholding is not on the GPU path")
     if profile.reference_schedule_mode not in (
         ReferenceScheduleMode.GENERATED,
         ReferenceScheduleMode.OFF,
@@ -182,14 +190,6 @@ def check_poisson_options(profile) -> None:
     """Reject the non-default Poisson options that are not on the GPU path."""
     if profile.poisson_ht_match_policy is not PoissonHTMatchPolicy.FIXED:
         raise unsupported("only the 'fixed' Poisson HT match policy is on the GPU path")
-    if profile.poisson_wiener_gain_mode is not PoissonWienerGainMode.VARIANCE_SCALED:
-        raise unsupported("only the 'variance-scaled' Poisson Wiener gain is on the GPU path")
-    if profile.poisson_variance_source_wiener is not PoissonVarianceSource.PILOT:
-        raise unsupported("only the pilot Wiener variance source is on the GPU path")
-    if profile.poisson_wiener_match_source is not PoissonVarianceSource.PILOT:
-        raise unsupported("only pilot Wiener matching is on the GPU path")
-    if profile.ht_use_soft_thresholding:
-        raise unsupported("soft thresholding is not on the GPU path")
     if profile.blockmatch_distance is BlockMatchDistance.SSD and float(profile.gamma) != 0.0:
         raise unsupported("the Poisson SSD noise-bias correction (gamma != 0) is not on the GPU path")
     if profile.reference_schedule_mode not in (

@@ -151,8 +151,20 @@ typedef struct BmndStageParams {
      * same functional of its noisy patches, the numerator is re-aggregated and
      * the estimate is numerator / denominator (no eps) */
     int32_t mass_conserve;
-    int32_t reserved2;
+    /* Poisson Wiener options (bmndalgo.py:635-646, :720-741; wiener.py:24-95) */
+    int32_t wiener_gain_mode;        /* BMND_GAIN_VARIANCE_SCALED (default), _CLASSIC, _NOISE_FLOOR */
+    int32_t wiener_variance_source;  /* BMND_SOURCE_PILOT (default) or BMND_SOURCE_OBSERVATION */
+    int32_t wiener_match_source;     /* BMND_SOURCE_PILOT (default) or BMND_SOURCE_OBSERVATION */
+    /* hard-thresholding stage: soft thresholding, sign(c) max(|c| - lambda sigma, 0)
+     * (bmndalgo.py:476-486) */
+    int32_t soft_threshold;
 } BmndStageParams;
+
+#define BMND_GAIN_VARIANCE_SCALED 0
+#define BMND_GAIN_CLASSIC 1
+#define BMND_GAIN_NOISE_FLOOR 2
+#define BMND_SOURCE_PILOT 0
+#define BMND_SOURCE_OBSERVATION 1
 
 /* ABI version this library was built with (BMND_ABI_VERSION). */
 int32_t bmnd_abi_version(void);

@@ -299,6 +299,15 @@ OPTION_CASES = {
                            dict(poisson_group_mass_conservation="ht")),
     "mass_bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=23),
                            dict(poisson_group_mass_conservation="both")),
+    "gain_classic_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=24),
+                             dict(poisson_wiener_gain_mode="classic")),
+    "gain_floor_bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=25),
+                                 dict(poisson_wiener_gain_mode="noise-floor")),
+    "obs_variance_bm3d_40x24": ("bm3d", "ragged2d", dict(shape=(40, 24), seed=26),
+                                dict(poisson_variance_source_wiener="observation")),
+    "obs_match_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=27),
+                          dict(poisson_wiener_match_source="observation")),
+    "soft_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=28), dict(ht_use_soft_thresholding=True)),
 }
 
 
@@ -346,6 +355,7 @@ GAUSS_CASES = {
     "bm3d_psd_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=14), 2.5, dict(psd=True), {}),
     "bm3d_conv_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=15), 3.0, {}, dict(nf=0)),
     "bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=16), 1.5, {}, {}),
+    "bm3d_soft_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=17), 3.0, {}, dict(ht_use_soft_thresholding=True)),
 }
 
 
@@ -403,7 +413,8 @@ def run_gauss(name: str) -> None:
                    sigma_ht=np.asarray(smap["ht"], dtype=np.float32),
                    sigma_wiener=np.asarray(smap["wiener"], dtype=np.float32), seconds=np.float64(elapsed),
                    sigma=np.float64(-1.0 if "sigma" not in call else sigma),
-                   nf=np.array(-1 if "nf" not in extra else extra["nf"]))
+                   nf=np.array(-1 if "nf" not in extra else extra["nf"]),
+                   soft=np.array(int(bool(extra.get("ht_use_soft_thresholding", False)))))
     if psd is not None:
         payload["sigma_psd"] = psd
     for stage, (sel, counts, accepted, refs) in matches.items():

@@ -23,6 +23,8 @@ def _profile(g):
     kind = str(g["kind"])
     nf = int(g["nf"])
     extra = {} if nf < 0 else dict(nf=nf)
+    if "soft" in g.files and int(g["soft"]):
+        extra["ht_use_soft_thresholding"] = True
     return (bg.BM3DProfile if kind == "bm3d" else bg.BM4DProfile)(**extra)
 
 

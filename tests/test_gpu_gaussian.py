@@ -3,7 +3,7 @@
 Cases (``tests/golden/gauss_*.npz``, made by ``make_golden.py gauss``): BM3D
 with a scalar sigma, a ragged 2-D volume, sigma estimated from the data, a
 coloured ``sigma_psd``, conventional mode (``nf=0``: no gamma correction,
-k = 0) and a ragged BM4D volume.
+k = 0), soft thresholding, and a ragged BM4D volume.
 
 Stated tolerance:
 * stage-1 match sets (SSD with the gamma noise-bias correction) equal the
@@ -36,6 +36,8 @@ def _profile(g):
 
     nf = int(g["nf"])
     extra = {} if nf < 0 else dict(nf=nf)
+    if "soft" in g.files and int(g["soft"]):
+        extra["ht_use_soft_thresholding"] = True
     return (bg.BM3DProfile if str(g["kind"]) == "bm3d" else bg.BM4DProfile)(**extra)
 
 

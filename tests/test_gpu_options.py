@@ -2,7 +2,9 @@
 
 Cases (``tests/golden/opt_*.npz``, made by ``make_golden.py option``): group-mass
 conservation in both stages (2-D and 3-D) and in the hard-thresholding stage
-only (ragged 2-D).
+only (ragged 2-D); the classic and noise-floor Wiener gains; the observation
+as the Wiener variance source and as the Wiener matching source; soft
+thresholding.
 
 Stated tolerance (as for the default Poisson pipeline): stage-1 match sets
 equal the reference's except where the selection boundary is tied within the

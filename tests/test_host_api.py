@@ -167,7 +167,7 @@ def test_profile_enum_coercion_in_place():
 def test_unsupported_options_raise_not_implemented():
     vol = np.ones((24, 24), dtype=np.float32)
     with pytest.raises(NotImplementedError):
-        bg.bmnd(vol, bg.BM3DProfile(ht_use_soft_thresholding=True), sigma=1.0)
+        bg.bmnd(vol, bg.BM3DProfile(reference_schedule_mode="official"), sigma=1.0)
     with pytest.raises(NotImplementedError):
         bg.bmnd(vol, _poisson(poisson_ht_match_policy="candidate_standardized"))
 
