@@ -42,6 +42,9 @@ WEIGHT_VARIANCE = 1
 GAIN_VARIANCE_SCALED = 0
 GAIN_CLASSIC = 1
 GAIN_NOISE_FLOOR = 2
+POLICY_FIXED = 0
+POLICY_REFERENCE_FINITE_COUNT = 1
+POLICY_CANDIDATE_STANDARDIZED = 2
 SOURCE_PILOT = 0
 SOURCE_OBSERVATION = 1
 
@@ -119,6 +122,11 @@ class StageParams(ctypes.Structure):
         ("wiener_variance_source", _I32),
         ("wiener_match_source", _I32),
         ("soft_threshold", _I32),
+        ("match_policy", _I32),
+        ("null_max_count", _I32),
+        ("null_moments", ctypes.c_void_p),
+        ("policy_beta", ctypes.c_double),
+        ("policy_power", ctypes.c_double),
     ]
 
 

@@ -25,7 +25,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import _abi, gaussian, plan
+from . import _abi, gaussian, plan, policies
 from .enums import BlockMatchDistance, CacheMode, coerce_enum
 from .validation import resolve_profile
 
@@ -155,6 +155,25 @@ def _match_result(schedule: plan.Schedule, counts, sel, cnt, acc) -> BlockMatchR
 _MATCH_PRECISIONS = {"exact": _abi.MATCH_EXACT, "fast": _abi.MATCH_FAST, "approx": _abi.MATCH_APPROX}
 
 
+_NULL_TABLES: dict = {}
+
+
+def null_table_device(profile, resolved, device):
+    """The null moment table of the profile's Poisson HT match policy as a
+    CUDA tensor, or None for the fixed policy (cached per device)."""
+    from .enums import PoissonHTMatchPolicy
+
+    if not resolved.is_poisson or profile.poisson_ht_match_policy is PoissonHTMatchPolicy.FIXED:
+        return None
+    key = (resolved.blockmatch_distance, int(profile.poisson_ht_match_moment_max_count), str(device))
+    hit = _NULL_TABLES.get(key)
+    if hit is None:
+        table = policies.null_moment_table(key[0], key[1])
+        hit = _torch().from_numpy(np.array(table, dtype=np.float64)).to(device)
+        _NULL_TABLES[key] = hit
+    return hit
+
+
 def gaussian_tables(model: gaussian.GaussianModel, profile, shape, resolved, device) -> dict:
     """Device tables of both stages for stationary Gaussian noise: the
     covariance maps of each stage's transformed patches ([lag][coefficient])
@@ -205,7 +224,8 @@ def bmnd_device(noisy, profile, *, resolved=None, match_precision: str = "exact"
     need = 0
     for stage in ("ht", "wiener"):
         p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance,
-                              resolved.variance_k, precision, None if gauss is None else gauss[stage])
+                              resolved.variance_k, precision, None if gauss is None else gauss[stage],
+                              null_table_device(profile, resolved, device))
         block = tuple(int(b) for b in getattr(profile, f"{stage}_block_size"))
         counts = tuple(s - b + 1 for s, b in zip(shape, block))
         sched = plan.reference_schedule(profile, counts, stage)
@@ -309,7 +329,7 @@ def stage_device(noisy, profile, stage: str, pilot=None, *, resolved=None, match
     if stream is None:
         stream = torch.cuda.current_stream(device)
     p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k, precision,
-                          None if gauss is None else gauss[stage])
+                          None if gauss is None else gauss[stage], null_table_device(profile, resolved, device))
     block = tuple(int(b) for b in getattr(profile, f"{stage}_block_size"))
     counts = tuple(s - b + 1 for s, b in zip(shape, block))
     sched = plan.reference_schedule(profile, counts, stage)

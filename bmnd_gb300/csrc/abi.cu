@@ -89,6 +89,13 @@ int32_t validate_stage(const BmndStageParams& sp) {
     if (!(sp.match_threshold >= 0.0f) || !std::isfinite(sp.match_threshold))
         return fail(BMND_ERR_INVALID_ARG, "match threshold must be finite and >= 0");
     if (sp.wiener_gain_mode < 0 || sp.wiener_gain_mode > 2) return fail(BMND_ERR_INVALID_ARG, "unknown gain mode");
+    if (sp.match_policy < 0 || sp.match_policy > 2) return fail(BMND_ERR_INVALID_ARG, "unknown match policy");
+    if (sp.match_policy != BMND_POLICY_FIXED) {
+        if (!sp.null_moments || sp.null_max_count < 1)
+            return fail(BMND_ERR_INVALID_ARG, "the match policy needs the null moment table");
+        if (sp.distance == BMND_DIST_SSD)
+            return fail(BMND_ERR_INVALID_ARG, "the match policy needs a Poisson distance");
+    }
     if ((sp.wiener_variance_source != 0 && sp.wiener_variance_source != 1) ||
         (sp.wiener_match_source != 0 && sp.wiener_match_source != 1))
         return fail(BMND_ERR_INVALID_ARG, "unknown Wiener source");
@@ -117,6 +124,7 @@ struct StageWorkspace {
     float* st;  // P x kron_stride(P) Kronecker table of the patch transforms
     uint32_t* mm;  // SSD threshold: order bits of the matched volume's min and max
     float* thr;    // SSD threshold, computed on the device
+    float* thr_ref;  // per-reference thresholds (reference-finite-count policy)
     uint64_t bytes;
 };
 
@@ -139,6 +147,7 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
     const uint64_t P = static_cast<uint64_t>(patch_volume(sp));
     uint64_t o_st = take(4ull * P * static_cast<uint64_t>(kron_stride(static_cast<int>(P))));
     uint64_t o_mm = take(16);
+    uint64_t o_tr = take(sp.match_policy == BMND_POLICY_REFERENCE_FINITE_COUNT ? 4ull * n_refs : 16);
     w.bytes = off;
     if (base) {
         char* b = static_cast<char*>(base);
@@ -150,6 +159,7 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
         w.st = reinterpret_cast<float*>(b + o_st);
         w.mm = reinterpret_cast<uint32_t*>(b + o_mm);
         w.thr = reinterpret_cast<float*>(b + o_mm + 8);
+        w.thr_ref = reinterpret_cast<float*>(b + o_tr);
     }
     return w;
 }
@@ -213,9 +223,25 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
         if (rc) return rc;
         thr_dev = w.thr;
     }
-    rc = launch_blockmatch_volume(mp, match_src, sp.shape, sp.block, refs, n_refs, nullptr,
+    // Poisson HT match policies (blockmatching.py:29-148, :372-428)
+    const float* thr_per_ref = nullptr;
+    const double* null_moments = nullptr;
+    if (sp.filter == BMND_FILTER_HARD_THRESHOLD && sp.match_policy == BMND_POLICY_REFERENCE_FINITE_COUNT) {
+        int32_t counts[BMND_MAX_DIMS];
+        for (int d = 0; d < sp.ndim; ++d) counts[d] = sp.shape[d] - sp.block[d] + 1;
+        rc = launch_reference_thresholds(match_src, refs, n_refs, sp.ndim, counts, sp.block, sp.shape,
+                                         sp.count_scale, sp.null_moments, sp.null_max_count, sp.ssd_threshold,
+                                         sp.policy_beta, sp.policy_power, w.thr_ref, stream);
+        if (rc) return rc;
+        thr_per_ref = w.thr_ref;
+    } else if (sp.filter == BMND_FILTER_HARD_THRESHOLD && sp.match_policy == BMND_POLICY_CANDIDATE_STANDARDIZED) {
+        null_moments = sp.null_moments;
+        mp.precision = BMND_MATCH_EXACT;
+    }
+    rc = launch_blockmatch_volume(mp, match_src, sp.shape, sp.block, refs, n_refs, thr_per_ref,
                                   sp.match_threshold, w.sel, w.count, w.accepted, stream, thr_dev,
-                                  sp.match_noise_ssd, sp.ssd_gamma, allow_alloc);
+                                  sp.match_noise_ssd, sp.ssd_gamma, allow_alloc, null_moments,
+                                  sp.null_max_count);
     if (rc) return rc;
     rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, w.st, sig_num, stream);
     if (rc) return rc;

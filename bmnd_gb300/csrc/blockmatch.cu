@@ -70,6 +70,10 @@ struct MatchArgs {
     // threshold computed on the device (one float), overrides the scalar one
     const float* thr_dev;
     int32_t no_alloc;  // 1: no stream-ordered scratch (approx mode then runs the bounded form)
+    // candidate standardisation (blockmatching.py:372-428): null means then
+    // variances by pooled count 0..null_max, or null
+    const double* null_moments;
+    int32_t null_max;
 };
 
 constexpr int kTable = 64;  // counts 0..63 are tabulated
@@ -145,6 +149,47 @@ __device__ __forceinline__ float patch_distance(const float* __restrict__ ref,
     }
     if (d < 0.0f) d = 0.0f;
     return div_rn(d, static_cast<float>(P));
+}
+
+// (sum of terms - sum of null means) / sqrt(sum of null variances), every sum
+// in float32 in patch order, the null moments of the pooled count rint(r + c)
+// (float32 copies of the float64 table; above the table: mean 1, variance 2)
+template <int CODE>
+__device__ __forceinline__ float standardized_distance(const float* __restrict__ ref,
+                                                       const float* __restrict__ src, int64_t origin,
+                                                       const int32_t* __restrict__ poff, int P, float inv,
+                                                       const double* __restrict__ moments, int max_count) {
+    float dsum = 0.0f, msum = 0.0f, vsum = 0.0f;
+    for (int p = 0; p < P; ++p) {
+        float r = mul_rn(ref[p], inv);
+        if (r < 0.0f) r = 0.0f;
+        float c = mul_rn(__ldg(src + origin + poff[p]), inv);
+        if (c < 0.0f) c = 0.0f;
+        const float s = add_rn(r, c);
+        if (!(s > 0.0f)) continue;
+        if (CODE == BMND_DIST_POISSON_DEVIANCE) {
+            dsum = add_rn(dsum, deviance_term(r, c));
+        } else if (CODE == BMND_DIST_PEARSON) {
+            const float diff = sub_rn(c, r);
+            dsum = add_rn(dsum, div_rn(mul_rn(diff, diff), s));
+        } else {
+            const float rs = mul_rn(2.0f, __fsqrt_rn(add_rn(r, 0.375f)));
+            const float cs = mul_rn(2.0f, __fsqrt_rn(add_rn(c, 0.375f)));
+            const float diff = sub_rn(cs, rs);
+            dsum = add_rn(dsum, mul_rn(mul_rn(0.5f, diff), diff));
+        }
+        const float k = rintf(s);
+        if (k <= static_cast<float>(max_count)) {
+            const int ki = static_cast<int>(k);
+            msum = add_rn(msum, static_cast<float>(__ldg(moments + ki)));
+            vsum = add_rn(vsum, static_cast<float>(__ldg(moments + max_count + 1 + ki)));
+        } else {
+            msum = add_rn(msum, 1.0f);
+            vsum = add_rn(vsum, 2.0f);
+        }
+    }
+    if (vsum <= 0.0f) return 0.0f;
+    return div_rn(sub_rn(dsum, msum), __fsqrt_rn(vsum));
 }
 
 // insert `key` into an ascending list of `size` entries (capacity `cap`),
@@ -322,8 +367,11 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
         for (int64_t c = lane; c < window; c += 32) {
             int64_t lin;
             const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
-            float dist = use_table ? deviance_tabulated(ref_s, ref_row, a.src, origin, poff_s, P, table)
-                                   : patch_distance<CODE>(ref_s, a.src, origin, poff_s, P, a.inv_scale);
+            float dist = a.null_moments
+                             ? standardized_distance<CODE>(ref_s, a.src, origin, poff_s, P, a.inv_scale, a.null_moments,
+                                                           a.null_max)
+                         : use_table ? deviance_tabulated(ref_s, ref_row, a.src, origin, poff_s, P, table)
+                                     : patch_distance<CODE>(ref_s, a.src, origin, poff_s, P, a.inv_scale);
             if (CODE == BMND_DIST_SSD && a.noise_ssd) {
                 // offset of the candidate from the reference, C order over 2 r + 1 per axis
                 int64_t rem = c, gidx = 0, mul = 1;
@@ -1381,6 +1429,11 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     int64_t wmax = 1;
     for (int d = 0; d < a.ndim; ++d) wmax *= std::min<int64_t>(2 * a.radius[d] + 1, a.counts[d]);
     a.approx = precision == BMND_MATCH_APPROX;
+    if (a.null_moments) {
+        // candidate standardisation: exact warp kernel, per-term evaluation
+        a.use_table = 0;
+        return launch_exact(a, code, stream);
+    }
     const bool screened = code == BMND_DIST_POISSON_DEVIANCE && a.stab &&
                           (precision == BMND_MATCH_FAST || precision == BMND_MATCH_APPROX ||
                            precision == BMND_MATCH_REAL_VALUED) &&
@@ -1545,7 +1598,7 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
                                  int64_t n_refs, const float* thresholds, float scalar_threshold,
                                  int32_t* sel, int32_t* count, int32_t* accepted,
                                  cudaStream_t stream, const float* thr_dev, const float* noise_ssd,
-                                 float gamma, bool allow_alloc) {
+                                 float gamma, bool allow_alloc, const double* null_moments, int null_max) {
     int32_t rc = validate_match(mp);
     if (rc) return rc;
     if (noise_ssd && mp.distance != BMND_DIST_SSD)
@@ -1556,6 +1609,10 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
     a.noise_ssd = noise_ssd;
     a.gamma = gamma;
     a.no_alloc = allow_alloc ? 0 : 1;
+    a.null_moments = null_moments;
+    a.null_max = null_max;
+    if (null_moments && mp.distance == BMND_DIST_SSD)
+        return fail(BMND_ERR_INVALID_ARG, "candidate standardisation needs a Poisson distance");
     int P = 1;
     int64_t vstride[BMND_MAX_DIMS];
     int64_t s = 1;
@@ -1618,6 +1675,76 @@ __global__ void ssd_threshold_kernel(const uint32_t* __restrict__ mm, double t, 
     *thr = static_cast<float>(t * ds * ds);
 }
 }  // namespace
+
+namespace {
+// reference-finite-count thresholds (blockmatching.py:86-148): per reference,
+// mean of the null means + t sqrt(sum of null variances) / P + beta mean^power
+// over the reference patch's pooled-count estimates rint(2 r), float64
+__global__ void reference_thresholds_kernel(const float* __restrict__ vol, const int32_t* __restrict__ refs,
+                                            int64_t n, int ndim, int3 counts, int3 block, int3 vstride,
+                                            double count_scale, const double* __restrict__ moments, int max_count,
+                                            double t, double beta, double power, float* __restrict__ out) {
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < n;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int c[3] = {refs[r * ndim], ndim > 1 ? refs[r * ndim + 1] : 0, ndim > 2 ? refs[r * ndim + 2] : 0};
+        const int b[3] = {block.x, block.y, block.z};
+        const int s[3] = {vstride.x, vstride.y, vstride.z};
+        int64_t origin = 0;
+        int P = 1;
+        for (int d = 0; d < ndim; ++d) {
+            origin += static_cast<int64_t>(c[d]) * s[d];
+            P *= b[d];
+        }
+        double msum = 0.0, vsum = 0.0, isum = 0.0;
+        for (int p = 0; p < P; ++p) {
+            int rem = p;
+            int64_t off = 0;
+            for (int d = ndim - 1; d >= 0; --d) {
+                off += static_cast<int64_t>(rem % b[d]) * s[d];
+                rem /= b[d];
+            }
+            double rc = static_cast<double>(vol[origin + off]) / count_scale;
+            if (rc < 0.0) rc = 0.0;
+            const double pooled = rint(2.0 * rc);
+            double m = 1.0, v = 2.0;
+            if (pooled <= static_cast<double>(max_count)) {
+                const int k = static_cast<int>(pooled);
+                m = moments[k];
+                v = moments[max_count + 1 + k];
+            }
+            msum += m;
+            vsum += v;
+            isum += rc;
+        }
+        const double pm = msum / P, pv = vsum / (static_cast<double>(P) * P), inten = isum / P;
+        out[r] = static_cast<float>(pm + t * sqrt(pv > 0.0 ? pv : 0.0) + beta * pow(inten, power));
+    }
+}
+}  // namespace
+
+int32_t launch_reference_thresholds(const float* volume, const int32_t* refs, int64_t n_refs, int ndim,
+                                    const int32_t* counts, const int32_t* block, const int32_t* shape,
+                                    double count_scale, const double* moments, int max_count, double t,
+                                    double beta, double power, float* out, cudaStream_t stream) {
+    if (n_refs == 0) return BMND_OK;
+    int st[3] = {1, 1, 1}, bl[3] = {1, 1, 1}, cn[3] = {1, 1, 1};
+    int64_t sv = 1;
+    for (int d = ndim - 1; d >= 0; --d) {
+        st[d] = static_cast<int>(sv);
+        sv *= shape[d];
+    }
+    for (int d = 0; d < ndim; ++d) {
+        bl[d] = block[d];
+        cn[d] = counts[d];
+    }
+    int64_t blocks = (n_refs + 127) / 128;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    reference_thresholds_kernel<<<static_cast<unsigned>(blocks), 128, 0, stream>>>(
+        volume, refs, n_refs, ndim, make_int3(cn[0], cn[1], cn[2]), make_int3(bl[0], bl[1], bl[2]),
+        make_int3(st[0], st[1], st[2]), count_scale, moments, max_count, t, beta, power, out);
+    BMND_LAUNCH_CHECK("reference_thresholds_kernel");
+    return BMND_OK;
+}
 
 int32_t launch_ssd_threshold(const float* volume, int64_t n, double t, uint32_t* mm, float* thr,
                              cudaStream_t stream) {

@@ -184,7 +184,12 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
                                  const float* thresholds, float scalar_threshold, int32_t* sel,
                                  int32_t* count, int32_t* accepted, cudaStream_t stream,
                                  const float* thr_dev = nullptr, const float* noise_ssd = nullptr,
-                                 float gamma = 0.0f, bool allow_alloc = true);
+                                 float gamma = 0.0f, bool allow_alloc = true,
+                                 const double* null_moments = nullptr, int null_max = 0);
+int32_t launch_reference_thresholds(const float* volume, const int32_t* refs, int64_t n_refs, int ndim,
+                                    const int32_t* counts, const int32_t* block, const int32_t* shape,
+                                    double count_scale, const double* moments, int max_count, double t,
+                                    double beta, double power, float* out, cudaStream_t stream);
 // mm: two uint32 of device scratch; thr: one device float
 int32_t launch_ssd_threshold(const float* volume, int64_t n, double t, uint32_t* mm, float* thr,
                              cudaStream_t stream);

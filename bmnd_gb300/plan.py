@@ -68,14 +68,16 @@ def spatial_forward(profile, ndim: int, stage: str) -> list:
 
 
 def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMatchDistance,
-                 variance_k: int, match_precision: int = _abi.MATCH_EXACT, gauss: dict | None = None
-                 ) -> _abi.StageParams:
+                 variance_k: int, match_precision: int = _abi.MATCH_EXACT, gauss: dict | None = None,
+                 null_table=None) -> _abi.StageParams:
     """Fill the ``StageParams`` of ``stage`` ("ht" or "wiener").
 
     ``gauss`` (stationary Gaussian noise) holds the device tables of the stage:
     ``cov`` (float32 CUDA tensor [lag][coefficient]), ``domain`` (its lag
     domain), ``ssd`` (SSD noise bias over the search offsets, or None) and
-    ``gamma``; without it the stage models direct Poisson noise."""
+    ``gamma``; without it the stage models direct Poisson noise.  ``null_table``
+    (float64 CUDA tensor [2, max_count + 1], ``policies.null_moment_table``)
+    enables the profile's Poisson HT match policy."""
     ndim = len(shape)
     if ndim < 1 or ndim > _abi.MAX_DIMS:
         raise unsupported(f"{ndim}-D volumes are not supported (1 to {_abi.MAX_DIMS} dimensions)")
@@ -133,6 +135,17 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
             else _abi.SOURCE_PILOT
         p.wiener_match_source = _abi.SOURCE_OBSERVATION if profile.poisson_wiener_match_source is obs \
             else _abi.SOURCE_PILOT
+        policy = profile.poisson_ht_match_policy
+        if stage == "ht" and policy is not PoissonHTMatchPolicy.FIXED:
+            if null_table is None:
+                raise ValueError("the Poisson HT match policy needs the null moment table")
+            p.match_policy = (_abi.POLICY_REFERENCE_FINITE_COUNT
+                              if policy is PoissonHTMatchPolicy.REFERENCE_FINITE_COUNT
+                              else _abi.POLICY_CANDIDATE_STANDARDIZED)
+            p.null_max_count = int(profile.poisson_ht_match_moment_max_count)
+            p.null_moments = null_table.data_ptr()
+            p.policy_beta = float(profile.poisson_ht_match_structure_beta)
+            p.policy_power = float(profile.poisson_ht_match_intensity_power)
         mass = profile.poisson_group_mass_conservation
         p.mass_conserve = int(mass is PoissonGroupMassConservation.BOTH
                               or (mass is PoissonGroupMassConservation.HT and stage == "ht")
@@ -175,8 +188,19 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     return p
 
 
+def check_weight_options(profile) -> None:
+    """Reject the aggregation-weight options that are not on the GPU path."""
+    for stage in ("ht", "wiener"):
+        if getattr(profile, f"{stage}_weight_scope") is not AggregationWeightScope.PATCH:
+            raise unsupported("group-scope aggregation weights are not on the GPU path")
+        model = getattr(profile, f"{stage}_weight_model")
+        if model not in (AggregationWeightModel.VARIANCE, AggregationWeightModel.CLASSIC):
+            raise unsupported(f"{model.value!r} aggregation weights are not on the GPU path")
+
+
 def check_gaussian_options(profile) -> None:
     """Reject the Gaussian options that are not on the GPU path."""
+    check_weight_options(profile)
     if profile.reference_schedule_mode not in (
         ReferenceScheduleMode.GENERATED,
         ReferenceScheduleMode.OFF,
@@ -188,8 +212,7 @@ def check_gaussian_options(profile) -> None:
 
 def check_poisson_options(profile) -> None:
     """Reject the non-default Poisson options that are not on the GPU path."""
-    if profile.poisson_ht_match_policy is not PoissonHTMatchPolicy.FIXED:
-        raise unsupported("only the 'fixed' Poisson HT match policy is on the GPU path")
+    check_weight_options(profile)
     if profile.blockmatch_distance is BlockMatchDistance.SSD and float(profile.gamma) != 0.0:
         raise unsupported("the Poisson SSD noise-bias correction (gamma != 0) is not on the GPU path")
     if profile.reference_schedule_mode not in (

@@ -140,9 +140,10 @@ typedef struct BmndStageParams {
     const float* match_noise_ssd;
     float ssd_gamma;
     int32_t reserved1;
-    /* SSD matching threshold multiplier: the threshold is
-     * float32(ssd_threshold * (max - min)^2) over the matched volume
-     * (blockmatching.py:168-184), evaluated on the device */
+    /* the stage's match threshold in float64: for SSD matching the threshold
+     * is float32(ssd_threshold * (max - min)^2) over the matched volume
+     * (blockmatching.py:168-184), evaluated on the device; the
+     * reference-finite-count policy uses it as its multiplier t */
     double ssd_threshold;
     /* Poisson group-mass conservation of this stage (poisson.py:161-265,
      * bmndalgo.py:610-625 / :1023-1038): after the usual aggregation, every
@@ -158,11 +159,22 @@ typedef struct BmndStageParams {
     /* hard-thresholding stage: soft thresholding, sign(c) max(|c| - lambda sigma, 0)
      * (bmndalgo.py:476-486) */
     int32_t soft_threshold;
+    /* Poisson HT match policy (blockmatching.py:29-148, :372-428) */
+    int32_t match_policy;            /* BMND_POLICY_FIXED (default), _REFERENCE_FINITE_COUNT, _CANDIDATE_STANDARDIZED */
+    int32_t null_max_count;          /* poisson_ht_match_moment_max_count */
+    /* device: null means then null variances of the per-voxel distance of two
+     * Poisson counts with a pooled count k = 0..null_max_count, float64 */
+    const double* null_moments;
+    double policy_beta;              /* poisson_ht_match_structure_beta */
+    double policy_power;             /* poisson_ht_match_intensity_power */
 } BmndStageParams;
 
 #define BMND_GAIN_VARIANCE_SCALED 0
 #define BMND_GAIN_CLASSIC 1
 #define BMND_GAIN_NOISE_FLOOR 2
+#define BMND_POLICY_FIXED 0
+#define BMND_POLICY_REFERENCE_FINITE_COUNT 1
+#define BMND_POLICY_CANDIDATE_STANDARDIZED 2
 #define BMND_SOURCE_PILOT 0
 #define BMND_SOURCE_OBSERVATION 1
 

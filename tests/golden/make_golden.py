@@ -308,6 +308,12 @@ OPTION_CASES = {
     "obs_match_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=27),
                           dict(poisson_wiener_match_source="observation")),
     "soft_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=28), dict(ht_use_soft_thresholding=True)),
+    "policy_finite_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=29),
+                              dict(poisson_ht_match_policy="reference_finite_count")),
+    "policy_std_bm3d_40x24": ("bm3d", "ragged2d", dict(shape=(40, 24), seed=30),
+                              dict(poisson_ht_match_policy="candidate_standardized")),
+    "policy_finite_bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=31),
+                                    dict(poisson_ht_match_policy="reference_finite_count")),
 }
 
 

@@ -4,7 +4,8 @@ Cases (``tests/golden/opt_*.npz``, made by ``make_golden.py option``): group-mas
 conservation in both stages (2-D and 3-D) and in the hard-thresholding stage
 only (ragged 2-D); the classic and noise-floor Wiener gains; the observation
 as the Wiener variance source and as the Wiener matching source; soft
-thresholding.
+thresholding; the reference-finite-count and candidate-standardised HT match
+policies.
 
 Stated tolerance (as for the default Poisson pipeline): stage-1 match sets
 equal the reference's except where the selection boundary is tied within the
@@ -62,9 +63,15 @@ def test_option_pipeline_matches_reference(cuda, native, oracle_lib, case):
     thr = float(np.float32(profile.ht_match_threshold))
 
     sel, cnt = matches["ht"]
-    _, _, bad = compare_match_sets(oracle_lib, g["noisy"], blocks["ht"], g["ht_refs"], sel, cnt,
-                                   g["ht_sel"], g["ht_count"], 1, thr)
-    assert not bad, f"{case}/ht: unexplained match-set differences in groups {bad[:8]}"
+    if profile.poisson_ht_match_policy.value == "fixed":
+        _, _, bad = compare_match_sets(oracle_lib, g["noisy"], blocks["ht"], g["ht_refs"], sel, cnt,
+                                       g["ht_sel"], g["ht_count"], 1, thr)
+        assert not bad, f"{case}/ht: unexplained match-set differences in groups {bad[:8]}"
+    else:
+        # per-reference thresholds or standardised distances: the oracle's tie
+        # explanation does not apply; the match sets must still agree almost everywhere
+        same = np.all(sel == g["ht_sel"], axis=1) & (cnt == g["ht_count"])
+        assert same.mean() >= 0.97, (case, "ht match sets", same.mean())
     foot = tie_footprint(shape, blocks["ht"], sel, cnt, g["ht_sel"], g["ht_count"])
     par = output_parity(stages["ht"], g["ht"], g["clean"], exclude=foot)
     assert par["frac_within"] >= 0.999, (case, "ht", par)
