@@ -38,6 +38,7 @@ GROUP_NONE = 2
 
 WEIGHT_CLASSIC = 0
 WEIGHT_VARIANCE = 1
+WEIGHT_RISK = 2
 
 GAIN_VARIANCE_SCALED = 0
 GAIN_CLASSIC = 1
@@ -127,6 +128,8 @@ class StageParams(ctypes.Structure):
         ("null_moments", ctypes.c_void_p),
         ("policy_beta", ctypes.c_double),
         ("policy_power", ctypes.c_double),
+        ("weight_group_scope", _I32),
+        ("reserved3", _I32),
     ]
 
 

@@ -420,9 +420,9 @@ def bmnd(
         return zero
 
     if resolved.is_poisson:
-        plan.check_poisson_options(profile)
+        plan.check_poisson_options(profile, resolved.variance_k)
     else:
-        plan.check_gaussian_options(profile)
+        plan.check_gaussian_options(profile, resolved.variance_k)
 
     torch = _torch()
     if not torch.cuda.is_available():

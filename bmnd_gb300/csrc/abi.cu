@@ -80,8 +80,11 @@ int32_t validate_stage(const BmndStageParams& sp) {
     if (sp.group_transform < 0 || sp.group_transform > 2)
         return fail(BMND_ERR_INVALID_ARG, "unknown group transform");
     if (sp.variance_k < 0) return fail(BMND_ERR_INVALID_ARG, "variance_k must be >= 0");
-    if (sp.weight_model != BMND_WEIGHT_CLASSIC && sp.weight_model != BMND_WEIGHT_VARIANCE)
+    if (sp.weight_model != BMND_WEIGHT_CLASSIC && sp.weight_model != BMND_WEIGHT_VARIANCE &&
+        sp.weight_model != BMND_WEIGHT_RISK)
         return fail(BMND_ERR_INVALID_ARG, "unknown weight model");
+    if (sp.weight_model == BMND_WEIGHT_RISK && sp.filter != BMND_FILTER_WIENER)
+        return fail(BMND_ERR_INVALID_ARG, "risk weights apply to the Wiener stage");
     if (!(sp.count_scale > 0.0) || !std::isfinite(sp.count_scale))
         return fail(BMND_ERR_INVALID_ARG, "count_scale must be finite and positive");
     if (!(sp.variance_floor >= 0.0)) return fail(BMND_ERR_INVALID_ARG, "variance_floor must be >= 0");

@@ -938,7 +938,9 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
     transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, 0);
     if (wiener) transform_group<ND, B0, B1, B2>(geo, a, smem, n, R, 0);
 
-    // ---- shrinkage: coefficients in X, attenuation in V, noise variance in S ----
+    // ---- shrinkage: coefficients in X, attenuation in V, and in S each
+    // coefficient's aggregation error: a^2 (classic), a^2 sigma^2 (variance) or
+    // a^2 sigma^2 + (1 - a)^2 signal power (risk) (aggregationweights.py:213-259) ----
     const float eps_f = static_cast<float>(sp.eps);
     float* SG = sm<float>(smem, a.L.sg);
     float sig_sum = 0.0f;  // Wiener sigma map: this thread's share of the group's sigma sum
@@ -950,6 +952,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         }
         float nv = mul_rn(sig, sig);
         float att;
+        float spw = 0.0f;  // Wiener signal power (risk weights)
         if (!wiener && sp.soft_threshold) {
             // soft thresholding (bmndalgo.py:476-486): sign(c) max(|c| - lambda sigma, 0)
             const float thr = mul_rn(sp.ht_lambda, sig);
@@ -958,7 +961,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
             att = mag > 0.0f ? div_rn(shr, mag) : 0.0f;
             X[e] = copysignf(shr, X[e]);
             V[e] = att;
-            S[e] = nv;
+            S[e] = sp.weight_model == BMND_WEIGHT_CLASSIC ? att * att : att * att * nv;
             continue;
         } else if (!wiener && gauss) {
             // |c| >= lambda sigma, the group DC always kept (bmndalgo.py:462-475)
@@ -975,6 +978,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
             float den = add_rn(pr, eff);
             float gain = den > 0.0f ? div_rn(pr, den) : 0.0f;
             att = fminf(fmaxf(gain, 0.0f), 1.0f);
+            spw = pr;
         } else {
             // signal power by gain mode (wiener.py:24-47)
             float eff = mul_rn(sp.wiener_scale, nv);
@@ -987,10 +991,17 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
             }
             float gain = div_rn(spow, add_rn(add_rn(spow, eff), eps_f));
             att = fminf(fmaxf(gain, 0.0f), 1.0f);
+            spw = spow;
         }
         X[e] = mul_rn(X[e], att);
         V[e] = att;
-        S[e] = nv;
+        float err = att * att;
+        if (sp.weight_model != BMND_WEIGHT_CLASSIC) err *= nv;
+        if (sp.weight_model == BMND_WEIGHT_RISK) {
+            const float rj = 1.0f - att;
+            err += rj * rj * spw;
+        }
+        S[e] = err;
     }
     __syncthreads();
 
@@ -1020,9 +1031,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
         for (int g = warp; g < n; g += nwarps) {
             float risk = 0.0f;
             for (int j = lane; j < P; j += 32) {
-                const float at = V[g * P + j];
-                float err = at * at;
-                if (sp.weight_model != BMND_WEIGHT_CLASSIC) err *= S[g * P + j];
+                float err = S[g * P + j];
                 if (sp.windowed_synthesis) err *= static_cast<float>(mdiag[j]);
                 risk += err;
             }
@@ -1034,9 +1043,15 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kerne
     __syncthreads();
     if (tid < n) {
         float risk = 0.0f;
-        for (int g = 0; g < n; ++g) {
-            const float gi = G[g * n + tid];  // Ginv[o, g] = G[g, o]
-            risk = fmaf(gi * gi, static_cast<float>(plane[g]), risk);
+        if (sp.weight_group_scope) {
+            // one weight for the whole group: the summed risk (the group
+            // transforms are orthonormal, so the group metric is the identity)
+            for (int g = 0; g < n; ++g) risk += static_cast<float>(plane[g]);
+        } else {
+            for (int g = 0; g < n; ++g) {
+                const float gi = G[g * n + tid];  // Ginv[o, g] = G[g, o]
+                risk = fmaf(gi * gi, static_cast<float>(plane[g]), risk);
+            }
         }
         wts[tid] = (isfinite(risk) && risk >= 0.0f) ? 1.0f / (risk + static_cast<float>(sp.eps)) : 0.0f;
     }

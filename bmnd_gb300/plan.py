@@ -92,10 +92,7 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     model = getattr(profile, f"{stage}_weight_model")
     domain = getattr(profile, f"{stage}_weight_domain")
     scope = getattr(profile, f"{stage}_weight_scope")
-    if scope is not AggregationWeightScope.PATCH:
-        raise unsupported("group-scope aggregation weights are not on the GPU path")
-    if model not in (AggregationWeightModel.VARIANCE, AggregationWeightModel.CLASSIC):
-        raise unsupported(f"{model.value!r} aggregation weights are not on the GPU path")
+    _check_stage_weights(stage, model, domain, scope, variance_k)
 
     group_kind, spatial = resolve_axes(getattr(profile, f"{stage}_transform"), ndim)
     p = _abi.StageParams()
@@ -112,9 +109,10 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     p.filter = _abi.FILTER_HARD_THRESHOLD if stage == "ht" else _abi.FILTER_WIENER
     p.group_transform = _GROUP_CODES[group_kind]
     p.variance_k = int(variance_k)
-    p.weight_model = (
-        _abi.WEIGHT_VARIANCE if model is AggregationWeightModel.VARIANCE else _abi.WEIGHT_CLASSIC
-    )
+    p.weight_model = {AggregationWeightModel.VARIANCE: _abi.WEIGHT_VARIANCE,
+                      AggregationWeightModel.CLASSIC: _abi.WEIGHT_CLASSIC,
+                      AggregationWeightModel.RISK: _abi.WEIGHT_RISK}[model]
+    p.weight_group_scope = int(scope is AggregationWeightScope.GROUP)
     p.windowed_synthesis = int(domain is AggregationWeightDomain.WINDOWED_SYNTHESIS)
     p.match_threshold = float(np.float32(getattr(profile, f"{stage}_match_threshold")))
     p.ht_lambda = float(profile.ht_lambda_threshold)
@@ -188,19 +186,28 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     return p
 
 
-def check_weight_options(profile) -> None:
+def _check_stage_weights(stage, model, domain, scope, variance_k) -> None:
+    if model is AggregationWeightModel.RISK and stage != "wiener":
+        raise unsupported("risk aggregation weights apply to the Wiener stage only")
+    exact = (model in (AggregationWeightModel.VARIANCE, AggregationWeightModel.RISK)
+             and domain is AggregationWeightDomain.WINDOWED_SYNTHESIS
+             and scope is AggregationWeightScope.GROUP and int(variance_k) > 0)
+    if exact:
+        raise unsupported("the covariance-aware exact group weighting (group scope, windowed synthesis, k > 0) "
+                          "is not on the GPU path")
+
+
+def check_weight_options(profile, variance_k: int) -> None:
     """Reject the aggregation-weight options that are not on the GPU path."""
     for stage in ("ht", "wiener"):
-        if getattr(profile, f"{stage}_weight_scope") is not AggregationWeightScope.PATCH:
-            raise unsupported("group-scope aggregation weights are not on the GPU path")
-        model = getattr(profile, f"{stage}_weight_model")
-        if model not in (AggregationWeightModel.VARIANCE, AggregationWeightModel.CLASSIC):
-            raise unsupported(f"{model.value!r} aggregation weights are not on the GPU path")
+        _check_stage_weights(stage, getattr(profile, f"{stage}_weight_model"),
+                             getattr(profile, f"{stage}_weight_domain"),
+                             getattr(profile, f"{stage}_weight_scope"), variance_k)
 
 
-def check_gaussian_options(profile) -> None:
+def check_gaussian_options(profile, variance_k: int) -> None:
     """Reject the Gaussian options that are not on the GPU path."""
-    check_weight_options(profile)
+    check_weight_options(profile, variance_k)
     if profile.reference_schedule_mode not in (
         ReferenceScheduleMode.GENERATED,
         ReferenceScheduleMode.OFF,
@@ -210,9 +217,9 @@ def check_gaussian_options(profile) -> None:
         )
 
 
-def check_poisson_options(profile) -> None:
+def check_poisson_options(profile, variance_k: int) -> None:
     """Reject the non-default Poisson options that are not on the GPU path."""
-    check_weight_options(profile)
+    check_weight_options(profile, variance_k)
     if profile.blockmatch_distance is BlockMatchDistance.SSD and float(profile.gamma) != 0.0:
         raise unsupported("the Poisson SSD noise-bias correction (gamma != 0) is not on the GPU path")
     if profile.reference_schedule_mode not in (

@@ -64,6 +64,7 @@ extern "C" {
 /* aggregation weight model (src/bmnd/enums.py:30-33); scope is always "patch" */
 #define BMND_WEIGHT_CLASSIC 0
 #define BMND_WEIGHT_VARIANCE 1
+#define BMND_WEIGHT_RISK 2 /* Wiener stage only: adds (1 - a)^2 x signal power */
 
 /* noise model of a stage */
 #define BMND_NOISE_POISSON 0  /* variance volume max(count_scale * max(x, 0), floor) */
@@ -167,6 +168,10 @@ typedef struct BmndStageParams {
     const double* null_moments;
     double policy_beta;              /* poisson_ht_match_structure_beta */
     double policy_power;             /* poisson_ht_match_intensity_power */
+    /* one aggregation weight per group (weight_scope "group") instead of one
+     * per patch; the covariance-aware exact weighting is not available */
+    int32_t weight_group_scope;
+    int32_t reserved3;
 } BmndStageParams;
 
 #define BMND_GAIN_VARIANCE_SCALED 0

@@ -314,6 +314,15 @@ OPTION_CASES = {
                               dict(poisson_ht_match_policy="candidate_standardized")),
     "policy_finite_bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=31),
                                     dict(poisson_ht_match_policy="reference_finite_count")),
+    "risk_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=32), dict(wiener_weight_model="risk")),
+    "group_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=33),
+                      dict(ht_weight_scope="group", wiener_weight_scope="group")),
+    "group_windowed_k0_bm3d_40x24": ("bm3d", "ragged2d", dict(shape=(40, 24), seed=34),
+                                     dict(ht_weight_scope="group", ht_weight_domain="windowed_synthesis",
+                                          wiener_weight_scope="group", wiener_weight_domain="windowed_synthesis",
+                                          k=0)),
+    "risk_windowed_bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=35),
+                                    dict(wiener_weight_model="risk", wiener_weight_domain="windowed_synthesis")),
 }
 
 

@@ -169,7 +169,7 @@ def test_unsupported_options_raise_not_implemented():
     with pytest.raises(NotImplementedError):
         bg.bmnd(vol, bg.BM3DProfile(reference_schedule_mode="official"), sigma=1.0)
     with pytest.raises(NotImplementedError):
-        bg.bmnd(vol, _poisson(ht_weight_scope="group"))
+        bg.bmnd(vol, _poisson(ht_weight_scope="group", ht_weight_domain="windowed_synthesis"))
 
 
 def test_stage_params_defaults():
