@@ -578,7 +578,7 @@ __device__ void exact_planes_any(const float* __restrict__ lval, const int* __re
 }
 
 template <int ND, int B0, int B1, int B2, int NT>
-__global__ void __launch_bounds__(NT, NT == kThreads ? 2 : 1) group_filter_kernel(FilterArgs a) {
+__global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) group_filter_kernel(FilterArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     using GM = Geom<ND, B0, B1, B2>;
     const BmndStageParams& sp = a.sp;
