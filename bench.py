@@ -237,7 +237,8 @@ def time_kernels(torch, noisy_t, profile, reps: int = 2, stages=("ht", "wiener")
     for stage in stages:
         stage_prec = precision[stage]
         p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k,
-                              stage_prec if stage_prec == _abi.MATCH_APPROX else _abi.MATCH_EXACT,
+                              stage_prec if stage_prec in (_abi.MATCH_APPROX, _abi.MATCH_SUBSAMPLED)
+                              else _abi.MATCH_EXACT,
                               None if gauss is None else gauss[stage])
         block = tuple(getattr(profile, f"{stage}_block_size"))
         counts = tuple(s - b + 1 for s, b in zip(shape, block))
@@ -308,12 +309,17 @@ def time_kernels(torch, noisy_t, profile, reps: int = 2, stages=("ht", "wiener")
             hi = np.minimum(refs_h[:, a] + p.search_radius[a], counts[a] - 1)
             pairs *= hi - lo + 1
         P = int(np.prod(block))
+        terms = int(pairs.sum()) * P
+        if stage_prec == _abi.MATCH_SUBSAMPLED:
+            # the even sub-lattice for every candidate, the full patch for 4 K of them
+            ps = int(np.prod([(b + 1) // 2 for b in block]))
+            terms = int(pairs.sum()) * ps + n * min(4 * p.max_stack, 512) * P
         res[stage] = {
             "match_ms": float(np.median(times)),
             "stage_ms": float(np.median(stimes)),
             "groups": n,
             "pairs": int(pairs.sum()),
-            "voxel_terms": int(pairs.sum()) * P,
+            "voxel_terms": terms,
             "mean_group": float(counts_h.mean()),
             "P": P,
         }
@@ -435,7 +441,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     if fast is not None:
         fprof = pl.fast_profile(profile)
         kf = time_kernels(torch, x, fprof, stages=("wiener",), pilot=fast["pilot"],
-                          precision={"wiener": _abi.MATCH_APPROX})
+                          precision={"wiener": bg.api._MATCH_PRECISIONS[pl.FAST_MATCH_PRECISION]})
         kt["fast_wiener"] = kf["wiener"]
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -445,7 +451,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         e1.synchronize()
         kt["pilot_net_ms"] = e0.elapsed_time(e1) / 3
         k = kf["wiener"]
-        cands.append((k["match_ms"], "blockmatch_wiener_approx", "fast_wiener"))
+        cands.append((k["match_ms"], f"blockmatch_wiener_{pl.FAST_MATCH_PRECISION}", "fast_wiener"))
         cands.append((k["stage_ms"] - k["match_ms"], "groupfilter_wiener_fast", "fast_wiener"))
         cands.append((kt["pilot_net_ms"], "pilot_net", None))
     else:
@@ -473,7 +479,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
                 "what": "SSD voxel terms" if gauss is not None else "Poisson-deviance voxel terms",
                 "achieved_gterms_s": k["voxel_terms"] / (dom_ms * 1e-3) / 1e9,
             }
-            if dom_name == "blockmatch_wiener_approx":
+            if dom_name in ("blockmatch_wiener_approx", "blockmatch_wiener_subsampled"):
                 # one lg2 per term on the SFU (16 results per clock per SM)
                 sfu = 152 * 16 * sm_mhz * 1e6
                 compute["sfu_bound_gterms_s"] = sfu / 1e9
@@ -482,7 +488,19 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
             # read noisy (+ pilot) once, write float64 numerator and denominator once
             alg_bytes = nvox * (8 if wiener else 4) + nvox * 16
             kk = min(int(fprof.k) if dom_stage == "fast_wiener" else 4, int(k["mean_group"]))
-            if gauss is not None:
+            if kk == 0 and gauss is None:
+                # no exact planes: the separable transforms dominate.  Per group four
+                # passes (observation, pilot, squared variance forward; inverse), each
+                # n P (sum of the patch edges) spatial plus n^2 P group-axis multiply-adds
+                n_ = k["mean_group"]
+                edges = float(sum(getattr(fprof if dom_stage == "fast_wiener" else profile, "wiener_block_size")))
+                macs = k["groups"] * 4 * (n_ * k["P"] * edges + n_ * n_ * k["P"])
+                compute = {
+                    "what": "separable transform multiply-adds (four passes per group)",
+                    "achieved_tmacs_s": macs / (dom_ms * 1e-3) / 1e12,
+                    "fp32_ops_frac_of_peak": 2 * macs / (dom_ms * 1e-3) / fp32_peak,
+                }
+            elif gauss is not None:
                 n_ = k["mean_group"]
                 terms = k["groups"] * (n_ * (n_ + 1) / 2) * k["P"] * kk
                 compute = {
@@ -508,7 +526,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         psnr_fast = psnr(fast["out"].cpu().numpy(), clean)
         fast_block = {
             "path": "learned pilot (BF16 tensor-core residual net) + per-tile deviance fallback + Wiener stage "
-                    "with reference step 4, approximate Poisson sigma, approximate screening",
+                    f"with reference step 4, approximate Poisson sigma, {pl.FAST_MATCH_PRECISION} screening",
             "value": nvox * world / (fast["ms"] * 1e-3) / 1e6,
             "ms_per_step": fast["ms"],
             "psnr_db": psnr_fast,

@@ -55,6 +55,7 @@ NOISE_GAUSSIAN = 1
 MATCH_EXACT = 0
 MATCH_FAST = 1
 MATCH_APPROX = 2
+MATCH_SUBSAMPLED = 3
 CONV_TCGEN05 = 0
 CONV_MMA_SYNC = 1
 

@@ -152,7 +152,8 @@ def _match_result(schedule: plan.Schedule, counts, sel, cnt, acc) -> BlockMatchR
     return BlockMatchResult(groups=groups)
 
 
-_MATCH_PRECISIONS = {"exact": _abi.MATCH_EXACT, "fast": _abi.MATCH_FAST, "approx": _abi.MATCH_APPROX}
+_MATCH_PRECISIONS = {"exact": _abi.MATCH_EXACT, "fast": _abi.MATCH_FAST, "approx": _abi.MATCH_APPROX,
+                     "subsampled": _abi.MATCH_SUBSAMPLED}
 
 
 _NULL_TABLES: dict = {}
@@ -372,7 +373,8 @@ def bmnd(
         _validate_sigma(sigma)
     _validate_max_cache_bytes(max_cache_bytes)
     if match_precision not in _MATCH_PRECISIONS:
-        raise ValueError(f"match_precision must be 'exact', 'fast' or 'approx', got {match_precision!r}.")
+        raise ValueError(
+            f"match_precision must be 'exact', 'fast', 'approx' or 'subsampled', got {match_precision!r}.")
 
     torch_input = type(volume).__module__.startswith("torch")
     shape = tuple(int(s) for s in volume.shape)

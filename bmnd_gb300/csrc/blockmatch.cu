@@ -70,6 +70,11 @@ struct MatchArgs {
     // threshold computed on the device (one float), overrides the scalar one
     const float* thr_dev;
     int32_t no_alloc;  // 1: no stream-ordered scratch (approx mode then runs the bounded form)
+    // subsampled mode: prescreen on the patch's even sub-lattice (box sums in
+    // boxb_sub), then the screening form for the presel smallest
+    int32_t sub;
+    int32_t presel;
+    const float* boxb_sub;
     // candidate standardisation (blockmatching.py:372-428): null means then
     // variances by pooled count 0..null_max, or null
     const double* null_moments;
@@ -555,8 +560,9 @@ __global__ void approx_voxel_kernel(const float* __restrict__ src, float inv, in
     }
 }
 
-// boxb[o] = sum over the patch at origin o of bv (0 where no patch starts)
-template <int ND, int B0, int B1, int B2>
+// boxb[o] = sum over the patch at origin o of bv (0 where no patch starts);
+// S = 2: over the patch's even sub-lattice only
+template <int ND, int B0, int B1, int B2, int S>
 __global__ void approx_box_kernel(const float* __restrict__ bv, int n0, int n1, int n2, float* __restrict__ boxb) {
     const int64_t n = static_cast<int64_t>(n0) * n1 * n2;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
@@ -567,13 +573,13 @@ __global__ void approx_box_kernel(const float* __restrict__ bv, int n0, int n1, 
         float sum = 0.0f;
         if (ND == 3 ? (z <= n0 - B0 && y <= n1 - B1 && x <= n2 - B2) : (y <= n1 - B0 && x <= n2 - B1)) {
 #pragma unroll 1
-            for (int a0 = 0; a0 < B0; ++a0) {
+            for (int a0 = 0; a0 < B0; a0 += S) {
 #pragma unroll
-                for (int a1 = 0; a1 < (ND == 3 ? B1 : 1); ++a1) {
+                for (int a1 = 0; a1 < (ND == 3 ? B1 : 1); a1 += (ND == 3 ? S : 1)) {
                     const float* row = ND == 3 ? bv + i + (static_cast<int64_t>(a0) * n1 + a1) * n2
                                                : bv + i + static_cast<int64_t>(a0) * n2;
 #pragma unroll
-                    for (int a2 = 0; a2 < (ND == 3 ? B2 : B1); ++a2) sum += __ldg(row + a2);
+                    for (int a2 = 0; a2 < (ND == 3 ? B2 : B1); a2 += S) sum += __ldg(row + a2);
                 }
             }
         }
@@ -583,7 +589,15 @@ __global__ void approx_box_kernel(const float* __restrict__ bv, int n0, int n1, 
 
 // -sum_p s_p log2 s_p for the XR candidates at origin + j (j < XR) along x;
 // ref[p].y holds max(r, 2^-100), so s > 0; xroom voxels of the row exist
-template <int ND, int B0, int B1, int B2, int XR>
+// whether patch element p (C order) lies on the even sub-lattice of the patch
+template <int ND, int B0, int B1, int B2>
+__device__ __forceinline__ bool sub_lattice(int p) {
+    if (ND == 3) return ((p / (B1 * B2)) % 2 == 0) && (((p / B2) % B1) % 2 == 0) && ((p % B2) % 2 == 0);
+    return ((p / B1) % 2 == 0) && ((p % B1) % 2 == 0);
+}
+
+// S = 1: every patch element; S = 2: the even sub-lattice only
+template <int ND, int B0, int B1, int B2, int XR, int S>
 __device__ __forceinline__ void approx_unit(const float2* __restrict__ ref, const float* __restrict__ cv,
                                             int64_t origin, int64_t s0, int64_t s1, int xroom, float (&acc)[XR]) {
     constexpr int BX = ND == 3 ? B2 : B1;  // patch extent along x
@@ -593,15 +607,15 @@ __device__ __forceinline__ void approx_unit(const float2* __restrict__ ref, cons
     for (int j = 0; j < XR; ++j) acc[j] = 0.0f;
     const float* base = cv + origin;
 #pragma unroll 1
-    for (int a0 = 0; a0 < B0; ++a0) {
+    for (int a0 = 0; a0 < B0; a0 += S) {
 #pragma unroll
-        for (int a1 = 0; a1 < BR; ++a1) {
+        for (int a1 = 0; a1 < BR; a1 += (ND == 3 ? S : 1)) {
             const float* row = base + a0 * s0 + (ND == 3 ? a1 * s1 : 0);
             float xv[NL];
 #pragma unroll
             for (int i = 0; i < NL; ++i) xv[i] = i < xroom ? __ldg(row + i) : 0.0f;
 #pragma unroll
-            for (int ax = 0; ax < BX; ++ax) {
+            for (int ax = 0; ax < BX; ax += S) {
                 const float r = ref[(a0 * BR + a1) * BX + ax].y;
 #pragma unroll
                 for (int j = 0; j < XR; ++j) {
@@ -719,17 +733,28 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
         const bool small_window = window < (int64_t(1) << 21);
         __syncthreads();  // previous reference's shared data is no longer read
         const bool cheap = fixed && a.approx && a.cv != nullptr;
-        float sa = 0.0f;  // cheap mode: sum_p A_r
+        float sa = 0.0f, sa_sub = 0.0f;  // cheap mode: sum_p A_r over the patch and over its even sub-lattice
         for (int p = tid; p < P; p += blockDim.x) {
             float rv = mul_rn(__ldg(a.src + center_origin + poff_s[p]), a.inv_scale);
             if (rv < 0.0f) rv = 0.0f;
-            if (cheap) sa += rv > 0.0f ? rv + rv * log2f(rv) : 0.0f;
+            if (cheap) {
+                const float av = rv > 0.0f ? rv + rv * log2f(rv) : 0.0f;
+                sa += av;
+                if constexpr (ND > 0)
+                    if (sub_lattice<ND, B0, B1, B2>(p)) sa_sub += av;
+            }
             ref[p] = make_float2(rv, cheap ? fmaxf(rv, 7.88860905e-31f) : rv + rv);
         }
         if (cheap) {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) sa += __shfl_xor_sync(0xffffffffu, sa, o);
-            if (lane == 0) redf[4 + warp] = sa;
+            for (int o = 16; o > 0; o >>= 1) {
+                sa += __shfl_xor_sync(0xffffffffu, sa, o);
+                sa_sub += __shfl_xor_sync(0xffffffffu, sa_sub, o);
+            }
+            if (lane == 0) {
+                redf[4 + warp] = sa;
+                reinterpret_cast<float*>(redi + 16)[warp] = sa_sub;
+            }
         }
         for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0u;
         if (tid == 0) {
@@ -740,67 +765,8 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
         const float thr = a.thresholds ? a.thresholds[r] : (a.thr_dev ? *a.thr_dev : a.scalar_threshold);
         const float tkey = canonical_key(thr);
 
-        // pass A: screening distances and the reference-wide absolute bound
-        float dmax = 0.0f;
-        if (cheap) {
-            if constexpr (ND > 0) {
-                constexpr int XR = BMND_APPROX_XR;
-                constexpr int BX = ND == 3 ? B2 : B1;
-                const float sum_a = redf[4] + redf[5] + redf[6] + redf[7];
-                const int ex = ext[ND - 1];
-                const int nu = (ex + XR - 1) / XR;
-                const float inv_nu = 1.0f / static_cast<float>(nu);
-                const int nx = a.counts[ND - 1] + BX - 1;  // voxels along x
-                const int64_t units = window / ex * nu;
-                for (int64_t u = tid; u < units; u += blockDim.x) {
-                    // unit -> (row of the window, x run); rows are C-ordered over the outer axes
-                    const int ui = static_cast<int>(u);
-                    const int rowi = small_div(ui, inv_nu);
-                    const int k = ui - rowi * nu;
-                    int64_t origin = 0;
-                    if (ND == 3) {
-                        const int i0 = small_div(rowi, inv_ext[1]);
-                        const int i1 = rowi - i0 * ext[1];
-                        origin = static_cast<int64_t>(lo[0] + i0) * a.grid_stride[0] +
-                                 static_cast<int64_t>(lo[1] + i1) * a.grid_stride[1];
-                    } else {
-                        origin = static_cast<int64_t>(lo[0] + rowi) * a.grid_stride[0];
-                    }
-                    const int x0 = lo[ND - 1] + k * XR;
-                    origin += x0;
-                    float acc[XR];
-                    approx_unit<ND, B0, B1, B2, XR>(ref, a.cv, origin, a.vstride[0], a.vstride[ND > 1 ? 1 : 0],
-                                                    nx - x0, acc);
-                    const int64_t c0 = static_cast<int64_t>(rowi) * ex + k * XR;
-                    const int nvalid = min(XR, ex - k * XR);
-#pragma unroll
-                    for (int j = 0; j < XR; ++j) {
-                        if (j < nvalid) {
-                            const float d = 1.38629436f * (sum_a + __ldg(a.boxb + origin + j) + acc[j]);
-                            cand[c0 + j] = fmaxf(d, 0.0f) / static_cast<float>(P);
-                        }
-                    }
-                }
-            }
-        } else {
-            for (int64_t c = tid; c < window; c += blockDim.x) {
-                int64_t lin;
-                const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
-                const float2 sd = fixed ? screen_deviance_fixed<ND, B0, B1, B2>(ref, a.src, origin, a.vstride[0],
-                                                                                a.vstride[ND > 1 ? 1 : 0], poff_s)
-                                        : screen_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
-                cand[c] = sd.x;
-                dmax = fmaxf(dmax, sd.y);
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-        if (lane == 0) redf[warp] = dmax;
-        __syncthreads();
-        float Dabs = redf[0];
-        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) Dabs = fmaxf(Dabs, redf[w]);
-        if (a.approx) Dabs = 0.0f;
-
+        float Dabs = 0.0f;  // the reference-wide absolute bound, set after pass A
+        const float drel_k = drel;
         // radix select over the upper bounds d + D of the certainly accepted
         // (of every candidate with `all`): the smallest v with >= need of them
         // bounded by it, or infinity when there are fewer
@@ -823,7 +789,7 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                     uint32_t bin = 0;
                     if (c < window) {
                         const float dv = cand[c];
-                        const float up = dv + (Dabs + drel * dv);
+                        const float up = dv + (Dabs + drel_k * dv);
                         if (all || canonical_key(up) < tkey) {
                             const uint32_t bits = __float_as_uint(up);
                             if (pass == 0 || (bits >> (32 - 8 * pass)) == prefix) {
@@ -898,6 +864,138 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
             }
             return found ? __uint_as_float((prefix << 8) | 0xffu) : INFINITY;
         };
+
+        // pass A: screening distances and the reference-wide absolute bound
+        float dmax = 0.0f;
+        if (cheap && !a.sub) {
+            if constexpr (ND > 0) {
+                constexpr int XR = BMND_APPROX_XR;
+                constexpr int BX = ND == 3 ? B2 : B1;
+                const float sum_a = redf[4] + redf[5] + redf[6] + redf[7];
+                const int ex = ext[ND - 1];
+                const int nu = (ex + XR - 1) / XR;
+                const float inv_nu = 1.0f / static_cast<float>(nu);
+                const int nx = a.counts[ND - 1] + BX - 1;  // voxels along x
+                const int64_t units = window / ex * nu;
+                for (int64_t u = tid; u < units; u += blockDim.x) {
+                    // unit -> (row of the window, x run); rows are C-ordered over the outer axes
+                    const int ui = static_cast<int>(u);
+                    const int rowi = small_div(ui, inv_nu);
+                    const int k = ui - rowi * nu;
+                    int64_t origin = 0;
+                    if (ND == 3) {
+                        const int i0 = small_div(rowi, inv_ext[1]);
+                        const int i1 = rowi - i0 * ext[1];
+                        origin = static_cast<int64_t>(lo[0] + i0) * a.grid_stride[0] +
+                                 static_cast<int64_t>(lo[1] + i1) * a.grid_stride[1];
+                    } else {
+                        origin = static_cast<int64_t>(lo[0] + rowi) * a.grid_stride[0];
+                    }
+                    const int x0 = lo[ND - 1] + k * XR;
+                    origin += x0;
+                    float acc[XR];
+                    approx_unit<ND, B0, B1, B2, XR, 1>(ref, a.cv, origin, a.vstride[0], a.vstride[ND > 1 ? 1 : 0],
+                                                       nx - x0, acc);
+                    const int64_t c0 = static_cast<int64_t>(rowi) * ex + k * XR;
+                    const int nvalid = min(XR, ex - k * XR);
+#pragma unroll
+                    for (int j = 0; j < XR; ++j) {
+                        if (j < nvalid) {
+                            const float d = 1.38629436f * (sum_a + __ldg(a.boxb + origin + j) + acc[j]);
+                            cand[c0 + j] = fmaxf(d, 0.0f) / static_cast<float>(P);
+                        }
+                    }
+                }
+            }
+        } else if (cheap) {
+            // subsampled mode, pass A': the same screening form on the even
+            // sub-lattice of the patch for every candidate, then the full form
+            // for the a.presel smallest; the rest are out of the race
+            if constexpr (ND > 0) {
+                constexpr int XR = BMND_APPROX_XR;
+                constexpr int BX = ND == 3 ? B2 : B1;
+                constexpr int PS = ((B0 + 1) / 2) * ((B1 + 1) / 2) * (ND == 3 ? (B2 + 1) / 2 : 1);
+                const float* fs = reinterpret_cast<const float*>(redi + 16);
+                const float sum_s = fs[0] + fs[1] + fs[2] + fs[3];
+                const int ex = ext[ND - 1];
+                const int nu = (ex + XR - 1) / XR;
+                const float inv_nu = 1.0f / static_cast<float>(nu);
+                const int nx = a.counts[ND - 1] + BX - 1;
+                const int64_t units = window / ex * nu;
+                for (int64_t u = tid; u < units; u += blockDim.x) {
+                    const int ui = static_cast<int>(u);
+                    const int rowi = small_div(ui, inv_nu);
+                    const int k = ui - rowi * nu;
+                    int64_t origin = 0;
+                    if (ND == 3) {
+                        const int i0 = small_div(rowi, inv_ext[1]);
+                        const int i1 = rowi - i0 * ext[1];
+                        origin = static_cast<int64_t>(lo[0] + i0) * a.grid_stride[0] +
+                                 static_cast<int64_t>(lo[1] + i1) * a.grid_stride[1];
+                    } else {
+                        origin = static_cast<int64_t>(lo[0] + rowi) * a.grid_stride[0];
+                    }
+                    const int x0 = lo[ND - 1] + k * XR;
+                    origin += x0;
+                    float acc[XR];
+                    approx_unit<ND, B0, B1, B2, XR, 2>(ref, a.cv, origin, a.vstride[0], a.vstride[ND > 1 ? 1 : 0],
+                                                       nx - x0, acc);
+                    const int64_t c0 = static_cast<int64_t>(rowi) * ex + k * XR;
+                    const int nvalid = min(XR, ex - k * XR);
+#pragma unroll
+                    for (int j = 0; j < XR; ++j) {
+                        if (j < nvalid) {
+                            const float d = 1.38629436f * (sum_s + __ldg(a.boxb_sub + origin + j) + acc[j]);
+                            cand[c0 + j] = fmaxf(d, 0.0f) / static_cast<float>(PS);
+                        }
+                    }
+                }
+                __syncthreads();
+                const float vs = select_kth(a.presel, true);
+                const float vskey = canonical_key(vs);
+                if (tid == 0) redi[0] = 0;
+                __syncthreads();
+                for (int64_t c = tid; c < window; c += blockDim.x) {
+                    if (canonical_key(cand[c]) <= vskey) {
+                        const int slot = atomicAdd(redi, 1);
+                        if (slot < kSQueue) qidx[slot] = static_cast<int32_t>(c);
+                    }
+                    cand[c] = 1e30f;  // out of the race (finite: the bound arithmetic below stays NaN-free)
+                }
+                __syncthreads();
+                const int nsel = min(redi[0], kSQueue);
+                const float sum_a = redf[4] + redf[5] + redf[6] + redf[7];
+                for (int i = tid; i < nsel; i += blockDim.x) {
+                    int64_t lin;
+                    const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, qidx[i], &lin);
+                    float acc[1];
+                    approx_unit<ND, B0, B1, B2, 1, 1>(ref, a.cv, origin, a.vstride[0], a.vstride[ND > 1 ? 1 : 0],
+                                                      BX, acc);
+                    const float d = 1.38629436f * (sum_a + __ldg(a.boxb + origin) + acc[0]);
+                    cand[qidx[i]] = fmaxf(d, 0.0f) / static_cast<float>(P);
+                }
+                __syncthreads();
+                if (tid == 0) redi[0] = 0;
+            }
+        } else {
+            for (int64_t c = tid; c < window; c += blockDim.x) {
+                int64_t lin;
+                const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
+                const float2 sd = fixed ? screen_deviance_fixed<ND, B0, B1, B2>(ref, a.src, origin, a.vstride[0],
+                                                                                a.vstride[ND > 1 ? 1 : 0], poff_s)
+                                        : screen_deviance(ref, a.src, origin, poff_s, P, a.inv_scale);
+                cand[c] = sd.x;
+                dmax = fmaxf(dmax, sd.y);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        if (lane == 0) redf[warp] = dmax;
+        __syncthreads();
+        Dabs = redf[0];
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) Dabs = fmaxf(Dabs, redf[w]);
+        if (a.approx) Dabs = 0.0f;
+
         const float vstar = select_kth(K, false);
         // at least K certainly accepted candidates have exact distances <= vstar
         const float vkey = canonical_key(vstar);
@@ -1428,7 +1526,9 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     if (a.n_refs == 0) return BMND_OK;
     int64_t wmax = 1;
     for (int d = 0; d < a.ndim; ++d) wmax *= std::min<int64_t>(2 * a.radius[d] + 1, a.counts[d]);
-    a.approx = precision == BMND_MATCH_APPROX;
+    a.approx = precision == BMND_MATCH_APPROX || precision == BMND_MATCH_SUBSAMPLED;
+    a.sub = precision == BMND_MATCH_SUBSAMPLED;
+    a.presel = std::min(4 * a.max_m, kSQueue);
     if (a.null_moments) {
         // candidate standardisation: exact warp kernel, per-term evaluation
         a.use_table = 0;
@@ -1436,6 +1536,7 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     }
     const bool screened = code == BMND_DIST_POISSON_DEVIANCE && a.stab &&
                           (precision == BMND_MATCH_FAST || precision == BMND_MATCH_APPROX ||
+                           precision == BMND_MATCH_SUBSAMPLED ||
                            precision == BMND_MATCH_REAL_VALUED) &&
                           a.max_m <= 32 && screened_smem_bytes(a.max_m, a.P, wmax) <= 200 * 1024;
     if (!screened) {
@@ -1459,24 +1560,30 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
             n[3 - a.ndim + d] = a.counts[d] + a.block[d] - 1;
             nvox *= n[3 - a.ndim + d];
         }
-        if (cudaMallocAsync(reinterpret_cast<void**>(&aux), static_cast<size_t>(nvox) * 3 * sizeof(float), stream) ==
-            cudaSuccess) {
+        if (cudaMallocAsync(reinterpret_cast<void**>(&aux), static_cast<size_t>(nvox) * (a.sub ? 4 : 3) * sizeof(float),
+                            stream) == cudaSuccess) {
             float* cv = aux;
             float* bv = aux + nvox;
             float* boxb = aux + 2 * nvox;
+            float* boxb_sub = a.sub ? aux + 3 * nvox : nullptr;
             int64_t nb = (nvox + 255) / 256;
             if (nb > 152 * 16) nb = 152 * 16;
             approx_voxel_kernel<<<static_cast<unsigned>(nb), 256, 0, stream>>>(a.src, a.inv_scale, nvox, cv, bv);
             BMND_LAUNCH_CHECK("approx_voxel_kernel");
+            auto boxes = [&](auto full, auto half) {
+                full<<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, n[0], n[1], n[2], boxb);
+                if (boxb_sub) half<<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, n[0], n[1], n[2], boxb_sub);
+            };
             if (a.ndim == 2)
-                approx_box_kernel<2, 8, 8, 1><<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, 1, n[1], n[2], boxb);
+                boxes(approx_box_kernel<2, 8, 8, 1, 1>, approx_box_kernel<2, 8, 8, 1, 2>);
             else if (bl[0] == 5)
-                approx_box_kernel<3, 5, 5, 5><<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, n[0], n[1], n[2], boxb);
+                boxes(approx_box_kernel<3, 5, 5, 5, 1>, approx_box_kernel<3, 5, 5, 5, 2>);
             else
-                approx_box_kernel<3, 4, 4, 4><<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, n[0], n[1], n[2], boxb);
+                boxes(approx_box_kernel<3, 4, 4, 4, 1>, approx_box_kernel<3, 4, 4, 4, 2>);
             BMND_LAUNCH_CHECK("approx_box_kernel");
             a.cv = cv;
             a.boxb = boxb;
+            a.boxb_sub = boxb_sub;
         } else {
             (void)cudaGetLastError();
             aux = nullptr;
@@ -1509,6 +1616,7 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     if (aux) BMND_CUDA_TRY(cudaFreeAsync(aux, stream));
     a.cv = nullptr;
     a.boxb = nullptr;
+    a.boxb_sub = nullptr;
     if (rc) return rc;
     // references that need the best rejected candidates are redone exactly
     MatchArgs fix = a;

@@ -76,6 +76,9 @@ extern "C" {
 #define BMND_MATCH_APPROX 2 /* screening distances select the group; only the selected candidates
                                are rescored exactly (Poisson deviance only; the match set may
                                differ from the exact one where the two orders disagree) */
+#define BMND_MATCH_SUBSAMPLED 3 /* as BMND_MATCH_APPROX after a prescreen: the screening form on the
+                                   patch's even sub-lattice for every candidate, the full form for
+                                   the 4 x max_matches smallest only */
 
 /*
  * Block matching on one patch grid.  Replaces

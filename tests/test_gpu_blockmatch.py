@@ -311,6 +311,36 @@ def test_approx_matching_selects_near_optimal_groups(cuda, native, shape, block,
     assert tot_a <= tot_e * (1 + 1e-4) + 1e-6, (tot_a, tot_e)
 
 
+@pytest.mark.parametrize("shape,block,radius,max_m,thr", [
+    ((22, 20, 24), (5, 5, 5), (7, 7, 7), 16, 2.9527),
+    ((46, 41), (8, 8), (19, 19), 16, 2.9527),
+])
+def test_subsampled_matching_selects_good_groups(cuda, native, shape, block, radius, max_m, thr):
+    """precision=subsampled prescreens on the patch's even sub-lattice, so its
+    groups may differ from the exact ones more often than approx's; their
+    summed exact distances must stay within 2% of the exact optimum overall."""
+    from bmnd_gb300 import _abi
+
+    rng = np.random.default_rng(41 + len(shape))
+    grids = np.meshgrid(*[np.linspace(0, 1, s) for s in shape], indexing="ij")
+    smooth = 5.0 + 20.0 * np.sin(3 * grids[0]) ** 2 + 10.0 * grids[-1]
+    vol = np.maximum(smooth + rng.normal(0, 0.5, size=shape), 0.0).astype(np.float32)
+    counts = tuple(s - b + 1 for s, b in zip(shape, block))
+    refs = np.stack(np.meshgrid(*[np.arange(0, c, 3) for c in counts], indexing="ij"), -1)
+    refs = refs.reshape(-1, len(shape)).astype(np.int32)
+    ex = _match_volume(cuda, native, vol, block, radius, max_m, 2, thr, _abi.MATCH_EXACT, refs)
+    sb = _match_volume(cuda, native, vol, block, radius, max_m, 2, thr, _abi.MATCH_SUBSAMPLED, refs)
+    same = sb[1] == ex[1]
+    assert same.mean() >= 0.95, same.mean()
+    tot_s = tot_e = 0.0
+    for i in np.flatnonzero(same):
+        rl = int(np.ravel_multi_index(tuple(refs[i]), counts))
+        assert sb[0][i, 0] == rl
+        tot_s += _exact_deviance(vol, block, counts, rl, sb[0][i, : sb[1][i]]).sum()
+        tot_e += _exact_deviance(vol, block, counts, rl, ex[0][i, : ex[1][i]]).sum()
+    assert tot_s <= tot_e * 1.02 + 1e-6, (tot_s, tot_e)
+
+
 def _patch_table(vol, block):
     """patches_flat of a volume: row = patch-grid linear index, column = patch element (C order)."""
     win = np.lib.stride_tricks.sliding_window_view(vol, block)
