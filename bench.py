@@ -216,7 +216,7 @@ def cpu_baseline(workload: str, seed: int, budget_s: float = 20.0) -> dict:
 # GPU arm
 # ---------------------------------------------------------------------------
 def time_kernels(torch, noisy_t, profile, reps: int = 2, stages=("ht", "wiener"), pilot=None,
-                 precision=None, gauss=None) -> dict:
+                 precision=None, gauss=None, fast_transforms: bool = False) -> dict:
     """CUDA-event times of the block-matching kernels and of each stage.
 
     ``pilot`` (optional) is the Wiener stage's pilot; by default it is the
@@ -239,7 +239,7 @@ def time_kernels(torch, noisy_t, profile, reps: int = 2, stages=("ht", "wiener")
         p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k,
                               stage_prec if stage_prec in (_abi.MATCH_APPROX, _abi.MATCH_SUBSAMPLED)
                               else _abi.MATCH_EXACT,
-                              None if gauss is None else gauss[stage])
+                              None if gauss is None else gauss[stage], fast_transforms=fast_transforms)
         block = tuple(getattr(profile, f"{stage}_block_size"))
         counts = tuple(s - b + 1 for s, b in zip(shape, block))
         sched = plan.reference_schedule(profile, counts, stage)
@@ -441,7 +441,8 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     if fast is not None:
         fprof = pl.fast_profile(profile)
         kf = time_kernels(torch, x, fprof, stages=("wiener",), pilot=fast["pilot"],
-                          precision={"wiener": bg.api._MATCH_PRECISIONS[pl.FAST_MATCH_PRECISION]})
+                          precision={"wiener": bg.api._MATCH_PRECISIONS[pl.FAST_MATCH_PRECISION]},
+                          fast_transforms=True)
         kt["fast_wiener"] = kf["wiener"]
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -491,10 +492,12 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
             if kk == 0 and gauss is None:
                 # no exact planes: the separable transforms dominate.  Per group four
                 # passes (observation, pilot, squared variance forward; inverse), each
-                # n P (sum of the patch edges) spatial plus n^2 P group-axis multiply-adds
+                # n P (sum of the patch edges) spatial multiply-adds plus the group axis:
+                # n^2 P as a matrix product, about 3 n P by the fast path's sum pyramid
                 n_ = k["mean_group"]
                 edges = float(sum(getattr(fprof if dom_stage == "fast_wiener" else profile, "wiener_block_size")))
-                macs = k["groups"] * 4 * (n_ * k["P"] * edges + n_ * n_ * k["P"])
+                group_macs = 3 * n_ * k["P"] if dom_stage == "fast_wiener" else n_ * n_ * k["P"]
+                macs = k["groups"] * 4 * (n_ * k["P"] * edges + group_macs)
                 compute = {
                     "what": "separable transform multiply-adds (four passes per group)",
                     "achieved_tmacs_s": macs / (dom_ms * 1e-3) / 1e12,

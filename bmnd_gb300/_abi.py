@@ -130,7 +130,7 @@ class StageParams(ctypes.Structure):
         ("policy_beta", ctypes.c_double),
         ("policy_power", ctypes.c_double),
         ("weight_group_scope", _I32),
-        ("reserved3", _I32),
+        ("fast_group_transform", _I32),
     ]
 
 

@@ -312,10 +312,11 @@ def estimate_poisson_global_sigma(volume, eps: float = 1e-10) -> float:
 
 
 def stage_device(noisy, profile, stage: str, pilot=None, *, resolved=None, match_precision: str = "exact",
-                 stream=None, gauss: dict | None = None):
+                 stream=None, gauss: dict | None = None, fast_transforms: bool = False):
     """One filtering stage on a float32 CUDA tensor: "ht" on ``noisy``, or
     "wiener" on ``noisy`` with ``pilot`` as the stage-1 estimate.  Returns the
-    stage estimate as a new CUDA tensor."""
+    stage estimate as a new CUDA tensor.  ``fast_transforms`` selects the Haar
+    group axis by its sum pyramid (the fast path's choice)."""
     torch = _torch()
     shape = tuple(int(s) for s in noisy.shape)
     if resolved is None:
@@ -330,7 +331,8 @@ def stage_device(noisy, profile, stage: str, pilot=None, *, resolved=None, match
     if stream is None:
         stream = torch.cuda.current_stream(device)
     p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k, precision,
-                          None if gauss is None else gauss[stage], null_table_device(profile, resolved, device))
+                          None if gauss is None else gauss[stage], null_table_device(profile, resolved, device),
+                          fast_transforms)
     block = tuple(int(b) for b in getattr(profile, f"{stage}_block_size"))
     counts = tuple(s - b + 1 for s, b in zip(shape, block))
     sched = plan.reference_schedule(profile, counts, stage)

@@ -239,6 +239,68 @@ __device__ void group_axis_inplace(float* buf, int P, const float* G) {
     }
 }
 
+// Haar group axis by its sum pyramid (one thread per column, O(N) operations):
+// row (l, j) of the orthonormal Haar matrix, block width w = N / 2^(l-1), is
+// (first-half sum - second-half sum) / sqrt(w); its elementwise square gives the
+// block sum / w; the inverse adds and subtracts the detail down the pyramid.
+// The rounding differs from the matrix product, so only the fast path uses it.
+template <int N, int KIND>
+__device__ void haar_axis_fast(float* buf, int P) {
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        float x[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k) x[k] = buf[k * P + p];
+        float out[N];
+        if (KIND == 1) {
+            // x = H^T c: start from the DC, refine block by block
+            out[0] = x[0] * rsqrtf(static_cast<float>(N));
+#pragma unroll
+            for (int w = N; w >= 2; w >>= 1) {
+                const int nb = N / w;
+                const float sc = rsqrtf(static_cast<float>(w));
+#pragma unroll
+                for (int j = nb - 1; j >= 0; --j) {
+                    const float d = x[nb + j] * sc;
+                    const float a = out[j];
+                    out[2 * j + 1] = a - d;
+                    out[2 * j] = a + d;
+                }
+            }
+        } else {
+            float sm_[N];
+#pragma unroll
+            for (int k = 0; k < N; ++k) sm_[k] = x[k];
+#pragma unroll
+            for (int w = 2; w <= N; w <<= 1) {
+                const int nb = N / w;
+                const float sc = KIND == 2 ? 1.0f / static_cast<float>(w) : rsqrtf(static_cast<float>(w));
+#pragma unroll
+                for (int j = 0; j < nb; ++j) {
+                    const float a = sm_[2 * j], b = sm_[2 * j + 1];
+                    out[nb + j] = (KIND == 2 ? a + b : a - b) * sc;
+                    sm_[j] = a + b;
+                }
+            }
+            out[0] = sm_[0] * (KIND == 2 ? 1.0f / static_cast<float>(N) : rsqrtf(static_cast<float>(N)));
+        }
+#pragma unroll
+        for (int k = 0; k < N; ++k) buf[k * P + p] = out[k];
+    }
+    __syncthreads();
+}
+
+template <int KIND>
+__device__ bool haar_axis_any(float* buf, int n, int P) {
+    switch (n) {
+        case 2: haar_axis_fast<2, KIND>(buf, P); return true;
+        case 4: haar_axis_fast<4, KIND>(buf, P); return true;
+        case 8: haar_axis_fast<8, KIND>(buf, P); return true;
+        case 16: haar_axis_fast<16, KIND>(buf, P); return true;
+        case 32: haar_axis_fast<32, KIND>(buf, P); return true;
+        default: return false;
+    }
+}
+
 // runtime group size (not a power of two): one thread per column
 template <int KIND>
 __device__ void group_axis_generic(float* buf, int n, int P, const float* G) {
@@ -337,7 +399,12 @@ __device__ void transform_group(const GM& geo, const FilterArgs& a, unsigned cha
                                 int kind) {
     const float* G = sm<float>(smem, a.L.g);
     const float* F = sm<float>(smem, kind == 1 ? a.L.fi : (kind == 3 ? a.L.fit : a.L.fw));
-    if (a.sp.group_transform != BMND_GROUP_NONE) {
+    const bool fast_haar = a.sp.fast_group_transform && a.sp.group_transform == BMND_GROUP_HAAR &&
+                           (kind == 0 ? haar_axis_any<0>(buf, n, geo.P())
+                                      : kind == 1 ? haar_axis_any<1>(buf, n, geo.P())
+                                                  : kind == 2 ? haar_axis_any<2>(buf, n, geo.P())
+                                                              : haar_axis_any<0>(buf, n, geo.P()));
+    if (!fast_haar && a.sp.group_transform != BMND_GROUP_NONE) {
         // kind 3 (transposed inverse): the group transforms are orthonormal, so
         // the transposed inverse of the group axis is the forward transform
         if (kind == 0 || kind == 3) group_axis_any<0>(buf, n, geo.P(), G);

@@ -445,7 +445,8 @@ def bmnd_fast(noisy, profile, net: PilotNet, *, tile: int | None = None, excess_
         details.update(pilot=pilot, excess=excess, fallback_tiles=n_fb,
                        tiles=int(np.prod([(s + tile - 1) // tile for s in shape])))
     p2 = fast_profile(profile) if stage2 else profile
-    return stage_device(x, p2, "wiener", pilot, match_precision=match_precision if stage2 else "exact")
+    return stage_device(x, p2, "wiener", pilot, match_precision=match_precision if stage2 else "exact",
+                        fast_transforms=stage2)
 
 
 def calibrate_excess_high(pairs, tile: int | None = None, spread: float = 3.0) -> float:

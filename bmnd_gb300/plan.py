@@ -69,7 +69,7 @@ def spatial_forward(profile, ndim: int, stage: str) -> list:
 
 def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMatchDistance,
                  variance_k: int, match_precision: int = _abi.MATCH_EXACT, gauss: dict | None = None,
-                 null_table=None) -> _abi.StageParams:
+                 null_table=None, fast_transforms: bool = False) -> _abi.StageParams:
     """Fill the ``StageParams`` of ``stage`` ("ht" or "wiener").
 
     ``gauss`` (stationary Gaussian noise) holds the device tables of the stage:
@@ -77,7 +77,8 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     domain), ``ssd`` (SSD noise bias over the search offsets, or None) and
     ``gamma``; without it the stage models direct Poisson noise.  ``null_table``
     (float64 CUDA tensor [2, max_count + 1], ``policies.null_moment_table``)
-    enables the profile's Poisson HT match policy."""
+    enables the profile's Poisson HT match policy.  ``fast_transforms`` computes
+    the Haar group axis by its sum pyramid (same transform, different rounding)."""
     ndim = len(shape)
     if ndim < 1 or ndim > _abi.MAX_DIMS:
         raise unsupported(f"{ndim}-D volumes are not supported (1 to {_abi.MAX_DIMS} dimensions)")
@@ -113,6 +114,7 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
                       AggregationWeightModel.CLASSIC: _abi.WEIGHT_CLASSIC,
                       AggregationWeightModel.RISK: _abi.WEIGHT_RISK}[model]
     p.weight_group_scope = int(scope is AggregationWeightScope.GROUP)
+    p.fast_group_transform = int(bool(fast_transforms))
     p.windowed_synthesis = int(domain is AggregationWeightDomain.WINDOWED_SYNTHESIS)
     p.match_threshold = float(np.float32(getattr(profile, f"{stage}_match_threshold")))
     p.ht_lambda = float(profile.ht_lambda_threshold)

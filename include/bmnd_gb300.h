@@ -174,7 +174,9 @@ typedef struct BmndStageParams {
     /* one aggregation weight per group (weight_scope "group") instead of one
      * per patch; the covariance-aware exact weighting is not available */
     int32_t weight_group_scope;
-    int32_t reserved3;
+    /* Haar group axis by its sum pyramid instead of the matrix product (same
+     * transform, different rounding; used by the fast path) */
+    int32_t fast_group_transform;
 } BmndStageParams;
 
 #define BMND_GAIN_VARIANCE_SCALED 0

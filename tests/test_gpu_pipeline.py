@@ -168,3 +168,22 @@ def test_zero_and_extreme_rates(cuda, native):
             vol[3, 3] = 1.0
         res = bg.bmnd(vol, _profile("bm3d"))
         assert np.all(np.isfinite(res))
+
+
+@pytest.mark.parametrize("case", ["bm3d_32", "bm4d_12x16x20"])
+def test_fast_haar_group_axis_matches_matrix_product(cuda, native, case):
+    """The fast path's Haar group axis (sum pyramid) computes the same
+    transform as the matrix product: both stages agree to float32 rounding."""
+    import bmnd_gb300 as bg
+    from bmnd_gb300.api import stage_device
+
+    g = np.load(os.path.join(GOLDEN, f"pipe_{case}.npz"))
+    profile = _profile(str(g["kind"]))
+    x = cuda.from_numpy(g["noisy"]).cuda()
+    for stage in ("ht", "wiener"):
+        pilot = None if stage == "ht" else cuda.from_numpy(g["ht"]).cuda()
+        a = stage_device(x, profile, stage, pilot).cpu().numpy()
+        b = stage_device(x, profile, stage, pilot, fast_transforms=True).cpu().numpy()
+        par = output_parity(b, a)
+        assert par["frac_within"] >= 0.999, (case, stage, par)
+    assert bg is not None
