@@ -654,6 +654,7 @@ struct ScreenSmem {
                + cand(wmax)                                           // screening distances
                + 256 * 4                                              // histogram
                + kSQueue * 4 + kSQueue * 8                            // queue index, exact keys
+               + kSQueue * 4                                          // subsampled mode: compact -> window index
                + 64 * 8                                               // scratch (reductions, top list)
                + 64;
     }
@@ -690,6 +691,8 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
     b += kSQueue * 4;
     uint64_t* qkey = reinterpret_cast<uint64_t*>(b);
     b += kSQueue * 8;
+    int32_t* cmap = reinterpret_cast<int32_t*>(b);
+    b += kSQueue * 4;
     uint64_t* top = reinterpret_cast<uint64_t*>(b);  // [32]
     float* redf = reinterpret_cast<float*>(top + 32);  // [4 warps]
     int* redi = reinterpret_cast<int*>(redf + 8);      // [8]
@@ -767,6 +770,11 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
 
         float Dabs = 0.0f;  // the reference-wide absolute bound, set after pass A
         const float drel_k = drel;
+        // candidates still in the race: the whole window, or (subsampled mode)
+        // the prescreened ones, compacted to cand[0, wlen) with cmap[] their
+        // window indices
+        int64_t wlen = window;
+        bool compact = false;
         // radix select over the upper bounds d + D of the certainly accepted
         // (of every candidate with `all`): the smallest v with >= need of them
         // bounded by it, or infinity when there are fewer
@@ -783,11 +791,11 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                 }
                 // warp-uniform sweep; lanes that share a bin add once (most
                 // candidates share the leading bits, so plain atomics serialise)
-                for (int64_t base = static_cast<int64_t>(warp) * 32; base < window; base += blockDim.x) {
+                for (int64_t base = static_cast<int64_t>(warp) * 32; base < wlen; base += blockDim.x) {
                     const int64_t c = base + lane;
                     bool take = false;
                     uint32_t bin = 0;
-                    if (c < window) {
+                    if (c < wlen) {
                         const float dv = cand[c];
                         const float up = dv + (Dabs + drel_k * dv);
                         if (all || canonical_key(up) < tkey) {
@@ -960,7 +968,6 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                         const int slot = atomicAdd(redi, 1);
                         if (slot < kSQueue) qidx[slot] = static_cast<int32_t>(c);
                     }
-                    cand[c] = 1e30f;  // out of the race (finite: the bound arithmetic below stays NaN-free)
                 }
                 __syncthreads();
                 const int nsel = min(redi[0], kSQueue);
@@ -972,9 +979,12 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                     approx_unit<ND, B0, B1, B2, 1, 1>(ref, a.cv, origin, a.vstride[0], a.vstride[ND > 1 ? 1 : 0],
                                                       BX, acc);
                     const float d = 1.38629436f * (sum_a + __ldg(a.boxb + origin) + acc[0]);
-                    cand[qidx[i]] = fmaxf(d, 0.0f) / static_cast<float>(P);
+                    cand[i] = fmaxf(d, 0.0f) / static_cast<float>(P);  // compacted (nothing reads cand here)
+                    cmap[i] = qidx[i];
                 }
                 __syncthreads();
+                wlen = nsel;
+                compact = true;
                 if (tid == 0) redi[0] = 0;
             }
         } else {
@@ -1002,7 +1012,7 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
 
         // pass C: classify; queue the uncertain and the possible top-K members
         int acc_t = 0;
-        for (int64_t c = tid; c < window; c += blockDim.x) {
+        for (int64_t c = tid; c < wlen; c += blockDim.x) {
             const float dv = cand[c];
             const float D = Dabs + drel * dv;
             const float lo_key = canonical_key(fmaxf(dv - D, 0.0f));
@@ -1012,7 +1022,8 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
             if (poss && (!cert || lo_key <= vkey)) {
                 const int slot = atomicAdd(redi, 1);
                 if (slot < kSQueue)
-                    qidx[slot] = static_cast<int32_t>(c) | (cert ? static_cast<int32_t>(0x80000000u) : 0);
+                    qidx[slot] = (compact ? cmap[c] : static_cast<int32_t>(c)) |
+                                 (cert ? static_cast<int32_t>(0x80000000u) : 0);
             }
         }
         __syncthreads();
@@ -1088,7 +1099,7 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                 redi[3] = 0;
             }
             __syncthreads();
-            for (int64_t c = tid; c < window; c += blockDim.x) {
+            for (int64_t c = tid; c < wlen; c += blockDim.x) {
                 if (canonical_key(cand[c]) <= v2key) {
                     const int slot = atomicAdd(redi, 1);
                     if (slot < kSQueue) qidx[slot] = static_cast<int32_t>(c);
@@ -1099,7 +1110,7 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
             if (qn2 <= kSQueue) {
                 for (int i = tid; i < qn2; i += blockDim.x) {
                     int64_t lin;
-                    (void)window_origin(a, lo, ext, inv_ext, small_window, qidx[i], &lin);
+                    (void)window_origin(a, lo, ext, inv_ext, small_window, compact ? cmap[qidx[i]] : qidx[i], &lin);
                     qkey[i] = composite_key(canonical_key(cand[qidx[i]]), static_cast<int32_t>(lin));
                 }
                 __syncthreads();
