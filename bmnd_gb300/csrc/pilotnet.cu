@@ -74,6 +74,15 @@ __device__ __forceinline__ int64_t vox_index(const NetGeo& g, int b, int z, int 
     return ((static_cast<int64_t>(b) * g.D + z) * g.H + y) * g.W + x;
 }
 
+// Hidden activations and their gradients are stored chunk-planar,
+// [C / 8][voxel][8 channels]: one 8-channel chunk of a row of voxels is
+// contiguous, so a halo row arrives as one TMA row of 16 * hx bytes.
+// One-channel tensors (the Anscombe input, the output) are plain [voxel].
+template <int CH>
+__host__ __device__ __forceinline__ int64_t hid(int64_t v, int c, int64_t nv) {
+    return CH < 8 ? v * CH + c : (static_cast<int64_t>(c >> 3) * nv + v) * 8 + (c & 7);
+}
+
 __device__ __forceinline__ void vox_decode(const NetGeo& g, int64_t v, int& b, int& z, int& y, int& x) {
     x = static_cast<int>(v % g.W);
     v /= g.W;
@@ -107,6 +116,7 @@ __global__ void conv_in_kernel(const float* __restrict__ a, const float* __restr
     for (int i = threadIdx.x; i < C; i += blockDim.x) bs[i] = bias[i];
     __syncthreads();
     const int wp = (g.W + 1) / 2;  // voxel pairs per row
+    const int64_t nv = g.voxels();
     const int64_t npair = static_cast<int64_t>(g.nb) * g.D * g.H * wp;
     for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; q < npair;
          q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -153,11 +163,11 @@ __global__ void conv_in_kernel(const float* __restrict__ a, const float* __restr
             __align__(16) bf16 o[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) o[j] = __float2bfloat16_rn(fmaxf(acc0[j], 0.0f));
-            *reinterpret_cast<uint4*>(h + v0 * C + c0) = *reinterpret_cast<const uint4*>(o);
+            *reinterpret_cast<uint4*>(h + hid<C>(v0, c0, nv)) = *reinterpret_cast<const uint4*>(o);
             if (two) {
 #pragma unroll
                 for (int j = 0; j < 8; ++j) o[j] = __float2bfloat16_rn(fmaxf(acc1[j], 0.0f));
-                *reinterpret_cast<uint4*>(h + (v0 + 1) * C + c0) = *reinterpret_cast<const uint4*>(o);
+                *reinterpret_cast<uint4*>(h + hid<C>(v0 + 1, c0, nv)) = *reinterpret_cast<const uint4*>(o);
             }
         }
     }
@@ -189,6 +199,7 @@ __global__ void __launch_bounds__(128) conv_out_kernel(const bf16* __restrict__ 
     bf16* ring = reinterpret_cast<bf16*>(out_smem + static_cast<size_t>(T) * C * 4);
     for (int i = threadIdx.x; i < T * C; i += blockDim.x) ws[i] = w[i];
     const float b0 = bias[0];
+    const int64_t nv = g.voxels();
     const int tiles_x = (g.W + OT::tx - 1) / OT::tx;
     const int tiles_y = (g.H + OT::ty - 1) / OT::ty;
     const int zblocks = (g.D + OT::zb - 1) / OT::zb;
@@ -203,11 +214,11 @@ __global__ void __launch_bounds__(128) conv_out_kernel(const bf16* __restrict__ 
     auto load_plane = [&](int zz, int slot) {
         bf16* dst = ring + static_cast<size_t>(slot) * HV * CP;
         for (int i = threadIdx.x; i < HV * CH; i += blockDim.x) {
-            const int hv = i / CH, ch = i - hv * CH;
+            const int ch = i / HV, hv = i - ch * HV;  // chunk-major: a warp reads consecutive voxels
             const int xx = x0 - 1 + hv % OT::hx, yy = y0 - 1 + hv / OT::hx;
             uint4 v = make_uint4(0u, 0u, 0u, 0u);
             if (zz >= 0 && zz < g.D && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W)
-                v = *reinterpret_cast<const uint4*>(h + vox_index(g, b, zz, yy, xx) * C + ch * 8);
+                v = *reinterpret_cast<const uint4*>(h + hid<C>(vox_index(g, b, zz, yy, xx), ch * 8, nv));
             *reinterpret_cast<uint4*>(dst + static_cast<size_t>(hv) * CP + ch * 8) = v;
         }
     };
@@ -311,7 +322,7 @@ __global__ void conv_out_dgrad_kernel(const float* __restrict__ gy, const float*
         }
 #pragma unroll
         for (int c0 = 0; c0 < C; c0 += 8) {
-            const uint4 raw = *reinterpret_cast<const uint4*>(h + u * C + c0);
+            const uint4 raw = *reinterpret_cast<const uint4*>(h + hid<C>(u, c0, n));
             const bf16* hm = reinterpret_cast<const bf16*>(&raw);
             float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
@@ -322,7 +333,7 @@ __global__ void conv_out_dgrad_kernel(const float* __restrict__ gy, const float*
 #pragma unroll
             for (int j = 0; j < 8; ++j)
                 o[j] = __float2bfloat16_rn(__bfloat162float(hm[j]) > 0.0f ? acc[j] : 0.0f);
-            *reinterpret_cast<uint4*>(gh + u * C + c0) = *reinterpret_cast<const uint4*>(o);
+            *reinterpret_cast<uint4*>(gh + hid<C>(u, c0, n)) = *reinterpret_cast<const uint4*>(o);
         }
     }
 }
@@ -406,6 +417,7 @@ __global__ void __launch_bounds__(256, 1) conv_mid_kernel(const bf16* __restrict
     const int tiles_z = (g.D + TL::tz - 1) / TL::tz;
     const int64_t ntiles = static_cast<int64_t>(tiles_x) * tiles_y * tiles_z * g.nb;
     constexpr int chunks = C / 8;  // 16-byte chunks per voxel
+    const int64_t nv = g.voxels();
     const uint32_t tile_base = static_cast<uint32_t>(__cvta_generic_to_shared(tile));
 
     for (int64_t tl = blockIdx.x; tl < ntiles; tl += gridDim.x) {
@@ -418,12 +430,12 @@ __global__ void __launch_bounds__(256, 1) conv_mid_kernel(const bf16* __restrict
         const int b = static_cast<int>(r / tiles_z);
         __syncthreads();  // the previous tile is no longer read (and the weights are in place)
         for (int i = tid; i < TL::halo * chunks; i += blockDim.x) {
-            const int vox = i / chunks, ch = i % chunks;
+            const int ch = i / TL::halo, vox = i - ch * TL::halo;  // chunk-major: coalesced reads
             const int hxi = vox % TL::hx, hyi = (vox / TL::hx) % TL::hy, hzi = vox / (TL::hx * TL::hy);
             const int xx = x0 + hxi - 1, yy = y0 + hyi - 1, zz = ND == 3 ? z0 + hzi - 1 : z0;
             uint4 v = make_uint4(0u, 0u, 0u, 0u);
             if (xx >= 0 && xx < g.W && yy >= 0 && yy < g.H && zz >= 0 && zz < g.D)
-                v = *reinterpret_cast<const uint4*>(in + vox_index(g, b, zz, yy, xx) * C + ch * 8);
+                v = *reinterpret_cast<const uint4*>(in + hid<C>(vox_index(g, b, zz, yy, xx), ch * 8, nv));
             *reinterpret_cast<uint4*>(tile + static_cast<size_t>(vox) * S::cp + ch * 8) = v;
         }
         __syncthreads();
@@ -482,14 +494,14 @@ __global__ void __launch_bounds__(256, 1) conv_mid_kernel(const bf16* __restrict
                     const int co = n * 8 + 2 * (lane % 4);
                     float v0 = acc[i][n][2 * hh], v1 = acc[i][n][2 * hh + 1];
                     if (mask) {
-                        const __nv_bfloat162 m2 = *reinterpret_cast<const __nv_bfloat162*>(mask + v * C + co);
+                        const __nv_bfloat162 m2 = *reinterpret_cast<const __nv_bfloat162*>(mask + hid<C>(v, co, nv));
                         v0 = __low2float(m2) > 0.0f ? v0 : 0.0f;
                         v1 = __high2float(m2) > 0.0f ? v1 : 0.0f;
                     } else {
                         v0 = fmaxf(v0 + bias[co], 0.0f);
                         v1 = fmaxf(v1 + bias[co + 1], 0.0f);
                     }
-                    *reinterpret_cast<__nv_bfloat162*>(out + v * C + co) = __floats2bfloat162_rn(v0, v1);
+                    *reinterpret_cast<__nv_bfloat162*>(out + hid<C>(v, co, nv)) = __floats2bfloat162_rn(v0, v1);
                 }
             }
         }
@@ -503,7 +515,8 @@ __global__ void __launch_bounds__(256, 1) conv_mid_kernel(const bf16* __restrict
 // Output tile: one z plane of 16 rows x 8 voxels = the M = 128 rows of one
 // tcgen05.mma (kind::f16, BF16 in, FP32 accumulate, N = C, K = 16).  The
 // input halo of the tile (10 x 18 voxels, x 3 planes in 3-D) arrives by TMA,
-// one 4-D box per 8-channel chunk, so shared memory holds it chunk-major:
+// one 4-D box per 8-channel chunk plane of the chunk-planar activations (each
+// box row is 16 * hx contiguous bytes), so shared memory holds it chunk-major:
 // [chunk][halo voxel][16 bytes], chunks 128-byte aligned.  For every tap the A
 // operand is then a no-swizzle K-major matrix: a core matrix is 8 consecutive
 // voxels of one row (128 contiguous bytes), the next 8 rows of M are the next
@@ -815,6 +828,7 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
         // ---- epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31 ----
         const int q = warp & 3;
         const int m = 32 * q + lane;  // accumulator row = voxel of the tile
+        const int64_t nv = g.voxels();
         int it = 0;
         for (int64_t tl = blockIdx.x; tl < ntiles; tl += gridDim.x, ++it) {
             const int s = it & 1;
@@ -854,7 +868,7 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
                     __align__(16) bf16 o[8];
                     if (mask) {
                         __align__(16) bf16 mk[8];
-                        *reinterpret_cast<uint4*>(mk) = *reinterpret_cast<const uint4*>(mask + v * C + c0);
+                        *reinterpret_cast<uint4*>(mk) = *reinterpret_cast<const uint4*>(mask + hid<C>(v, c0, nv));
 #pragma unroll
                         for (int j = 0; j < 8; ++j)
                             o[j] = __float2bfloat16_rn(__bfloat162float(mk[j]) > 0.0f ? __uint_as_float(r[c0 + j])
@@ -864,7 +878,7 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
                         for (int j = 0; j < 8; ++j)
                             o[j] = __float2bfloat16_rn(fmaxf(__uint_as_float(r[c0 + j]) + __ldg(bias + c0 + j), 0.0f));
                     }
-                    *reinterpret_cast<uint4*>(out + v * C + c0) = *reinterpret_cast<const uint4*>(o);
+                    *reinterpret_cast<uint4*>(out + hid<C>(v, c0, nv)) = *reinterpret_cast<const uint4*>(o);
                 }
             }
         }
@@ -919,21 +933,23 @@ __global__ void __launch_bounds__(256) wgrad_kernel(const TI* __restrict__ in, c
     r /= tiles_y;
     const int z0 = static_cast<int>(r % tiles_z) * TL::tz;
     const int b = static_cast<int>(r / tiles_z);
-    for (int i = threadIdx.x; i < TL::halo * CIN; i += blockDim.x) {
-        const int vox = i / CIN, c = i % CIN;
+    const int64_t nv = g.voxels();
+    for (int j = threadIdx.x; j < TL::halo * CIN; j += blockDim.x) {
+        const int c = j / TL::halo, vox = j - c * TL::halo;  // channel-major: coalesced reads
+        const int i = vox * CIN + c;
         const int hxi = vox % TL::hx, hyi = (vox / TL::hx) % TL::hy, hzi = vox / (TL::hx * TL::hy);
         const int xx = x0 + hxi - 1, yy = y0 + hyi - 1, zz = ND == 3 ? z0 + hzi - 1 : z0;
         float v = 0.0f;
         if (xx >= 0 && xx < g.W && yy >= 0 && yy < g.H && zz >= 0 && zz < g.D)
-            v = to_f<TI>(in[vox_index(g, b, zz, yy, xx) * CIN + c]);
+            v = to_f<TI>(in[hid<CIN>(vox_index(g, b, zz, yy, xx), c, nv)]);
         sin[i] = v;
     }
-    for (int i = threadIdx.x; i < 256 * COUT; i += blockDim.x) {
-        const int m = i / COUT, c = i % COUT;
+    for (int j = threadIdx.x; j < 256 * COUT; j += blockDim.x) {
+        const int c = j / 256, m = j - c * 256;
         const int xx = x0 + m % TL::tx, yy = y0 + (m / TL::tx) % TL::ty, zz = z0 + m / (TL::tx * TL::ty);
         float v = 0.0f;
-        if (xx < g.W && yy < g.H && zz < g.D) v = to_f<TG>(gout[vox_index(g, b, zz, yy, xx) * COUT + c]);
-        sg[i] = v;
+        if (xx < g.W && yy < g.H && zz < g.D) v = to_f<TG>(gout[hid<COUT>(vox_index(g, b, zz, yy, xx), c, nv)]);
+        sg[m * COUT + c] = v;
     }
     __syncthreads();
     float* out = partial + static_cast<int64_t>(blockIdx.x) * nparams;
@@ -1264,14 +1280,14 @@ int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf1
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(TT::bytes)));
     if ((reinterpret_cast<uintptr_t>(in) & 15u) != 0 || (reinterpret_cast<uintptr_t>(wtc) & 15u) != 0)
         return fail(BMND_ERR_INVALID_ARG, "pilot net buffers must be 16-byte aligned");
-    // one 4-D map per 8-channel chunk: (8 channels, x, y, z * batch), a box of
-    // (8, hx, hy, hz) voxels; out-of-range elements read as zero
+    // one 4-D map per 8-channel chunk plane: (8 channels, x, y, z * batch), a
+    // box of (8, hx, hy, hz) voxels whose rows are 16 * hx contiguous bytes;
+    // out-of-range elements read as zero
     TcMaps maps;
     memset(&maps, 0, sizeof(maps));
     const cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(g.W), static_cast<cuuint64_t>(g.H),
                                 static_cast<cuuint64_t>(g.D) * static_cast<cuuint64_t>(g.nb)};
-    const cuuint64_t strides[3] = {static_cast<cuuint64_t>(C) * 2, static_cast<cuuint64_t>(g.W) * C * 2,
-                                   static_cast<cuuint64_t>(g.H) * g.W * C * 2};
+    const cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(g.W) * 16, static_cast<cuuint64_t>(g.H) * g.W * 16};
     const cuuint32_t box[4] = {8, TT::hx, TT::hy, TT::hz};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     // the driver's encoder, fetched through the runtime (no link-time dependency on the driver library)
@@ -1285,7 +1301,8 @@ int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf1
     }
     for (int ch = 0; ch < TT::chunks; ++ch) {
         const CUresult rc = encode(
-            &maps.m[ch], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(in) + ch * 8, dims, strides, box,
+            &maps.m[ch], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(in) + hid<C>(0, ch * 8, g.voxels()),
+            dims, strides, box,
             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (rc != CUDA_SUCCESS) return fail(BMND_ERR_CUDA, "cuTensorMapEncodeTiled failed for the pilot net input");
