@@ -668,6 +668,12 @@ struct ScreenSmem {
 #ifndef BMND_APPROX_XR
 #define BMND_APPROX_XR 2
 #endif
+// x-run of the subsampled prescreen.  3 divides the default 15-wide window
+// rows, but its warps span more window rows per load; at 256^3 the matching
+// took 31.0 ms with 3 against 28.1 ms with 2
+#ifndef BMND_SUB_XR
+#define BMND_SUB_XR 2
+#endif
 
 template <int ND, int B0, int B1, int B2>
 __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_screened_kernel(MatchArgs a,
@@ -920,7 +926,7 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
             // sub-lattice of the patch for every candidate, then the full form
             // for the a.presel smallest; the rest are out of the race
             if constexpr (ND > 0) {
-                constexpr int XR = BMND_APPROX_XR;
+                constexpr int XR = BMND_SUB_XR;
                 constexpr int BX = ND == 3 ? B2 : B1;
                 constexpr int PS = ((B0 + 1) / 2) * ((B1 + 1) / 2) * (ND == 3 ? (B2 + 1) / 2 : 1);
                 const float* fs = reinterpret_cast<const float*>(redi + 16);
