@@ -117,7 +117,7 @@ class StageParams(ctypes.Structure):
         ("cov_maps", ctypes.c_void_p),
         ("match_noise_ssd", ctypes.c_void_p),
         ("ssd_gamma", ctypes.c_float),
-        ("reserved1", _I32),
+        ("ssd_poisson_bias", _I32),
         ("ssd_threshold", ctypes.c_double),
         ("mass_conserve", _I32),
         ("wiener_gain_mode", _I32),
@@ -170,6 +170,11 @@ SIGNATURES = {
         [ctypes.POINTER(MatchParams), ctypes.c_void_p, _I32P, _I32P, ctypes.c_void_p, _I64,
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
          _U64],
+    ),
+    "bmnd_blockmatch_volume_poisson_biased": (
+        _I32,
+        [ctypes.POINTER(MatchParams), ctypes.c_void_p, _I32P, _I32P, ctypes.c_void_p, _I64,
+         ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _U64],
     ),
     "bmnd_stage_workspace_bytes": (_I32, [ctypes.POINTER(StageParams), _I64, _U64P]),
     "bmnd_stage": (

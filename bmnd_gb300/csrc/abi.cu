@@ -109,8 +109,14 @@ int32_t validate_stage(const BmndStageParams& sp) {
         for (int d = 0; d < sp.ndim; ++d)
             if (sp.cov_domain[d] < 1) return fail(BMND_ERR_INVALID_ARG, "covariance domain must be positive");
     }
-    if (sp.match_noise_ssd && sp.distance != BMND_DIST_SSD)
+    if ((sp.match_noise_ssd || sp.ssd_poisson_bias) && sp.distance != BMND_DIST_SSD)
         return fail(BMND_ERR_INVALID_ARG, "the noise-bias correction applies to SSD matching only");
+    if (sp.ssd_poisson_bias != 0 && sp.ssd_poisson_bias != 1)
+        return fail(BMND_ERR_INVALID_ARG, "ssd_poisson_bias must be 0 or 1");
+    if (sp.ssd_poisson_bias && (sp.noise_model != BMND_NOISE_POISSON || sp.match_noise_ssd))
+        return fail(BMND_ERR_INVALID_ARG, "the Poisson SSD noise bias needs the Poisson model and no bias table");
+    if ((sp.match_noise_ssd || sp.ssd_poisson_bias) && (!(sp.ssd_gamma >= 0.0f) || !std::isfinite(sp.ssd_gamma)))
+        return fail(BMND_ERR_INVALID_ARG, "gamma must be finite and non-negative");
     if (sp.distance == BMND_DIST_SSD && (!(sp.ssd_threshold >= 0.0) || !std::isfinite(sp.ssd_threshold)))
         return fail(BMND_ERR_INVALID_ARG, "SSD threshold multiplier must be finite and >= 0");
     if (group_filter_smem_bytes(sp) > 227 * 1024)
@@ -244,7 +250,7 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
     rc = launch_blockmatch_volume(mp, match_src, sp.shape, sp.block, refs, n_refs, thr_per_ref,
                                   sp.match_threshold, w.sel, w.count, w.accepted, stream, thr_dev,
                                   sp.match_noise_ssd, sp.ssd_gamma, allow_alloc, null_moments,
-                                  sp.null_max_count);
+                                  sp.null_max_count, sp.ssd_poisson_bias != 0);
     if (rc) return rc;
     rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, w.st, sig_num, stream);
     if (rc) return rc;
@@ -384,6 +390,20 @@ int32_t bmnd_blockmatch_volume_biased(const BmndMatchParams* params, const float
     return launch_blockmatch_volume(*params, d_volume, shape, block, d_refs, n_refs, d_thresholds, 0.0f, d_sel,
                                     d_count, d_accepted, reinterpret_cast<cudaStream_t>(stream), nullptr,
                                     d_noise_ssd, gamma);
+}
+
+int32_t bmnd_blockmatch_volume_poisson_biased(const BmndMatchParams* params, const float* d_volume,
+                                              const int32_t* shape, const int32_t* block, const int32_t* d_refs,
+                                              int64_t n_refs, const float* d_thresholds, float gamma,
+                                              int32_t* d_sel, int32_t* d_count, int32_t* d_accepted,
+                                              uint64_t stream) {
+    clear_error();
+    if (!params || !d_volume || !shape || !block || !d_thresholds || !d_sel || !d_count || !d_accepted ||
+        (n_refs > 0 && !d_refs))
+        return fail(BMND_ERR_INVALID_ARG, "null argument");
+    return launch_blockmatch_volume(*params, d_volume, shape, block, d_refs, n_refs, d_thresholds, 0.0f, d_sel,
+                                    d_count, d_accepted, reinterpret_cast<cudaStream_t>(stream), nullptr, nullptr,
+                                    gamma, true, nullptr, 0, true);
 }
 
 int32_t bmnd_blockmatch_volume(const BmndMatchParams* params, const float* d_volume,

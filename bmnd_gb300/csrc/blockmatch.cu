@@ -24,6 +24,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cmath>
 
 #include "bmnd_common.cuh"
 
@@ -67,6 +68,11 @@ struct MatchArgs {
     // gamma * noise_ssd[offset of the candidate from the reference], or null
     const float* noise_ssd;
     float gamma;
+    // Poisson SSD noise-bias correction (blockmatching.py:1140-1145,
+    // :432-443): distance -= gamma * sum_p bias_scale * (r_p + c_p) over
+    // r_p + c_p > 0, for every candidate but the reference itself
+    int32_t poisson_bias;
+    float bias_scale;
     // threshold computed on the device (one float), overrides the scalar one
     const float* thr_dev;
     int32_t no_alloc;  // 1: no stream-ordered scratch (approx mode then runs the bounded form)
@@ -117,6 +123,25 @@ __device__ __forceinline__ float deviance_tabulated(const float* __restrict__ re
     }
     if (d < 0.0f) d = 0.0f;
     return div_rn(d, static_cast<float>(P));
+}
+
+// SSD and the Poisson SSD noise bias of one candidate in one pass, float32
+// in patch order as the reference evaluates them (blockmatching.py:323-336,
+// :432-443): bias = sum over r + c > 0 of scale * (r + c)
+__device__ __forceinline__ float ssd_pooled_bias(const float* __restrict__ ref, const float* __restrict__ src,
+                                                 int64_t origin, const int32_t* __restrict__ poff, int P,
+                                                 float scale, float& bias) {
+    float d = 0.0f, b = 0.0f;
+    for (int p = 0; p < P; ++p) {
+        const float r = ref[p];
+        const float c = __ldg(src + origin + poff[p]);
+        const float diff = sub_rn(c, r);
+        d = add_rn(d, mul_rn(diff, diff));
+        const float pooled = add_rn(r, c);
+        if (pooled > 0.0f) b = add_rn(b, mul_rn(scale, pooled));
+    }
+    bias = b;
+    return d;
 }
 
 template <int CODE>
@@ -372,11 +397,17 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
         for (int64_t c = lane; c < window; c += 32) {
             int64_t lin;
             const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
-            float dist = a.null_moments
-                             ? standardized_distance<CODE>(ref_s, a.src, origin, poff_s, P, a.inv_scale, a.null_moments,
-                                                           a.null_max)
-                         : use_table ? deviance_tabulated(ref_s, ref_row, a.src, origin, poff_s, P, table)
-                                     : patch_distance<CODE>(ref_s, a.src, origin, poff_s, P, a.inv_scale);
+            float dist;
+            if (CODE == BMND_DIST_SSD && a.poisson_bias) {
+                float bias;
+                dist = ssd_pooled_bias(ref_s, a.src, origin, poff_s, P, a.bias_scale, bias);
+                if (lin != center_lin) dist = sub_rn(dist, mul_rn(a.gamma, bias));
+            } else {
+                dist = a.null_moments ? standardized_distance<CODE>(ref_s, a.src, origin, poff_s, P, a.inv_scale,
+                                                                    a.null_moments, a.null_max)
+                       : use_table    ? deviance_tabulated(ref_s, ref_row, a.src, origin, poff_s, P, table)
+                                      : patch_distance<CODE>(ref_s, a.src, origin, poff_s, P, a.inv_scale);
+            }
             if (CODE == BMND_DIST_SSD && a.noise_ssd) {
                 // offset of the candidate from the reference, C order over 2 r + 1 per axis
                 int64_t rem = c, gidx = 0, mul = 1;
@@ -1723,16 +1754,25 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
                                  int64_t n_refs, const float* thresholds, float scalar_threshold,
                                  int32_t* sel, int32_t* count, int32_t* accepted,
                                  cudaStream_t stream, const float* thr_dev, const float* noise_ssd,
-                                 float gamma, bool allow_alloc, const double* null_moments, int null_max) {
+                                 float gamma, bool allow_alloc, const double* null_moments, int null_max,
+                                 bool poisson_bias) {
     int32_t rc = validate_match(mp);
     if (rc) return rc;
-    if (noise_ssd && mp.distance != BMND_DIST_SSD)
+    if ((noise_ssd || poisson_bias) && mp.distance != BMND_DIST_SSD)
         return fail(BMND_ERR_INVALID_ARG, "the noise-bias correction applies to SSD matching only");
+    if (noise_ssd && poisson_bias)
+        return fail(BMND_ERR_INVALID_ARG, "one noise-bias correction at a time");
+    if (poisson_bias && (!(mp.count_scale > 0.0) || !std::isfinite(mp.count_scale)))
+        return fail(BMND_ERR_INVALID_ARG, "poisson_count_scale must be finite and positive");
+    if ((noise_ssd || poisson_bias) && (!(gamma >= 0.0f) || !std::isfinite(gamma)))
+        return fail(BMND_ERR_INVALID_ARG, "gamma must be finite and non-negative");
     MatchArgs a{};
     fill_common(a, mp);
     a.thr_dev = thr_dev;
     a.noise_ssd = noise_ssd;
     a.gamma = gamma;
+    a.poisson_bias = poisson_bias ? 1 : 0;
+    a.bias_scale = static_cast<float>(mp.count_scale);  // the Python float meets float32 data
     a.no_alloc = allow_alloc ? 0 : 1;
     a.null_moments = null_moments;
     a.null_max = null_max;

@@ -185,7 +185,8 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
                                  int32_t* count, int32_t* accepted, cudaStream_t stream,
                                  const float* thr_dev = nullptr, const float* noise_ssd = nullptr,
                                  float gamma = 0.0f, bool allow_alloc = true,
-                                 const double* null_moments = nullptr, int null_max = 0);
+                                 const double* null_moments = nullptr, int null_max = 0,
+                                 bool poisson_bias = false);
 int32_t launch_reference_thresholds(const float* volume, const int32_t* refs, int64_t n_refs, int ndim,
                                     const int32_t* counts, const int32_t* block, const int32_t* shape,
                                     double count_scale, const double* moments, int max_count, double t,

@@ -125,6 +125,11 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     if gauss is None:
         p.noise_model = _abi.NOISE_POISSON
         p.count_scale = float(profile.poisson_count_scale)
+        if stage == "ht" and distance is BlockMatchDistance.SSD and float(profile.gamma) != 0.0:
+            # Poisson SSD noise bias, hard thresholding only (bmndalgo.py:292-294,
+            # blockmatching.py:244-262, :1140-1145); gamma reaches the kernel as float32
+            p.ssd_poisson_bias = 1
+            p.ssd_gamma = float(np.float32(profile.gamma))
         p.variance_floor = float(profile.poisson_variance_floor)
         gain = profile.poisson_wiener_gain_mode
         p.wiener_gain_mode = {PoissonWienerGainMode.VARIANCE_SCALED: _abi.GAIN_VARIANCE_SCALED,
@@ -222,8 +227,6 @@ def check_gaussian_options(profile, variance_k: int) -> None:
 def check_poisson_options(profile, variance_k: int) -> None:
     """Reject the non-default Poisson options that are not on the GPU path."""
     check_weight_options(profile, variance_k)
-    if profile.blockmatch_distance is BlockMatchDistance.SSD and float(profile.gamma) != 0.0:
-        raise unsupported("the Poisson SSD noise-bias correction (gamma != 0) is not on the GPU path")
     if profile.reference_schedule_mode not in (
         ReferenceScheduleMode.GENERATED,
         ReferenceScheduleMode.OFF,

@@ -143,7 +143,10 @@ typedef struct BmndStageParams {
      * (blockmatching.py:1133-1139), or NULL */
     const float* match_noise_ssd;
     float ssd_gamma;
-    int32_t reserved1;
+    /* Poisson SSD matching: 1 subtracts ssd_gamma * sum_p count_scale *
+     * (r_p + c_p) over r_p + c_p > 0 from every candidate's SSD but the
+     * reference's own (blockmatching.py:1140-1145, :432-443); 0 none */
+    int32_t ssd_poisson_bias;
     /* the stage's match threshold in float64: for SSD matching the threshold
      * is float32(ssd_threshold * (max - min)^2) over the matched volume
      * (blockmatching.py:168-184), evaluated on the device; the
@@ -247,6 +250,21 @@ int32_t bmnd_blockmatch_volume_biased(const BmndMatchParams* params, const float
                                       const float* d_thresholds, const float* d_noise_ssd, float gamma,
                                       int32_t* d_sel, int32_t* d_count, int32_t* d_accepted,
                                       uint64_t stream);
+
+/*
+ * bmnd_blockmatch_volume with the Poisson SSD noise-bias correction of
+ * blockmatch_groups(poisson_gamma=True, gamma=...) (blockmatching.py:1140-1145,
+ * :432-443): every candidate's SSD but the reference's own minus
+ * gamma * sum_p count_scale * (r_p + c_p) over r_p + c_p > 0, float32 in
+ * patch order.  params->distance must be BMND_DIST_SSD and
+ * params->count_scale the profile's poisson_count_scale.
+ */
+int32_t bmnd_blockmatch_volume_poisson_biased(const BmndMatchParams* params, const float* d_volume,
+                                              const int32_t* shape, const int32_t* block,
+                                              const int32_t* d_refs, int64_t n_refs,
+                                              const float* d_thresholds, float gamma,
+                                              int32_t* d_sel, int32_t* d_count, int32_t* d_accepted,
+                                              uint64_t stream);
 
 /*
  * Workspace bytes bmnd_stage() needs for `params` and n_refs references.

@@ -323,6 +323,9 @@ OPTION_CASES = {
                                           k=0)),
     "risk_windowed_bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=35),
                                     dict(wiener_weight_model="risk", wiener_weight_domain="windowed_synthesis")),
+    "ssd_gamma_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=36), dict(blockmatch_distance="ssd")),
+    "ssd_gamma_bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=37),
+                                dict(blockmatch_distance="ssd", gamma=2.5)),
 }
 
 

@@ -53,6 +53,84 @@ def selected(sel, cnt, i):
 SSD, DEV, PEARSON, ANSCOMBE = 0, 1, 2, 3
 
 
+def _volume_match(torch, native, volume, block, refs, radius, max_m, min_m, thr, gamma=None, scale=1.0):
+    """SSD matching over a volume through the C ABI; with ``gamma`` the Poisson
+    SSD noise-bias correction (bmnd_blockmatch_volume_poisson_biased)."""
+    from bmnd_gb300 import _abi
+
+    dev = torch.device("cuda:0")
+    vol = np.ascontiguousarray(volume, dtype=np.float32)
+    counts = tuple(s - b + 1 for s, b in zip(vol.shape, block))
+    vt = torch.from_numpy(vol).to(dev)
+    rt = torch.from_numpy(np.ascontiguousarray(refs, dtype=np.int32).reshape(-1, vol.ndim)).to(dev)
+    n = rt.shape[0]
+    tt = torch.full((n,), float(np.float32(thr)), dtype=torch.float32, device=dev)
+    sel = torch.full((n, max_m), -7, dtype=torch.int32, device=dev)
+    cnt = torch.zeros(n, dtype=torch.int32, device=dev)
+    acc = torch.zeros(n, dtype=torch.int32, device=dev)
+    p = _mp(counts, radius, max_m, min_m, SSD, stabilize=False, scale=scale, pow2=False)
+    shape = (ctypes.c_int32 * vol.ndim)(*vol.shape)
+    blk = (ctypes.c_int32 * vol.ndim)(*block)
+    if gamma is None:
+        rc = native.bmnd_blockmatch_volume(ctypes.byref(p), vt.data_ptr(), shape, blk, rt.data_ptr(), n,
+                                           tt.data_ptr(), sel.data_ptr(), cnt.data_ptr(), acc.data_ptr(), 0)
+    else:
+        rc = native.bmnd_blockmatch_volume_poisson_biased(ctypes.byref(p), vt.data_ptr(), shape, blk,
+                                                          rt.data_ptr(), n, tt.data_ptr(), float(gamma),
+                                                          sel.data_ptr(), cnt.data_ptr(), acc.data_ptr(), 0)
+    _abi.check(rc)
+    torch.cuda.synchronize()
+    return sel.cpu().numpy(), cnt.cpu().numpy(), acc.cpu().numpy()
+
+
+def test_poisson_gamma_corrects_ssd_noise_bias(cuda, native):
+    # tests/test_blockmatching_internal_unit.py:203-229: patches [0] and [2],
+    # threshold 1; the bias 1 * (0 + 2) times gamma 2 brings the SSD 4 to 0
+    vol = np.array([0.0, 2.0], dtype=np.float32)
+    sel, cnt, _ = _volume_match(cuda, native, vol, (1,), [[0]], (1,), 2, 1, 1.0)
+    assert selected(sel, cnt, 0) == [0]
+    sel, cnt, acc = _volume_match(cuda, native, vol, (1,), [[0]], (1,), 2, 1, 1.0, gamma=2.0)
+    assert selected(sel, cnt, 0) == [0, 1]
+    assert acc[0] == 2
+
+
+def test_poisson_gamma_bias_order_and_centre(cuda, native):
+    """Against a float32 restatement of the reference's loop (blockmatching.py:
+    323-336, :432-443, :1114-1145) on a random 2-D volume with a count scale:
+    accepted counts and match sets equal, the reference patch uncorrected."""
+    rng = np.random.default_rng(5)
+    vol = rng.poisson(6.0, size=(14, 13)).astype(np.float32)
+    vol[3:6, 4:9] = 0.0
+    block, radius, scale, gamma, thr, max_m = (4, 4), (3, 3), 0.75, 1.5, 40.0, 8
+    counts = (vol.shape[0] - 3, vol.shape[1] - 3)
+    refs = [(r, c) for r in range(0, counts[0], 2) for c in range(0, counts[1], 3)]
+    sel, cnt, acc = _volume_match(cuda, native, vol, block, refs, radius, max_m, 1, thr, gamma=gamma, scale=scale)
+    s32, g32 = np.float32(scale), np.float32(gamma)
+    for i, (r0, c0) in enumerate(refs):
+        ref = vol[r0:r0 + 4, c0:c0 + 4].reshape(-1)
+        scored = []
+        for r in range(max(r0 - 3, 0), min(r0 + 3, counts[0] - 1) + 1):
+            for c in range(max(c0 - 3, 0), min(c0 + 3, counts[1] - 1) + 1):
+                cand = vol[r:r + 4, c:c + 4].reshape(-1)
+                d = np.float32(0.0)
+                b = np.float32(0.0)
+                for p in range(16):
+                    diff = np.float32(cand[p] - ref[p])
+                    d = np.float32(d + np.float32(diff * diff))
+                    pooled = np.float32(ref[p] + cand[p])
+                    if pooled > 0.0:
+                        b = np.float32(b + np.float32(s32 * pooled))
+                if (r, c) != (r0, c0):
+                    d = np.float32(d - np.float32(g32 * b))
+                scored.append((d, r * counts[1] + c))
+        accepted = sorted(x for x in scored if x[0] < np.float32(thr))
+        centre = r0 * counts[1] + c0
+        # the row: the reference patch first, then the accepted by (distance, index)
+        want = [centre] + [lin for _, lin in accepted if lin != centre][: max_m - 1]
+        assert acc[i] == len(accepted), (i, acc[i], len(accepted))
+        assert selected(sel, cnt, i) == want, (i, selected(sel, cnt, i), want)
+
+
 def test_self_only_with_zero_radius(cuda, native):
     # tests/test_blockmatching_unit.py:11-30
     patches = np.array([[0.0, 0.0], [1.0, 1.0], [2.0, 2.0]], dtype=np.float32)

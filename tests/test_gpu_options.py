@@ -5,7 +5,9 @@ conservation in both stages (2-D and 3-D) and in the hard-thresholding stage
 only (ragged 2-D); the classic and noise-floor Wiener gains; the observation
 as the Wiener variance source and as the Wiener matching source; soft
 thresholding; the reference-finite-count and candidate-standardised HT match
-policies.
+policies; SSD matching with the Poisson noise-bias correction (gamma 3 and
+2.5), whose distances the GPU evaluates in the reference's float32 operation
+order, so its HT match sets must equal the reference's exactly.
 
 Stated tolerance (as for the default Poisson pipeline): stage-1 match sets
 equal the reference's except where the selection boundary is tied within the
@@ -63,7 +65,10 @@ def test_option_pipeline_matches_reference(cuda, native, oracle_lib, case):
     thr = float(np.float32(profile.ht_match_threshold))
 
     sel, cnt = matches["ht"]
-    if profile.poisson_ht_match_policy.value == "fixed":
+    if profile.blockmatch_distance.value == "ssd":
+        np.testing.assert_array_equal(cnt, g["ht_count"])
+        np.testing.assert_array_equal(sel, g["ht_sel"])
+    elif profile.poisson_ht_match_policy.value == "fixed":
         _, _, bad = compare_match_sets(oracle_lib, g["noisy"], blocks["ht"], g["ht_refs"], sel, cnt,
                                        g["ht_sel"], g["ht_count"], 1, thr)
         assert not bad, f"{case}/ht: unexplained match-set differences in groups {bad[:8]}"
