@@ -330,6 +330,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     import torch
 
     import bmnd_gb300 as bg
+    from bmnd_gb300 import _abi
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     dist = None
@@ -345,15 +346,18 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
-    def timed_loop(fn):
+    def timed_loop(fn, counts=None):
         """W untimed calls, then K calls each bracketed by CUDA events on the
-        launching stream, L2 flushed before each; returns (ms per call, last output)."""
+        launching stream, L2 flushed before each; returns (ms per call, last
+        output).  ``counts`` (a list) receives the native library's kernel
+        launches over the K timed calls."""
         for _ in range(args.warmup):
             res = fn()
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
+        n0 = _abi.launch_count()
         total = 0.0
         for _ in range(args.steps):
             flush.fill_(1)
@@ -364,6 +368,8 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
             e1.synchronize()
             total += e0.elapsed_time(e1)
         torch.cuda.synchronize()
+        if counts is not None:
+            counts.append(_abi.launch_count() - n0)
         t = total / args.steps
         if dist:
             dist.barrier()
@@ -384,7 +390,9 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
 
     sampler = ClockSampler(torch.cuda.current_device())
     sampler.start()
-    ms, out = timed_loop(lambda: bg.bmnd_device(x, profile, match_precision=args.precision, gauss=gauss))
+    plain_launches = []
+    ms, out = timed_loop(lambda: bg.bmnd_device(x, profile, match_precision=args.precision, gauss=gauss),
+                         plain_launches)
 
     # learned-pilot fast path (network trained by bmnd_gb300.train_pilot)
     from bmnd_gb300 import pilot as pl
@@ -395,7 +403,8 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     if os.path.exists(wpath) and gauss is None:
         net = pl.PilotNet.load(wpath)
         fdet = {}
-        ms_fast, out_fast = timed_loop(lambda: pl.bmnd_fast(x, profile, net, details=fdet))
+        fast_launches = []
+        ms_fast, out_fast = timed_loop(lambda: pl.bmnd_fast(x, profile, net, details=fdet), fast_launches)
         ms_fs2, out_fs2 = timed_loop(lambda: pl.stage_device(
             x, pl.fast_profile(profile), "wiener", pl.stage_device(x, profile, "ht"),
             match_precision=pl.FAST_MATCH_PRECISION))
@@ -522,7 +531,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         achieved = alg_bytes / (dom_ms * 1e-3) / 1e9
         bound, unit, peak_v = "hbm", "GB/s", peaks["hbm_gbs"]
     traffic = profile_traffic(dom_name, args.workload)
-    launches_per_step = 6  # per stage: blockmatch, group filter, finalize
+    launches = plain_launches[0]  # native kernels over the K timed calls
     plain_value = nvox * world / (ms * 1e-3) / 1e6
     psnr_plain = psnr(out.cpu().numpy(), clean)
     if fast is not None:
@@ -547,7 +556,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
             },
         }
         value = fast_block["value"]
-        launches_per_step = 16  # net: 9, residual check: 1, Wiener stage: 6
+        launches = fast_launches[0]
     elif gauss is not None:
         fast_block = {"unavailable": "the learned pilot is trained for Poisson counts only"}
         value = plain_value
@@ -604,7 +613,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         },
         "kernels": kt,
         "clocks": clocks,
-        "gpu_launches": launches_per_step * args.steps,
+        "gpu_launches": launches,
         "psnr_db": psnr_fast if fast is not None else psnr_plain,
     }
     if not args.skip_cpu:

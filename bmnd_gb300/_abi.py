@@ -151,6 +151,7 @@ _VP = ctypes.c_void_p
 SIGNATURES = {
     "bmnd_abi_version": (_I32, []),
     "bmnd_last_error": (ctypes.c_char_p, []),
+    "bmnd_launch_count": (_I32, [_U64P]),
     "bmnd_reference_schedule": (
         _I32,
         [_I32, _I32P, _I32P, _I32P, ctypes.c_double, _I32, _I32P, _I32P, _I32P, _I64, _I64P],
@@ -264,3 +265,10 @@ def check(code: int) -> None:
     if code != OK:
         msg = lib().bmnd_last_error()
         raise BmndError(code, msg.decode() if msg else "")
+
+
+def launch_count() -> int:
+    """Kernel launches of the native library since it was loaded."""
+    n = ctypes.c_uint64(0)
+    check(lib().bmnd_launch_count(ctypes.byref(n)))
+    return int(n.value)

@@ -3,6 +3,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <mutex>
 #include <set>
@@ -15,8 +16,10 @@ namespace bmnd {
 
 namespace {
 thread_local std::string g_last_error;
+std::atomic<uint64_t> g_launches{0};
 }
 
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void set_error(const std::string& msg) { g_last_error = msg; }
 void clear_error() { g_last_error.clear(); }
 int32_t fail(int32_t code, const std::string& msg) {
@@ -304,6 +307,13 @@ extern "C" {
 int32_t bmnd_abi_version(void) { return BMND_ABI_VERSION; }
 
 const char* bmnd_last_error(void) { return g_last_error.c_str(); }
+
+int32_t bmnd_launch_count(uint64_t* count) {
+    clear_error();
+    if (!count) return fail(BMND_ERR_INVALID_ARG, "null argument");
+    *count = g_launches.load(std::memory_order_relaxed);
+    return BMND_OK;
+}
 
 int32_t bmnd_reference_schedule(int32_t ndim, const int32_t* counts, const int32_t* block,
                                 const int32_t* step, double shift_density,

@@ -1620,7 +1620,10 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
             BMND_LAUNCH_CHECK("approx_voxel_kernel");
             auto boxes = [&](auto full, auto half) {
                 full<<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, n[0], n[1], n[2], boxb);
-                if (boxb_sub) half<<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, n[0], n[1], n[2], boxb_sub);
+                if (boxb_sub) {
+                    half<<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, n[0], n[1], n[2], boxb_sub);
+                    note_launch();  // the check below counts the full-box launch
+                }
             };
             if (a.ndim == 2)
                 boxes(approx_box_kernel<2, 8, 8, 1, 1>, approx_box_kernel<2, 8, 8, 1, 2>);

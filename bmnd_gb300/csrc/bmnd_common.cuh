@@ -22,6 +22,8 @@ void set_error(const std::string& msg);
 void clear_error();
 int32_t fail(int32_t code, const std::string& msg);
 int32_t cuda_fail(cudaError_t err, const char* what);
+// counts kernel launches of this library (bmnd_launch_count)
+void note_launch();
 
 #define BMND_CUDA_TRY(expr)                                      \
     do {                                                         \
@@ -29,8 +31,10 @@ int32_t cuda_fail(cudaError_t err, const char* what);
         if (_e != cudaSuccess) return ::bmnd::cuda_fail(_e, #expr); \
     } while (0)
 
+// after every kernel launch: counts it and reports a launch error
 #define BMND_LAUNCH_CHECK(what)                                   \
     do {                                                          \
+        ::bmnd::note_launch();                                    \
         cudaError_t _e = cudaGetLastError();                      \
         if (_e != cudaSuccess) return ::bmnd::cuda_fail(_e, what); \
     } while (0)

@@ -197,6 +197,10 @@ int32_t bmnd_abi_version(void);
 /* Message of the last failure on the calling thread ("" if none). */
 const char* bmnd_last_error(void);
 
+/* Kernel launches this library has made since it was loaded (all threads);
+ * the difference of two readings counts the launches between them. */
+int32_t bmnd_launch_count(uint64_t* count);
+
 /*
  * Host-only.  GENERATED reference schedule: replaces get_reference_schedule
  * with mode="generated" (src/bmnd/shifts.py:405-423, :519-576, :229-266).

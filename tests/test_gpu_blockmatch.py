@@ -86,10 +86,14 @@ def _volume_match(torch, native, volume, block, refs, radius, max_m, min_m, thr,
 def test_poisson_gamma_corrects_ssd_noise_bias(cuda, native):
     # tests/test_blockmatching_internal_unit.py:203-229: patches [0] and [2],
     # threshold 1; the bias 1 * (0 + 2) times gamma 2 brings the SSD 4 to 0
+    from bmnd_gb300 import _abi
+
     vol = np.array([0.0, 2.0], dtype=np.float32)
     sel, cnt, _ = _volume_match(cuda, native, vol, (1,), [[0]], (1,), 2, 1, 1.0)
     assert selected(sel, cnt, 0) == [0]
+    n0 = _abi.launch_count()
     sel, cnt, acc = _volume_match(cuda, native, vol, (1,), [[0]], (1,), 2, 1, 1.0, gamma=2.0)
+    assert _abi.launch_count() - n0 == 1  # one exact warp-kernel launch, counted by the library
     assert selected(sel, cnt, 0) == [0, 1]
     assert acc[0] == 2
 

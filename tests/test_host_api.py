@@ -34,6 +34,13 @@ def test_library_exports_every_declared_symbol(native):
     assert native.bmnd_abi_version() == _abi.ABI_VERSION
 
 
+def test_launch_counter_reads_without_a_gpu(native):
+    """bmnd_launch_count needs no device; nothing has launched in a CPU-only process."""
+    n = _abi.launch_count()
+    assert isinstance(n, int) and n >= 0
+    assert _abi.launch_count() == n
+
+
 def test_struct_layout_matches_header(tmp_path):
     """ctypes mirrors of the ABI structs have the C compiler's layout."""
     import shutil
