@@ -879,14 +879,7 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                         }
                     }
                     const unsigned has = __ballot_sync(0xffffffffu, bin >= 0);
-                    if (lane == 0) {
-                        if (!has) {
-                            redi[1] = -1;
-                        } else {
-                            const int src_lane = __ffs(has) - 1;
-                            (void)src_lane;
-                        }
-                    }
+                    if (lane == 0 && !has) redi[1] = -1;
                     if (has) {
                         const int src_lane = __ffs(has) - 1;
                         const int bsel = __shfl_sync(0xffffffffu, bin, src_lane);

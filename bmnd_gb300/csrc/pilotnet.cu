@@ -1290,7 +1290,7 @@ int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf1
     const cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(g.W) * 16, static_cast<cuuint64_t>(g.H) * g.W * 16};
     const cuuint32_t box[4] = {8, TT::hx, TT::hy, TT::hz};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
-    // the driver's encoder, fetched through the runtime (no link-time dependency on the driver library)
+    // the CUDA driver API's tensor-map encoder, fetched through the runtime (no link-time dependency on libcuda)
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
         cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
