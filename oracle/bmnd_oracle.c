@@ -241,6 +241,10 @@ typedef struct {
     int shape[MAXD];
     int block[MAXD];
     int use_f64;
+    /* Poisson SSD noise bias (blockmatching.py:1140-1145, :432-443): gamma
+     * and the count scale, both float32 as they meet the float32 patches */
+    int poisson_bias;
+    float bias_gamma, bias_scale;
 } match_ctx;
 
 static void get_patch(const match_ctx* m, int64_t lin, float* out) {
@@ -344,6 +348,15 @@ static void match_one(const match_ctx* m, const int32_t* center, float threshold
             dist = (float)oracle_patch_distance_f64(refp, candp, P, m->code, m->scale);
         else
             dist = oracle_patch_distance(refp, candp, P, m->code, m->scale);
+        if (m->poisson_bias && lin != center_lin) {
+            /* sum over r + c > 0 of scale * (r + c), float32 in patch order */
+            float bias = 0.0f;
+            for (int p = 0; p < P; ++p) {
+                float pooled = refp[p] + candp[p];
+                if (pooled > 0.0f) bias = bias + m->bias_scale * pooled;
+            }
+            dist = dist - m->bias_gamma * bias;
+        }
         float key = stab ? oracle_canonical(dist) : dist;
         if (key < tkey) {
             ++accepted;
@@ -437,6 +450,34 @@ int oracle_blockmatch_patches(const BmndMatchParams* p, const float* patches, in
     m.table = patches;
     m.patch_vol = patch_vol;
     m.use_f64 = use_f64;
+    return run_match(&m, refs, n_refs, thresholds, sel, count, accepted, threads);
+}
+
+/* oracle_blockmatch_volume with the Poisson SSD noise bias when gamma != 0
+ * (p->distance SSD, p->count_scale the profile's poisson_count_scale) */
+int oracle_blockmatch_volume_biased(const BmndMatchParams* p, const float* volume, const int32_t* shape,
+                                    const int32_t* block, const int32_t* refs, int64_t n_refs,
+                                    const float* thresholds, float gamma, int32_t* sel, int32_t* count,
+                                    int32_t* accepted, int32_t threads) {
+    match_ctx m;
+    memset(&m, 0, sizeof(m));
+    m.ndim = p->ndim;
+    for (int d = 0; d < p->ndim; ++d) {
+        m.counts[d] = p->counts[d];
+        m.radius[d] = p->search_radius[d];
+        m.shape[d] = shape[d];
+        m.block[d] = block[d];
+    }
+    m.max_m = p->max_matches;
+    m.min_m = p->min_matches;
+    m.pow2 = p->prefer_power_of_two;
+    m.code = p->distance;
+    m.stab = p->stabilize_ties;
+    m.scale = 1.0;
+    m.volume = volume;
+    m.poisson_bias = p->distance == BMND_DIST_SSD && gamma != 0.0f;
+    m.bias_gamma = gamma;
+    m.bias_scale = (float)p->count_scale;
     return run_match(&m, refs, n_refs, thresholds, sel, count, accepted, threads);
 }
 

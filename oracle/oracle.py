@@ -20,6 +20,7 @@ __all__ = [
     "canonical",
     "blockmatch_patches",
     "blockmatch_volume",
+    "blockmatch_volume_poisson_biased",
     "stage",
     "bmnd",
 ]
@@ -57,6 +58,9 @@ def load() -> ctypes.CDLL:
         L.oracle_blockmatch_volume.restype = i32
         L.oracle_blockmatch_volume.argtypes = [ctypes.POINTER(_abi.MatchParams), vp, vp, vp, vp, i64,
                                                vp, vp, vp, vp, i32, i32]
+        L.oracle_blockmatch_volume_biased.restype = i32
+        L.oracle_blockmatch_volume_biased.argtypes = [ctypes.POINTER(_abi.MatchParams), vp, vp, vp, vp, i64,
+                                                      vp, ctypes.c_float, vp, vp, vp, i32]
         L.oracle_stage.restype = i32
         L.oracle_stage.argtypes = [ctypes.POINTER(_abi.StageParams), vp, vp, vp, i64, vp, vp, vp, vp,
                                    i32]
@@ -148,6 +152,28 @@ def blockmatch_volume(volume, block, refs, radius, max_m, min_m, thresholds, cod
     acc = np.zeros(n, dtype=np.int32)
     assert L.oracle_blockmatch_volume(ctypes.byref(p), _ptr(volume), _ptr(shape), _ptr(blk), _ptr(refs),
                                       n, _ptr(thr), _ptr(sel), _ptr(cnt), _ptr(acc), int(f64), threads) == 0
+    return sel, cnt, acc
+
+
+def blockmatch_volume_poisson_biased(volume, block, refs, radius, max_m, min_m, thresholds, gamma,
+                                     count_scale=1.0, pow2=True, threads=0):
+    """SSD matching minus gamma times the Poisson pooled-count noise bias
+    (blockmatching.py:1140-1145, :432-443)."""
+    L = load()
+    volume = np.ascontiguousarray(volume, dtype=np.float32)
+    shape = np.asarray(volume.shape, dtype=np.int32)
+    blk = np.asarray(block, dtype=np.int32)
+    counts = shape - blk + 1
+    refs = np.ascontiguousarray(refs, dtype=np.int32).reshape(-1, volume.ndim)
+    n = refs.shape[0]
+    thr = np.ascontiguousarray(np.broadcast_to(np.asarray(thresholds, dtype=np.float32), (n,)))
+    p = _match_params(volume.ndim, counts, radius, max_m, min_m, 0, False, count_scale, pow2)
+    sel = np.full((n, max_m), -1, dtype=np.int32)
+    cnt = np.zeros(n, dtype=np.int32)
+    acc = np.zeros(n, dtype=np.int32)
+    assert L.oracle_blockmatch_volume_biased(ctypes.byref(p), _ptr(volume), _ptr(shape), _ptr(blk), _ptr(refs),
+                                             n, _ptr(thr), float(np.float32(gamma)), _ptr(sel), _ptr(cnt),
+                                             _ptr(acc), threads) == 0
     return sel, cnt, acc
 
 

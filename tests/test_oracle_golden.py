@@ -95,3 +95,38 @@ def test_oracle_schedule_matches_reference(oracle_lib, idx):
     np.testing.assert_array_equal(a, u[f"sched{idx}_abs"])
     np.testing.assert_array_equal(sh, u[f"sched{idx}_shifted"])
     np.testing.assert_array_equal(sf, u[f"sched{idx}_shift"])
+
+
+def test_oracle_poisson_ssd_bias_known_answer(oracle_lib):
+    # tests/test_blockmatching_internal_unit.py:203-229: patches [0] and [2],
+    # threshold 1; gamma 2 times the bias 1 * (0 + 2) brings the SSD 4 to 0
+    vol = np.array([0.0, 2.0], dtype=np.float32)
+    sel, cnt, _ = oracle_lib.blockmatch_volume_poisson_biased(vol, (1,), [[0]], (1,), 2, 1, 1.0, 0.0, pow2=False)
+    assert sel[0, : cnt[0]].tolist() == [0]
+    sel, cnt, acc = oracle_lib.blockmatch_volume_poisson_biased(vol, (1,), [[0]], (1,), 2, 1, 1.0, 2.0,
+                                                                pow2=False)
+    assert sel[0, : cnt[0]].tolist() == [0, 1] and acc[0] == 2
+
+
+@pytest.mark.parametrize("case", ["ssd_gamma_bm3d_32", "ssd_gamma_bm4d_12x16x20"])
+def test_oracle_poisson_ssd_bias_matches_reference(oracle_lib, case):
+    """The oracle's SSD matching with the Poisson noise bias reproduces the
+    reference's stage-1 match sets exactly (threshold float32(t (max - min)^2)
+    over the noisy volume, blockmatching.py:168-184)."""
+    import json
+
+    import bmnd_gb300 as bg
+
+    g = np.load(os.path.join(GOLDEN, f"opt_{case}.npz"))
+    cls = bg.BM3DProfile if str(g["kind"]) == "bm3d" else bg.BM4DProfile
+    profile = cls(noise_model=bg.NoiseModel.POISSON, **json.loads(str(g["extra_json"])))
+    noisy = g["noisy"]
+    d = np.float32(noisy.max()) - np.float32(noisy.min())
+    thr = np.float32(float(profile.ht_match_threshold) * float(d) * float(d))
+    sel, cnt, acc = oracle_lib.blockmatch_volume_poisson_biased(
+        noisy, tuple(profile.ht_block_size), g["ht_refs"], tuple(profile.ht_search_window),
+        int(profile.ht_max_stack_size), int(profile.ht_min_stack_size), thr, float(profile.gamma),
+        count_scale=float(profile.poisson_count_scale))
+    np.testing.assert_array_equal(cnt, g["ht_count"])
+    np.testing.assert_array_equal(sel, g["ht_sel"])
+    np.testing.assert_array_equal(acc, g["ht_accepted"])
