@@ -3,13 +3,16 @@
 Workload (default): 256^3 float32 BM4D-Poisson volume of 30 random ellipsoids
 (semi-axes 10-80 voxels, intensities U[5, 30], background 2, Poisson noise;
 seeded synthetic data, see bmnd_gb300/phantoms.py) denoised with
-BM4DProfile(noise_model="poisson") defaults: both stages (hard thresholding,
-then Wiener on the pilot).  One step = one full bmnd() call.
+BM4DProfile(noise_model="poisson") defaults.  One step = one denoising call.
 
-* ``value``  -- voxels / device time of bmnd_device() with the input resident
-  in HBM (CUDA events on the launching stream; L2 flushed between steps).
-* ``e2e``    -- the same metric through the public bmnd() call on a host
-  NumPy array: host->device copy, both stages, device->host copy.
+* ``value``  -- voxels / device time of the learned-pilot fast path
+  (pilot.bmnd_fast: the net, the per-tile check, the fast Wiener stage) with
+  the input resident in HBM (CUDA events on the launching stream; L2 flushed
+  between steps); without trained weights, of the plain path bmnd_device()
+  (hard thresholding, then Wiener on its pilot), which is also reported as
+  ``plain`` beside the fast path.
+* ``e2e``    -- the same path from host memory to host memory: copy in from a
+  page-locked buffer, denoise, copy the estimate back.
 * ``roofline`` -- the dominant kernel (largest share of the step), timed with
   CUDA events inside this script.
 * ``cpu_baseline`` -- the C oracle (the reference algorithm restated in C,
@@ -326,6 +329,19 @@ def time_kernels(torch, noisy_t, profile, reps: int = 2, stages=("ht", "wiener")
     return res
 
 
+def max_over_ranks(values, dist, device: str) -> list[float]:
+    """Element-wise maximum of per-rank floats over all ranks.  Every rank calls
+    it; ``dist`` None means a single rank.  ``device`` holds the reduction
+    tensor: "cuda" under NCCL, "cpu" under gloo."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def run_gpu(args, rank: int, world: int) -> dict | None:
     import torch
 
@@ -373,9 +389,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         t = total / args.steps
         if dist:
             dist.barrier()
-            tt = torch.tensor([t], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            t = float(tt.item())
+            t = max_over_ranks([t], dist, "cuda")[0]
         return t, res
 
     gauss = None
@@ -433,9 +447,8 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
             host_fast = pin_out.numpy()
         e2e_fast_s = (time.perf_counter() - t0) / e2e_steps
     if dist:
-        t = torch.tensor([e2e_s, e2e_fast_s or 0.0], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s, e2e_fast_s = float(t[0].item()), (float(t[1].item()) if fast is not None else None)
+        e2e_s, e2e_fast_max = max_over_ranks([e2e_s, e2e_fast_s or 0.0], dist, "cuda")
+        e2e_fast_s = e2e_fast_max if fast is not None else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
