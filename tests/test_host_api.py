@@ -191,3 +191,40 @@ def test_stage_params_defaults():
     assert ht.max_stack == 16 and wi.max_stack == 32 and ht.variance_k == 4
     assert abs(ht.match_threshold - 2.9527) < 1e-6 and abs(wi.match_threshold - 0.7689) < 1e-6
     assert abs(ht.ht_lambda - 3.0) < 1e-7 and abs(wi.wiener_scale - 0.4) < 1e-7
+
+
+def test_poisson_ssd_bias_parameters():
+    """The planner asks for the Poisson SSD noise bias in hard thresholding only,
+    with SSD matching and gamma != 0, gamma as float32 (bmndalgo.py:292-294,
+    blockmatching.py:244-262); the library's stage validation rejects an
+    inconsistent request before any launch (no GPU needed)."""
+    import ctypes
+
+    from bmnd_gb300.enums import BlockMatchDistance
+    from bmnd_gb300.validation import resolve_profile
+
+    shape = (32, 32)
+    prof = bg.BM3DProfile(noise_model="poisson", blockmatch_distance="ssd", gamma=2.5)
+    res = resolve_profile(prof, shape)
+    assert res.blockmatch_distance is BlockMatchDistance.SSD
+    ht = plan.stage_params(prof, shape, "ht", res.blockmatch_distance, res.variance_k)
+    wi = plan.stage_params(prof, shape, "wiener", res.blockmatch_distance, res.variance_k)
+    assert ht.distance == _abi.DIST_SSD and ht.ssd_poisson_bias == 1 and ht.ssd_gamma == np.float32(2.5)
+    assert wi.ssd_poisson_bias == 0
+    for other in (bg.BM3DProfile(noise_model="poisson", blockmatch_distance="ssd", gamma=0.0),
+                  bg.BM3DProfile(noise_model="poisson")):
+        r = resolve_profile(other, shape)
+        assert plan.stage_params(other, shape, "ht", r.blockmatch_distance, r.variance_k).ssd_poisson_bias == 0
+
+    L = _abi.lib()
+    nbytes = ctypes.c_uint64(0)
+    assert L.bmnd_stage_workspace_bytes(ctypes.byref(ht), 8, ctypes.byref(nbytes)) == _abi.OK
+    bad = plan.stage_params(prof, shape, "ht", res.blockmatch_distance, res.variance_k)
+    bad.distance = _abi.DIST_POISSON_DEVIANCE
+    assert L.bmnd_stage_workspace_bytes(ctypes.byref(bad), 8, ctypes.byref(nbytes)) != _abi.OK
+    bad = plan.stage_params(prof, shape, "ht", res.blockmatch_distance, res.variance_k)
+    bad.ssd_gamma = float("nan")
+    assert L.bmnd_stage_workspace_bytes(ctypes.byref(bad), 8, ctypes.byref(nbytes)) != _abi.OK
+    bad = plan.stage_params(prof, shape, "ht", res.blockmatch_distance, res.variance_k)
+    bad.ssd_poisson_bias = 2
+    assert L.bmnd_stage_workspace_bytes(ctypes.byref(bad), 8, ctypes.byref(nbytes)) != _abi.OK
