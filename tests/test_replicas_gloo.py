@@ -48,7 +48,7 @@ def test_max_over_ranks_two_gloo_ranks():
     ctx = mp.get_context("spawn")
     queue = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, queue)) for r in range(2)]
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, queue), daemon=True) for r in range(2)]
     for p in procs:
         p.start()
     try:
@@ -56,6 +56,9 @@ def test_max_over_ranks_two_gloo_ranks():
     finally:
         for p in procs:
             p.join(timeout=60)
+            if p.is_alive():  # a rank that never returned: end it (it is this test's own child)
+                p.terminate()
+                p.join(timeout=10)
     assert all(p.exitcode == 0 for p in procs)
     assert got[0] == got[1] == [2.5, 20.0, 0.25]
 
