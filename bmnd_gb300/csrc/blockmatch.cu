@@ -1609,8 +1609,16 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
             float* boxb_sub = a.sub ? aux + 3 * nvox : nullptr;
             int64_t nb = (nvox + 255) / 256;
             if (nb > 152 * 16) nb = 152 * 16;
+            // launch checks that release the scratch before reporting a failure
+            auto checked = [&](const char* what) -> int32_t {
+                note_launch();
+                const cudaError_t e = cudaGetLastError();
+                if (e == cudaSuccess) return BMND_OK;
+                (void)cudaFreeAsync(aux, stream);
+                return cuda_fail(e, what);
+            };
             approx_voxel_kernel<<<static_cast<unsigned>(nb), 256, 0, stream>>>(a.src, a.inv_scale, nvox, cv, bv);
-            BMND_LAUNCH_CHECK("approx_voxel_kernel");
+            if (int32_t rc0 = checked("approx_voxel_kernel")) return rc0;
             auto boxes = [&](auto full, auto half) {
                 full<<<static_cast<unsigned>(nb), 256, 0, stream>>>(bv, n[0], n[1], n[2], boxb);
                 if (boxb_sub) {
@@ -1624,7 +1632,7 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
                 boxes(approx_box_kernel<3, 5, 5, 5, 1>, approx_box_kernel<3, 5, 5, 5, 2>);
             else
                 boxes(approx_box_kernel<3, 4, 4, 4, 1>, approx_box_kernel<3, 4, 4, 4, 2>);
-            BMND_LAUNCH_CHECK("approx_box_kernel");
+            if (int32_t rc0 = checked("approx_box_kernel")) return rc0;
             a.cv = cv;
             a.boxb = boxb;
             a.boxb_sub = boxb_sub;
