@@ -566,10 +566,32 @@ static void group_matrix(int kind, int n, float* fwd, float* inv) {
         for (int j = 0; j < n; ++j) inv[i * n + j] = fwd[j * n + i];
 }
 
-/* out = M (applied along one axis) in, with fmaf accumulation in k order.
-   data: dims[0..nd-1] C order; axis a has extent dims[a] == m. */
-static void apply_axis(const float* in, float* out, const int* dims, int nd, int axis,
-                       const float* M) {
+/* ------------------------------------------------------------------ */
+/* filtering arithmetic type                                          */
+/* ------------------------------------------------------------------ */
+/* The default build rounds every filtering operation to float32, as the
+   reference does.  Built with -DORACLE_F64 (libbmnd_oracle_f64.so) the same
+   code carries transforms, noise statistics, shrinkage, weights, aggregation
+   and the final division in float64 on the same float32 transform matrices:
+   the reference's algorithm without its float32 rounding, against which the
+   per-stage error of a float32 implementation is measured.  Matching is
+   float32 in both builds (its decisions define the groups). */
+#ifdef ORACLE_F64
+typedef double real;
+#define RFMA fma
+#define RSQRT sqrt
+#define RABS fabs
+#else
+typedef float real;
+#define RFMA fmaf
+#define RSQRT sqrtf
+#define RABS fabsf
+#endif
+
+/* out = M (applied along one axis) in, with one fused multiply-add per term
+   in k order.  data: dims[0..nd-1] C order; axis a has extent dims[a] == m. */
+static void apply_axis(const real* in, real* out, const int* dims, int nd, int axis,
+                       const real* M) {
     int m = dims[axis];
     int64_t outer = 1, inner = 1;
     for (int d = 0; d < axis; ++d) outer *= dims[d];
@@ -577,9 +599,9 @@ static void apply_axis(const float* in, float* out, const int* dims, int nd, int
     for (int64_t o = 0; o < outer; ++o)
         for (int i = 0; i < m; ++i)
             for (int64_t t = 0; t < inner; ++t) {
-                float acc = 0.0f;
+                real acc = 0;
                 for (int k = 0; k < m; ++k)
-                    acc = fmaf(M[i * m + k], in[(o * m + k) * inner + t], acc);
+                    acc = RFMA(M[i * m + k], in[(o * m + k) * inner + t], acc);
                 out[(o * m + i) * inner + t] = acc;
             }
 }
@@ -592,13 +614,15 @@ typedef struct {
     const BmndStageParams* sp;
     int P;
     int counts[MAXD];
-    float gfwd[BMND_MAX_STACK + 1][BMND_MAX_STACK * BMND_MAX_STACK];
-    float ginv[BMND_MAX_STACK + 1][BMND_MAX_STACK * BMND_MAX_STACK];
-    float* S; /* kron of spatial forward matrices, P x P */
+    real gfwd[BMND_MAX_STACK + 1][BMND_MAX_STACK * BMND_MAX_STACK];
+    real ginv[BMND_MAX_STACK + 1][BMND_MAX_STACK * BMND_MAX_STACK];
+    real sfwd[MAXD][BMND_MAX_EDGE * BMND_MAX_EDGE];
+    real sinv[MAXD][BMND_MAX_EDGE * BMND_MAX_EDGE];
+    real* S; /* kron of spatial forward matrices, P x P */
 } stage_ctx;
 
-static void gather_patch(const float* vol, const int* shape, const int* block, int ndim,
-                         const int* pos, float* out) {
+static void gather_patch(const real* vol, const int* shape, const int* block, int ndim,
+                         const int* pos, real* out) {
     int idx = 0;
     if (ndim == 1) {
         for (int a = 0; a < block[0]; ++a) out[idx++] = vol[pos[0] + a];
@@ -615,80 +639,77 @@ static void gather_patch(const float* vol, const int* shape, const int* block, i
     }
 }
 
-static float variance_value(float x, const BmndStageParams* sp) {
-    /* variance.py:581-585: max(scale * max(x, 0), floor) in float32 */
-    float nn = x > 0.0f ? x : 0.0f;
-    float v = (float)sp->count_scale * nn;
-    float fl = (float)sp->variance_floor;
+static real variance_value(float x, const BmndStageParams* sp) {
+    /* variance.py:581-585: max(scale * max(x, 0), floor) */
+    real nn = x > 0.0f ? (real)x : (real)0;
+    real v = (real)sp->count_scale * nn;
+    real fl = (real)sp->variance_floor;
     return v > fl ? v : fl;
 }
 
 /* forward / inverse separable transform of an (n, block...) group */
-static void transform_group(const stage_ctx* c, int n, const float* in, float* out, float* tmp,
+static void transform_group(const stage_ctx* c, int n, const real* in, real* out, real* tmp,
                             int inverse) {
     const BmndStageParams* sp = c->sp;
     int dims[MAXD + 1];
     dims[0] = n;
     for (int d = 0; d < sp->ndim; ++d) dims[1 + d] = sp->block[d];
     int total = n * c->P;
-    memcpy(tmp, in, sizeof(float) * (size_t)total);
-    float* a = tmp;
-    float* b = out;
-    const float* G = inverse ? c->ginv[n] : c->gfwd[n];
-    int applied = 0;
+    memcpy(tmp, in, sizeof(real) * (size_t)total);
+    real* a = tmp;
+    real* b = out;
+    const real* G = inverse ? c->ginv[n] : c->gfwd[n];
     if (sp->group_transform != BMND_GROUP_NONE) {
         apply_axis(a, b, dims, sp->ndim + 1, 0, G);
-        float* t = a;
+        real* t = a;
         a = b;
         b = t;
-        ++applied;
     }
     for (int d = 0; d < sp->ndim; ++d) {
-        const float* M = inverse ? sp->spatial_inv[d] : sp->spatial_fwd[d];
+        const real* M = inverse ? c->sinv[d] : c->sfwd[d];
         apply_axis(a, b, dims, sp->ndim + 1, d + 1, M);
-        float* t = a;
+        real* t = a;
         a = b;
         b = t;
-        ++applied;
     }
-    if (a != out) memcpy(out, a, sizeof(float) * (size_t)total);
+    if (a != out) memcpy(out, a, sizeof(real) * (size_t)total);
 }
 
 /* approximate variance: squared transforms applied to the variance group
    (variance.py:613-623, :1647-1653); returns variance (not yet sqrt) */
-static void approx_variance(const stage_ctx* c, int n, const float* vg, float* out, float* tmp) {
+static void approx_variance(const stage_ctx* c, int n, const real* vg, real* out, real* tmp) {
     const BmndStageParams* sp = c->sp;
     int dims[MAXD + 1];
     dims[0] = n;
     for (int d = 0; d < sp->ndim; ++d) dims[1 + d] = sp->block[d];
     int total = n * c->P;
-    float* a = tmp;
-    float* b = out;
-    for (int i = 0; i < total; ++i) a[i] = vg[i] > 0.0f ? vg[i] : 0.0f;
-    float sq[BMND_MAX_STACK * BMND_MAX_STACK];
+    real* a = tmp;
+    real* b = out;
+    for (int i = 0; i < total; ++i) a[i] = vg[i] > 0 ? vg[i] : (real)0;
+    real sq[BMND_MAX_STACK * BMND_MAX_STACK] = {0};
     if (sp->group_transform != BMND_GROUP_NONE) {
         for (int i = 0; i < n * n; ++i) sq[i] = c->gfwd[n][i] * c->gfwd[n][i];
         apply_axis(a, b, dims, sp->ndim + 1, 0, sq);
-        float* t = a;
+        real* t = a;
         a = b;
         b = t;
     }
     for (int d = 0; d < sp->ndim; ++d) {
         int e = sp->block[d];
-        for (int i = 0; i < e * e; ++i) sq[i] = sp->spatial_fwd[d][i] * sp->spatial_fwd[d][i];
+        for (int i = 0; i < e * e; ++i) sq[i] = c->sfwd[d][i] * c->sfwd[d][i];
         apply_axis(a, b, dims, sp->ndim + 1, d + 1, sq);
-        float* t = a;
+        real* t = a;
         a = b;
         b = t;
     }
-    if (a != out) memcpy(out, a, sizeof(float) * (size_t)total);
+    if (a != out) memcpy(out, a, sizeof(real) * (size_t)total);
 }
 
 /* exact overlap-aware variance of the first kk planes
    (variance.py:758-851, :920-975): var[i,j] = sum_v V_v (sum_{e in v} E[e,(i,j)])^2 */
 static void exact_variance(const stage_ctx* c, int n, int kk, const int* pos /* n x ndim abs */,
-                           const float* Vvol, float* var /* kk x P */, int* cellmask_buf,
-                           float* contrib) {
+                           const real* Vvol, real* var /* kk x P */, int* cellmask_buf,
+                           real* contrib) {
     const BmndStageParams* sp = c->sp;
     int ndim = sp->ndim, P = c->P;
     int minp[MAXD], ushape[MAXD], shifted[BMND_MAX_STACK][MAXD];
@@ -722,7 +743,7 @@ static void exact_variance(const stage_ctx* c, int n, int kk, const int* pos /* 
         }
     }
     int coefs = kk * P;
-    for (int i = 0; i < coefs; ++i) var[i] = 0.0f;
+    for (int i = 0; i < coefs; ++i) var[i] = 0;
     for (int64_t cell = 0; cell < ucells; ++cell) {
         uint32_t m = mask[cell];
         if (!m) continue;
@@ -736,95 +757,99 @@ static void exact_variance(const stage_ctx* c, int n, int kk, const int* pos /* 
         for (int d = 0; d < ndim; ++d) apos[d] = ucoord[d] + minp[d];
         int64_t vidx = 0;
         for (int d = 0; d < ndim; ++d) vidx = vidx * sp->shape[d] + apos[d];
-        float V = Vvol[vidx];
-        for (int i = 0; i < coefs; ++i) contrib[i] = 0.0f;
+        real V = Vvol[vidx];
+        for (int i = 0; i < coefs; ++i) contrib[i] = 0;
         for (int g = 0; g < n; ++g) {
             if (!(m & (1u << g))) continue;
             int p = 0;
             for (int d = 0; d < ndim; ++d) p = p * sp->block[d] + (ucoord[d] - shifted[g][d]);
             for (int i = 0; i < kk; ++i) {
-                float G = c->gfwd[n][i * n + g];
+                real G = c->gfwd[n][i * n + g];
                 for (int j = 0; j < P; ++j) contrib[i * P + j] += G * c->S[j * P + p];
             }
         }
         for (int i = 0; i < coefs; ++i) {
-            float v = contrib[i];
+            real v = contrib[i];
             var[i] = var[i] + V * v * v;
         }
     }
 }
 
 /* noise std of every coefficient (variance.py:1634-1711, :1572-1631) */
-static void group_sigma(const stage_ctx* c, int n, const int* pos, const float* vgroup,
-                        const float* Vvol, float* sigma, float* work, int* cellbuf) {
+static void group_sigma(const stage_ctx* c, int n, const int* pos, const real* vgroup,
+                        const real* Vvol, real* sigma, real* work, int* cellbuf) {
     const BmndStageParams* sp = c->sp;
     int P = c->P, total = n * P;
-    float* approx = work;             /* total */
-    float* tmp = work + total;        /* total */
-    float* exact = work + 2 * total;  /* kk*P */
-    float* contrib = work + 3 * total; /* kk*P */
+    real* approx = work;             /* total */
+    real* tmp = work + total;        /* total */
+    real* exact = work + 2 * total;  /* kk*P */
+    real* contrib = work + 3 * total; /* kk*P */
     int k = sp->variance_k;
     if (k <= 0) {
         approx_variance(c, n, vgroup, approx, tmp);
-        for (int i = 0; i < total; ++i) sigma[i] = sqrtf(approx[i] > 0.0f ? approx[i] : 0.0f);
+        for (int i = 0; i < total; ++i) sigma[i] = RSQRT(approx[i] > 0 ? approx[i] : (real)0);
         return;
     }
     int kk = k < n ? k : n;
     exact_variance(c, n, kk, pos, Vvol, exact, cellbuf, contrib);
-    for (int i = 0; i < kk * P; ++i) exact[i] = sqrtf(exact[i] > 0.0f ? exact[i] : 0.0f);
+    for (int i = 0; i < kk * P; ++i) exact[i] = RSQRT(exact[i] > 0 ? exact[i] : (real)0);
     if (kk == n) {
-        memcpy(sigma, exact, sizeof(float) * (size_t)total);
+        memcpy(sigma, exact, sizeof(real) * (size_t)total);
         return;
     }
     approx_variance(c, n, vgroup, approx, tmp);
-    for (int i = 0; i < total; ++i) approx[i] = sqrtf(approx[i] > 0.0f ? approx[i] : 0.0f);
+    for (int i = 0; i < total; ++i) approx[i] = RSQRT(approx[i] > 0 ? approx[i] : (real)0);
     /* limit_poisson_group_variance_planes */
     for (int j = 0; j < P; ++j) {
-        float sum_a = 0.0f, sum_e = 0.0f, rem_a = 0.0f;
+        real sum_a = 0, sum_e = 0, rem_a = 0;
         for (int i = 0; i < n; ++i) {
-            float s = approx[i * P + j] > 0.0f ? approx[i * P + j] : 0.0f;
+            real s = approx[i * P + j] > 0 ? approx[i * P + j] : (real)0;
             sum_a = sum_a + s * s;
         }
         for (int i = 0; i < kk; ++i) {
-            float s = exact[i * P + j] > 0.0f ? exact[i * P + j] : 0.0f;
+            real s = exact[i * P + j] > 0 ? exact[i * P + j] : (real)0;
             sum_e = sum_e + s * s;
         }
         for (int i = kk; i < n; ++i) {
-            float s = approx[i * P + j] > 0.0f ? approx[i * P + j] : 0.0f;
+            real s = approx[i * P + j] > 0 ? approx[i * P + j] : (real)0;
             rem_a = rem_a + s * s;
         }
-        float target = sum_a - sum_e;
-        if (target < 0.0f) target = 0.0f;
-        float scale = rem_a > 0.0f ? target / rem_a : 0.0f;
+        real target = sum_a - sum_e;
+        if (target < 0) target = 0;
+        real scale = rem_a > 0 ? target / rem_a : (real)0;
         for (int i = 0; i < n; ++i) {
-            float v;
+            real v;
             if (i < kk) {
-                float s = exact[i * P + j] > 0.0f ? exact[i * P + j] : 0.0f;
+                real s = exact[i * P + j] > 0 ? exact[i * P + j] : (real)0;
                 v = s * s;
             } else {
-                float s = approx[i * P + j] > 0.0f ? approx[i * P + j] : 0.0f;
+                real s = approx[i * P + j] > 0 ? approx[i * P + j] : (real)0;
                 v = s * s;
                 v = v * scale;
-                if (!(rem_a > 0.0f)) v = target / (float)(double)(n - kk);
+                if (!(rem_a > 0)) v = target / (real)(n - kk);
             }
-            sigma[i * P + j] = sqrtf(v > 0.0f ? v : 0.0f);
+            sigma[i * P + j] = RSQRT(v > 0 ? v : (real)0);
         }
     }
 }
 
-/* poisson.py:30-46 */
-static int ht_keep(float mag, float thr, double scale) {
+/* poisson.py:30-46: keep iff cc > tc + 128 eps32 max(cc, tc, 1) in float64.
+   *margin receives |cc - boundary| / boundary, the decision's relative
+   distance from its threshold. */
+static int ht_keep(real mag, real thr, double scale, double* margin) {
     double cc = (double)mag / scale;
     double tc = (double)thr / scale;
     double cs = cc > tc ? cc : tc;
     if (cs < 1.0) cs = 1.0;
     double tol = 128.0 * (double)1.1920928955078125e-07 * cs;
-    return cc > tc + tol;
+    double bound = tc + tol;
+    *margin = bound > 0.0 ? fabs(cc - bound) / bound : INFINITY;
+    return cc > bound;
 }
 
 /* aggregationweights.py:213-259, :616-630 */
-static void patch_weights(const stage_ctx* c, int n, const float* att, const float* nvar,
-                          float* w) {
+static void patch_weights(const stage_ctx* c, int n, const real* att, const real* nvar,
+                          real* w) {
     const BmndStageParams* sp = c->sp;
     int P = c->P;
     double plane[BMND_MAX_STACK];
@@ -846,22 +871,23 @@ static void patch_weights(const stage_ctx* c, int n, const float* att, const flo
             risk += (gi * gi) * plane[g];
         }
         if (!isfinite(risk) || risk < 0.0)
-            w[o] = 0.0f;
+            w[o] = 0;
         else
-            w[o] = (float)(1.0 / (risk + sp->eps));
+            w[o] = (real)(1.0 / (risk + sp->eps));
     }
 }
 
 typedef struct {
     int n;
     int32_t lins[BMND_MAX_STACK];
-    float weights[BMND_MAX_STACK];
-    float* filt; /* n x P */
+    real weights[BMND_MAX_STACK];
+    double margin; /* smallest relative distance of a hard-threshold decision from its threshold */
+    real* filt;    /* n x P */
 } filtered_t;
 
-static void filter_group(const stage_ctx* c, const float* noisy, const float* pilot,
-                         const float* Vvol, const int32_t* sel, int n, filtered_t* res,
-                         float* buf, int* cellbuf) {
+static void filter_group(const stage_ctx* c, const real* noisy, const real* pilot,
+                         const real* Vvol, const int32_t* sel, int n, filtered_t* res,
+                         real* buf, int* cellbuf) {
     const BmndStageParams* sp = c->sp;
     int P = c->P, ndim = sp->ndim, total = n * P;
     int pos[BMND_MAX_STACK * MAXD];
@@ -872,17 +898,15 @@ static void filter_group(const stage_ctx* c, const float* noisy, const float* pi
             rem /= c->counts[d];
         }
     }
-    float* grp = buf;              /* total */
-    float* coef = buf + total;     /* total */
-    float* tmp = buf + 2 * total;  /* total */
-    float* vg = buf + 3 * total;   /* total */
-    float* sigma = buf + 4 * total; /* total */
-    float* att = buf + 5 * total;  /* total */
-    float* nv = buf + 6 * total;   /* total */
-    float* rcoef = buf + 7 * total; /* total */
-    float* work = buf + 8 * total; /* 4*total */
-    const float* varsrc = sp->filter == BMND_FILTER_WIENER ? pilot : noisy;
-    (void)varsrc;
+    real* grp = buf;              /* total */
+    real* coef = buf + total;     /* total */
+    real* tmp = buf + 2 * total;  /* total */
+    real* vg = buf + 3 * total;   /* total */
+    real* sigma = buf + 4 * total; /* total */
+    real* att = buf + 5 * total;  /* total */
+    real* nv = buf + 6 * total;   /* total */
+    real* rcoef = buf + 7 * total; /* total */
+    real* work = buf + 8 * total; /* 4*total */
     for (int g = 0; g < n; ++g) {
         gather_patch(noisy, sp->shape, sp->block, ndim, pos + g * ndim, grp + g * P);
         gather_patch(Vvol, sp->shape, sp->block, ndim, pos + g * ndim, vg + g * P);
@@ -890,26 +914,29 @@ static void filter_group(const stage_ctx* c, const float* noisy, const float* pi
     transform_group(c, n, grp, coef, tmp, 0);
     group_sigma(c, n, pos, vg, Vvol, sigma, work, cellbuf);
     for (int i = 0; i < total; ++i) nv[i] = sigma[i] * sigma[i];
+    res->margin = INFINITY;
     if (sp->filter == BMND_FILTER_HARD_THRESHOLD) {
         for (int i = 0; i < total; ++i) {
-            float thr = sp->ht_lambda * sigma[i];
-            int keep = ht_keep(fabsf(coef[i]), thr, sp->count_scale);
-            att[i] = keep ? 1.0f : 0.0f;
-            coef[i] = coef[i] * (keep ? 1.0f : 0.0f);
+            real thr = (real)sp->ht_lambda * sigma[i];
+            double mg;
+            int keep = ht_keep(RABS(coef[i]), thr, sp->count_scale, &mg);
+            if (mg < res->margin) res->margin = mg;
+            att[i] = keep ? (real)1 : (real)0;
+            coef[i] = coef[i] * (keep ? (real)1 : (real)0);
         }
     } else {
         for (int g = 0; g < n; ++g)
             gather_patch(pilot, sp->shape, sp->block, ndim, pos + g * ndim, grp + g * P);
         transform_group(c, n, grp, rcoef, tmp, 0);
         for (int i = 0; i < total; ++i) {
-            float eff = sp->wiener_scale * nv[i];
-            float pr = fabsf(rcoef[i]);
+            real eff = (real)sp->wiener_scale * nv[i];
+            real pr = RABS(rcoef[i]);
             pr = pr * pr;
-            float spow = pr - eff;
-            if (spow < 0.0f) spow = 0.0f;
-            float gain = spow / (spow + eff + (float)sp->eps);
-            if (gain < 0.0f) gain = 0.0f;
-            if (gain > 1.0f) gain = 1.0f;
+            real spow = pr - eff;
+            if (spow < 0) spow = 0;
+            real gain = spow / (spow + eff + (real)sp->eps);
+            if (gain < 0) gain = 0;
+            if (gain > 1) gain = 1;
             att[i] = gain;
             coef[i] = coef[i] * gain;
         }
@@ -920,28 +947,55 @@ static void filter_group(const stage_ctx* c, const float* noisy, const float* pi
     for (int g = 0; g < n; ++g) res->lins[g] = sel[g];
 }
 
-int oracle_stage(const BmndStageParams* sp, const float* noisy, const float* pilot,
-                 const int32_t* refs, int64_t n_refs, float* out, int32_t* sel_out,
-                 int32_t* count_out, int32_t* accepted_out, int32_t threads) {
+static real* widen_volume(const float* v, int64_t nvox) {
+    real* out = (real*)malloc(sizeof(real) * (size_t)nvox);
+    for (int64_t i = 0; i < nvox; ++i) out[i] = (real)v[i];
+    return out;
+}
+
+/*
+ * One stage (bmndalgo.py:230-633 hard thresholding, :648-1046 Wiener).
+ * With use_sel set, sel_io / count_io are inputs: the stage filters those
+ * groups instead of matching (accepted_out is then untouched); otherwise they
+ * receive the match sets when not NULL.  margin_out (n_refs doubles, or NULL)
+ * receives each group's smallest relative distance of a hard-threshold
+ * decision from its threshold (+inf for Wiener groups).
+ */
+int oracle_stage_ex(const BmndStageParams* sp, const float* noisy, const float* pilot,
+                    const int32_t* refs, int64_t n_refs, float* out, int32_t* sel_io,
+                    int32_t* count_io, int32_t* accepted_out, int32_t use_sel, double* margin_out,
+                    int32_t threads) {
     int ndim = sp->ndim;
-    stage_ctx c;
-    memset(&c, 0, sizeof(c));
-    c.sp = sp;
-    c.P = 1;
+    stage_ctx* cp = (stage_ctx*)calloc(1, sizeof(stage_ctx));
+    stage_ctx* c = cp;
+    c->sp = sp;
+    c->P = 1;
     int64_t nvox = 1;
     for (int d = 0; d < ndim; ++d) {
-        c.P *= sp->block[d];
-        c.counts[d] = sp->shape[d] - sp->block[d] + 1;
+        c->P *= sp->block[d];
+        c->counts[d] = sp->shape[d] - sp->block[d] + 1;
         nvox *= sp->shape[d];
     }
-    int P = c.P;
-    for (int n = 1; n <= sp->max_stack; ++n) group_matrix(sp->group_transform, n, c.gfwd[n], c.ginv[n]);
-    /* S = kron of spatial forwards, built axis by axis in float32 */
-    c.S = (float*)malloc(sizeof(float) * (size_t)P * (size_t)P);
+    int P = c->P;
+    for (int n = 1; n <= sp->max_stack; ++n) {
+        float f[BMND_MAX_STACK * BMND_MAX_STACK], iv[BMND_MAX_STACK * BMND_MAX_STACK];
+        group_matrix(sp->group_transform, n, f, iv);
+        for (int i = 0; i < n * n; ++i) {
+            c->gfwd[n][i] = (real)f[i];
+            c->ginv[n][i] = (real)iv[i];
+        }
+    }
+    for (int d = 0; d < ndim; ++d)
+        for (int i = 0; i < sp->block[d] * sp->block[d]; ++i) {
+            c->sfwd[d][i] = (real)sp->spatial_fwd[d][i];
+            c->sinv[d][i] = (real)sp->spatial_inv[d][i];
+        }
+    /* S = kron of spatial forwards, built axis by axis */
+    c->S = (real*)malloc(sizeof(real) * (size_t)P * (size_t)P);
     {
-        float* full = (float*)malloc(sizeof(float) * (size_t)P * (size_t)P);
-        float* nxt = (float*)malloc(sizeof(float) * (size_t)P * (size_t)P);
-        full[0] = 1.0f;
+        real* full = (real*)malloc(sizeof(real) * (size_t)P * (size_t)P);
+        real* nxt = (real*)malloc(sizeof(real) * (size_t)P * (size_t)P);
+        full[0] = 1;
         int fs = 1;
         for (int d = 0; d < ndim; ++d) {
             int e = sp->block[d], ns = fs * e;
@@ -949,57 +1003,66 @@ int oracle_stage(const BmndStageParams* sp, const float* noisy, const float* pil
                 for (int j = 0; j < fs; ++j)
                     for (int a = 0; a < e; ++a)
                         for (int b = 0; b < e; ++b)
-                            nxt[(i * e + a) * ns + j * e + b] = full[i * fs + j] * sp->spatial_fwd[d][a * e + b];
-            float* t = full;
+                            nxt[(i * e + a) * ns + j * e + b] = full[i * fs + j] * c->sfwd[d][a * e + b];
+            real* t = full;
             full = nxt;
             nxt = t;
             fs = ns;
         }
-        memcpy(c.S, full, sizeof(float) * (size_t)P * (size_t)P);
+        memcpy(c->S, full, sizeof(real) * (size_t)P * (size_t)P);
         free(full);
         free(nxt);
     }
     /* variance volume (from the observation for HT, from the pilot for Wiener) */
     const float* vsrc = sp->filter == BMND_FILTER_WIENER ? pilot : noisy;
-    float* Vvol = (float*)malloc(sizeof(float) * (size_t)nvox);
+    real* Vvol = (real*)malloc(sizeof(real) * (size_t)nvox);
     for (int64_t i = 0; i < nvox; ++i) Vvol[i] = variance_value(vsrc[i], sp);
-    /* matching source: the observation for HT, the pilot for Wiener */
-    const float* msrc = sp->filter == BMND_FILTER_WIENER ? pilot : noisy;
-    BmndMatchParams mp;
-    memset(&mp, 0, sizeof(mp));
-    mp.ndim = ndim;
-    for (int d = 0; d < ndim; ++d) {
-        mp.counts[d] = c.counts[d];
-        mp.search_radius[d] = sp->search_radius[d];
+    real* noisy_r = widen_volume(noisy, nvox);
+    real* pilot_r = pilot ? widen_volume(pilot, nvox) : NULL;
+    int32_t* sel = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n_refs > 0 ? n_refs : 1) * (size_t)sp->max_stack);
+    int32_t* cnt = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n_refs > 0 ? n_refs : 1));
+    if (use_sel) {
+        memcpy(sel, sel_io, sizeof(int32_t) * (size_t)n_refs * (size_t)sp->max_stack);
+        memcpy(cnt, count_io, sizeof(int32_t) * (size_t)n_refs);
+    } else {
+        /* matching source: the observation for HT, the pilot for Wiener */
+        const float* msrc = sp->filter == BMND_FILTER_WIENER ? pilot : noisy;
+        BmndMatchParams mp;
+        memset(&mp, 0, sizeof(mp));
+        mp.ndim = ndim;
+        for (int d = 0; d < ndim; ++d) {
+            mp.counts[d] = c->counts[d];
+            mp.search_radius[d] = sp->search_radius[d];
+        }
+        mp.max_matches = sp->max_stack;
+        mp.min_matches = sp->min_stack;
+        mp.prefer_power_of_two = 1;
+        mp.distance = sp->distance;
+        mp.stabilize_ties = sp->stabilize_ties;
+        mp.count_scale = sp->count_scale;
+        int32_t* acc = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n_refs > 0 ? n_refs : 1));
+        float* thr = (float*)malloc(sizeof(float) * (size_t)(n_refs > 0 ? n_refs : 1));
+        for (int64_t i = 0; i < n_refs; ++i) thr[i] = sp->match_threshold;
+        int32_t shape[MAXD], block[MAXD];
+        for (int d = 0; d < ndim; ++d) {
+            shape[d] = sp->shape[d];
+            block[d] = sp->block[d];
+        }
+        oracle_blockmatch_volume(&mp, msrc, shape, block, refs, n_refs, thr, sel, cnt, acc, 0, threads);
+        if (sel_io) memcpy(sel_io, sel, sizeof(int32_t) * (size_t)n_refs * (size_t)sp->max_stack);
+        if (count_io) memcpy(count_io, cnt, sizeof(int32_t) * (size_t)n_refs);
+        if (accepted_out) memcpy(accepted_out, acc, sizeof(int32_t) * (size_t)n_refs);
+        free(acc);
+        free(thr);
     }
-    mp.max_matches = sp->max_stack;
-    mp.min_matches = sp->min_stack;
-    mp.prefer_power_of_two = 1;
-    mp.distance = sp->distance;
-    mp.stabilize_ties = sp->stabilize_ties;
-    mp.count_scale = sp->count_scale;
-    int32_t* sel = (int32_t*)malloc(sizeof(int32_t) * (size_t)n_refs * (size_t)sp->max_stack);
-    int32_t* cnt = (int32_t*)malloc(sizeof(int32_t) * (size_t)n_refs);
-    int32_t* acc = (int32_t*)malloc(sizeof(int32_t) * (size_t)n_refs);
-    float* thr = (float*)malloc(sizeof(float) * (size_t)n_refs);
-    for (int64_t i = 0; i < n_refs; ++i) thr[i] = sp->match_threshold;
-    int32_t shape[MAXD], block[MAXD];
-    for (int d = 0; d < ndim; ++d) {
-        shape[d] = sp->shape[d];
-        block[d] = sp->block[d];
-    }
-    oracle_blockmatch_volume(&mp, msrc, shape, block, refs, n_refs, thr, sel, cnt, acc, 0, threads);
-    if (sel_out) memcpy(sel_out, sel, sizeof(int32_t) * (size_t)n_refs * (size_t)sp->max_stack);
-    if (count_out) memcpy(count_out, cnt, sizeof(int32_t) * (size_t)n_refs);
-    if (accepted_out) memcpy(accepted_out, acc, sizeof(int32_t) * (size_t)n_refs);
 
-    float* num = (float*)calloc((size_t)nvox, sizeof(float));
-    float* den = (float*)calloc((size_t)nvox, sizeof(float));
+    real* num = (real*)calloc((size_t)nvox, sizeof(real));
+    real* den = (real*)calloc((size_t)nvox, sizeof(real));
     int64_t ushape_cap = 1;
     for (int d = 0; d < ndim; ++d) ushape_cap *= (2 * sp->search_radius[d] + sp->block[d] + 1);
     const int64_t chunk = 2048;
     filtered_t* res = (filtered_t*)malloc(sizeof(filtered_t) * (size_t)chunk);
-    float* filt_store = (float*)malloc(sizeof(float) * (size_t)chunk * (size_t)sp->max_stack * (size_t)P);
+    real* filt_store = (real*)malloc(sizeof(real) * (size_t)chunk * (size_t)sp->max_stack * (size_t)P);
     for (int64_t i = 0; i < chunk; ++i) res[i].filt = filt_store + i * sp->max_stack * P;
 #ifdef _OPENMP
     if (threads <= 0) threads = omp_get_max_threads();
@@ -1010,7 +1073,7 @@ int oracle_stage(const BmndStageParams* sp, const float* noisy, const float* pil
 #pragma omp parallel num_threads(threads)
 #endif
         {
-            float* buf = (float*)malloc(sizeof(float) * (size_t)12 * (size_t)sp->max_stack * (size_t)P);
+            real* buf = (real*)malloc(sizeof(real) * (size_t)12 * (size_t)sp->max_stack * (size_t)P);
             int* cellbuf = (int*)malloc(sizeof(int) * (size_t)ushape_cap);
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 8)
@@ -1018,22 +1081,25 @@ int oracle_stage(const BmndStageParams* sp, const float* noisy, const float* pil
             for (int64_t i = 0; i < m; ++i) {
                 int64_t r = base + i;
                 res[i].n = 0;
+                res[i].margin = INFINITY;
                 if (cnt[r] <= 0) continue;
-                filter_group(&c, noisy, pilot, Vvol, sel + r * sp->max_stack, cnt[r], &res[i], buf, cellbuf);
+                filter_group(c, noisy_r, pilot_r, Vvol, sel + r * sp->max_stack, cnt[r], &res[i], buf,
+                             cellbuf);
             }
             free(buf);
             free(cellbuf);
         }
         /* scatter in schedule order (patchaggregation.py:170-199) */
         for (int64_t i = 0; i < m; ++i) {
+            if (margin_out) margin_out[base + i] = res[i].margin;
             for (int g = 0; g < res[i].n; ++g) {
                 int p0[MAXD];
                 int64_t rem = res[i].lins[g];
                 for (int d = ndim - 1; d >= 0; --d) {
-                    p0[d] = (int)(rem % c.counts[d]);
-                    rem /= c.counts[d];
+                    p0[d] = (int)(rem % c->counts[d]);
+                    rem /= c->counts[d];
                 }
-                float w = res[i].weights[g];
+                real w = res[i].weights[g];
                 for (int p = 0; p < P; ++p) {
                     int loc[MAXD], prem = p;
                     for (int d = ndim - 1; d >= 0; --d) {
@@ -1042,7 +1108,7 @@ int oracle_stage(const BmndStageParams* sp, const float* noisy, const float* pil
                     }
                     int64_t x = 0;
                     for (int d = 0; d < ndim; ++d) x = x * sp->shape[d] + p0[d] + loc[d];
-                    float ww = w * sp->window[p];
+                    real ww = w * (real)sp->window[p];
                     num[x] = num[x] + res[i].filt[g * P + p] * ww;
                     den[x] = den[x] + ww;
                 }
@@ -1050,16 +1116,24 @@ int oracle_stage(const BmndStageParams* sp, const float* noisy, const float* pil
         }
     }
     for (int64_t i = 0; i < nvox; ++i)
-        out[i] = den[i] > 0.0f ? num[i] / (den[i] + (float)sp->eps) : noisy[i];
+        out[i] = den[i] > 0 ? (float)(num[i] / (den[i] + (real)sp->eps)) : noisy[i];
     free(res);
     free(filt_store);
     free(num);
     free(den);
     free(sel);
     free(cnt);
-    free(acc);
-    free(thr);
     free(Vvol);
-    free(c.S);
+    free(noisy_r);
+    free(pilot_r);
+    free(c->S);
+    free(cp);
     return BMND_OK;
+}
+
+int oracle_stage(const BmndStageParams* sp, const float* noisy, const float* pilot,
+                 const int32_t* refs, int64_t n_refs, float* out, int32_t* sel_out,
+                 int32_t* count_out, int32_t* accepted_out, int32_t threads) {
+    return oracle_stage_ex(sp, noisy, pilot, refs, n_refs, out, sel_out, count_out, accepted_out, 0, NULL,
+                           threads);
 }

@@ -10,11 +10,14 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_ref", "libbmnd_oracle.so")
+LIB64_PATH = os.path.join(HERE, "_ref", "libbmnd_oracle_f64.so")
 _lib = None
+_lib64 = None
 
 __all__ = [
     "build",
     "load",
+    "load_f64",
     "schedule",
     "patch_distance",
     "canonical",
@@ -27,12 +30,35 @@ __all__ = [
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (gcc only)."""
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(
-        os.path.join(HERE, "bmnd_oracle.c")
-    ):
+    """Compile the oracle (float32 and float64 builds) with its Makefile (gcc only)."""
+    src = os.path.getmtime(os.path.join(HERE, "bmnd_oracle.c"))
+    stale = any(not os.path.exists(p) or os.path.getmtime(p) < src for p in (LIB_PATH, LIB64_PATH))
+    if force or stale:
         subprocess.run(["make", "-s", "-C", HERE] + (["-B"] if force else []), check=True)
     return LIB_PATH
+
+
+def _bind_stage(L) -> None:
+    from bmnd_gb300 import _abi
+
+    i32, i64, vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p
+    L.oracle_stage.restype = i32
+    L.oracle_stage.argtypes = [ctypes.POINTER(_abi.StageParams), vp, vp, vp, i64, vp, vp, vp, vp, i32]
+    L.oracle_stage_ex.restype = i32
+    L.oracle_stage_ex.argtypes = [ctypes.POINTER(_abi.StageParams), vp, vp, vp, i64, vp, vp, vp, vp, i32, vp,
+                                  i32]
+
+
+def load_f64() -> ctypes.CDLL:
+    """The float64-filtering build of the oracle (same matching, float64 transforms,
+    noise statistics, shrinkage, weights, aggregation and division)."""
+    global _lib64
+    if _lib64 is None:
+        build()
+        L = ctypes.CDLL(LIB64_PATH)
+        _bind_stage(L)
+        _lib64 = L
+    return _lib64
 
 
 def load() -> ctypes.CDLL:
@@ -61,9 +87,7 @@ def load() -> ctypes.CDLL:
         L.oracle_blockmatch_volume_biased.restype = i32
         L.oracle_blockmatch_volume_biased.argtypes = [ctypes.POINTER(_abi.MatchParams), vp, vp, vp, vp, i64,
                                                       vp, ctypes.c_float, vp, vp, vp, i32]
-        L.oracle_stage.restype = i32
-        L.oracle_stage.argtypes = [ctypes.POINTER(_abi.StageParams), vp, vp, vp, i64, vp, vp, vp, vp,
-                                   i32]
+        _bind_stage(L)
         _lib = L
     return _lib
 
@@ -177,20 +201,35 @@ def blockmatch_volume_poisson_biased(volume, block, refs, radius, max_m, min_m, 
     return sel, cnt, acc
 
 
-def stage(params, noisy, pilot, refs, threads=0):
-    """Run one stage; returns (estimate, sel, count, accepted)."""
-    L = load()
+def stage(params, noisy, pilot, refs, threads=0, sel=None, count=None, f64=False, margins=False):
+    """Run one stage; returns (estimate, sel, count, accepted), plus each
+    group's hard-threshold margin when ``margins`` is set.
+
+    With ``sel`` and ``count`` given (n x max_stack and n int32, e.g. another
+    implementation's match sets) the stage filters those groups instead of
+    matching, which isolates the filtering arithmetic; ``accepted`` is then
+    None.  ``f64`` runs the float64-filtering build.  A group's margin is the
+    smallest relative distance |c - b| / b of a hard-threshold decision from
+    its boundary b (poisson.py:30-46), +inf for Wiener groups."""
+    L = load_f64() if f64 else load()
     noisy = np.ascontiguousarray(noisy, dtype=np.float32)
     pilot = None if pilot is None else np.ascontiguousarray(pilot, dtype=np.float32)
     refs = np.ascontiguousarray(refs, dtype=np.int32)
     n = refs.shape[0]
     out = np.empty_like(noisy)
-    sel = np.full((n, params.max_stack), -1, dtype=np.int32)
-    cnt = np.zeros(n, dtype=np.int32)
-    acc = np.zeros(n, dtype=np.int32)
-    assert L.oracle_stage(ctypes.byref(params), _ptr(noisy), _ptr(pilot), _ptr(refs), n, _ptr(out),
-                          _ptr(sel), _ptr(cnt), _ptr(acc), threads) == 0
-    return out, sel, cnt, acc
+    use_sel = sel is not None
+    if use_sel:
+        sel = np.ascontiguousarray(sel, dtype=np.int32).reshape(n, params.max_stack).copy()
+        cnt = np.ascontiguousarray(count, dtype=np.int32).reshape(n).copy()
+        acc = None
+    else:
+        sel = np.full((n, params.max_stack), -1, dtype=np.int32)
+        cnt = np.zeros(n, dtype=np.int32)
+        acc = np.zeros(n, dtype=np.int32)
+    marg = np.empty(n, dtype=np.float64) if margins else None
+    assert L.oracle_stage_ex(ctypes.byref(params), _ptr(noisy), _ptr(pilot), _ptr(refs), n, _ptr(out),
+                             _ptr(sel), _ptr(cnt), _ptr(acc), int(use_sel), _ptr(marg), threads) == 0
+    return (out, sel, cnt, acc, marg) if margins else (out, sel, cnt, acc)
 
 
 def bmnd(noisy, profile, threads=0, return_details=False):

@@ -7,9 +7,9 @@ semantics.  The fixtures are committed; this script is only needed to
 regenerate them and needs the reference checkout, which the GPU machines do
 not have.
 
-Usage::
+Usage (``BMND_REFERENCE_SRC`` names the reference's ``src/`` directory)::
 
-    python tests/golden/make_golden.py unit
+    BMND_REFERENCE_SRC=<reference>/src python tests/golden/make_golden.py unit
     python tests/golden/make_golden.py pipeline bm3d_32 [bm4d_16 ...]
     python tests/golden/make_golden.py sigma bm3d_32 [bm4d_12x16x20 ...]
     python tests/golden/make_golden.py gauss [bm3d_32 ...]
@@ -32,7 +32,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REFERENCE_SRC = os.environ.get("BMND_REFERENCE_SRC", "/root/reference/src")
+REFERENCE_SRC = os.environ.get("BMND_REFERENCE_SRC")
+if not REFERENCE_SRC or not os.path.isdir(REFERENCE_SRC):
+    sys.exit("set BMND_REFERENCE_SRC to the reference package's src/ directory (the one holding bmnd/)")
 sys.dont_write_bytecode = True
 sys.path.insert(0, os.path.join(REPO, "oracle", "shim"))
 sys.path.insert(1, REFERENCE_SRC)

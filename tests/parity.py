@@ -117,3 +117,35 @@ def output_parity(out, ref, clean=None, tol=1e-3, exclude=None):
         res["psnr_ref"] = psnr(ref, clean, peak)
         res["psnr_delta"] = abs(res["psnr_out"] - res["psnr_ref"])
     return res
+
+
+def group_footprint(shape, block, sel, cnt, rows):
+    """Voxels covered by the patches of the given groups."""
+    mask = np.zeros(shape, dtype=bool)
+    counts = tuple(s - b + 1 for s, b in zip(shape, block))
+    for i in rows:
+        for lin in sel[i, : cnt[i]]:
+            q = unravel(int(lin), counts)
+            mask[tuple(slice(a, a + b) for a, b in zip(q, block))] = True
+    return mask
+
+
+def groups_touching(shape, block, sel, cnt, mask):
+    """Indices of the groups with a patch that overlaps ``mask``."""
+    counts = tuple(s - b + 1 for s, b in zip(shape, block))
+    rows = []
+    for i in range(len(cnt)):
+        for lin in sel[i, : cnt[i]]:
+            q = unravel(int(lin), counts)
+            if mask[tuple(slice(a, a + b) for a, b in zip(q, block))].any():
+                rows.append(i)
+                break
+    return rows
+
+
+def max_abs_outside(a, b, exclude=None) -> float:
+    """Largest |a - b| over the voxels outside ``exclude`` (0 if none remain)."""
+    diff = np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64))
+    if exclude is not None:
+        diff = diff[~exclude]
+    return float(diff.max()) if diff.size else 0.0
