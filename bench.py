@@ -179,6 +179,19 @@ def profile_desc(workload: str) -> str:
     return f"{name}(noise_model=poisson) defaults"
 
 
+# The reference package itself, timed once in the build container (x86-64, one
+# thread): Numba is not installable there, so it ran as plain Python through the
+# import stand-ins of oracle/shim.  The 256^2 BM3D-Poisson image (12 rectangles
+# and discs, seed 0) took 2 h 20 min.
+REFERENCE_MEASURED = {
+    "what": "the reference bmnd() itself, pure Python (Numba unavailable), one thread, x86-64",
+    "workload": "256^2 BM3D-Poisson, 12 rectangles/discs, seed 0",
+    "seconds": 8400.0,
+    "value": 65536 / 8400.0 / 1e6,
+    "unit": "Mvoxel/s",
+}
+
+
 def cpu_baseline(workload: str, seed: int, budget_s: float = 20.0) -> dict:
     if is_gaussian(workload):
         return {"value": None, "unit": "Mvoxel/s", "cores": 0, "kind": "none",
@@ -209,9 +222,11 @@ def cpu_baseline(workload: str, seed: int, budget_s: float = 20.0) -> dict:
         "value": sample.size / dt / 1e6,
         "unit": "Mvoxel/s",
         "cores": threads,
+        "cpu_model": cpu_model(),
         "kind": "port",
         "sample": desc,
         "seconds_per_call": dt,
+        "reference_itself": REFERENCE_MEASURED,
     }
 
 
@@ -329,6 +344,50 @@ def time_kernels(torch, noisy_t, profile, reps: int = 2, stages=("ht", "wiener")
     return res
 
 
+def run_config(args, shape, world: int, fast: bool) -> dict:
+    """The workload and the settings of the path ``value`` measures."""
+    cfg = {
+        "workload": WORKLOADS[args.workload]["desc"],
+        "shape": list(shape),
+        "profile": profile_desc(args.workload),
+        "parallelism": f"replicas{world}",
+        "l2": "flushed between timed steps (256 MiB write)",
+    }
+    if fast:
+        from bmnd_gb300 import pilot as pl
+
+        nd = len(shape)
+        stage2 = dict(pl.FAST_STAGE2[nd])
+        cfg.update({
+            "path": "bmnd(volume, profile, pilot='learned')",
+            "pilot": "learned: residual conv net, BF16 weights and activations, FP32 accumulation, tcgen05 "
+                     "implicit GEMM; per-tile Poisson-deviance fallback to the plain stage 1",
+            "wiener_step": list(stage2.get("wiener_step", ())) or "profile default",
+            "wiener_variance_k": stage2.get("k", "profile default (4)"),
+            "wiener_match_precision": pl.FAST_MATCH_PRECISION,
+            "wiener_group_transform": "Haar by its sum pyramid",
+            "plain_reported_beside": "bmnd(volume, profile) with match_precision "
+                                     f"{args.precision!r}: exact FP32 matching, k = 4",
+        })
+    else:
+        cfg.update({"path": "bmnd(volume, profile)", "match_precision": args.precision})
+    return cfg
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), or the platform string."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
 def max_over_ranks(values, dist, device: str) -> list[float]:
     """Element-wise maximum of per-rank floats over all ranks.  Every rank calls
     it; ``dist`` None means a single rank.  ``device`` holds the reduction
@@ -435,17 +494,15 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_fast_s = None
     if fast is not None:
-        # the host input and output live in page-locked buffers allocated once;
-        # every timed step copies the input in and the estimate out
-        pin_in = torch.from_numpy(noisy).pin_memory()
-        pin_out = torch.empty(noisy.shape, dtype=torch.float32).pin_memory()
+        # the public call a user makes: NumPy array in, NumPy array out, with the
+        # argument checks, the copy to the device and the copy back inside
+        bg.bmnd(noisy, profile, pilot="learned")
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            xin = pin_in.cuda(non_blocking=True)
-            pin_out.copy_(pl.bmnd_fast(xin, profile, fast["net"]))
-            host_fast = pin_out.numpy()
+            host_fast = bg.bmnd(noisy, profile, pilot="learned")
         e2e_fast_s = (time.perf_counter() - t0) / e2e_steps
+        assert host_fast.shape == noisy.shape
     if dist:
         e2e_s, e2e_fast_max = max_over_ranks([e2e_s, e2e_fast_s or 0.0], dist, "cuda")
         e2e_fast_s = e2e_fast_max if fast is not None else None
@@ -594,14 +651,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         "vs_baseline": None,
         "dtype": "f32",
         "data": data_desc(args.workload),
-        "config": {
-            "workload": WORKLOADS[args.workload]["desc"],
-            "shape": list(noisy.shape),
-            "profile": profile_desc(args.workload),
-            "match_precision": args.precision,
-            "parallelism": f"replicas{world}",
-            "l2": "flushed between timed steps (256 MiB write)",
-        },
+        "config": run_config(args, noisy.shape, world, fast is not None),
         "e2e": {
             "value": nvox * world / (e2e_fast_s if fast is not None else e2e_s) / 1e6,
             "unit": "Mvoxel/s",

@@ -196,6 +196,11 @@ SIGNATURES = {
         [ctypes.POINTER(StageParams), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _I64,
          ctypes.c_void_p, _U64],
     ),
+    "bmnd_group_probe_workspace_bytes": (_I32, [ctypes.POINTER(StageParams), _U64P]),
+    "bmnd_group_probe": (
+        _I32,
+        [ctypes.POINTER(StageParams), _VP, _VP, _VP, _VP, _I64, _VP, _VP, _VP, _VP, _VP, _VP, _U64, _U64],
+    ),
     "bmnd_pilotnet_param_count": (_I32, [_PNP, _I64P]),
     "bmnd_pilotnet_packed_bytes": (_I32, [_PNP, _U64P]),
     "bmnd_pilotnet_workspace_bytes": (_I32, [_PNP, _I32, _U64P]),

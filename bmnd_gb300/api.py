@@ -29,7 +29,7 @@ from . import _abi, gaussian, plan, policies
 from .enums import BlockMatchDistance, CacheMode, coerce_enum
 from .validation import resolve_profile
 
-__all__ = ["bmnd", "BlockMatchGroup", "BlockMatchResult", "bmnd_device"]
+__all__ = ["bmnd", "BlockMatchGroup", "BlockMatchResult", "bmnd_device", "group_probe"]
 
 
 @dataclass
@@ -106,6 +106,68 @@ class _Workspace:
 
 _WORKSPACE = _Workspace()
 _REFS_CACHE: dict = {}
+
+
+class _Staging:
+    """Page-locked host buffers for the NumPy path of :func:`bmnd`, grown on
+    demand and reused: the input is copied into one and sent to the device
+    asynchronously, the result comes back through the other.  A lock makes
+    concurrent host threads take turns."""
+
+    def __init__(self):
+        self._lock = threading.Lock()
+        self._bufs = {}
+
+    def _get(self, key, numel):
+        torch = _torch()
+        buf = self._bufs.get(key)
+        if buf is None or buf.numel() < numel:
+            buf = torch.empty(max(int(numel), 1), dtype=torch.float32).pin_memory()
+            self._bufs[key] = buf
+        return buf[:numel]
+
+    def upload(self, arr: np.ndarray):
+        torch = _torch()
+        with self._lock:
+            host = self._get("in", arr.size)
+            host.numpy().reshape(arr.shape)[...] = arr
+            dev = torch.empty(arr.shape, dtype=torch.float32, device=torch.cuda.current_device())
+            dev.copy_(host.view(arr.shape), non_blocking=True)
+            # the staging buffer is reused by the next call: wait for the copy
+            torch.cuda.current_stream().synchronize()
+        return dev
+
+    def download(self, t) -> np.ndarray:
+        with self._lock:
+            host = self._get("out", t.numel()).view(t.shape)
+            host.copy_(t)
+            return host.numpy().copy()
+
+
+_STAGING = _Staging()
+
+
+def _host_result(t) -> np.ndarray:
+    return _STAGING.download(t)
+
+
+_NETS: dict = {}
+
+
+def _learned_net(ndim: int, path: str | None, device):
+    """The learned pilot's net for ``ndim``-D volumes, loaded once per file and device."""
+    from . import pilot as pilot_mod
+
+    if path is None:
+        path = pilot_mod.default_net_path("bm4d" if ndim == 3 else "bm3d")
+    key = (path, str(device))
+    net = _NETS.get(key)
+    if net is None:
+        net = pilot_mod.PilotNet.load(path, device=str(device))
+        if net.ndim != ndim:
+            raise ValueError(f"pilot weights {path!r} are for {net.ndim}-D volumes, the input is {ndim}-D")
+        _NETS[key] = net
+    return net
 
 
 def _device_refs(schedule: plan.Schedule, device):
@@ -347,6 +409,37 @@ def stage_device(noisy, profile, stage: str, pilot=None, *, resolved=None, match
     return out
 
 
+def group_probe(params, noisy, sel, count, pilot=None, stream=None) -> dict:
+    """Filter explicit groups on the device and return their intermediate
+    arrays (``bmnd_group_probe``): for every group i of ``count[i]`` members
+    ``sel[i, :count[i]]`` (patch-grid lins), "coef" (forward transform of the
+    observation group), "sigma" (noise std), "atten" (hard-threshold mask or
+    Wiener gain) and "filt" (inverse of the shrunk coefficients), each
+    n_groups x max_stack x P, and "weights" (n_groups x max_stack), as NumPy
+    float32 arrays.  ``params`` is a filled ``StageParams``; ``noisy`` (and
+    ``pilot`` for the Wiener filter) are float32 CUDA tensors."""
+    torch = _torch()
+    L = _abi.lib()
+    device = noisy.device
+    if stream is None:
+        stream = torch.cuda.current_stream(device)
+    sel_t = torch.from_numpy(np.ascontiguousarray(sel, dtype=np.int32)).to(device)
+    cnt_t = torch.from_numpy(np.ascontiguousarray(count, dtype=np.int32)).to(device)
+    n = int(cnt_t.numel())
+    P = int(np.prod([params.block[a] for a in range(params.ndim)]))
+    nb = ctypes.c_uint64(0)
+    _abi.check(L.bmnd_group_probe_workspace_bytes(ctypes.byref(params), ctypes.byref(nb)))
+    ws = torch.empty(max(int(nb.value), 256), dtype=torch.uint8, device=device)
+    out = {k: torch.zeros((n, params.max_stack, P), dtype=torch.float32, device=device)
+           for k in ("coef", "sigma", "atten", "filt")}
+    out["weights"] = torch.zeros((n, params.max_stack), dtype=torch.float32, device=device)
+    _abi.check(L.bmnd_group_probe(
+        ctypes.byref(params), noisy.data_ptr(), None if pilot is None else pilot.data_ptr(), sel_t.data_ptr(),
+        cnt_t.data_ptr(), n, out["coef"].data_ptr(), out["sigma"].data_ptr(), out["atten"].data_ptr(),
+        out["weights"].data_ptr(), out["filt"].data_ptr(), ws.data_ptr(), ws.numel(), int(stream.cuda_stream)))
+    return {k: v.cpu().numpy() for k, v in out.items()}
+
+
 def bmnd(
     volume,
     profile,
@@ -357,26 +450,47 @@ def bmnd(
     blockmatch_callback: Callable[[str, BlockMatchResult], None] | None = None,
     max_cache_bytes=CacheMode.AUTO,
     *,
-    match_precision: str = "exact",
+    match_precision: str | None = None,
+    pilot: str = "plain",
+    pilot_weights: str | None = None,
 ):
     """Denoise ``volume`` with ``profile`` (drop-in for the reference ``bmnd``).
 
     ``volume`` may be a NumPy array (the result is a NumPy float32 array of
     the same shape) or a CUDA tensor (the result stays on that device).
-    ``match_precision`` selects exact float32 matching for every candidate
-    ("exact"), screening plus exact rescoring near the selection boundary
-    ("fast", same match sets), or selection by the screening distances with
-    exact rescoring of the selected candidates only ("approx"; the match sets
-    may differ where the screening and exact orders disagree).
+
+    Keyword-only additions, none of which the reference has:
+
+    * ``pilot`` -- "plain" (default) runs the reference's two stages.
+      "learned" replaces the hard-thresholding stage by the learned pilot (a
+      BF16 residual convolution net on the tensor cores) with its per-tile
+      Poisson-deviance fallback to the plain stage 1, then runs the Wiener
+      stage with the fast path's settings (``pilot.FAST_STAGE2``: reference
+      step 4 and the approximate Poisson sigma in 3-D; subsampled screening
+      matching).  Direct-Poisson 2-D and 3-D profiles only; the sigma maps and
+      the block-matching callback are not available on it, and
+      ``stage_callback`` receives the pilot as the "ht" estimate.
+    * ``pilot_weights`` -- the net's ``.npz`` file; default: the weights
+      shipped for the volume's dimensionality (``bmnd_gb300/weights``).
+    * ``match_precision`` -- "exact" (the default of the plain pilot): float32
+      per-term distances for every candidate; "fast": screening plus exact
+      rescoring near the selection boundary (same match sets); "approx":
+      selection by the screening distances with exact rescoring of the
+      selected candidates only (the match sets may differ where the two orders
+      disagree); "subsampled" (the default of the learned pilot's Wiener
+      stage): "approx" after a prescreen on the patch's even sub-lattice.
     """
     if sigma is not None and sigma_psd is not None:
         raise ValueError("sigma and sigma_psd are mutually exclusive.")
     if sigma is not None:
         _validate_sigma(sigma)
     _validate_max_cache_bytes(max_cache_bytes)
-    if match_precision not in _MATCH_PRECISIONS:
+    if pilot not in ("plain", "learned"):
+        raise ValueError(f"pilot must be 'plain' or 'learned', got {pilot!r}.")
+    if match_precision is not None and match_precision not in _MATCH_PRECISIONS:
         raise ValueError(
             f"match_precision must be 'exact', 'fast', 'approx' or 'subsampled', got {match_precision!r}.")
+    learned = pilot == "learned"
 
     torch_input = type(volume).__module__.startswith("torch")
     shape = tuple(int(s) for s in volume.shape)
@@ -399,15 +513,26 @@ def bmnd(
         all_zero = not bool((dev_vol != 0).any())
     else:
         arr = np.asarray(volume)
-        if not np.all(np.isfinite(arr)):
-            raise ValueError("volume must contain only finite values.")
-        with np.errstate(over="ignore", invalid="ignore"):
-            vol = arr.astype(np.float32, copy=False)
-        if not np.all(np.isfinite(vol)):
-            raise ValueError("volume values must be representable as finite float32 values.")
-        if resolved.is_poisson and np.any(vol < 0.0):
-            raise ValueError("Direct Poisson input must contain only non-negative values.")
-        all_zero = not np.any(vol != 0.0)
+        if arr.dtype == np.float32 and arr.size:
+            # one min and one max pass: NaN propagates through both, so both are
+            # finite exactly when every value is (the same checks, in the same order)
+            lo, hi = float(np.min(arr)), float(np.max(arr))
+            if not (np.isfinite(lo) and np.isfinite(hi)):
+                raise ValueError("volume must contain only finite values.")
+            vol = arr
+            if resolved.is_poisson and lo < 0.0:
+                raise ValueError("Direct Poisson input must contain only non-negative values.")
+            all_zero = lo == 0.0 and hi == 0.0
+        else:
+            if not np.all(np.isfinite(arr)):
+                raise ValueError("volume must contain only finite values.")
+            with np.errstate(over="ignore", invalid="ignore"):
+                vol = arr.astype(np.float32, copy=False)
+            if not np.all(np.isfinite(vol)):
+                raise ValueError("volume values must be representable as finite float32 values.")
+            if resolved.is_poisson and np.any(vol < 0.0):
+                raise ValueError("Direct Poisson input must contain only non-negative values.")
+            all_zero = not np.any(vol != 0.0)
 
     if sigma_psd is not None:
         gaussian.validate_sigma_psd(shape, sigma_psd)
@@ -427,6 +552,13 @@ def bmnd(
         plan.check_poisson_options(profile, resolved.variance_k)
     else:
         plan.check_gaussian_options(profile, resolved.variance_k)
+    if learned:
+        if not resolved.is_poisson:
+            raise plan.unsupported("the learned pilot is trained for direct-Poisson profiles only")
+        if len(shape) not in (2, 3):
+            raise plan.unsupported("the learned pilot exists for 2-D and 3-D volumes only")
+        if return_sigma_map or blockmatch_callback is not None:
+            raise plan.unsupported("return_sigma_map and blockmatch_callback need pilot='plain'")
 
     torch = _torch()
     if not torch.cuda.is_available():
@@ -436,8 +568,7 @@ def bmnd(
         if not dev.is_cuda:
             dev = dev.cuda()
     else:
-        host = torch.from_numpy(np.ascontiguousarray(vol))
-        dev = host.pin_memory().cuda(non_blocking=True)
+        dev = _STAGING.upload(np.ascontiguousarray(vol))
     maps = None
     global_sigma = 0.0
     gauss = None
@@ -458,9 +589,20 @@ def bmnd(
         vvol = np.maximum(np.float32(profile.poisson_count_scale) * np.maximum(host_vol, np.float32(0.0)),
                           np.float32(floor)).astype(np.float32)
         global_sigma = estimate_poisson_global_sigma(vvol, eps=max(floor, 1e-10))
-    out = bmnd_device(dev, profile, resolved=resolved, match_precision=match_precision,
-                      stage_callback=stage_callback, blockmatch_callback=blockmatch_callback,
-                      sigma_maps=maps, global_sigma=global_sigma, gauss=gauss)
+    if learned:
+        from . import pilot as pilot_mod
+
+        net = _learned_net(len(shape), pilot_weights, dev.device)
+        details = {} if stage_callback is not None else None
+        out = pilot_mod.bmnd_fast(dev, profile, net, details=details,
+                                  match_precision=match_precision or pilot_mod.FAST_MATCH_PRECISION)
+        if stage_callback is not None:
+            stage_callback("ht", details["pilot"].cpu().numpy().copy())
+            stage_callback("wiener", out.cpu().numpy().copy())
+    else:
+        out = bmnd_device(dev, profile, resolved=resolved, match_precision=match_precision or "exact",
+                          stage_callback=stage_callback, blockmatch_callback=blockmatch_callback,
+                          sigma_maps=maps, global_sigma=global_sigma, gauss=gauss)
     if torch_input:
         res = out if volume.is_cuda else out.cpu()
         if maps is None:
@@ -468,6 +610,6 @@ def bmnd(
         conv = (lambda t: t) if volume.is_cuda else (lambda t: t.cpu())
         return res, {"global": global_sigma, "ht": conv(maps["ht"]), "wiener": conv(maps["wiener"])}
     if maps is None:
-        return out.cpu().numpy()
-    return out.cpu().numpy(), {"global": global_sigma, "ht": maps["ht"].cpu().numpy(),
+        return _host_result(out)
+    return _host_result(out), {"global": global_sigma, "ht": maps["ht"].cpu().numpy(),
                                "wiener": maps["wiener"].cpu().numpy()}

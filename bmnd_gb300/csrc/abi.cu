@@ -1,11 +1,14 @@
 // abi.cu -- the extern "C" entry points declared in include/bmnd_gb300.h.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <set>
 #include <string>
 #include <vector>
@@ -32,6 +35,70 @@ int32_t cuda_fail(cudaError_t err, const char* what) {
 }
 
 int64_t group_filter_smem_bytes(const BmndStageParams& sp);
+
+namespace {
+struct ShapeKey {
+    int dev;
+    const void* fn;
+    int threads;
+    size_t smem;
+    bool fit;
+    bool operator<(const ShapeKey& o) const {
+        return std::tie(dev, fn, threads, smem, fit) < std::tie(o.dev, o.fn, o.threads, o.smem, o.fit);
+    }
+};
+struct FnState {
+    size_t smem_limit = 0;  // the kernel's dynamic shared-memory limit as set
+    int carveout = -1;      // its preferred carveout as set
+};
+std::mutex g_shape_mutex;
+std::map<ShapeKey, std::pair<int, int>> g_shapes;       // -> (resident CTAs per SM, carveout)
+std::map<std::pair<int, const void*>, FnState> g_fns;  // per device and kernel
+std::map<int, int> g_sm_count;                          // per device
+}  // namespace
+
+int32_t kernel_residency(const void* fn, int threads, size_t smem, bool fit_carveout, int* per_sm, int* sms) {
+    int dev = 0;
+    BMND_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> guard(g_shape_mutex);
+    auto sit = g_sm_count.find(dev);
+    if (sit == g_sm_count.end()) {
+        int n = 0;
+        BMND_CUDA_TRY(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+        sit = g_sm_count.emplace(dev, n).first;
+    }
+    FnState& st = g_fns[{dev, fn}];
+    if (smem > st.smem_limit) {
+        BMND_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        st.smem_limit = smem;
+    }
+    const ShapeKey key{dev, fn, threads, smem, fit_carveout};
+    auto it = g_shapes.find(key);
+    if (it == g_shapes.end()) {
+        int resident = 0, pct = -1;
+        if (fit_carveout) {
+            BMND_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+            st.carveout = 100;
+        }
+        BMND_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, fn, threads, smem));
+        if (fit_carveout && resident > 0) {
+            int smem_sm = 0;
+            BMND_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+            const int64_t want = static_cast<int64_t>(resident) * (static_cast<int64_t>(smem) + 1024);
+            pct = smem_sm > 0 ? static_cast<int>((want * 100 + smem_sm - 1) / smem_sm) : 100;
+            if (pct > 100) pct = 100;
+        }
+        it = g_shapes.emplace(key, std::make_pair(resident, pct)).first;
+    }
+    const int pct = it->second.second;
+    if (fit_carveout && pct >= 0 && pct != st.carveout) {
+        BMND_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+        st.carveout = pct;
+    }
+    *per_sm = it->second.first;
+    *sms = sit->second;
+    return BMND_OK;
+}
 
 namespace {
 
@@ -137,10 +204,14 @@ struct StageWorkspace {
     uint32_t* mm;  // SSD threshold: order bits of the matched volume's min and max
     float* thr;    // SSD threshold, computed on the device
     float* thr_ref;  // per-reference thresholds (reference-finite-count policy)
+    float* aux;      // approximate screening form: per-voxel arrays of the matched volume
+    int64_t aux_floats;
     uint64_t bytes;
 };
 
 uint64_t align256(uint64_t v) { return (v + 255) & ~uint64_t(255); }
+
+BmndMatchParams match_params_of(const BmndStageParams& sp);
 
 StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
     StageWorkspace w{};
@@ -160,6 +231,9 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
     uint64_t o_st = take(4ull * P * static_cast<uint64_t>(kron_stride(static_cast<int>(P))));
     uint64_t o_mm = take(16);
     uint64_t o_tr = take(sp.match_policy == BMND_POLICY_REFERENCE_FINITE_COUNT ? 4ull * n_refs : 16);
+    const BmndMatchParams mp = match_params_of(sp);
+    w.aux_floats = approx_scratch_floats(mp, sp.shape, sp.block);
+    uint64_t o_aux = take(w.aux_floats > 0 ? 4ull * static_cast<uint64_t>(w.aux_floats) : 16);
     w.bytes = off;
     if (base) {
         char* b = static_cast<char*>(base);
@@ -172,6 +246,7 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
         w.mm = reinterpret_cast<uint32_t*>(b + o_mm);
         w.thr = reinterpret_cast<float*>(b + o_mm + 8);
         w.thr_ref = reinterpret_cast<float*>(b + o_tr);
+        w.aux = w.aux_floats > 0 ? reinterpret_cast<float*>(b + o_aux) : nullptr;
     }
     return w;
 }
@@ -253,7 +328,7 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
     rc = launch_blockmatch_volume(mp, match_src, sp.shape, sp.block, refs, n_refs, thr_per_ref,
                                   sp.match_threshold, w.sel, w.count, w.accepted, stream, thr_dev,
                                   sp.match_noise_ssd, sp.ssd_gamma, allow_alloc, null_moments,
-                                  sp.null_max_count, sp.ssd_poisson_bias != 0);
+                                  sp.null_max_count, sp.ssd_poisson_bias != 0, w.aux, w.aux_floats);
     if (rc) return rc;
     rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, w.st, sig_num, stream);
     if (rc) return rc;
@@ -273,27 +348,49 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
 }
 
 // Fixed scratch array behind bmnd_stage_noalloc.  Host code must not use the
-// symbol itself as a device pointer: its device address is looked up once per
-// device with cudaGetSymbolAddress and cached.
+// symbol itself as a device pointer: its device address is looked up with
+// cudaGetSymbolAddress once per CUDA context (a device's primary context, or a
+// new one after cudaDeviceReset, which reloads the module at a new address) and
+// cached.
 static __device__ __align__(256) unsigned char g_static_scratch[BMND_STATIC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
 std::mutex g_static_scratch_mutex;
-void* g_static_scratch_ptr[kMaxDevices] = {};
+std::map<CUcontext, void*> g_static_scratch_ptr;
+
+// the calling thread's current context, through the driver entry point the
+// runtime hands out (no link-time dependency on the driver library)
+int32_t current_context(CUcontext* ctx) {
+    using CtxGetCurrent = CUresult (*)(CUcontext*);
+    static CtxGetCurrent get = nullptr;
+    if (!get) {
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        void* fn = nullptr;
+        BMND_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !fn) return fail(BMND_ERR_CUDA, "cuCtxGetCurrent not available");
+        get = reinterpret_cast<CtxGetCurrent>(fn);
+    }
+    if (get(ctx) != CUDA_SUCCESS) return fail(BMND_ERR_CUDA, "cuCtxGetCurrent failed");
+    return BMND_OK;
+}
 
 int32_t static_scratch_address(void** out) {
     int dev = 0;
     BMND_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return fail(BMND_ERR_UNSUPPORTED, "device index out of range");
+    CUcontext ctx = nullptr;
+    if (int32_t rc = current_context(&ctx)) return rc;
     std::lock_guard<std::mutex> guard(g_static_scratch_mutex);
-    if (!g_static_scratch_ptr[dev]) {
+    auto it = ctx ? g_static_scratch_ptr.find(ctx) : g_static_scratch_ptr.end();
+    if (it == g_static_scratch_ptr.end()) {
+        // the first call in this context: the lookup also makes the context current
         void* p = nullptr;
         cudaError_t err = cudaGetSymbolAddress(&p, g_static_scratch);
         if (err != cudaSuccess) return cuda_fail(err, "cudaGetSymbolAddress(static scratch)");
         if (!p) return fail(BMND_ERR_CUDA, "static scratch has no device address");
-        g_static_scratch_ptr[dev] = p;
+        if (!ctx && (current_context(&ctx) != BMND_OK || !ctx))
+            return fail(BMND_ERR_CUDA, "no current CUDA context after the scratch lookup");
+        it = g_static_scratch_ptr.emplace(ctx, p).first;
     }
-    *out = g_static_scratch_ptr[dev];
+    *out = it->second;
     return BMND_OK;
 }
 
@@ -483,6 +580,61 @@ int32_t bmnd_run(const BmndStageParams* ht, const BmndStageParams* wiener, const
     if (rc) return rc;
     return run_stage(*wiener, d_noisy, d_ht_out, d_refs_wiener, n_refs_wiener, d_out, nullptr,
                      nullptr, nullptr, d_workspace, workspace_bytes, s);
+}
+
+// The probe's groups need not come from matching, so its layout covers a
+// union box as large as the volume when that fits in shared memory (the
+// kernel skips and reports any group wider than its layout).
+BmndStageParams probe_layout_params(const BmndStageParams& sp) {
+    BmndStageParams q = sp;
+    for (int d = 0; d < sp.ndim; ++d) q.search_radius[d] = std::max(sp.search_radius[d], sp.shape[d]);
+    return group_filter_smem_bytes(q) <= 227 * 1024 ? q : sp;
+}
+
+int32_t bmnd_group_probe_workspace_bytes(const BmndStageParams* params, uint64_t* out_bytes) {
+    clear_error();
+    if (!params || !out_bytes) return fail(BMND_ERR_INVALID_ARG, "null argument");
+    if (int32_t rc = validate_stage(*params)) return rc;
+    const uint64_t P = static_cast<uint64_t>(patch_volume(*params));
+    // the Kronecker table, then the status word
+    *out_bytes = align256(4ull * P * static_cast<uint64_t>(kron_stride(static_cast<int>(P)))) + 256;
+    return BMND_OK;
+}
+
+int32_t bmnd_group_probe(const BmndStageParams* params, const float* d_noisy, const float* d_pilot,
+                         const int32_t* d_sel, const int32_t* d_count, int64_t n_groups, float* d_coef,
+                         float* d_sigma, float* d_atten, float* d_weights, float* d_filt, void* d_workspace,
+                         uint64_t workspace_bytes, uint64_t stream) {
+    clear_error();
+    if (!params) return fail(BMND_ERR_INVALID_ARG, "null params");
+    const BmndStageParams& sp = *params;
+    if (int32_t rc = validate_stage(sp)) return rc;
+    if (sp.mass_conserve) return fail(BMND_ERR_INVALID_ARG, "the group probe has no mass-conservation pass");
+    if (!d_noisy) return fail(BMND_ERR_INVALID_ARG, "d_noisy is required");
+    if (sp.filter == BMND_FILTER_WIENER && !d_pilot)
+        return fail(BMND_ERR_INVALID_ARG, "the Wiener filter needs the pilot");
+    if (n_groups < 0 || (n_groups > 0 && (!d_sel || !d_count)))
+        return fail(BMND_ERR_INVALID_ARG, "bad group list");
+    uint64_t need = 0;
+    if (int32_t rc = bmnd_group_probe_workspace_bytes(params, &need)) return rc;
+    if (!d_workspace || workspace_bytes < need) return fail(BMND_ERR_WORKSPACE, "workspace too small");
+    if (reinterpret_cast<uintptr_t>(d_workspace) % 256 != 0)
+        return fail(BMND_ERR_INVALID_ARG, "workspace must be 256-byte aligned");
+    GroupProbe probe{1, d_coef, d_sigma, d_atten, d_weights, d_filt};
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int* status = reinterpret_cast<int*>(static_cast<char*>(d_workspace) + need - 256);
+    BMND_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), s));
+    const BmndStageParams q = probe_layout_params(sp);
+    int32_t rc = launch_group_filter(q, d_noisy, d_pilot, d_sel, d_count, n_groups, nullptr, nullptr,
+                                     static_cast<float*>(d_workspace), nullptr, s, nullptr, status, &probe);
+    if (rc) return rc;
+    int h_status = 0;
+    BMND_CUDA_TRY(cudaMemcpyAsync(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    BMND_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h_status)
+        return fail(BMND_ERR_INVALID_ARG, "a group has a member outside the patch grid, more members than "
+                                          "max_stack, or a union box larger than the kernel's layout");
+    return BMND_OK;
 }
 
 int32_t bmnd_stage_noalloc(const BmndStageParams* params, const float* d_noisy,

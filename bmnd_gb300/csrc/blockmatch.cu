@@ -76,6 +76,8 @@ struct MatchArgs {
     // threshold computed on the device (one float), overrides the scalar one
     const float* thr_dev;
     int32_t no_alloc;  // 1: no stream-ordered scratch (approx mode then runs the bounded form)
+    float* aux_ws;          // caller workspace for the approximate form's per-voxel arrays, or null
+    int64_t aux_ws_floats;  // its size in floats
     // subsampled mode: prescreen on the patch's even sub-lattice (box sums in
     // boxb_sub), then the screening form for the presel smallest
     int32_t sub;
@@ -1528,14 +1530,11 @@ int32_t launch_counts(MatchArgs& a, cudaStream_t stream) {
     const size_t smem = counts_smem_bytes(a);
     const int32_t rows = a.max_m + a.required;
     auto run = [&](auto kernel) -> int32_t {
-        BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(smem)));
-        int per_sm = 0;
-        BMND_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kCThreads, smem));
+        int per_sm = 0, sms = 0;
+        if (int32_t rc = kernel_residency(reinterpret_cast<const void*>(kernel), kCThreads, smem, false, &per_sm,
+                                          &sms))
+            return rc;
         if (per_sm < 1) per_sm = 1;
-        int dev = 0, sms = 0;
-        BMND_CUDA_TRY(cudaGetDevice(&dev));
-        BMND_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         int64_t blocks = static_cast<int64_t>(sms) * per_sm;
         if (blocks > a.n_refs) blocks = a.n_refs;
         kernel<<<static_cast<unsigned>(blocks), kCThreads, smem, stream>>>(a, rows);
@@ -1559,6 +1558,19 @@ size_t match_smem_bytes(int K, int R, int P, bool table) {
     return static_cast<size_t>(kWarps) * (rows * 32 + rows) * sizeof(uint64_t) +
            static_cast<size_t>(P) * sizeof(int32_t) + static_cast<size_t>(kWarps) * P * sizeof(float) +
            static_cast<size_t>(kWarps) * P * sizeof(int) + (table ? kTable * kTable * sizeof(float) : 0);
+}
+
+// patch shapes with a box-sum kernel for the approximate screening form
+bool approx_box_shape(int ndim, const int32_t* b) {
+    return (ndim == 2 && b[0] == 8 && b[1] == 8) || (ndim == 3 && b[0] == 5 && b[1] == 5 && b[2] == 5) ||
+           (ndim == 3 && b[0] == 4 && b[1] == 4 && b[2] == 4);
+}
+
+// raise a kernel's dynamic shared-memory limit (cached, see kernel_residency)
+template <typename K>
+int32_t set_smem_limit(K kernel, size_t smem) {
+    int per_sm = 0, sms = 0;
+    return kernel_residency(reinterpret_cast<const void*>(kernel), kWarps * 32, smem, false, &per_sm, &sms);
 }
 
 int32_t launch_exact(MatchArgs& a, int code, cudaStream_t stream);
@@ -1587,22 +1599,33 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     }
     size_t smem = screened_smem_bytes(a.max_m, a.P, wmax);
     // approximate mode on a volume: per-voxel c and per-origin box sums of
-    // c + c log2 c, in stream-ordered scratch freed after the launch; without
-    // it the bounded form runs with a zero bound
+    // c + c log2 c, in the caller's workspace when given, else in stream-ordered
+    // scratch freed after the launch; without either the bounded form runs with
+    // a zero bound
     float* aux = nullptr;
+    bool aux_owned = false;
     const int* bl = a.block;
-    const bool box_ok = (a.ndim == 2 && bl[0] == 8 && bl[1] == 8) ||
-                        (a.ndim == 3 && bl[0] == 5 && bl[1] == 5 && bl[2] == 5) ||
-                        (a.ndim == 3 && bl[0] == 4 && bl[1] == 4 && bl[2] == 4);
-    if (a.approx && !a.table && !a.no_alloc && box_ok && a.inv_scale == 1.0f && a.grid_stride[a.ndim - 1] == 1) {
+    if (a.approx && !a.table && approx_box_shape(a.ndim, bl) && a.inv_scale == 1.0f &&
+        a.grid_stride[a.ndim - 1] == 1) {
         int n[3] = {1, 1, 1};
         int64_t nvox = 1;
         for (int d = 0; d < a.ndim; ++d) {
             n[3 - a.ndim + d] = a.counts[d] + a.block[d] - 1;
             nvox *= n[3 - a.ndim + d];
         }
-        if (cudaMallocAsync(reinterpret_cast<void**>(&aux), static_cast<size_t>(nvox) * (a.sub ? 4 : 3) * sizeof(float),
-                            stream) == cudaSuccess) {
+        const int64_t need = nvox * (a.sub ? 4 : 3);
+        if (a.aux_ws && a.aux_ws_floats >= need) {
+            aux = a.aux_ws;
+        } else if (!a.no_alloc) {
+            if (cudaMallocAsync(reinterpret_cast<void**>(&aux), static_cast<size_t>(need) * sizeof(float), stream) ==
+                cudaSuccess) {
+                aux_owned = true;
+            } else {
+                (void)cudaGetLastError();
+                aux = nullptr;
+            }
+        }
+        if (aux) {
             float* cv = aux;
             float* bv = aux + nvox;
             float* boxb = aux + 2 * nvox;
@@ -1614,7 +1637,7 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
                 note_launch();
                 const cudaError_t e = cudaGetLastError();
                 if (e == cudaSuccess) return BMND_OK;
-                (void)cudaFreeAsync(aux, stream);
+                if (aux_owned) (void)cudaFreeAsync(aux, stream);
                 return cuda_fail(e, what);
             };
             approx_voxel_kernel<<<static_cast<unsigned>(nb), 256, 0, stream>>>(a.src, a.inv_scale, nvox, cv, bv);
@@ -1636,20 +1659,15 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
             a.cv = cv;
             a.boxb = boxb;
             a.boxb_sub = boxb_sub;
-        } else {
-            (void)cudaGetLastError();
-            aux = nullptr;
         }
     }
     auto run = [&](auto kernel) -> int32_t {
-        BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(smem)));
         // persistent CTAs, exactly one resident wave (a partial second wave
         // leaves most SMs idle at the end)
-        int dev = 0, sms = 0, per_sm = 0;
-        BMND_CUDA_TRY(cudaGetDevice(&dev));
-        BMND_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        BMND_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kSThreads, smem));
+        int sms = 0, per_sm = 0;
+        if (int32_t rc = kernel_residency(reinterpret_cast<const void*>(kernel), kSThreads, smem, false, &per_sm,
+                                          &sms))
+            return rc;
         int64_t blocks = static_cast<int64_t>(sms) * (per_sm > 0 ? per_sm : 1);
         if (blocks > a.n_refs) blocks = a.n_refs;
         kernel<<<static_cast<unsigned>(blocks), kSThreads, smem, stream>>>(a, static_cast<int32_t>(wmax));
@@ -1665,7 +1683,7 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
         rc = run(blockmatch_screened_kernel<3, 4, 4, 4>);
     else
         rc = run(blockmatch_screened_kernel<0, 1, 1, 1>);
-    if (aux) BMND_CUDA_TRY(cudaFreeAsync(aux, stream));
+    if (aux_owned) BMND_CUDA_TRY(cudaFreeAsync(aux, stream));
     a.cv = nullptr;
     a.boxb = nullptr;
     a.boxb_sub = nullptr;
@@ -1689,23 +1707,19 @@ int32_t launch_exact(MatchArgs& a, int code, cudaStream_t stream) {
     dim3 grid(static_cast<unsigned>(blocks));
     switch (code) {
         case BMND_DIST_SSD:
-            BMND_CUDA_TRY(cudaFuncSetAttribute(blockmatch_kernel<BMND_DIST_SSD>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            if (int32_t rc = set_smem_limit(blockmatch_kernel<BMND_DIST_SSD>, smem)) return rc;
             blockmatch_kernel<BMND_DIST_SSD><<<grid, kWarps * 32, smem, stream>>>(a);
             break;
         case BMND_DIST_POISSON_DEVIANCE:
-            BMND_CUDA_TRY(cudaFuncSetAttribute(blockmatch_kernel<BMND_DIST_POISSON_DEVIANCE>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            if (int32_t rc = set_smem_limit(blockmatch_kernel<BMND_DIST_POISSON_DEVIANCE>, smem)) return rc;
             blockmatch_kernel<BMND_DIST_POISSON_DEVIANCE><<<grid, kWarps * 32, smem, stream>>>(a);
             break;
         case BMND_DIST_PEARSON:
-            BMND_CUDA_TRY(cudaFuncSetAttribute(blockmatch_kernel<BMND_DIST_PEARSON>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            if (int32_t rc = set_smem_limit(blockmatch_kernel<BMND_DIST_PEARSON>, smem)) return rc;
             blockmatch_kernel<BMND_DIST_PEARSON><<<grid, kWarps * 32, smem, stream>>>(a);
             break;
         case BMND_DIST_ANSCOMBE_SSD:
-            BMND_CUDA_TRY(cudaFuncSetAttribute(blockmatch_kernel<BMND_DIST_ANSCOMBE_SSD>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            if (int32_t rc = set_smem_limit(blockmatch_kernel<BMND_DIST_ANSCOMBE_SSD>, smem)) return rc;
             blockmatch_kernel<BMND_DIST_ANSCOMBE_SSD><<<grid, kWarps * 32, smem, stream>>>(a);
             break;
         default:
@@ -1759,7 +1773,7 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
                                  int32_t* sel, int32_t* count, int32_t* accepted,
                                  cudaStream_t stream, const float* thr_dev, const float* noise_ssd,
                                  float gamma, bool allow_alloc, const double* null_moments, int null_max,
-                                 bool poisson_bias) {
+                                 bool poisson_bias, float* aux_ws, int64_t aux_ws_floats) {
     int32_t rc = validate_match(mp);
     if (rc) return rc;
     if ((noise_ssd || poisson_bias) && mp.distance != BMND_DIST_SSD)
@@ -1778,6 +1792,8 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
     a.poisson_bias = poisson_bias ? 1 : 0;
     a.bias_scale = static_cast<float>(mp.count_scale);  // the Python float meets float32 data
     a.no_alloc = allow_alloc ? 0 : 1;
+    a.aux_ws = aux_ws;
+    a.aux_ws_floats = aux_ws_floats;
     a.null_moments = null_moments;
     a.null_max = null_max;
     if (null_moments && mp.distance == BMND_DIST_SSD)
@@ -1810,6 +1826,16 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
     a.count = count;
     a.accepted = accepted;
     return launch(a, mp.distance, mp.precision, stream);
+}
+
+int64_t approx_scratch_floats(const BmndMatchParams& mp, const int32_t* shape, const int32_t* block) {
+    const bool approx = mp.precision == BMND_MATCH_APPROX || mp.precision == BMND_MATCH_SUBSAMPLED;
+    if (!approx || mp.distance != BMND_DIST_POISSON_DEVIANCE || mp.count_scale != 1.0 ||
+        !approx_box_shape(mp.ndim, block))
+        return 0;
+    int64_t nvox = 1;
+    for (int d = 0; d < mp.ndim; ++d) nvox *= shape[d];
+    return nvox * (mp.precision == BMND_MATCH_SUBSAMPLED ? 4 : 3);
 }
 
 namespace {

@@ -182,6 +182,14 @@ __host__ __device__ constexpr int kron_stride(int P) {
     return (P + 32 * kron_jr(P) - 1) / (32 * kron_jr(P)) * (32 * kron_jr(P));
 }
 
+// Launch shape of `fn` with `threads` threads and `smem` bytes of dynamic
+// shared memory: its resident CTAs per SM and the device's SM count.  Raises the
+// kernel's dynamic shared-memory limit to `smem` when needed; with
+// fit_carveout the kernel's preferred shared-memory carveout is what its
+// resident CTAs need, so the rest of the unified L1 caches global loads.  The
+// queries are made once per device, kernel and shape, then served from a cache.
+int32_t kernel_residency(const void* fn, int threads, size_t smem, bool fit_carveout, int* per_sm, int* sms);
+
 // launch helpers implemented in the .cu files
 int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume, const int32_t* shape,
                                  const int32_t* block, const int32_t* refs, int64_t n_refs,
@@ -190,7 +198,9 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
                                  const float* thr_dev = nullptr, const float* noise_ssd = nullptr,
                                  float gamma = 0.0f, bool allow_alloc = true,
                                  const double* null_moments = nullptr, int null_max = 0,
-                                 bool poisson_bias = false);
+                                 bool poisson_bias = false, float* aux_ws = nullptr, int64_t aux_ws_floats = 0);
+// floats of workspace the approximate screening form of a volume needs (0: none)
+int64_t approx_scratch_floats(const BmndMatchParams& mp, const int32_t* shape, const int32_t* block);
 int32_t launch_reference_thresholds(const float* volume, const int32_t* refs, int64_t n_refs, int ndim,
                                     const int32_t* counts, const int32_t* block, const int32_t* shape,
                                     double count_scale, const double* moments, int max_count, double t,
@@ -202,10 +212,22 @@ int32_t launch_blockmatch_patches(const BmndMatchParams& mp, const float* patche
                                   const int32_t* refs, int64_t n_refs, const float* thresholds,
                                   int32_t* sel, int32_t* count, int32_t* accepted,
                                   cudaStream_t stream);
+// per-group intermediate arrays of the group filter (bmnd_group_probe); any
+// pointer may be null.  Row i of the coefficient-shaped outputs starts at
+// i * max_stack * P, of the weights at i * max_stack.
+struct GroupProbe {
+    int active;
+    float* coef;     // forward transform of the observation group
+    float* sigma;    // noise standard deviation of every coefficient
+    float* atten;    // hard-threshold mask or Wiener gain
+    float* weights;  // aggregation weight of every member
+    float* filt;     // inverse transform of the shrunk coefficients
+};
 int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const float* pilot,
                             const int32_t* sel, const int32_t* count, int64_t n_refs, double* num,
                             double* den, float* st, double* sig_num, cudaStream_t stream,
-                            const double* den_ro = nullptr, int* err = nullptr);
+                            const double* den_ro = nullptr, int* err = nullptr,
+                            const GroupProbe* probe = nullptr);
 int32_t launch_finalize_sigma(const BmndStageParams& sp, const double* sig_num, const double* den,
                               float global_sigma, float* out, cudaStream_t stream);
 int32_t launch_finalize(const BmndStageParams& sp, const double* num, const double* den,

@@ -68,7 +68,11 @@ struct FilterArgs {
     // group-mass conservation, second pass: the first pass's denominator
     // (read only); the kernel then re-aggregates the numerator alone
     const double* den_ro;
-    int* err;  // set when a group's mass correction is undefined
+    int* err;  // 1: a group's mass correction is undefined; 2: a group was skipped (bad members)
+    // group probe: per-group intermediate arrays instead of the aggregation
+    GroupProbe probe;
+    int64_t n_lins;      // patch-grid positions: a member's lin lies in [0, n_lins)
+    int64_t ucells_cap;  // union-box cells the occupancy grid of the layout holds
 };
 
 __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax, int64_t ucells, bool sigma) {
@@ -655,6 +659,10 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
     const int P = geo.P();
     const int n = a.count[gid];
     if (n <= 0) return;
+    if (n > a.nmax) {
+        if (tid == 0 && a.err) atomicExch(a.err, 2);
+        return;
+    }
     const bool wiener = sp.filter == BMND_FILTER_WIENER;
 
     float* G = sm<float>(smem, a.L.g);
@@ -684,12 +692,19 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
     const int kpad = (a.kmax + 3) / 4 * 4;
 
     // ---- setup: positions, matrices, window ----
+    // a member outside the patch grid skips the group (matching never makes one)
+    bool bad_member = false;
     if (tid < n) {
         int64_t rem = a.sel[gid * sp.max_stack + tid];
-        for (int d = geo.nd() - 1; d >= 0; --d) {
+        bad_member = rem < 0 || rem >= a.n_lins;
+        for (int d = geo.nd() - 1; d >= 0 && !bad_member; --d) {
             pos[tid * BMND_MAX_DIMS + d] = static_cast<int>(rem % a.counts[d]);
             rem /= a.counts[d];
         }
+    }
+    if (__syncthreads_or(bad_member)) {
+        if (tid == 0 && a.err) atomicExch(a.err, 2);
+        return;
     }
     for (int e = tid; e < n * n; e += blockDim.x) G[e] = group_entry(sp.group_transform, n, e / n, e % n);
     for (int e = tid; e < BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE; e += blockDim.x) {
@@ -746,6 +761,17 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
     const bool need_approx = (k <= 0) || (kk < n);
 
     const bool gauss = sp.noise_model == BMND_NOISE_GAUSSIAN;
+    if (!gauss && kk > 0) {
+        // the exact phase's occupancy grid covers a union box of at most
+        // ucells_cap cells: members within the search window of their reference
+        // always fit; a group spread wider is skipped and reported
+        int64_t uc = 1;
+        for (int d = 0; d < geo.nd(); ++d) uc *= misc[4 + d];
+        if (uc > a.ucells_cap) {
+            if (tid == 0 && a.err) atomicExch(a.err, 2);
+            return;
+        }
+    }
     if (gauss) {
         // ---- stationary Gaussian noise (variance.py:2036-2106) ----
         // exact planes g < kk: sum_{i,j} G[g,i] G[g,j] C_c((x_i - x_j) mod domain),
@@ -1004,6 +1030,13 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
     __syncthreads();
     transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, 0);
     if (wiener) transform_group<ND, B0, B1, B2>(geo, a, smem, n, R, 0);
+    const int64_t probe_base = gid * static_cast<int64_t>(a.nmax) * P;
+    if (a.probe.active) {
+        for (int e = tid; e < total; e += blockDim.x) {
+            if (a.probe.coef) a.probe.coef[probe_base + e] = X[e];
+            if (a.probe.sigma) a.probe.sigma[probe_base + e] = S[e];
+        }
+    }
 
     // ---- shrinkage: coefficients in X, attenuation in V, and in S each
     // coefficient's aggregation error: a^2 (classic), a^2 sigma^2 (variance) or
@@ -1071,6 +1104,9 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
         S[e] = err;
     }
     __syncthreads();
+
+    if (a.probe.active && a.probe.atten)
+        for (int e = tid; e < total; e += blockDim.x) a.probe.atten[probe_base + e] = V[e];
 
     // Wiener sigma map: the group's mean coefficient sigma (bmndalgo.py:874-875),
     // summed per warp and then over warps in warp order
@@ -1241,6 +1277,12 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
 
     // ---- inverse transform and scatter ----
     transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, 1);
+    if (a.probe.active) {
+        if (a.probe.weights && tid < n) a.probe.weights[gid * static_cast<int64_t>(a.nmax) + tid] = wts[tid];
+        if (a.probe.filt)
+            for (int e = tid; e < total; e += blockDim.x) a.probe.filt[probe_base + e] = X[e];
+        return;
+    }
     for (int e = tid; e < total; e += blockDim.x) {
         const int g = e / P;
         const int p = e - g * P;
@@ -1327,7 +1369,7 @@ int64_t group_filter_smem_bytes(const BmndStageParams& sp) {
 int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const float* pilot,
                             const int32_t* sel, const int32_t* count, int64_t n_refs, double* num,
                             double* den, float* st, double* sig_num, cudaStream_t stream, const double* den_ro,
-                            int* err) {
+                            int* err, const GroupProbe* probe) {
     if (n_refs == 0) return BMND_OK;
     {
         const int P = patch_volume(sp);
@@ -1347,9 +1389,14 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
         a.vstride[d] = s;
         s *= sp.shape[d];
     }
-    for (int d = 0; d < sp.ndim; ++d) a.counts[d] = sp.shape[d] - sp.block[d] + 1;
+    a.n_lins = 1;
+    for (int d = 0; d < sp.ndim; ++d) {
+        a.counts[d] = sp.shape[d] - sp.block[d] + 1;
+        a.n_lins *= a.counts[d];
+    }
     a.sig_num = sig_num;
-    a.L = make_layout(sp, a.P, a.nmax, a.kmax, union_cells_bound(sp), sig_num != nullptr);
+    a.ucells_cap = union_cells_bound(sp);
+    a.L = make_layout(sp, a.P, a.nmax, a.kmax, a.ucells_cap, sig_num != nullptr);
     a.noisy = noisy;
     a.pilot = pilot;
     a.sel = sel;
@@ -1359,25 +1406,18 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
     a.den = den;
     a.den_ro = den_ro;
     a.err = err;
+    if (probe) a.probe = *probe;
+    if (a.probe.active && den_ro) return fail(BMND_ERR_INVALID_ARG, "the group probe has no mass-conservation pass");
     if (a.L.total > 227 * 1024)
         return fail(BMND_ERR_UNSUPPORTED, "group filter shared memory exceeds 227 KB for this profile");
     if (n_refs > 0x7fffffffLL) return fail(BMND_ERR_UNSUPPORTED, "too many groups");
     auto run = [&](auto kernel, int threads) -> int32_t {
-        BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(a.L.total)));
         // give shared memory only what the resident CTAs need, so the rest of
         // the unified L1 caches the Kronecker table and the volumes
-        int per_sm = 0, dev = 0, smem_sm = 0;
-        BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-        BMND_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, a.L.total));
-        BMND_CUDA_TRY(cudaGetDevice(&dev));
-        BMND_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
-        if (per_sm > 0 && smem_sm > 0) {
-            const int64_t want = static_cast<int64_t>(per_sm) * (a.L.total + 1024);
-            int pct = static_cast<int>((want * 100 + smem_sm - 1) / smem_sm);
-            if (pct > 100) pct = 100;
-            BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
-        }
+        int per_sm = 0, sms = 0;
+        if (int32_t rc = kernel_residency(reinterpret_cast<const void*>(kernel), threads,
+                                          static_cast<size_t>(a.L.total), true, &per_sm, &sms))
+            return rc;
         kernel<<<static_cast<unsigned>(n_refs), threads, a.L.total, stream>>>(a);
         BMND_LAUNCH_CHECK("group_filter_kernel");
         return BMND_OK;

@@ -1253,11 +1253,9 @@ int32_t run_mid(const bf16* in, const uint2* wpk, const float* bias, const bf16*
                 cudaStream_t stream) {
     using S = MidSmem<ND, C>;
     auto kernel = conv_mid_kernel<ND, C>;
-    BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(S::bytes)));
-    int dev = 0, sms = 0, per_sm = 0;
-    BMND_CUDA_TRY(cudaGetDevice(&dev));
-    BMND_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    BMND_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, S::bytes));
+    int sms = 0, per_sm = 0;
+    if (int32_t rc = kernel_residency(reinterpret_cast<const void*>(kernel), 256, S::bytes, false, &per_sm, &sms))
+        return rc;
     if (per_sm < 1) return fail(BMND_ERR_UNSUPPORTED, "pilot net layer does not fit on an SM");
     using TL = Tile<ND>;
     const int64_t ntiles = static_cast<int64_t>((g.W + TL::tx - 1) / TL::tx) * ((g.H + TL::ty - 1) / TL::ty) *
@@ -1276,8 +1274,10 @@ int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf1
                    int* err, cudaStream_t stream) {
     using TT = TcTile<ND, C>;
     auto kernel = conv_mid_tc_kernel<ND, C>;
-    BMND_CUDA_TRY(
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(TT::bytes)));
+    int sms = 0, per_sm = 0;
+    if (int32_t rc = kernel_residency(reinterpret_cast<const void*>(kernel), TT::threads, TT::bytes, false, &per_sm,
+                                      &sms))
+        return rc;
     if ((reinterpret_cast<uintptr_t>(in) & 15u) != 0 || (reinterpret_cast<uintptr_t>(wtc) & 15u) != 0)
         return fail(BMND_ERR_INVALID_ARG, "pilot net buffers must be 16-byte aligned");
     // one 4-D map per 8-channel chunk plane: (8 channels, x, y, z * batch), a
@@ -1307,9 +1307,6 @@ int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf1
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (rc != CUDA_SUCCESS) return fail(BMND_ERR_CUDA, "cuTensorMapEncodeTiled failed for the pilot net input");
     }
-    int dev = 0, sms = 0;
-    BMND_CUDA_TRY(cudaGetDevice(&dev));
-    BMND_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int64_t ntiles = static_cast<int64_t>((g.W + TT::tx - 1) / TT::tx) * ((g.H + TT::ty - 1) / TT::ty) * g.D *
                            g.nb;
     // one persistent CTA per SM: the weights fill most of the shared memory
@@ -1355,8 +1352,10 @@ int32_t forward_impl(const NetPlan& P, const unsigned char* packed, const float*
     {
         using OT = OutTile<ND>;
         constexpr size_t smem = out_smem_bytes<ND, C>();
-        BMND_CUDA_TRY(cudaFuncSetAttribute(conv_out_kernel<ND, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(smem)));
+        int sms = 0, per_sm = 0;
+        if (int32_t rc = kernel_residency(reinterpret_cast<const void*>(conv_out_kernel<ND, C>), OT::tx * OT::ty,
+                                          smem, false, &per_sm, &sms))
+            return rc;
         const int64_t blocks = static_cast<int64_t>((g.W + OT::tx - 1) / OT::tx) * ((g.H + OT::ty - 1) / OT::ty) *
                                ((g.D + OT::zb - 1) / OT::zb) * g.nb;
         conv_out_kernel<ND, C><<<static_cast<unsigned>(blocks), OT::tx * OT::ty, smem, stream>>>(
@@ -1371,7 +1370,9 @@ int32_t run_wgrad(const TI* in, const TG* gout, float* partial, float* grad, int
                   cudaStream_t stream) {
     using S = WgradSmem<ND, CIN, COUT, TI, TG>;
     auto kernel = wgrad_kernel<ND, CIN, COUT, TI, TG>;
-    BMND_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(S::bytes)));
+    int sms = 0, per_sm = 0;
+    if (int32_t rc = kernel_residency(reinterpret_cast<const void*>(kernel), 256, S::bytes, false, &per_sm, &sms))
+        return rc;
     kernel<<<static_cast<unsigned>(tiles), 256, S::bytes, stream>>>(in, gout, partial, g);
     BMND_LAUNCH_CHECK("wgrad_kernel");
     constexpr int64_t np = static_cast<int64_t>(Tile<ND>::taps) * CIN * COUT + COUT;

@@ -288,7 +288,9 @@ int32_t bmnd_stage_workspace_bytes(const BmndStageParams* params, int64_t n_refs
  *   d_sel/d_count/d_accepted  optional (NULL) copies of the match sets, laid
  *               out as in bmnd_blockmatch_patches
  * The workspace must be at least bmnd_stage_workspace_bytes() bytes and
- * 256-byte aligned.
+ * 256-byte aligned.  d_refs positions must lie on the patch grid (0 <= ref[d]
+ * < shape[d] - block[d] + 1, as bmnd_reference_schedule() makes them); they are
+ * not checked on the device.
  */
 int32_t bmnd_stage(const BmndStageParams* params, const float* d_noisy, const float* d_pilot,
                    const int32_t* d_refs, int64_t n_refs, float* d_out, int32_t* d_sel,
@@ -324,6 +326,31 @@ int32_t bmnd_run(const BmndStageParams* ht, const BmndStageParams* wiener,
                  float* d_out, void* d_workspace, uint64_t workspace_bytes, uint64_t stream);
 
 /*
+ * Group probe: filter explicit groups and return their intermediate arrays
+ * instead of aggregating them.  Replaces, for testing and inspection, the body
+ * of the reference's per-group closures filter_ht_group / filter_wiener_group
+ * (src/bmnd/bmndalgo.py:335-559, :760-981): the forward transform
+ * (transforms.py:209-255), the noise std (variance.py:1634-1711), the
+ * hard-threshold mask (poisson.py:30-46) or Wiener gain (wiener.py:78-95), the
+ * aggregation weights (aggregationweights.py:633-653) and the inverse
+ * transform.  Group i has d_count[i] members d_sel[i * max_stack + g]
+ * (patch-grid lins, 0 <= lin < prod(shape - block + 1)).  Outputs (device, any
+ * may be NULL; rows of members >= d_count[i] are left untouched):
+ *   d_coef, d_sigma, d_atten, d_filt  n_groups x max_stack x P float32
+ *   d_weights                          n_groups x max_stack float32
+ * params->mass_conserve must be 0.  The workspace (256-byte aligned) holds
+ * bmnd_group_probe_workspace_bytes() bytes.  The call synchronises the stream
+ * and returns BMND_ERR_INVALID_ARG if a group had a member outside the patch
+ * grid, more than max_stack members, or a union box the kernel's shared-memory
+ * layout cannot hold (such groups are skipped, their outputs untouched).
+ */
+int32_t bmnd_group_probe_workspace_bytes(const BmndStageParams* params, uint64_t* out_bytes);
+int32_t bmnd_group_probe(const BmndStageParams* params, const float* d_noisy, const float* d_pilot,
+                         const int32_t* d_sel, const int32_t* d_count, int64_t n_groups, float* d_coef,
+                         float* d_sigma, float* d_atten, float* d_weights, float* d_filt, void* d_workspace,
+                         uint64_t workspace_bytes, uint64_t stream);
+
+/*
  * Allocation-free variant of bmnd_stage().  It has no counterpart in the
  * reference.  It is meant for callers that may not allocate device memory
  * after start-up: hosts whose memory pool owns the whole device (acquisition
@@ -336,8 +363,15 @@ int32_t bmnd_run(const BmndStageParams* ht, const BmndStageParams* wiener,
  *     BMND_ERR_WORKSPACE before any device work (see
  *     bmnd_stage_workspace_bytes for the requirement).
  *   - The first call on a device looks up the array's device address (once
- *     per device, with that device current); make that first call before any
+ *     per CUDA context, with that device current; a context re-created after
+ *     cudaDeviceReset is looked up again); make that first call before any
  *     stream capture.
+ *   - Precision BMND_MATCH_APPROX and BMND_MATCH_SUBSAMPLED stages keep their
+ *     per-voxel screening arrays in the same array, as bmnd_stage keeps them
+ *     in its workspace, so both entry points run the same kernels.
+ *   - d_refs holds reference positions on the patch grid (0 <= ref[d] <
+ *     shape[d] - block[d] + 1), as from bmnd_reference_schedule(); positions
+ *     outside it are not checked on the device.
  *   - Every call shares the one array and leaves its contents behind; the
  *     accumulators are cleared at the start of each call.  Calls whose device
  *     work overlaps (other streams, other host threads) race on the array.

@@ -55,3 +55,45 @@ def test_trained_pilot_tracks_plain_stage1(cuda, case):
     # the net imitates plain stage 1: close to it, and far better than the input
     assert phantoms.psnr(learned, plain1) > 38.0
     assert phantoms.psnr(learned, clean) > phantoms.psnr(case["noisy"], clean) + 12.0
+
+
+def test_fast_path_within_budget_of_plain_path(cuda, case):
+    """The learned-pilot path keeps the plain path's quality (PSNR loss at most
+    0.05 dB on the held-out crop) and beats the method without the net: plain
+    stage 1 followed by the same fast Wiener stage."""
+    import bmnd_gb300 as bg
+    from bmnd_gb300 import phantoms
+    from bmnd_gb300.api import stage_device
+    from bmnd_gb300.pilot import FAST_MATCH_PRECISION, bmnd_fast, fast_profile
+
+    clean, x, prof, net = case["clean"], case["x"], case["prof"], case["net"]
+    plain = bg.bmnd_device(x, prof).cpu().numpy()
+    fast = bmnd_fast(x, prof, net).cpu().numpy()
+    no_net = stage_device(x, fast_profile(prof), "wiener", stage_device(x, prof, "ht"),
+                          match_precision=FAST_MATCH_PRECISION, fast_transforms=True).cpu().numpy()
+    p_plain, p_fast, p_nonet = (phantoms.psnr(v, clean) for v in (plain, fast, no_net))
+    print(f"held-out 128^3: plain {p_plain:.3f} dB, learned fast path {p_fast:.3f} dB, "
+          f"plain stage 1 + fast stage 2 {p_nonet:.3f} dB")
+    assert p_fast >= p_plain - 0.05, (p_fast, p_plain)
+    assert p_fast > p_nonet, (p_fast, p_nonet)
+
+
+def test_learned_pilot_through_bmnd(cuda, case):
+    """bmnd(..., pilot="learned") is the fast path behind the drop-in API: NumPy
+    in, NumPy out, the pilot reported as the "ht" stage estimate."""
+    import bmnd_gb300 as bg
+    from bmnd_gb300.pilot import bmnd_fast
+
+    noisy, x, prof, net = case["noisy"], case["x"], case["prof"], case["net"]
+    seen = {}
+    out = bg.bmnd(noisy, prof, pilot="learned", stage_callback=lambda s, e: seen.__setitem__(s, e))
+    assert isinstance(out, np.ndarray) and out.dtype == np.float32 and out.shape == noisy.shape
+    details = {}
+    ref = bmnd_fast(x, prof, net, details=details).cpu().numpy()
+    np.testing.assert_allclose(out, ref, rtol=0, atol=1e-4 * float(np.max(ref)))
+    np.testing.assert_array_equal(seen["wiener"], out)
+    np.testing.assert_allclose(seen["ht"], details["pilot"].cpu().numpy(), rtol=0, atol=1e-4 * float(np.max(ref)))
+    with pytest.raises(NotImplementedError):
+        bg.bmnd(noisy, prof, pilot="learned", return_sigma_map=True)
+    with pytest.raises(ValueError):
+        bg.bmnd(noisy, prof, pilot="neural")

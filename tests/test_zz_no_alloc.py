@@ -81,6 +81,29 @@ def test_noalloc_stage_matches_workspace_stage(cuda, native, kind):
         pilot = cuda.from_numpy(want).cuda()
 
 
+@pytest.mark.parametrize("precision", ["approx", "subsampled"])
+def test_noalloc_screening_precisions_match_workspace_stage(cuda, native, precision):
+    """The Wiener stage with the screening forms of matching (approximate and
+    subsampled): their per-voxel arrays come from the fixed array, as they come
+    from the workspace in bmnd_stage, so both entry points give the same match
+    sets and estimates, twice in a row."""
+    import bmnd_gb300 as bg
+    from bmnd_gb300 import _abi, phantoms
+    from bmnd_gb300.api import stage_device
+
+    _, noisy = phantoms.ellipsoids_3d(size=24, seed=23, count=8)
+    x = cuda.from_numpy(noisy).cuda()
+    prof = bg.BM4DProfile(noise_model="poisson")
+    pilot = stage_device(x, prof, "ht")
+    p, refs_h = _stage_inputs("wiener", noisy, prof)
+    p.match_precision = _abi.MATCH_APPROX if precision == "approx" else _abi.MATCH_SUBSAMPLED
+    refs = cuda.from_numpy(refs_h).cuda()
+    want = _with_workspace(cuda, native, p, x, pilot, refs).cpu().numpy()
+    for _ in range(2):
+        got = _no_alloc(cuda, native, p, x, pilot, refs).cpu().numpy()
+        assert np.max(np.abs(got - want)) <= TOL, (precision, float(np.max(np.abs(got - want))))
+
+
 def test_noalloc_rejects_oversized_stage(cuda, native):
     import bmnd_gb300 as bg
     from bmnd_gb300 import _abi
