@@ -515,9 +515,11 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
 
     kt = time_kernels(torch, x, profile, gauss=gauss)
     peaks = load_peaks()
-    sm_mhz = clocks.get("sm_mhz") or 2070.0
-    fp32_peak = 152 * 128 * sm_mhz * 1e6  # FP32 instructions per second
     from bmnd_gb300 import _abi
+
+    # the compute bounds, measured on this GPU now: MUFU lg2 and FP32 FMA issue rates
+    rates = _abi.unit_rates()
+    fp32_peak = 2.0 * rates["ffma_per_s"]  # FP32 flops per second (an FMA is two)
 
     # kernels of the measured path: the fast path when it ran (its Wiener
     # stage on the learned pilot, and the net), else the plain path
@@ -565,9 +567,10 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
                 "achieved_gterms_s": k["voxel_terms"] / (dom_ms * 1e-3) / 1e9,
             }
             if dom_name in ("blockmatch_wiener_approx", "blockmatch_wiener_subsampled"):
-                # one lg2 per term on the SFU (16 results per clock per SM)
-                sfu = 152 * 16 * sm_mhz * 1e6
+                # one MUFU lg2 per term: the measured lg2 issue rate bounds the terms per second
+                sfu = rates["lg2_per_s"]
                 compute["sfu_bound_gterms_s"] = sfu / 1e9
+                compute["sfu_bound_source"] = "measured (bmnd_unit_rates: lg2.approx.ftz.f32 chains on every SM)"
                 compute["frac_of_sfu_bound"] = k["voxel_terms"] / (dom_ms * 1e-3) / sfu
         else:
             # read noisy (+ pilot) once, write float64 numerator and denominator once
@@ -680,6 +683,8 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
             "compute": compute,
         },
         "kernels": kt,
+        "unit_rates": {"lg2_per_s": rates["lg2_per_s"], "ffma_per_s": rates["ffma_per_s"],
+                       "what": "measured by bmnd_unit_rates after the timed steps"},
         "clocks": clocks,
         "gpu_launches": launches,
         "psnr_db": psnr_fast if fast is not None else psnr_plain,

@@ -201,6 +201,7 @@ SIGNATURES = {
         _I32,
         [ctypes.POINTER(StageParams), _VP, _VP, _VP, _VP, _I64, _VP, _VP, _VP, _VP, _VP, _VP, _U64, _U64],
     ),
+    "bmnd_unit_rates": (_I32, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _VP, _U64]),
     "bmnd_pilotnet_param_count": (_I32, [_PNP, _I64P]),
     "bmnd_pilotnet_packed_bytes": (_I32, [_PNP, _U64P]),
     "bmnd_pilotnet_workspace_bytes": (_I32, [_PNP, _I32, _U64P]),
@@ -270,6 +271,19 @@ def check(code: int) -> None:
     if code != OK:
         msg = lib().bmnd_last_error()
         raise BmndError(code, msg.decode() if msg else "")
+
+
+def unit_rates(stream=None) -> dict:
+    """Measured MUFU lg2 and FP32 FMA issue rates of the current device, per
+    second (``bmnd_unit_rates``)."""
+    import torch
+
+    sink = torch.zeros(16, dtype=torch.float32, device=torch.cuda.current_device())
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    lg2, ffma = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    check(lib().bmnd_unit_rates(ctypes.byref(lg2), ctypes.byref(ffma), sink.data_ptr(), int(stream.cuda_stream)))
+    return {"lg2_per_s": lg2.value, "ffma_per_s": ffma.value}
 
 
 def launch_count() -> int:

@@ -194,9 +194,19 @@ int32_t validate_stage(const BmndStageParams& sp) {
     return BMND_OK;
 }
 
+// Stages aggregate deterministically (aggregate.cu) unless they conserve group
+// mass (whose second pass re-aggregates against the first pass's denominator)
+// or their patches exceed 128 voxels; the others, and the sigma-map entry
+// point, add into float64 volumes with atomics.
+bool deterministic_aggregation(const BmndStageParams& sp) {
+    return sp.mass_conserve == 0 && patch_volume(sp) <= 128;
+}
+
 struct StageWorkspace {
-    double* num;
+    double* num;  // float64 accumulators of the atomic aggregation, or null
     double* den;
+    char* agg_base;  // deterministic aggregation region, or null
+    AggregationLayout agg;
     int32_t* sel;
     int32_t* count;
     int32_t* accepted;
@@ -222,8 +232,11 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
         off += align256(bytes);
         return o;
     };
-    uint64_t o_num = take(8 * vox);
-    uint64_t o_den = take(8 * vox);
+    const bool det = deterministic_aggregation(sp);
+    if (det) w.agg = aggregation_layout(sp, n_refs);
+    uint64_t o_num = det ? 0 : take(8 * vox);
+    uint64_t o_den = det ? 0 : take(8 * vox);
+    uint64_t o_agg = det ? take(w.agg.bytes) : 0;
     uint64_t o_sel = take(4ull * n_refs * sp.max_stack);
     uint64_t o_cnt = take(4ull * n_refs);
     uint64_t o_acc = take(4ull * n_refs);
@@ -237,8 +250,9 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
     w.bytes = off;
     if (base) {
         char* b = static_cast<char*>(base);
-        w.num = reinterpret_cast<double*>(b + o_num);
-        w.den = reinterpret_cast<double*>(b + o_den);
+        w.num = det ? nullptr : reinterpret_cast<double*>(b + o_num);
+        w.den = det ? nullptr : reinterpret_cast<double*>(b + o_den);
+        w.agg_base = det ? b + o_agg : nullptr;
         w.sel = reinterpret_cast<int32_t*>(b + o_sel);
         w.count = reinterpret_cast<int32_t*>(b + o_cnt);
         w.accepted = reinterpret_cast<int32_t*>(b + o_acc);
@@ -268,9 +282,10 @@ BmndMatchParams match_params_of(const BmndStageParams& sp) {
     return mp;
 }
 
-// bytes of the stage workspace followed by the float64 sigma-map numerator
+// bytes of the stage workspace followed by the float64 numerator, denominator
+// and sigma-map numerator of the atomic aggregation the sigma maps use
 uint64_t sigma_workspace_bytes(const BmndStageParams& sp, int64_t n_refs) {
-    return carve(sp, n_refs, nullptr).bytes + align256(8ull * static_cast<uint64_t>(volume_voxels(sp)));
+    return carve(sp, n_refs, nullptr).bytes + 3 * align256(8ull * static_cast<uint64_t>(volume_voxels(sp)));
 }
 
 int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pilot,
@@ -293,12 +308,18 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
     if (count) w.count = count;
     if (accepted) w.accepted = accepted;
     uint64_t vox = static_cast<uint64_t>(volume_voxels(sp));
-    BMND_CUDA_TRY(cudaMemsetAsync(w.num, 0, 8 * vox, stream));
-    BMND_CUDA_TRY(cudaMemsetAsync(w.den, 0, 8 * vox, stream));
+    const bool det = w.agg_base != nullptr && !sigma_out;
     double* sig_num = nullptr;
     if (sigma_out) {
-        sig_num = reinterpret_cast<double*>(static_cast<char*>(ws) + need.bytes);
+        char* extra = static_cast<char*>(ws) + need.bytes;
+        w.num = reinterpret_cast<double*>(extra);
+        w.den = reinterpret_cast<double*>(extra + align256(8 * vox));
+        sig_num = reinterpret_cast<double*>(extra + 2 * align256(8 * vox));
         BMND_CUDA_TRY(cudaMemsetAsync(sig_num, 0, 8 * vox, stream));
+    }
+    if (!det) {
+        BMND_CUDA_TRY(cudaMemsetAsync(w.num, 0, 8 * vox, stream));
+        BMND_CUDA_TRY(cudaMemsetAsync(w.den, 0, 8 * vox, stream));
     }
     BmndMatchParams mp = match_params_of(sp);
     const bool on_pilot = sp.filter == BMND_FILTER_WIENER && sp.wiener_match_source == BMND_SOURCE_PILOT;
@@ -330,6 +351,18 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
                                   sp.match_noise_ssd, sp.ssd_gamma, allow_alloc, null_moments,
                                   sp.null_max_count, sp.ssd_poisson_bias != 0, w.aux, w.aux_floats);
     if (rc) return rc;
+    if (det) {
+        rc = launch_entry_index(sp, w.sel, w.count, n_refs, w.agg_base, w.agg, stream);
+        if (rc) return rc;
+        const AggStore store{reinterpret_cast<float*>(w.agg_base + w.agg.o_store),
+                             reinterpret_cast<float*>(w.agg_base + w.agg.o_wstore),
+                             reinterpret_cast<const int32_t*>(w.agg_base + w.agg.o_slot),
+                             static_cast<int>(agg_row_floats(sp))};
+        rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, nullptr, nullptr, w.st, nullptr, stream,
+                                 nullptr, nullptr, nullptr, &store);
+        if (rc) return rc;
+        return launch_gather(sp, noisy, out, w.agg_base, w.agg, stream);
+    }
     rc = launch_group_filter(sp, noisy, pilot, w.sel, w.count, n_refs, w.num, w.den, w.st, sig_num, stream);
     if (rc) return rc;
     if (sp.mass_conserve) {

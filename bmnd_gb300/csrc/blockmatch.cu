@@ -993,16 +993,31 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                 __syncthreads();
                 const float vs = select_kth(a.presel, true);
                 const float vskey = canonical_key(vs);
-                if (tid == 0) redi[0] = 0;
-                __syncthreads();
-                for (int64_t c = tid; c < window; c += blockDim.x) {
-                    if (canonical_key(cand[c]) <= vskey) {
-                        const int slot = atomicAdd(redi, 1);
+                // the prescreened candidates in window order (ballots and warp
+                // counts, no atomics), so that when ties at the cut fill the
+                // queue the same candidates are kept on every run
+                int nq = 0;
+                const int nwarps = static_cast<int>(blockDim.x >> 5);
+                for (int64_t c0 = 0; c0 < window; c0 += blockDim.x) {
+                    const int64_t c = c0 + tid;
+                    const bool take = c < window && canonical_key(cand[c]) <= vskey;
+                    const unsigned m = __ballot_sync(0xffffffffu, take);
+                    if (lane == 0) hist[warp] = static_cast<uint32_t>(__popc(m));
+                    __syncthreads();
+                    int before = nq, chunk = 0;
+                    for (int w = 0; w < nwarps; ++w) {
+                        const int cw = static_cast<int>(hist[w]);
+                        if (w < warp) before += cw;
+                        chunk += cw;
+                    }
+                    if (take) {
+                        const int slot = before + __popc(m & ((1u << lane) - 1u));
                         if (slot < kSQueue) qidx[slot] = static_cast<int32_t>(c);
                     }
+                    nq += chunk;
+                    __syncthreads();
                 }
-                __syncthreads();
-                const int nsel = min(redi[0], kSQueue);
+                const int nsel = min(nq, kSQueue);
                 const float sum_a = redf[4] + redf[5] + redf[6] + redf[7];
                 for (int i = tid; i < nsel; i += blockDim.x) {
                     int64_t lin;

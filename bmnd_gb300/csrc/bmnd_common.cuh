@@ -223,11 +223,33 @@ struct GroupProbe {
     float* weights;  // aggregation weight of every member
     float* filt;     // inverse transform of the shrunk coefficients
 };
+// deterministic aggregation (aggregate.cu): byte offsets of its arrays in a
+// 256-byte aligned region, for a stage with n_refs groups
+struct AggregationLayout {
+    int64_t n_lins;  // patch origins
+    uint64_t o_start, o_cursor, o_block_sums, o_entries, o_slot, o_store, o_wstore, o_planes, o_wsum;
+    uint64_t bytes;
+};
+AggregationLayout aggregation_layout(const BmndStageParams& sp, int64_t n_refs);
+int64_t agg_row_floats(const BmndStageParams& sp);
+// the group filter's output in deterministic mode: member g of group i writes
+// its weighted filtered patch to store[slot_of[i * max_stack + g] * row + p]
+// and its weight to wstore[slot]
+struct AggStore {
+    float* store;
+    float* wstore;
+    const int32_t* slot_of;
+    int row;
+};
+int32_t launch_entry_index(const BmndStageParams& sp, const int32_t* sel, const int32_t* count, int64_t n_refs,
+                           char* base, const AggregationLayout& L, cudaStream_t stream);
+int32_t launch_gather(const BmndStageParams& sp, const float* noisy, float* out, char* base,
+                      const AggregationLayout& L, cudaStream_t stream);
 int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const float* pilot,
                             const int32_t* sel, const int32_t* count, int64_t n_refs, double* num,
                             double* den, float* st, double* sig_num, cudaStream_t stream,
                             const double* den_ro = nullptr, int* err = nullptr,
-                            const GroupProbe* probe = nullptr);
+                            const GroupProbe* probe = nullptr, const AggStore* store = nullptr);
 int32_t launch_finalize_sigma(const BmndStageParams& sp, const double* sig_num, const double* den,
                               float global_sigma, float* out, cudaStream_t stream);
 int32_t launch_finalize(const BmndStageParams& sp, const double* num, const double* den,

@@ -73,6 +73,7 @@ struct FilterArgs {
     GroupProbe probe;
     int64_t n_lins;      // patch-grid positions: a member's lin lies in [0, n_lins)
     int64_t ucells_cap;  // union-box cells the occupancy grid of the layout holds
+    AggStore store;      // deterministic aggregation: rows of the entry store, or store.store == null
 };
 
 __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax, int64_t ucells, bool sigma) {
@@ -1283,6 +1284,23 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
             for (int e = tid; e < total; e += blockDim.x) a.probe.filt[probe_base + e] = X[e];
         return;
     }
+    if (a.store.store) {
+        // deterministic aggregation: every member's weighted filtered patch
+        // goes to the store row of its entry; the sums happen in aggregate.cu
+        int* slot = sm<int>(smem, a.L.shl);  // free after the exact phase
+        if (tid < n) {
+            const int s = a.store.slot_of[gid * static_cast<int64_t>(sp.max_stack) + tid];
+            slot[tid] = s;
+            a.store.wstore[s] = wts[tid];
+        }
+        __syncthreads();
+        for (int e = tid; e < total; e += blockDim.x) {
+            const int g = e / P;
+            const int p = e - g * P;
+            a.store.store[static_cast<int64_t>(slot[g]) * a.store.row + p] = mul_rn(X[e], mul_rn(wts[g], win[p]));
+        }
+        return;
+    }
     for (int e = tid; e < total; e += blockDim.x) {
         const int g = e / P;
         const int p = e - g * P;
@@ -1369,7 +1387,7 @@ int64_t group_filter_smem_bytes(const BmndStageParams& sp) {
 int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const float* pilot,
                             const int32_t* sel, const int32_t* count, int64_t n_refs, double* num,
                             double* den, float* st, double* sig_num, cudaStream_t stream, const double* den_ro,
-                            int* err, const GroupProbe* probe) {
+                            int* err, const GroupProbe* probe, const AggStore* store) {
     if (n_refs == 0) return BMND_OK;
     {
         const int P = patch_volume(sp);
@@ -1407,6 +1425,10 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
     a.den_ro = den_ro;
     a.err = err;
     if (probe) a.probe = *probe;
+    if (store) {
+        a.store = *store;
+        if (sig_num || den_ro) return fail(BMND_ERR_INVALID_ARG, "the entry store excludes sigma maps and mass passes");
+    }
     if (a.probe.active && den_ro) return fail(BMND_ERR_INVALID_ARG, "the group probe has no mass-conservation pass");
     if (a.L.total > 227 * 1024)
         return fail(BMND_ERR_UNSUPPORTED, "group filter shared memory exceeds 227 KB for this profile");

@@ -356,8 +356,8 @@ int32_t bmnd_group_probe(const BmndStageParams* params, const float* d_noisy, co
  * after start-up: hosts whose memory pool owns the whole device (acquisition
  * pipelines that reserve all memory up front), or bindings that have no way
  * to call into the CUDA allocator.  The caller still passes inputs and
- * outputs; the stage's scratch space (float64 numerator and denominator,
- * match table) is a fixed array of BMND_STATIC_SCRATCH_BYTES compiled into
+ * outputs; the stage's scratch space (aggregation arrays, match table) is a
+ * fixed array of BMND_STATIC_SCRATCH_BYTES compiled into
  * this library, held by every GPU that loads it until the process exits.
  *   - A stage needing more scratch than that is rejected with
  *     BMND_ERR_WORKSPACE before any device work (see
@@ -382,6 +382,17 @@ int32_t bmnd_group_probe(const BmndStageParams* params, const float* d_noisy, co
 int32_t bmnd_stage_noalloc(const BmndStageParams* params, const float* d_noisy,
                            const float* d_pilot, const int32_t* d_refs, int64_t n_refs,
                            float* d_out, uint64_t stream);
+
+/*
+ * Measurement support (no counterpart in the reference): the issue rates, per
+ * second, of the two units that bound this path's kernels on the current
+ * device at its current clock: MUFU lg2.approx (one per Poisson-deviance voxel
+ * term in the screening forms of matching) and FP32 fused multiply-add (the
+ * exact variance).  Runs two short kernels of independent dependency chains on
+ * every SM and synchronises the stream; d_sink is a device buffer of at least
+ * 4 bytes.
+ */
+int32_t bmnd_unit_rates(double* lg2_per_s, double* ffma_per_s, void* d_sink, uint64_t stream);
 
 /* ------------------------------------------------------------------------
  * Learned stage-1 pilot (fast path).  No counterpart in the reference: a
