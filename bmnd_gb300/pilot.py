@@ -258,17 +258,26 @@ def _init_params(ndim, channels, layers, seed, out_scale=0.1):
 # ---------------------------------------------------------------------------
 # training data
 # ---------------------------------------------------------------------------
+def lowcount_peak(seed: int) -> float:
+    """Peak count of the low-count 3-D phantoms: uniform in [2, 5], from the seed."""
+    return float(np.random.default_rng(10_000 + seed).uniform(2.0, 5.0))
+
+
 def training_pairs(kind: str = "bm4d", size: int = 128, count: int = 8, seed0: int = 1000, profile=None):
     """(noisy, plain stage-1 estimate) CUDA pairs on seeded phantoms (seeds
-    seed0 .. seed0 + count - 1, disjoint from the benchmark's)."""
+    seed0 .. seed0 + count - 1, disjoint from the benchmark's).  ``kind``
+    "bm4d_lowcount" scales each ellipsoid volume to a peak of
+    ``lowcount_peak(seed)`` counts."""
     torch = _torch()
     import bmnd_gb300 as bg
 
     if profile is None:
-        profile = (bg.BM4DProfile if kind == "bm4d" else bg.BM3DProfile)(noise_model=bg.NoiseModel.POISSON)
+        profile = (bg.BM3DProfile if kind == "bm3d" else bg.BM4DProfile)(noise_model=bg.NoiseModel.POISSON)
     pairs = []
     for i in range(count):
-        if kind == "bm4d":
+        if kind == "bm4d_lowcount":
+            _, noisy = phantoms.ellipsoids_3d(size, seed=seed0 + i, peak=lowcount_peak(seed0 + i))
+        elif kind == "bm4d":
             _, noisy = phantoms.ellipsoids_3d(size, seed=seed0 + i)
         elif size >= 1024:
             _, noisy = phantoms.blobs_2d(size, seed=seed0 + i)

@@ -18,7 +18,10 @@ import time
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kind", default="bm4d", choices=["bm4d", "bm3d"])
+    ap.add_argument("--kind", default="bm4d", choices=["bm4d", "bm3d", "bm4d_lowcount"])
+    ap.add_argument("--seed0", type=int, default=1000, help="first training phantom seed")
+    ap.add_argument("--eval-uneven", action="store_true",
+                    help="only evaluate the saved net on eight uneven volumes (128^3 .. 320^3)")
     ap.add_argument("--size", type=int, default=None)
     ap.add_argument("--count", type=int, default=8)
     ap.add_argument("--steps", type=int, default=3000)
@@ -38,17 +41,20 @@ def main(argv=None):
     from bmnd_gb300 import phantoms
     from bmnd_gb300.api import stage_device
     from bmnd_gb300.pilot import (PilotNet, bmnd_fast, calibrate_excess_high, default_net_path, fast_profile,
-                                  training_pairs)
+                                  lowcount_peak, training_pairs)
 
     torch.cuda.set_device(0)
-    nd = 3 if args.kind == "bm4d" else 2
+    nd = 2 if args.kind == "bm3d" else 3
+    if args.eval_uneven:
+        evaluate_uneven(args.kind, args.out or default_net_path(args.kind))
+        return
     channels = args.channels or (48 if nd == 3 else 32)
     layers = args.layers or (8 if nd == 3 else 10)
     crop = args.crop if nd == 3 else max(args.crop, 64)
     if args.size is None:
         args.size = 256 if nd == 3 else 2048
     t0 = time.time()
-    pairs = training_pairs(args.kind, args.size, args.count)
+    pairs = training_pairs(args.kind, args.size, args.count, seed0=args.seed0)
     torch.cuda.synchronize()
     t_data = time.time() - t0
     net = PilotNet(nd, channels, layers, seed=args.seed)
@@ -70,7 +76,9 @@ def main(argv=None):
 
     # held-out evaluation: pilot quality and the fast path against the plain path
     prof = (bg.BM4DProfile if nd == 3 else bg.BM3DProfile)(noise_model=bg.NoiseModel.POISSON)
-    if nd == 3:
+    if args.kind == "bm4d_lowcount":
+        clean, noisy = phantoms.ellipsoids_3d(args.size, seed=2000, peak=lowcount_peak(2000))
+    elif nd == 3:
         clean, noisy = phantoms.ellipsoids_3d(args.size, seed=2000)
     elif args.size >= 1024:
         clean, noisy = phantoms.blobs_2d(args.size, seed=2000)
@@ -110,6 +118,66 @@ def main(argv=None):
         excess_high=net.excess_high, fallback_tiles=d["fallback_tiles"], tiles=d["tiles"], weights=out,
     )
     print(json.dumps(r), flush=True)
+
+
+UNEVEN_SEED = 5000
+
+
+def uneven_shapes(count: int = 8, lo: int = 128, hi: int = 320, seed: int = UNEVEN_SEED):
+    """``count`` volume shapes with every extent drawn uniformly from [lo, hi]."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    return [tuple(int(v) for v in rng.integers(lo, hi + 1, size=3)) for _ in range(count)]
+
+
+def evaluate_uneven(kind: str, weights: str) -> list:
+    """The fast path with the net in ``weights`` against the plain path on eight
+    uneven volumes (30 ellipsoids, seeds 5000 + i; for "bm4d_lowcount" a peak of
+    U[2, 5] counts): PSNR against the clean phantom and against the plain
+    output, the tiles that fell back, and Mvoxel/s of both paths.  One JSON line
+    per volume."""
+    import torch
+
+    import bmnd_gb300 as bg
+    from bmnd_gb300 import phantoms
+    from bmnd_gb300.pilot import PilotNet, bmnd_fast, lowcount_peak
+
+    net = PilotNet.load(weights)
+    prof = bg.BM4DProfile(noise_model=bg.NoiseModel.POISSON)
+    rows = []
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        r = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return r, e0.elapsed_time(e1)
+
+    for i, shape in enumerate(uneven_shapes()):
+        seed = UNEVEN_SEED + i
+        peak = lowcount_peak(seed) if kind == "bm4d_lowcount" else None
+        clean, noisy = phantoms.ellipsoids_3d(shape, seed=seed, peak=peak)
+        x = torch.from_numpy(noisy).cuda()
+        plain, ms_plain = timed(lambda: bg.bmnd_device(x, prof))
+        d = {}
+        fast, ms_fast = timed(lambda: bmnd_fast(x, prof, net, details=d))
+        p_plain = phantoms.psnr(plain.cpu().numpy(), clean)
+        p_fast = phantoms.psnr(fast.cpu().numpy(), clean)
+        row = dict(shape=list(shape), peak=peak, psnr_noisy=phantoms.psnr(noisy, clean), psnr_plain=p_plain,
+                   psnr_fast=p_fast, fast_minus_plain_db=p_fast - p_plain,
+                   psnr_fast_vs_plain=phantoms.psnr(fast.cpu().numpy(), plain.cpu().numpy(), float(clean.max())),
+                   fallback_tiles=d["fallback_tiles"], tiles=d["tiles"],
+                   mvox_s_plain=noisy.size / (ms_plain * 1e-3) / 1e6, mvox_s_fast=noisy.size / (ms_fast * 1e-3) / 1e6,
+                   speedup=ms_plain / ms_fast)
+        rows.append(row)
+        print(json.dumps(row), flush=True)
+        del x, plain, fast
+        torch.cuda.empty_cache()
+    return rows
 
 
 if __name__ == "__main__":
