@@ -216,6 +216,8 @@ struct StageWorkspace {
     float* thr_ref;  // per-reference thresholds (reference-finite-count policy)
     float* aux;      // approximate screening form: per-voxel arrays of the matched volume
     int64_t aux_floats;
+    char* ssd;       // tensor-core SSD matching: norms, screening distances, tiles
+    uint64_t ssd_bytes;
     uint64_t bytes;
 };
 
@@ -247,6 +249,8 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
     const BmndMatchParams mp = match_params_of(sp);
     w.aux_floats = approx_scratch_floats(mp, sp.shape, sp.block);
     uint64_t o_aux = take(w.aux_floats > 0 ? 4ull * static_cast<uint64_t>(w.aux_floats) : 16);
+    w.ssd_bytes = ssd_tc_scratch_bytes(mp, sp.block, n_refs, sp.ssd_poisson_bias != 0);
+    uint64_t o_ssd = take(w.ssd_bytes > 0 ? w.ssd_bytes : 16);
     w.bytes = off;
     if (base) {
         char* b = static_cast<char*>(base);
@@ -261,12 +265,16 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
         w.thr = reinterpret_cast<float*>(b + o_mm + 8);
         w.thr_ref = reinterpret_cast<float*>(b + o_tr);
         w.aux = w.aux_floats > 0 ? reinterpret_cast<float*>(b + o_aux) : nullptr;
+        w.ssd = w.ssd_bytes > 0 ? b + o_ssd : nullptr;
     }
     return w;
 }
 
 BmndMatchParams match_params_of(const BmndStageParams& sp) {
     BmndMatchParams mp{};
+    // SSD matching of a volume: the tensor-core screening with exact rescoring
+    // gives the exact kernel's match sets (see ssd_select_kernel), so exact
+    // requests take it
     mp.ndim = sp.ndim;
     for (int d = 0; d < sp.ndim; ++d) {
         mp.counts[d] = sp.shape[d] - sp.block[d] + 1;
@@ -278,6 +286,8 @@ BmndMatchParams match_params_of(const BmndStageParams& sp) {
     mp.distance = sp.distance;
     mp.stabilize_ties = sp.stabilize_ties;
     mp.precision = sp.match_precision;
+    if (sp.distance == BMND_DIST_SSD && sp.match_precision == BMND_MATCH_EXACT && !sp.ssd_poisson_bias)
+        mp.precision = BMND_MATCH_FAST;
     mp.count_scale = sp.count_scale;
     return mp;
 }
@@ -349,7 +359,8 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
     rc = launch_blockmatch_volume(mp, match_src, sp.shape, sp.block, refs, n_refs, thr_per_ref,
                                   sp.match_threshold, w.sel, w.count, w.accepted, stream, thr_dev,
                                   sp.match_noise_ssd, sp.ssd_gamma, allow_alloc, null_moments,
-                                  sp.null_max_count, sp.ssd_poisson_bias != 0, w.aux, w.aux_floats);
+                                  sp.null_max_count, sp.ssd_poisson_bias != 0, w.aux, w.aux_floats, w.ssd,
+                                  w.ssd_bytes);
     if (rc) return rc;
     if (det) {
         rc = launch_entry_index(sp, w.sel, w.count, n_refs, w.agg_base, w.agg, stream);

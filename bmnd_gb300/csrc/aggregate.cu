@@ -349,6 +349,21 @@ AggregationLayout aggregation_layout(const BmndStageParams& sp, int64_t n_refs) 
     return L;
 }
 
+int32_t launch_exclusive_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* block_sums,
+                              cudaStream_t stream) {
+    const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
+    if (nb > 0) {
+        scan_block_kernel<<<static_cast<unsigned>(nb), kScanBlock, 0, stream>>>(in, n, out, block_sums);
+        BMND_LAUNCH_CHECK("scan_block_kernel");
+    }
+    scan_sums_kernel<<<1, kScanBlock, 0, stream>>>(block_sums, nb, block_sums + nb);
+    BMND_LAUNCH_CHECK("scan_sums_kernel");
+    scan_add_kernel<<<static_cast<unsigned>((n + 1 + 255) / 256), 256, 0, stream>>>(out, n, block_sums,
+                                                                                  block_sums + nb);
+    BMND_LAUNCH_CHECK("scan_add_kernel");
+    return BMND_OK;
+}
+
 int32_t launch_entry_index(const BmndStageParams& sp, const int32_t* sel, const int32_t* count, int64_t n_refs,
                            char* base, const AggregationLayout& L, cudaStream_t stream) {
     int32_t* start = reinterpret_cast<int32_t*>(base + L.o_start);
@@ -364,13 +379,7 @@ int32_t launch_entry_index(const BmndStageParams& sp, const int32_t* sel, const 
     entry_count_kernel<<<static_cast<unsigned>(grid_for(total, 256)), 256, 0, stream>>>(sel, count, n_refs,
                                                                                        sp.max_stack, cursor);
     BMND_LAUNCH_CHECK("entry_count_kernel");
-    const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
-    scan_block_kernel<<<static_cast<unsigned>(nb), kScanBlock, 0, stream>>>(cursor, n, start, sums);
-    BMND_LAUNCH_CHECK("scan_block_kernel");
-    scan_sums_kernel<<<1, kScanBlock, 0, stream>>>(sums, nb, sums + nb);
-    BMND_LAUNCH_CHECK("scan_sums_kernel");
-    scan_add_kernel<<<static_cast<unsigned>((n + 1 + 255) / 256), 256, 0, stream>>>(start, n, sums, sums + nb);
-    BMND_LAUNCH_CHECK("scan_add_kernel");
+    if (int32_t rc = launch_exclusive_scan(cursor, n, start, sums, stream)) return rc;
     BMND_CUDA_TRY(cudaMemsetAsync(cursor, 0, 4ull * static_cast<uint64_t>(n), stream));
     entry_fill_kernel<<<static_cast<unsigned>(grid_for(total, 256)), 256, 0, stream>>>(sel, count, n_refs,
                                                                                       sp.max_stack, start, cursor,

@@ -78,6 +78,8 @@ struct MatchArgs {
     int32_t no_alloc;  // 1: no stream-ordered scratch (approx mode then runs the bounded form)
     float* aux_ws;          // caller workspace for the approximate form's per-voxel arrays, or null
     int64_t aux_ws_floats;  // its size in floats
+    char* ssd_ws;           // caller workspace for the tensor-core SSD matching, or null
+    uint64_t ssd_ws_bytes;
     // subsampled mode: prescreen on the patch's even sub-lattice (box sums in
     // boxb_sub), then the screening form for the presel smallest
     int32_t sub;
@@ -466,6 +468,194 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
             for (int t = n; t < K; ++t) row[t] = -1;
             a.count[r] = n;
             a.accepted[r] = total_accepted;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// SSD matching on the tensor cores: selection with exact rescoring
+//
+// ssd_screen_tc_kernel (ssdtc.cu) writes, for every reference, the screening
+// distance d~ = |a|^2 + |b|^2 - 2 a.b of every window candidate, the cross
+// term from three BF16 tcgen05 products (hi/lo splits of a and b, FP32
+// accumulation).  Its error, with the reference's float32 per-term SSD, the
+// float32 norms and the rounding of the bounds below, stays under
+// 2^-10 (|a|^2 + |b|^2) (a worst-case analysis, every tensor-core addition
+// rounding with up to 17 terms, gives 2^-12.5; the rest is margin),
+// so the exact distance of candidate c lies in [lo_c, hi_c] = d~_c -+ that.
+// This kernel, one warp per reference (the exact kernel's layout):
+//   pass 1: counts the certainly accepted candidates (hi < threshold) and finds
+//           V, the K-th smallest (hi, lin) among them;
+//   pass 2: rescores exactly, in float32 per term in patch order (the exact
+//           kernel's arithmetic), every candidate that may be accepted and
+//           may reach the top K (lo < threshold and lo <= V) or whose accept
+//           decision is open (lo < threshold <= hi), and keeps the top K by
+//           (exact key, lin).
+// No other candidate can change the match set or the accepted count, so both
+// equal the exact kernel's bit for bit.  A reference with fewer than
+// min(min, max) certain accepts may need the best rejected candidates: it is
+// marked (count = -1) and redone by the exact kernel.
+// ---------------------------------------------------------------------------
+constexpr float kSsdBoundRel = 9.765625e-4f;  // 2^-10
+constexpr float kSsdBoundAbs = 1e-30f;         // products flushed to zero at the bottom of the range
+
+__global__ void __launch_bounds__(kWarps * 32) ssd_select_kernel(MatchArgs a, const float* __restrict__ dtil,
+                                                                 const float* __restrict__ norms, int64_t wmax,
+                                                                 const int* __restrict__ screen_err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int P = a.P;
+    const int K = a.max_m;
+    const int R = a.required;
+    const int list_rows = K + R;
+    uint64_t* lists = reinterpret_cast<uint64_t*>(smem_raw) +
+                      static_cast<size_t>(warp) * (list_rows * 32 + list_rows);
+    uint64_t* my_acc = lists + lane;
+    uint64_t* merged = lists + list_rows * 32;
+    int32_t* poff_s = reinterpret_cast<int32_t*>(reinterpret_cast<uint64_t*>(smem_raw) +
+                                                 static_cast<size_t>(kWarps) * (list_rows * 32 + list_rows));
+    float* ref_s = reinterpret_cast<float*>(poff_s + P) + static_cast<size_t>(warp) * P;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        int rem = i;
+        int64_t off = 0;
+        for (int d = a.ndim - 1; d >= 0; --d) {
+            off += static_cast<int64_t>(rem % a.block[d]) * a.vstride[d];
+            rem /= a.block[d];
+        }
+        poff_s[i] = static_cast<int32_t>(off);
+    }
+    __syncthreads();
+    const bool screened = *screen_err == 0;  // a screening that stopped early settles nothing
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * kWarps;
+    for (int64_t r = static_cast<int64_t>(blockIdx.x) * kWarps + warp; r < a.n_refs; r += stride) {
+        if (!screened) {
+            if (lane == 0) a.count[r] = -1;
+            continue;
+        }
+        int lo[BMND_MAX_DIMS] = {0, 0, 0}, ext[BMND_MAX_DIMS] = {1, 1, 1};
+        float inv_ext[BMND_MAX_DIMS] = {1.0f, 1.0f, 1.0f};
+        int64_t center_lin = 0, center_origin = 0, window = 1;
+#pragma unroll
+        for (int d = 0; d < BMND_MAX_DIMS; ++d) {
+            if (d < a.ndim) {
+                const int cd = a.refs[r * a.ndim + d];
+                center_lin = center_lin * a.counts[d] + cd;
+                center_origin += static_cast<int64_t>(cd) * a.grid_stride[d];
+                const int l = max(cd - a.radius[d], 0);
+                const int h = min(cd + a.radius[d], a.counts[d] - 1);
+                lo[d] = l;
+                ext[d] = h - l + 1;
+                inv_ext[d] = 1.0f / static_cast<float>(ext[d]);
+                window *= ext[d];
+            }
+        }
+        const bool small_window = window < (int64_t(1) << 21);
+        __syncwarp();
+        for (int p = lane; p < P; p += 32) ref_s[p] = __ldg(a.src + center_origin + poff_s[p]);
+        __syncwarp();
+        const float thr = a.thresholds ? a.thresholds[r] : (a.thr_dev ? *a.thr_dev : a.scalar_threshold);
+        const float na = __ldg(norms + center_origin);
+        const float* row = dtil + r * wmax;
+        // the bounds of candidate c, with the noise-bias correction of its offset
+        auto bounds = [&](int64_t c, int64_t origin, float& blo, float& bhi) {
+            const float del = fmaf(kSsdBoundRel, na + __ldg(norms + origin), kSsdBoundAbs);
+            const float dv = __ldg(row + c);
+            blo = dv - del;
+            bhi = dv + del;
+            if (a.noise_ssd) {
+                int64_t rem = c, gidx = 0, mul = 1;
+#pragma unroll
+                for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                    if (d < a.ndim) {
+                        const int cd = lo[d] + static_cast<int>(rem % ext[d]);
+                        rem /= ext[d];
+                        gidx += (cd - a.refs[r * a.ndim + d] + a.radius[d]) * mul;
+                        mul *= 2 * a.radius[d] + 1;
+                    }
+                }
+                const float g = mul_rn(a.gamma, __ldg(a.noise_ssd + gidx));
+                blo = sub_rn(blo, g);  // rounding is monotone: the bounds stay bounds
+                bhi = sub_rn(bhi, g);
+            }
+        };
+        // pass 1: certain accepts and the K-th smallest upper bound among them
+        int acc_size = 0, n_cert = 0;
+        for (int64_t c = lane; c < window; c += 32) {
+            int64_t lin;
+            const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
+            float blo, bhi;
+            bounds(c, origin, blo, bhi);
+            if (bhi < thr) {
+                ++n_cert;
+                acc_size = list_insert(my_acc, acc_size, K, composite_key(bhi, static_cast<int32_t>(lin)));
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) n_cert += __shfl_xor_sync(0xffffffffu, n_cert, o);
+        const int n_top = warp_merge(my_acc, acc_size, K, merged, lane);
+        __syncwarp();
+        if (n_cert < R) {
+            if (lane == 0) a.count[r] = -1;  // may need rejected candidates: the exact kernel redoes it
+            __syncwarp();
+            continue;
+        }
+        const float vkey = n_top >= K ? ordered_float(static_cast<uint32_t>(merged[K - 1] >> 32)) : thr;
+        __syncwarp();
+        // pass 2: exact rescoring of every candidate that can matter
+        acc_size = 0;
+        int acc_open = 0;
+        for (int64_t c = lane; c < window; c += 32) {
+            int64_t lin;
+            const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
+            float blo, bhi;
+            bounds(c, origin, blo, bhi);
+            const bool certain = bhi < thr;
+            if (!(blo < thr) || (certain && blo > vkey)) continue;
+            float dist = patch_distance<BMND_DIST_SSD>(ref_s, a.src, origin, poff_s, P, 1.0f);
+            if (a.noise_ssd) {
+                int64_t rem = c, gidx = 0, mul = 1;
+#pragma unroll
+                for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                    if (d < a.ndim) {
+                        const int cd = lo[d] + static_cast<int>(rem % ext[d]);
+                        rem /= ext[d];
+                        gidx += (cd - a.refs[r * a.ndim + d] + a.radius[d]) * mul;
+                        mul *= 2 * a.radius[d] + 1;
+                    }
+                }
+                dist = sub_rn(dist, mul_rn(a.gamma, __ldg(a.noise_ssd + gidx)));
+            }
+            if (dist < thr) {
+                if (!certain) ++acc_open;
+                acc_size = list_insert(my_acc, acc_size, K, composite_key(dist, static_cast<int32_t>(lin)));
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc_open += __shfl_xor_sync(0xffffffffu, acc_open, o);
+        const int n_acc = warp_merge(my_acc, acc_size, K, merged, lane);
+        __syncwarp();
+        if (lane == 0) {
+            int32_t* out_row = a.sel + r * K;
+            int n = 0;
+            out_row[n++] = static_cast<int32_t>(center_lin);
+            for (int t = 0; t < n_acc && n < K; ++t) {
+                const int32_t l = static_cast<int32_t>(merged[t] & 0xffffffffu);
+                if (l < 0 || l == center_lin) continue;
+                out_row[n++] = l;
+            }
+            if (a.pow2 && n > 0) {
+                int target = 1;
+                while ((target << 1) <= n) target <<= 1;
+                if (a.min_m > target) target = a.min_m;
+                if (target < n) n = target;
+            }
+            for (int t = n; t < K; ++t) out_row[t] = -1;
+            a.count[r] = n;
+            a.accepted[r] = n_cert + acc_open;
         }
         __syncwarp();
     }
@@ -1590,8 +1780,78 @@ int32_t set_smem_limit(K kernel, size_t smem) {
 
 int32_t launch_exact(MatchArgs& a, int code, cudaStream_t stream);
 
+// whether a volume's SSD matching can run on the tensor cores
+bool ssd_tc_applies(const MatchArgs& a) {
+    return !a.table && !a.fixup && !a.poisson_bias && !a.null_moments && a.max_m <= 32 &&
+           ssd_screen_shape(a.ndim, a.block) && a.grid_stride[a.ndim - 1] == 1 && a.P <= 128;
+}
+
+// SSD matching with tensor-core screening (ssdtc.cu) and exact rescoring
+// (ssd_select_kernel); the references it cannot settle go to the exact kernel
+int32_t launch_ssd_tc(MatchArgs& a, cudaStream_t stream) {
+    const SsdScratchLayout L = ssd_scratch_layout(a.ndim, a.counts, a.block, a.radius, a.n_refs);
+    char* base = nullptr;
+    bool owned = false;
+    if (a.ssd_ws && a.ssd_ws_bytes >= L.bytes) {
+        base = a.ssd_ws;
+    } else if (!a.no_alloc) {
+        if (cudaMallocAsync(reinterpret_cast<void**>(&base), L.bytes, stream) == cudaSuccess) {
+            owned = true;
+        } else {
+            (void)cudaGetLastError();
+            base = nullptr;
+        }
+    }
+    if (!base) return launch_exact(a, BMND_DIST_SSD, stream);
+    auto release = [&]() {
+        if (owned) (void)cudaFreeAsync(base, stream);
+    };
+    SsdScreenArgs sa{};
+    sa.src = a.src;
+    sa.ndim = a.ndim;
+    int64_t nvox = 1;
+    for (int d = 0; d < 3; ++d) {
+        sa.counts[d] = d < a.ndim ? a.counts[d] : 1;
+        sa.radius[d] = d < a.ndim ? a.radius[d] : 0;
+        sa.block[d] = d < a.ndim ? a.block[d] : 1;
+        sa.vstride[d] = d < a.ndim ? a.grid_stride[d] : 0;
+        if (d < a.ndim) nvox *= a.counts[d] + a.block[d] - 1;
+    }
+    sa.refs = a.refs;
+    int32_t rc = launch_ssd_screen(sa, nvox, a.n_refs, base, L, stream);
+    if (rc) {
+        release();
+        return rc;
+    }
+    const int list_rows = a.max_m + a.required;
+    const size_t smem = static_cast<size_t>(kWarps) * (list_rows * 32 + list_rows) * 8 +
+                        static_cast<size_t>(a.P) * 4 + static_cast<size_t>(kWarps) * a.P * 4;
+    if ((rc = set_smem_limit(ssd_select_kernel, smem))) {
+        release();
+        return rc;
+    }
+    int64_t blocks = (a.n_refs + kWarps - 1) / kWarps;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    ssd_select_kernel<<<static_cast<unsigned>(blocks), kWarps * 32, smem, stream>>>(
+        a, reinterpret_cast<const float*>(base + L.o_rows), reinterpret_cast<const float*>(base + L.o_norms), L.wmax,
+        reinterpret_cast<const int*>(base + L.o_err));
+    note_launch();
+    if (const cudaError_t e = cudaGetLastError(); e != cudaSuccess) {
+        release();
+        return cuda_fail(e, "ssd_select_kernel");
+    }
+    release();
+    // references that may need rejected candidates: the exact kernel
+    MatchArgs fix = a;
+    fix.fixup = 1;
+    fix.use_table = 0;
+    fix.approx = 0;
+    return launch_exact(fix, BMND_DIST_SSD, stream);
+}
+
 int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     if (a.n_refs == 0) return BMND_OK;
+    if (code == BMND_DIST_SSD && precision == BMND_MATCH_FAST && ssd_tc_applies(a)) return launch_ssd_tc(a, stream);
     int64_t wmax = 1;
     for (int d = 0; d < a.ndim; ++d) wmax *= std::min<int64_t>(2 * a.radius[d] + 1, a.counts[d]);
     a.approx = precision == BMND_MATCH_APPROX || precision == BMND_MATCH_SUBSAMPLED;
@@ -1788,7 +2048,8 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
                                  int32_t* sel, int32_t* count, int32_t* accepted,
                                  cudaStream_t stream, const float* thr_dev, const float* noise_ssd,
                                  float gamma, bool allow_alloc, const double* null_moments, int null_max,
-                                 bool poisson_bias, float* aux_ws, int64_t aux_ws_floats) {
+                                 bool poisson_bias, float* aux_ws, int64_t aux_ws_floats, char* ssd_ws,
+                                 uint64_t ssd_ws_bytes) {
     int32_t rc = validate_match(mp);
     if (rc) return rc;
     if ((noise_ssd || poisson_bias) && mp.distance != BMND_DIST_SSD)
@@ -1809,6 +2070,8 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
     a.no_alloc = allow_alloc ? 0 : 1;
     a.aux_ws = aux_ws;
     a.aux_ws_floats = aux_ws_floats;
+    a.ssd_ws = ssd_ws;
+    a.ssd_ws_bytes = ssd_ws_bytes;
     a.null_moments = null_moments;
     a.null_max = null_max;
     if (null_moments && mp.distance == BMND_DIST_SSD)
@@ -1841,6 +2104,13 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
     a.count = count;
     a.accepted = accepted;
     return launch(a, mp.distance, mp.precision, stream);
+}
+
+uint64_t ssd_tc_scratch_bytes(const BmndMatchParams& mp, const int32_t* block, int64_t n_refs, bool poisson_bias) {
+    if (mp.distance != BMND_DIST_SSD || mp.precision != BMND_MATCH_FAST || poisson_bias || mp.max_matches > 32 ||
+        !ssd_screen_shape(mp.ndim, block))
+        return 0;
+    return ssd_scratch_layout(mp.ndim, mp.counts, block, mp.search_radius, n_refs).bytes;
 }
 
 int64_t approx_scratch_floats(const BmndMatchParams& mp, const int32_t* shape, const int32_t* block) {

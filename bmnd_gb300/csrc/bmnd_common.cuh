@@ -91,6 +91,11 @@ __host__ __device__ inline uint32_t order_bits(float f) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
+// inverse of order_bits
+__device__ __forceinline__ float ordered_float(uint32_t b) {
+    return __uint_as_float((b & 0x80000000u) ? (b & 0x7fffffffu) : ~b);
+}
+
 __host__ __device__ inline uint64_t composite_key(float key, int32_t lin) {
     return (static_cast<uint64_t>(order_bits(key)) << 32) | static_cast<uint32_t>(lin);
 }
@@ -198,7 +203,10 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
                                  const float* thr_dev = nullptr, const float* noise_ssd = nullptr,
                                  float gamma = 0.0f, bool allow_alloc = true,
                                  const double* null_moments = nullptr, int null_max = 0,
-                                 bool poisson_bias = false, float* aux_ws = nullptr, int64_t aux_ws_floats = 0);
+                                 bool poisson_bias = false, float* aux_ws = nullptr, int64_t aux_ws_floats = 0,
+                                 char* ssd_ws = nullptr, uint64_t ssd_ws_bytes = 0);
+// bytes of workspace the tensor-core SSD matching of a volume needs (0: it does not apply)
+uint64_t ssd_tc_scratch_bytes(const BmndMatchParams& mp, const int32_t* block, int64_t n_refs, bool poisson_bias);
 // floats of workspace the approximate screening form of a volume needs (0: none)
 int64_t approx_scratch_floats(const BmndMatchParams& mp, const int32_t* shape, const int32_t* block);
 int32_t launch_reference_thresholds(const float* volume, const int32_t* refs, int64_t n_refs, int ndim,
@@ -223,6 +231,40 @@ struct GroupProbe {
     float* weights;  // aggregation weight of every member
     float* filt;     // inverse transform of the shrunk coefficients
 };
+// exclusive prefix sum of n ints into out[0..n] (out[n] = the total);
+// block_sums holds (n + 1023) / 1024 + 1 ints of scratch
+int32_t launch_exclusive_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* block_sums,
+                              cudaStream_t stream);
+
+// SSD matching on the tensor cores (ssdtc.cu): the screening distances of
+// every reference's window candidates, in window order, one row of wmax
+// floats per reference
+struct SsdScreenArgs {
+    const float* src;     // matched volume
+    const float* norms;   // per patch origin: sum of squares of its patch (written by the launch)
+    int32_t ndim;
+    int32_t counts[3], radius[3], block[3];
+    int64_t vstride[3];   // voxel offset of one patch-grid step per axis
+    const int32_t* refs;  // n_refs x ndim reference positions
+    const int32_t* perm;  // references sorted by spatial tile
+    const int32_t* tile_start;
+    int32_t n_tiles;
+    int32_t tile_edge[3], tiles[3];
+    float* out;           // n_refs x wmax screening distances
+    int64_t wmax;
+    int* err;             // set when a bounded wait ran out
+};
+struct SsdScratchLayout {
+    int64_t wmax, n_tiles;
+    uint64_t o_norms, o_rows, o_start, o_cursor, o_sums, o_perm, o_err;
+    uint64_t bytes;
+};
+bool ssd_screen_shape(int ndim, const int32_t* block);
+SsdScratchLayout ssd_scratch_layout(int ndim, const int32_t* counts, const int32_t* block, const int32_t* radius,
+                                    int64_t n_refs);
+int32_t launch_ssd_screen(SsdScreenArgs a, int64_t nvox, int64_t n_refs, char* base, const SsdScratchLayout& L,
+                          cudaStream_t stream);
+
 // deterministic aggregation (aggregate.cu): byte offsets of its arrays in a
 // 256-byte aligned region, for a stage with n_refs groups
 struct AggregationLayout {

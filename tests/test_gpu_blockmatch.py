@@ -463,3 +463,78 @@ def test_count_tabulated_volume_matching_equals_patch_table(cuda, native, shape,
     np.testing.assert_array_equal(vg[1], pg[1])
     np.testing.assert_array_equal(vg[2], pg[2])
     np.testing.assert_array_equal(vg[0], pg[0])
+
+
+def _match_volume_ssd(cuda, native, vol, block, radius, max_m, min_m, thr, precision, noise=None, gamma=0.0):
+    """SSD matching of a volume (every second position as reference), plain or
+    with the noise-bias table ``noise`` over the search offsets."""
+    from bmnd_gb300 import _abi
+
+    shape = vol.shape
+    counts = tuple(s - b + 1 for s, b in zip(shape, block))
+    refs = np.stack(np.meshgrid(*[np.arange(0, c, 2) for c in counts], indexing="ij"), -1)
+    refs = refs.reshape(-1, len(shape)).astype(np.int32)
+    dev = cuda.device("cuda:0")
+    vt = cuda.from_numpy(np.ascontiguousarray(vol, dtype=np.float32)).to(dev)
+    rt = cuda.from_numpy(refs).to(dev)
+    n = refs.shape[0]
+    tt = cuda.full((n,), float(np.float32(thr)), device=dev)
+    sel = cuda.full((n, max_m), -7, dtype=cuda.int32, device=dev)
+    cnt = cuda.full((n,), -7, dtype=cuda.int32, device=dev)
+    acc = cuda.full((n,), -7, dtype=cuda.int32, device=dev)
+    p = _mp(counts, radius, max_m, min_m, SSD, stabilize=False)
+    p.precision = precision
+    sh = (ctypes.c_int32 * len(shape))(*shape)
+    bl = (ctypes.c_int32 * len(shape))(*block)
+    if noise is None:
+        _abi.check(native.bmnd_blockmatch_volume(ctypes.byref(p), vt.data_ptr(), sh, bl, rt.data_ptr(), n,
+                                                 tt.data_ptr(), sel.data_ptr(), cnt.data_ptr(), acc.data_ptr(), 0))
+    else:
+        nt = cuda.from_numpy(np.ascontiguousarray(noise, dtype=np.float32)).to(dev)
+        _abi.check(native.bmnd_blockmatch_volume_biased(ctypes.byref(p), vt.data_ptr(), sh, bl, rt.data_ptr(), n,
+                                                        tt.data_ptr(), nt.data_ptr(), float(gamma), sel.data_ptr(),
+                                                        cnt.data_ptr(), acc.data_ptr(), 0))
+    cuda.cuda.synchronize()
+    return sel.cpu().numpy(), cnt.cpu().numpy(), acc.cpu().numpy()
+
+
+@pytest.mark.parametrize("shape,block,radius,max_m,thr_frac,kind", [
+    ((72, 80), (8, 8), (19, 19), 32, 0.4, "smooth"),
+    ((64, 72), (8, 8), (19, 19), 16, 3.0, "noise"),
+    ((60, 64), (8, 8), (19, 19), 32, 0.02, "flat"),
+    ((30, 34, 38), (5, 5, 5), (7, 7, 7), 32, 0.8, "smooth"),
+    ((32, 30, 36), (4, 4, 4), (7, 7, 7), 16, 3.0, "noise"),
+    ((26, 28, 30), (5, 5, 5), (7, 7, 7), 32, 0.8, "large"),
+])
+@pytest.mark.parametrize("bias", [False, True])
+def test_tensor_core_ssd_matching_equals_exact(cuda, native, shape, block, radius, max_m, thr_frac, kind, bias):
+    """SSD matching with the BF16 tensor-core screening and exact float32
+    rescoring (precision fast) gives the exact kernel's match tables and
+    accepted counts bit for bit, with and without the noise-bias correction."""
+    from bmnd_gb300 import _abi
+
+    rng = np.random.default_rng(abs(hash((shape, kind, bias))) % 2**32)
+    grids = np.meshgrid(*[np.linspace(0, 1, s) for s in shape], indexing="ij")
+    smooth = 5.0 + 20.0 * np.sin(3 * grids[0]) ** 2 + 10.0 * grids[-1]
+    if kind == "smooth":
+        vol = smooth + rng.normal(0, 1.0, size=shape)
+    elif kind == "noise":
+        vol = rng.normal(10.0, 3.0, size=shape)
+    elif kind == "large":
+        vol = 2000.0 + 50.0 * smooth + rng.normal(0, 5.0, size=shape)
+    else:
+        vol = np.full(shape, 7.25) + (rng.random(shape) < 0.02) * 3.0
+    vol = vol.astype(np.float32)
+    span = float(vol.max() - vol.min())
+    P = int(np.prod(block))
+    thr = thr_frac * P * (span / 8.0) ** 2
+    noise = gamma = None
+    if bias:
+        noise = rng.uniform(0.0, 2.0, size=tuple(2 * r + 1 for r in radius)).reshape(-1) * P
+        gamma = 1.5
+    args = (cuda, native, vol, block, radius, max_m, 2, thr)
+    ex = _match_volume_ssd(*args, _abi.MATCH_EXACT, noise=noise, gamma=gamma or 0.0)
+    tc = _match_volume_ssd(*args, _abi.MATCH_FAST, noise=noise, gamma=gamma or 0.0)
+    np.testing.assert_array_equal(tc[1], ex[1])
+    np.testing.assert_array_equal(tc[2], ex[2])
+    np.testing.assert_array_equal(tc[0], ex[0])
