@@ -11,7 +11,7 @@ import ctypes
 import os
 import threading
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_DIMS = 3
 MAX_EDGE = 8
 MAX_PATCH = 512
@@ -131,6 +131,8 @@ class StageParams(ctypes.Structure):
         ("policy_power", ctypes.c_double),
         ("weight_group_scope", _I32),
         ("fast_group_transform", _I32),
+        ("exact_risk_weights", _I32),
+        ("exact_source_variance", ctypes.c_float),
     ]
 
 
@@ -208,6 +210,7 @@ SIGNATURES = {
     "bmnd_pilotnet_pack": (_I32, [_PNP, _VP, _VP, _U64]),
     "bmnd_pilotnet_status": (_I32, [_PNP, _VP, _U64]),
     "bmnd_pilotnet_set_conv_engine": (_I32, [_I32]),
+    "bmnd_pilotnet_set_wait_probe": (_I32, [ctypes.c_uint64]),
     "bmnd_pilotnet_get_conv_engine": (_I32, [_I32P]),
     "bmnd_pilotnet_forward": (_I32, [_PNP, _VP, _VP, _VP, _VP, _VP, _U64, _U64]),
     "bmnd_pilotnet_gradient": (_I32, [_PNP, _VP, _VP, _VP, _VP, _VP, _VP, _U64, _U64]),

@@ -248,7 +248,8 @@ def gaussian_tables(model: gaussian.GaussianModel, profile, shape, resolved, dev
         block = tuple(int(b) for b in getattr(profile, f"{stage}_block_size"))
         maps = gaussian.covariance_maps(model, block, plan.spatial_forward(profile, len(shape), stage))
         cov = torch.from_numpy(np.ascontiguousarray(maps.reshape(maps.shape[0], -1).T)).to(device)
-        entry = {"cov": cov, "domain": model.domain, "ssd": None, "gamma": 0.0}
+        entry = {"cov": cov, "domain": model.domain, "ssd": None, "gamma": 0.0,
+                 "white_variance": gaussian.white_variance(model)}
         if stage == "ht" and resolved.blockmatch_distance is BlockMatchDistance.SSD:
             gamma = 0.0 if resolved.conventional_nf else float(profile.gamma)
             if gamma != 0.0:

@@ -189,6 +189,18 @@ int32_t validate_stage(const BmndStageParams& sp) {
         return fail(BMND_ERR_INVALID_ARG, "gamma must be finite and non-negative");
     if (sp.distance == BMND_DIST_SSD && (!(sp.ssd_threshold >= 0.0) || !std::isfinite(sp.ssd_threshold)))
         return fail(BMND_ERR_INVALID_ARG, "SSD threshold multiplier must be finite and >= 0");
+    if (sp.exact_risk_weights != 0 && sp.exact_risk_weights != 1)
+        return fail(BMND_ERR_INVALID_ARG, "exact_risk_weights must be 0 or 1");
+    if (sp.exact_risk_weights) {
+        if (!sp.weight_group_scope || !sp.windowed_synthesis || sp.variance_k <= 0 ||
+            sp.weight_model == BMND_WEIGHT_CLASSIC)
+            return fail(BMND_ERR_INVALID_ARG,
+                        "exact risk weights need group scope, windowed synthesis, variance or risk weights and k > 0");
+        if (P > 128) return fail(BMND_ERR_UNSUPPORTED, "exact risk weights need patches of at most 128 voxels");
+        if (sp.noise_model == BMND_NOISE_GAUSSIAN &&
+            (!(sp.exact_source_variance >= 0.0f) || !std::isfinite(sp.exact_source_variance)))
+            return fail(BMND_ERR_INVALID_ARG, "exact_source_variance must be finite and >= 0");
+    }
     if (group_filter_smem_bytes(sp) > 227 * 1024)
         return fail(BMND_ERR_UNSUPPORTED, "profile needs more than 227 KB of shared memory per group");
     return BMND_OK;
@@ -243,7 +255,8 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
     uint64_t o_cnt = take(4ull * n_refs);
     uint64_t o_acc = take(4ull * n_refs);
     const uint64_t P = static_cast<uint64_t>(patch_volume(sp));
-    uint64_t o_st = take(4ull * P * static_cast<uint64_t>(kron_stride(static_cast<int>(P))));
+    // the Kronecker table, then the risk metric SM (exact risk weights)
+    uint64_t o_st = take(8ull * P * static_cast<uint64_t>(kron_stride(static_cast<int>(P))));
     uint64_t o_mm = take(16);
     uint64_t o_tr = take(sp.match_policy == BMND_POLICY_REFERENCE_FINITE_COUNT ? 4ull * n_refs : 16);
     const BmndMatchParams mp = match_params_of(sp);
@@ -640,8 +653,8 @@ int32_t bmnd_group_probe_workspace_bytes(const BmndStageParams* params, uint64_t
     if (!params || !out_bytes) return fail(BMND_ERR_INVALID_ARG, "null argument");
     if (int32_t rc = validate_stage(*params)) return rc;
     const uint64_t P = static_cast<uint64_t>(patch_volume(*params));
-    // the Kronecker table, then the status word
-    *out_bytes = align256(4ull * P * static_cast<uint64_t>(kron_stride(static_cast<int>(P)))) + 256;
+    // the Kronecker table and the risk metric, then the status word
+    *out_bytes = align256(8ull * P * static_cast<uint64_t>(kron_stride(static_cast<int>(P)))) + 256;
     return BMND_OK;
 }
 

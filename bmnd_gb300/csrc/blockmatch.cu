@@ -477,12 +477,18 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
 // SSD matching on the tensor cores: selection with exact rescoring
 //
 // ssd_screen_tc_kernel (ssdtc.cu) writes, for every reference, the screening
-// distance d~ = |a|^2 + |b|^2 - 2 a.b of every window candidate, the cross
-// term from three BF16 tcgen05 products (hi/lo splits of a and b, FP32
-// accumulation).  Its error, with the reference's float32 per-term SSD, the
-// float32 norms and the rounding of the bounds below, stays under
-// 2^-10 (|a|^2 + |b|^2) (a worst-case analysis, every tensor-core addition
-// rounding with up to 17 terms, gives 2^-12.5; the rest is margin),
+// distance d~ = |a'|^2 + |b'|^2 - 2 a'.b' of every window candidate, where
+// a' = a - mu and b' = b - mu are the patches centred on their tile's mean mu
+// and the cross term comes from three BF16 tcgen05 products (hi/lo splits of
+// a' and b', FP32 accumulation).  Its error, with the reference's float32
+// per-term SSD and the rounding of the bounds below, stays under
+//   2^-10 (|a'|^2 + |b'|^2)              the products and their sums (a
+//       worst-case analysis, every tensor-core addition rounding with up to
+//       17 terms, gives 2^-12.5; the rest is margin), plus
+//   2^-14 (|a|^2 + |b|^2 + 2 P mu^2)     the centred norms, formed in float32
+//       from the sums of squares and the sums of the raw patches (each of
+//       those sums is off by at most P 2^-24 of |a|^2 + P mu^2 for P <= 128,
+//       the centring expression by 3 roundings of the same size),
 // so the exact distance of candidate c lies in [lo_c, hi_c] = d~_c -+ that.
 // This kernel, one warp per reference (the exact kernel's layout):
 //   pass 1: counts the certainly accepted candidates (hi < threshold) and finds
@@ -498,10 +504,13 @@ __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
 // marked (count = -1) and redone by the exact kernel.
 // ---------------------------------------------------------------------------
 constexpr float kSsdBoundRel = 9.765625e-4f;  // 2^-10
+constexpr float kSsdBoundCancel = 6.103515625e-5f;  // 2^-14
 constexpr float kSsdBoundAbs = 1e-30f;         // products flushed to zero at the bottom of the range
 
 __global__ void __launch_bounds__(kWarps * 32) ssd_select_kernel(MatchArgs a, const float* __restrict__ dtil,
-                                                                 const float* __restrict__ norms, int64_t wmax,
+                                                                 const float* __restrict__ norms,
+                                                                 const float* __restrict__ sums,
+                                                                 const float* __restrict__ ref_mu, int64_t wmax,
                                                                  const int* __restrict__ screen_err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5;
@@ -556,11 +565,18 @@ __global__ void __launch_bounds__(kWarps * 32) ssd_select_kernel(MatchArgs a, co
         for (int p = lane; p < P; p += 32) ref_s[p] = __ldg(a.src + center_origin + poff_s[p]);
         __syncwarp();
         const float thr = a.thresholds ? a.thresholds[r] : (a.thr_dev ? *a.thr_dev : a.scalar_threshold);
-        const float na = __ldg(norms + center_origin);
+        const float mu = __ldg(ref_mu + r);
+        const float na2 = __ldg(norms + center_origin);
+        const float na = centred_norm(na2, __ldg(sums + center_origin), mu, P);
+        const float pmu2 = 2.0f * static_cast<float>(P) * mu * mu;
         const float* row = dtil + r * wmax;
-        // the bounds of candidate c, with the noise-bias correction of its offset
+        // the bounds of candidate c, with the noise-bias correction of its offset:
+        // the products' error scales with the centred norms, the cancellation in
+        // the centred norms with the raw sums of squares
         auto bounds = [&](int64_t c, int64_t origin, float& blo, float& bhi) {
-            const float del = fmaf(kSsdBoundRel, na + __ldg(norms + origin), kSsdBoundAbs);
+            const float nb2 = __ldg(norms + origin);
+            const float nb = centred_norm(nb2, __ldg(sums + origin), mu, P);
+            const float del = fmaf(kSsdBoundRel, na + nb, fmaf(kSsdBoundCancel, na2 + nb2 + pmu2, kSsdBoundAbs));
             const float dv = __ldg(row + c);
             blo = dv - del;
             bhi = dv + del;
@@ -1833,7 +1849,8 @@ int32_t launch_ssd_tc(MatchArgs& a, cudaStream_t stream) {
     int64_t blocks = (a.n_refs + kWarps - 1) / kWarps;
     if (blocks > 152 * 16) blocks = 152 * 16;
     ssd_select_kernel<<<static_cast<unsigned>(blocks), kWarps * 32, smem, stream>>>(
-        a, reinterpret_cast<const float*>(base + L.o_rows), reinterpret_cast<const float*>(base + L.o_norms), L.wmax,
+        a, reinterpret_cast<const float*>(base + L.o_rows), reinterpret_cast<const float*>(base + L.o_norms),
+        reinterpret_cast<const float*>(base + L.o_psum), reinterpret_cast<const float*>(base + L.o_rmu), L.wmax,
         reinterpret_cast<const int*>(base + L.o_err));
     note_launch();
     if (const cudaError_t e = cudaGetLastError(); e != cudaSuccess) {

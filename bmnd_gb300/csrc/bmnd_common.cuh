@@ -205,6 +205,14 @@ int32_t launch_blockmatch_volume(const BmndMatchParams& mp, const float* volume,
                                  const double* null_moments = nullptr, int null_max = 0,
                                  bool poisson_bias = false, float* aux_ws = nullptr, int64_t aux_ws_floats = 0,
                                  char* ssd_ws = nullptr, uint64_t ssd_ws_bytes = 0);
+// squared norm of a patch centred on mu, from its sum of squares s2 and sum s1:
+// s2 - 2 mu s1 + P mu^2 (float32, clamped at zero); the screening and the
+// selection evaluate it with the same operations
+__device__ __forceinline__ float centred_norm(float s2, float s1, float mu, int P) {
+    const float v = __fadd_rn(__fsub_rn(s2, __fmul_rn(__fmul_rn(2.0f, mu), s1)),
+                              __fmul_rn(__fmul_rn(static_cast<float>(P), mu), mu));
+    return v > 0.0f ? v : 0.0f;
+}
 // bytes of workspace the tensor-core SSD matching of a volume needs (0: it does not apply)
 uint64_t ssd_tc_scratch_bytes(const BmndMatchParams& mp, const int32_t* block, int64_t n_refs, bool poisson_bias);
 // floats of workspace the approximate screening form of a volume needs (0: none)
@@ -242,6 +250,9 @@ int32_t launch_exclusive_scan(const int32_t* in, int64_t n, int32_t* out, int32_
 struct SsdScreenArgs {
     const float* src;     // matched volume
     const float* norms;   // per patch origin: sum of squares of its patch (written by the launch)
+    const float* sums;    // per patch origin: sum of its patch (written by the launch)
+    const float* mu;      // per tile: the mean the tile's patches are centred on (written by the launch)
+    float* ref_mu;        // per reference: the mean of its tile (written by the launch)
     int32_t ndim;
     int32_t counts[3], radius[3], block[3];
     int64_t vstride[3];   // voxel offset of one patch-grid step per axis
@@ -256,7 +267,7 @@ struct SsdScreenArgs {
 };
 struct SsdScratchLayout {
     int64_t wmax, n_tiles;
-    uint64_t o_norms, o_rows, o_start, o_cursor, o_sums, o_perm, o_err;
+    uint64_t o_norms, o_psum, o_mu, o_rmu, o_rows, o_start, o_cursor, o_sums, o_perm, o_err;
     uint64_t bytes;
 };
 bool ssd_screen_shape(int ndim, const int32_t* block);

@@ -19,7 +19,8 @@
 //      (bmndalgo.py:460-485, poisson.py:30-46) or the variance-scaled Poisson
 //      Wiener gain (wiener.py:24-95, bmndalgo.py:878-894);
 //   5. per-patch aggregation weights 1 / (sum_g Ginv[o,g]^2 plane_risk[g] +
-//      eps) (aggregationweights.py:213-259, :616-653);
+//      eps) (aggregationweights.py:213-259, :616-653), or one weight per group
+//      from its exact windowed-synthesis risk (wiener.py:638-822);
 //   6. inverse transform and weighted Kaiser-window scatter into float64
 //      numerator / denominator volumes (patchaggregation.py:170-199).
 //
@@ -42,10 +43,12 @@ constexpr int kThreads = 256;      // threads per group (CTA)
 // phase is done it holds the group buffers: S (noise sigma), X (noisy
 // coefficients) and R (pilot coefficients, Wiener) or V (attenuation, hard
 // thresholding).  Transforms run in place, so no scratch buffer is needed.
+// With exact risk weights the union-voxel lists are still needed after the
+// shrinkage, so they get a region of their own after the group buffers.
 struct Layout {
     // byte offsets into dynamic shared memory
     int64_t g, gt, fw, fi, fit, dir, win, mdiag, pos, shf, shl, sg, ex, lag, uni, s, x, r, v, grid, lval, lstart,
-        lent, scan, plane, wts, misc, total;
+        lent, scan, plane, wts, misc, risk, total;
 };
 
 struct FilterArgs {
@@ -112,6 +115,7 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     L.plane = take(8 * (nmax > 40 ? nmax : 40));  // also the mass phase's 8 warps x 5 sums
     L.wts = take(4 * nmax);
     L.misc = take(64);
+    L.risk = take(8 * (kThreads / 32 + 1));  // exact risk: per-warp partial sums, then the total
     // union region
     L.uni = off;
     const int64_t buf = round16(4 * np);
@@ -120,15 +124,18 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     L.r = L.x + buf;  // Wiener: pilot coefficients, then the attenuation
     L.v = L.r;        // hard thresholding: the attenuation
     const int64_t group_bytes = 3 * buf;
-    // union-voxel lists of the exact Poisson phase (none for Gaussian noise)
-    const int kl = gauss ? 0 : kmax;
+    // union-voxel lists of the exact phase (Poisson noise, or white Gaussian
+    // noise with exact risk weights), kept apart from the group buffers when
+    // the exact risk reads them after the shrinkage
+    const bool keep = sp.exact_risk_weights != 0;
+    const int kl = (gauss && !keep) ? 0 : kmax;
     const int64_t umax = kl > 0 ? (np < ucells ? np : ucells) : 0;
-    L.grid = L.uni;
+    L.grid = keep ? L.uni + group_bytes : L.uni;
     L.lval = L.grid + round16(kl > 0 ? 4 * ucells : 0);
     L.lstart = L.lval + round16(4 * umax);
     L.lent = L.lstart + round16(4 * (umax + 1));
-    const int64_t list_bytes = (L.lent + round16(kl > 0 ? 4 * np : 0)) - L.uni;
-    off = L.uni + (group_bytes > list_bytes ? group_bytes : list_bytes);
+    const int64_t list_end = L.lent + round16(kl > 0 ? 4 * np : 0);
+    off = keep ? list_end : L.uni + (group_bytes > list_end - L.uni ? group_bytes : list_end - L.uni);
     L.total = off;
     return L;
 }
@@ -649,6 +656,141 @@ __device__ void exact_planes_any(const float* __restrict__ lval, const int* __re
     else exact_planes<JR, 4>(lval, lstart, lent, U, GT, kpad, kk, st, P, EX);
 }
 
+// Exact noise risk of the first kk planes (wiener.py:638-711, :505-535; the
+// group metric Ginv^T Ginv of the orthonormal group transforms is the
+// identity, the reference's diagonal branch):
+//   risk = sum_u V_u sum_{g < kk} f_u[g]^T SM f_u[g],  f_u[g][j] = a[g][j] c_u[g][j],
+// c_u as in the exact variance and SM = S_inv^T diag(w^2) S_inv, row p at
+// sm + p * kron_stride(P).  Lane l holds coefficients j = JR l + r (P <= 32 JR:
+// one tile); (f SM)[j] = sum_p f[p] SM[p][j] takes f[p] from its lane by a
+// shuffle.  The voxel terms are float32, their sum over voxels float64.
+template <int JR, int NQ>
+__device__ double exact_risk_tile(const float* __restrict__ lval, const int* __restrict__ lstart,
+                                  const uint32_t* __restrict__ lent, int u_lo, int u_hi,
+                                  const float* __restrict__ GT, int kpad, int i0, int kk,
+                                  const float* __restrict__ st, const float* __restrict__ smt,
+                                  const float* __restrict__ att, int P) {
+    const int lane = threadIdx.x & 31;
+    const int stride = kron_stride(P);
+    const float* stl = st + JR * lane;
+    float gq[JR][NQ];
+#pragma unroll
+    for (int r = 0; r < JR; ++r)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const int j = JR * lane + r, i = i0 + q;
+            gq[r][q] = (j < P && i < kk) ? att[i * P + j] : 0.0f;
+        }
+    const float* gt0 = GT + i0;
+    double acc = 0.0;
+    for (int u = u_lo; u < u_hi; ++u) {
+        int e = lstart[u];
+        const int e1 = lstart[u + 1];
+        float c[JR][NQ];
+        {
+            const uint32_t ent = lent[e];
+            PlaneVec<NQ> gv;
+            gv.load(gt0 + (ent & 0xffu) * kpad);
+            KronVec<JR> sv;
+            sv.load(stl + (ent >> 8));
+#pragma unroll
+            for (int r = 0; r < JR; ++r)
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) c[r][q] = mul_rn(gv.v[q], sv.v[r]);
+        }
+        for (++e; e < e1; ++e) {
+            const uint32_t ent = lent[e];
+            PlaneVec<NQ> gv;
+            gv.load(gt0 + (ent & 0xffu) * kpad);
+            KronVec<JR> sv;
+            sv.load(stl + (ent >> 8));
+#pragma unroll
+            for (int r = 0; r < JR; ++r)
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) c[r][q] = fmaf(gv.v[q], sv.v[r], c[r][q]);
+        }
+        float f[JR][NQ], pr[JR][NQ];
+#pragma unroll
+        for (int r = 0; r < JR; ++r)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                f[r][q] = mul_rn(gq[r][q], c[r][q]);
+                pr[r][q] = 0.0f;
+            }
+        for (int sl = 0; sl < 32; ++sl) {
+#pragma unroll
+            for (int rr = 0; rr < JR; ++rr) {
+                const int p = sl * JR + rr;
+                if (p < P) {  // the same for every lane
+                    float fp[NQ];
+#pragma unroll
+                    for (int q = 0; q < NQ; ++q) fp[q] = __shfl_sync(0xffffffffu, f[rr][q], sl);
+                    KronVec<JR> mv;
+                    mv.load(smt + p * stride + JR * lane);
+#pragma unroll
+                    for (int r = 0; r < JR; ++r)
+#pragma unroll
+                        for (int q = 0; q < NQ; ++q) pr[r][q] = fmaf(fp[q], mv.v[r], pr[r][q]);
+                }
+            }
+        }
+        float t = 0.0f;
+#pragma unroll
+        for (int r = 0; r < JR; ++r)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) t = fmaf(f[r][q], pr[r][q], t);
+        acc = fma(static_cast<double>(lval[u]), static_cast<double>(t), acc);
+    }
+    return acc;
+}
+
+// the group's exact noise risk into *out (every thread returns after it is set):
+// warp w takes the voxels whose entry lists start in its share of all entries
+// (the exact variance's split); lanes, then warps, add in a fixed order
+template <int JR, int NQ>
+__device__ void exact_risk(const float* __restrict__ lval, const int* __restrict__ lstart,
+                           const uint32_t* __restrict__ lent, int U, const float* __restrict__ GT, int kpad,
+                           int kk, const float* __restrict__ st, const float* __restrict__ smt,
+                           const float* __restrict__ att, int P, double* __restrict__ part) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nw = blockDim.x >> 5;
+    const int E = lstart[U];
+    auto first_voxel = [&](int e) {
+        int lo = 0, hi = U;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (lstart[mid] < e) lo = mid + 1;
+            else hi = mid;
+        }
+        return lo;
+    };
+    const int u_lo = first_voxel(static_cast<int>(static_cast<int64_t>(E) * warp / nw));
+    const int u_hi = warp == nw - 1 ? U : first_voxel(static_cast<int>(static_cast<int64_t>(E) * (warp + 1) / nw));
+    double acc = 0.0;
+    for (int i0 = 0; i0 < kk; i0 += NQ)
+        acc += exact_risk_tile<JR, NQ>(lval, lstart, lent, u_lo, u_hi, GT, kpad, i0, kk, st, smt, att, P);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) part[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < nw; ++w) t += part[w];
+        part[nw] = t;
+    }
+    __syncthreads();
+}
+
+template <int JR>
+__device__ void exact_risk_any(const float* __restrict__ lval, const int* __restrict__ lstart,
+                               const uint32_t* __restrict__ lent, int U, const float* __restrict__ GT, int kpad,
+                               int kk, const float* __restrict__ st, const float* __restrict__ smt,
+                               const float* __restrict__ att, int P, double* __restrict__ part) {
+    if (kk == 1) exact_risk<JR, 1>(lval, lstart, lent, U, GT, kpad, kk, st, smt, att, P, part);
+    else if (kk == 2) exact_risk<JR, 2>(lval, lstart, lent, U, GT, kpad, kk, st, smt, att, P, part);
+    else exact_risk<JR, 4>(lval, lstart, lent, U, GT, kpad, kk, st, smt, att, P, part);
+}
+
 template <int ND, int B0, int B1, int B2, int NT>
 __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) group_filter_kernel(FilterArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -762,7 +904,8 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
     const bool need_approx = (k <= 0) || (kk < n);
 
     const bool gauss = sp.noise_model == BMND_NOISE_GAUSSIAN;
-    if (!gauss && kk > 0) {
+    const bool exact_risk = sp.exact_risk_weights != 0 && kk > 0;
+    if ((!gauss || exact_risk) && kk > 0) {
         // the exact phase's occupancy grid covers a union box of at most
         // ucells_cap cells: members within the search window of their reference
         // always fit; a group spread wider is skipped and reported
@@ -836,8 +979,11 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
         __syncthreads();
     }
 
-    // ---- exact overlap-aware sigma of the first kk planes ----
-    if (!gauss && kk > 0) {
+    // ---- union voxels and the exact overlap-aware sigma of the first kk planes ----
+    // (with exact risk weights under white Gaussian noise: the union voxels
+    // alone, each with the noise variance, variance.py:1451-1496)
+    int U = 0;
+    if ((!gauss || exact_risk) && kk > 0) {
         int ush[BMND_MAX_DIMS] = {1, 1, 1}, org[BMND_MAX_DIMS] = {0, 0, 0};
         int ucells = 1;
         for (int d = 0; d < geo.nd(); ++d) {
@@ -937,11 +1083,15 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
                 }
             }
         }
-        const int U = scan[blockDim.x].x;
+        U = scan[blockDim.x].x;
         if (tid == 0) lstart[U] = scan[blockDim.x].y;
         __syncthreads();
         // variance of every union voxel, all loads in flight together
         for (int u = tid; u < U; u += blockDim.x) {
+            if (gauss) {
+                lval[u] = sp.exact_source_variance;
+                continue;
+            }
             int rem = reinterpret_cast<const int*>(lval)[u];
             int64_t vox = 0;
 #pragma unroll
@@ -954,7 +1104,9 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
             lval[u] = variance_of(__ldg(varsrc + vox), scale_f, floor_f);
         }
         __syncthreads();
-        if constexpr (ND > 0) {
+        if (gauss) {
+            // sigma comes from the covariance maps
+        } else if constexpr (ND > 0) {
             exact_planes_any<kron_jr(B0 * B1 * B2)>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
         } else {
             const int jr = kron_jr(P);
@@ -1063,6 +1215,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
             X[e] = copysignf(shr, X[e]);
             V[e] = att;
             S[e] = sp.weight_model == BMND_WEIGHT_CLASSIC ? att * att : att * att * nv;
+            if (exact_risk && e < kk * P) S[e] = 0.0f;  // the exact pass below holds these planes' noise
             continue;
         } else if (!wiener && gauss) {
             // |c| >= lambda sigma, the group DC always kept (bmndalgo.py:462-475)
@@ -1098,6 +1251,9 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
         V[e] = att;
         float err = att * att;
         if (sp.weight_model != BMND_WEIGHT_CLASSIC) err *= nv;
+        // exact risk weights: the noise of the first kk planes comes from the
+        // exact pass below; their bias term stays (wiener.py:760-797)
+        if (exact_risk && e < kk * P) err = 0.0f;
         if (sp.weight_model == BMND_WEIGHT_RISK) {
             const float rj = 1.0f - att;
             err += rj * rj * spw;
@@ -1105,6 +1261,20 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
         S[e] = err;
     }
     __syncthreads();
+
+    // ---- exact noise risk of the first kk planes (wiener.py:638-711) ----
+    // (stages with exact risk weights run the runtime-geometry instantiation,
+    // so the specialised ones carry none of this code)
+    double* riskp = sm<double>(smem, a.L.risk);
+    if constexpr (ND == 0) {
+        if (exact_risk) {
+            const float* smt = a.st + static_cast<int64_t>(P) * kron_stride(P);
+            const int jr = kron_jr(P);
+            if (jr == 1) exact_risk_any<1>(lval, lstart, lent, U, GT, kpad, kk, a.st, smt, V, P, riskp);
+            else if (jr == 2) exact_risk_any<2>(lval, lstart, lent, U, GT, kpad, kk, a.st, smt, V, P, riskp);
+            else exact_risk_any<4>(lval, lstart, lent, U, GT, kpad, kk, a.st, smt, V, P, riskp);
+        }
+    }
 
     if (a.probe.active && a.probe.atten)
         for (int e = tid; e < total; e += blockDim.x) a.probe.atten[probe_base + e] = V[e];
@@ -1147,7 +1317,13 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
     __syncthreads();
     if (tid < n) {
         float risk = 0.0f;
-        if (sp.weight_group_scope) {
+        if (exact_risk) {
+            // one weight for the group: its exact risk in float64
+            // (wiener.py:760-822, aggregationweights.py:656-676)
+            double r = riskp[blockDim.x >> 5];
+            for (int g = 0; g < n; ++g) r += plane[g];
+            risk = static_cast<float>(r);
+        } else if (sp.weight_group_scope) {
             // one weight for the whole group: the summed risk (the group
             // transforms are orthonormal, so the group metric is the identity)
             for (int g = 0; g < n; ++g) risk += static_cast<float>(plane[g]);
@@ -1342,6 +1518,39 @@ __global__ void spatial_kron_kernel(BmndStageParams sp, int P, int stride, float
     }
 }
 
+// risk metric SM = S_inv^T diag(w^2) S_inv of the windowed synthesis
+// (variance.py:1546-1557): S_inv the Kronecker product of the inverse patch
+// matrices (float32 products in axis order, variance.py:744-755), w^2 and
+// w^2 S_inv rounded to float32 as the reference's, each entry summed in
+// float64 and rounded once.  Row p at sm[p * stride], zero beyond column P.
+__global__ void risk_metric_kernel(BmndStageParams sp, int P, int stride, float* sm) {
+    auto synth = [&](int x, int c) {
+        int xd[BMND_MAX_DIMS], cd[BMND_MAX_DIMS];
+        for (int d = sp.ndim - 1; d >= 0; --d) {
+            xd[d] = x % sp.block[d];
+            x /= sp.block[d];
+            cd[d] = c % sp.block[d];
+            c /= sp.block[d];
+        }
+        float v = sp.spatial_inv[0][xd[0] * sp.block[0] + cd[0]];
+        for (int d = 1; d < sp.ndim; ++d) v = mul_rn(v, sp.spatial_inv[d][xd[d] * sp.block[d] + cd[d]]);
+        return v;
+    };
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < P * stride; idx += gridDim.x * blockDim.x) {
+        const int p = idx / stride, j = idx % stride;
+        if (j >= P) {
+            sm[idx] = 0.0f;
+            continue;
+        }
+        double acc = 0.0;
+        for (int x = 0; x < P; ++x) {
+            const float w2 = mul_rn(sp.window[x], sp.window[x]);
+            acc += static_cast<double>(synth(x, p)) * static_cast<double>(mul_rn(w2, synth(x, j)));
+        }
+        sm[idx] = static_cast<float>(acc);
+    }
+}
+
 __global__ void finalize_kernel(const double* __restrict__ num, const double* __restrict__ den,
                                 const float* __restrict__ noisy, float* __restrict__ out,
                                 int64_t n, float eps_f, int no_eps) {
@@ -1394,6 +1603,11 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
         const int stride = kron_stride(P);
         spatial_kron_kernel<<<(P * stride + 255) / 256, 256, 0, stream>>>(sp, P, stride, st);
         BMND_LAUNCH_CHECK("spatial_kron_kernel");
+        if (sp.exact_risk_weights) {
+            risk_metric_kernel<<<(P * stride + 255) / 256, 256, 0, stream>>>(sp, P, stride,
+                                                                            st + static_cast<int64_t>(P) * stride);
+            BMND_LAUNCH_CHECK("risk_metric_kernel");
+        }
     }
     FilterArgs a{};
     a.st = st;
@@ -1448,6 +1662,7 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
     // covered by the other's work (a single 512-thread CTA per SM, which
     // leaves L1 room for the 5x5x5 Kronecker table, measured 16% slower)
     const int* b = sp.block;
+    if (sp.exact_risk_weights) return run(group_filter_kernel<0, 0, 0, 0, kThreads>, kThreads);
     if (sp.ndim == 2 && b[0] == 8 && b[1] == 8) return run(group_filter_kernel<2, 8, 8, 1, kThreads>, kThreads);
     if (sp.ndim == 3 && b[0] == 4 && b[1] == 4 && b[2] == 4)
         return run(group_filter_kernel<3, 4, 4, 4, kThreads>, kThreads);

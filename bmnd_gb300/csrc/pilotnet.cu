@@ -596,12 +596,13 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
                                                              const bf16* __restrict__ wtc,
                                                              const float* __restrict__ bias,
                                                              const bf16* __restrict__ mask, bf16* __restrict__ out,
-                                                             NetGeo g, int* __restrict__ err) {
+                                                             NetGeo g, int* __restrict__ err, uint64_t probe_ns) {
     using TT = TcTile<ND, C>;
     extern __shared__ __align__(128) unsigned char tc_smem[];
     // full[2] (halo stage landed), empty[2] (stage read by the MMAs), afull[2]
-    // (accumulator complete), aempty[2] (accumulator read out), weights
-    __shared__ __align__(8) uint64_t bars[9];
+    // (accumulator complete), aempty[2] (accumulator read out), weights, and
+    // one barrier that nothing completes (the wait probe)
+    __shared__ __align__(8) uint64_t bars[10];
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
     volatile int* abort_v = &abort_flag;
@@ -614,6 +615,7 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
     auto afull = [&](int s) { return bar0 + 32u + 8u * s; };
     auto aempty = [&](int s) { return bar0 + 48u + 8u * s; };
     const uint32_t wbar = bar0 + 64u;
+    const uint32_t never = bar0 + 72u;
     constexpr uint64_t kWaitNs = 1000000000ull;  // one tile takes microseconds
 
     if (tid == 0) {
@@ -624,6 +626,7 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
             mbar_init(aempty(s), 4);  // one arrival per epilogue warp
         }
         mbar_init(wbar, 1);
+        mbar_init(never, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         abort_flag = (sbase & 127u) != 0u ? 1 : 0;  // TMA destinations need 128-byte alignment
         if (abort_flag) atomicExch(err, 2);
@@ -639,6 +642,16 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
+    if (probe_ns) {
+        // wait probe: a bounded wait on a barrier nothing completes runs out
+        // before any copy or product is issued; the launch then stops as on a
+        // real timeout (status set, tensor memory freed below)
+        if (tid == 0 && !mbar_wait(never, 0, probe_ns)) {
+            abort_flag = 1;
+            atomicExch(err, 1);
+        }
+        __syncthreads();
+    }
 
     const int tiles_x = (g.W + TT::tx - 1) / TT::tx;
     const int tiles_y = (g.H + TT::ty - 1) / TT::ty;
@@ -781,6 +794,7 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
         int it = 0;
         for (int64_t tl = blockIdx.x; tl < ntiles; tl += gridDim.x, ++it) {
             const int s = it & 1;
+            if (*abort_v) break;
             bool got = true;
             if (lane == 0) got = mbar_wait(afull(s), (it >> 1) & 1, kWaitNs);
             got = __shfl_sync(0xffffffffu, got ? 1 : 0, 0) != 0;
@@ -1217,6 +1231,7 @@ int32_t run_mid(const bf16* in, const uint2* wpk, const float* bias, const bf16*
 }
 
 int g_conv_engine = BMND_CONV_TCGEN05;
+uint64_t g_wait_probe_ns = 0;  // see bmnd_pilotnet_set_wait_probe
 
 template <int ND, int C>
 int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf16* mask, bf16* out, NetGeo g,
@@ -1261,7 +1276,8 @@ int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf1
     // one persistent CTA per SM: the weights fill most of the shared memory
     int64_t blocks = sms;
     if (blocks > ntiles) blocks = ntiles;
-    kernel<<<static_cast<unsigned>(blocks), TT::threads, TT::bytes, stream>>>(maps, wtc, bias, mask, out, g, err);
+    kernel<<<static_cast<unsigned>(blocks), TT::threads, TT::bytes, stream>>>(maps, wtc, bias, mask, out, g, err,
+                                                                             g_wait_probe_ns);
     BMND_LAUNCH_CHECK("conv_mid_tc_kernel");
     return BMND_OK;
 }
@@ -1420,6 +1436,13 @@ int32_t bmnd_pilotnet_get_conv_engine(int32_t* engine) {
     clear_error();
     if (!engine) return fail(BMND_ERR_INVALID_ARG, "null output");
     *engine = g_conv_engine;
+    return BMND_OK;
+}
+
+int32_t bmnd_pilotnet_set_wait_probe(uint64_t ns) {
+    clear_error();
+    if (ns > 1000000000ull) return fail(BMND_ERR_INVALID_ARG, "the wait probe is at most one second");
+    g_wait_probe_ns = ns;
     return BMND_OK;
 }
 

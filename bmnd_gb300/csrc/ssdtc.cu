@@ -4,9 +4,13 @@
 //
 // References are sorted into spatial tiles (12^3 patch-grid positions in 3-D,
 // 24^2 in 2-D) so that up to 128 nearby references share one union box of
-// candidate positions.  One CTA takes such a block of references:
+// candidate positions.  Squared distances do not change when both patches are
+// shifted by the same constant, so every tile works on values centred on mu_t,
+// the mean of its references' patches: the error of the BF16 products scales
+// with the centred norms, which for smooth data are far below the raw ones.
+// One CTA takes a block of references of one tile:
 //   A (M = 128 references x K = patch, zero padded to a multiple of 16) holds
-//     their patches split as a = hi + lo, hi = bf16(a), lo = bf16(a - hi);
+//     their centred patches split as a = hi + lo, hi = bf16(a), lo = bf16(a - hi);
 //   for every chunk of 128 candidates of the union box (x fastest), the CTA
 //     gathers the candidates' patches into B (N = 128 x K, the same split)
 //     and one thread issues 3 K/16 tcgen05.mma (kind::f16, BF16 in, FP32
@@ -71,7 +75,8 @@ __device__ __forceinline__ void split_store(const float (&v)[8], unsigned char* 
 // per patch origin: sum of squares of its patch (float32, patch order); the
 // rows of origins off the patch grid stay unread
 template <int ND, int B0, int B1, int B2>
-__global__ void sqbox_kernel(const float* __restrict__ src, SsdScreenArgs a, int64_t nvox, float* __restrict__ out) {
+__global__ void sqbox_kernel(const float* __restrict__ src, SsdScreenArgs a, int64_t nvox, float* __restrict__ out,
+                             float* __restrict__ out_sum) {
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nvox;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         int64_t rem = i;
@@ -83,7 +88,7 @@ __global__ void sqbox_kernel(const float* __restrict__ src, SsdScreenArgs a, int
             rem /= n;
             ok = ok && c[d] < a.counts[d];
         }
-        float s = 0.0f;
+        float s = 0.0f, s1 = 0.0f;
         if (ok) {
 #pragma unroll 1
             for (int p0 = 0; p0 < B0; ++p0)
@@ -95,14 +100,17 @@ __global__ void sqbox_kernel(const float* __restrict__ src, SsdScreenArgs a, int
                         for (int p2 = 0; p2 < B2; ++p2) {
                             const float v = __ldg(row + p2);
                             s = fmaf(v, v, s);
+                            s1 += v;
                         }
                     } else {
                         const float v = __ldg(row);
                         s = fmaf(v, v, s);
+                        s1 += v;
                     }
                 }
         }
         out[i] = s;
+        out_sum[i] = s1;
     }
 }
 
@@ -126,6 +134,29 @@ __global__ void tile_fill_kernel(SsdScreenArgs a, int64_t n_refs, const int32_t*
          r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int t = ref_tile(a, a.refs, r);
         perm[start[t] + atomicAdd(cursor + t, 1)] = static_cast<int32_t>(r);
+    }
+}
+
+// per tile: the mean value of its references' patches (one warp per tile,
+// a fixed order), the centre of the tile's screening
+__global__ void tile_mean_kernel(SsdScreenArgs a, int P, float* __restrict__ mu) {
+    const int lane = threadIdx.x & 31;
+    const int warps = static_cast<int>(gridDim.x * (blockDim.x >> 5));
+    for (int t = static_cast<int>(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); t < a.n_tiles; t += warps) {
+        const int t0 = a.tile_start[t], t1 = a.tile_start[t + 1];
+        float s = 0.0f;
+        for (int i = t0 + lane; i < t1; i += 32) {
+            const int32_t r = a.perm[i];
+            int64_t org = 0;
+            for (int d = 0; d < a.ndim; ++d) org += static_cast<int64_t>(a.refs[static_cast<int64_t>(r) * a.ndim + d]) *
+                                                  a.vstride[d];
+            s += __ldg(a.sums + org);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        const float m = t1 > t0 ? s / (static_cast<float>(t1 - t0) * static_cast<float>(P)) : 0.0f;
+        if (lane == 0) mu[t] = m;
+        for (int i = t0 + lane; i < t1; i += 32) a.ref_mu[a.perm[i]] = m;
     }
 }
 
@@ -234,6 +265,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) ssd_screen_tc_kernel(SsdScreenA
 
     for (int t = blockIdx.x; t < a.n_tiles && !*abort_v; t += gridDim.x) {
         const int t0 = a.tile_start[t], t1 = a.tile_start[t + 1];
+        const float mu = __ldg(a.mu + t);
         for (int mb = t0; mb < t1 && !*abort_v; mb += kTcM) {
             const int nref = min(kTcM, t1 - mb);
             // references of the block: position, clipped window, norm
@@ -249,7 +281,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) ssd_screen_tc_kernel(SsdScreenA
                         r_ext[d][tid] = min(cd + a.radius[d], a.counts[d] - 1) - l + 1;
                         org += static_cast<int64_t>(cd) * a.vstride[d];
                     }
-                    r_na[tid] = __ldg(a.norms + org);
+                    r_na[tid] = centred_norm(__ldg(a.norms + org), __ldg(a.sums + org), mu, P);
                 } else {
                     r_glob[tid] = -1;
                 }
@@ -279,7 +311,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) ssd_screen_tc_kernel(SsdScreenA
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
                     const int p = 8 * kg + e;
-                    v[e] = (m < nref && p < P) ? __ldg(a.src + org + poff[p]) : 0.0f;
+                    v[e] = (m < nref && p < P) ? __ldg(a.src + org + poff[p]) - mu : 0.0f;
                 }
                 const uint32_t off = static_cast<uint32_t>(kg) * S::lbo + static_cast<uint32_t>(m >> 3) * 128u +
                                      static_cast<uint32_t>(m & 7) * 16u;
@@ -307,13 +339,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) ssd_screen_tc_kernel(SsdScreenA
                         if (kg == 0) {
 #pragma unroll
                             for (int d = 0; d < ND; ++d) c_crd[s][d][n] = crd[d];
-                            c_nb[s][n] = ok ? __ldg(a.norms + org) : 0.0f;
+                            c_nb[s][n] = ok ? centred_norm(__ldg(a.norms + org), __ldg(a.sums + org), mu, P) : 0.0f;
                         }
                         float v[8];
 #pragma unroll
                         for (int e = 0; e < 8; ++e) {
                             const int p = 8 * kg + e;
-                            v[e] = (ok && p < P) ? __ldg(a.src + org + poff[p]) : 0.0f;
+                            v[e] = (ok && p < P) ? __ldg(a.src + org + poff[p]) - mu : 0.0f;
                         }
                         const uint32_t off = static_cast<uint32_t>(kg) * S::lbo +
                                              static_cast<uint32_t>(n >> 3) * 128u + static_cast<uint32_t>(n & 7) * 16u;
@@ -375,8 +407,11 @@ int64_t grid_cap(int64_t n, int threads, int64_t cap) {
 template <int ND, int B0, int B1, int B2>
 int32_t run_screen(SsdScreenArgs a, int64_t nvox, cudaStream_t stream) {
     sqbox_kernel<ND, B0, B1, B2><<<static_cast<unsigned>(grid_cap(nvox, 256, 152 * 32)), 256, 0, stream>>>(
-        a.src, a, nvox, const_cast<float*>(a.norms));
+        a.src, a, nvox, const_cast<float*>(a.norms), const_cast<float*>(a.sums));
     BMND_LAUNCH_CHECK("sqbox_kernel");
+    tile_mean_kernel<<<static_cast<unsigned>(grid_cap(a.n_tiles, 8, 152 * 16)), 256, 0, stream>>>(
+        a, B0 * B1 * B2, const_cast<float*>(a.mu));
+    BMND_LAUNCH_CHECK("tile_mean_kernel");
     constexpr int KP = (B0 * B1 * B2 + 15) / 16 * 16;
     using S = ScreenSmem<KP>;
     auto kernel = ssd_screen_tc_kernel<ND, B0, B1, B2>;
@@ -421,6 +456,9 @@ SsdScratchLayout ssd_scratch_layout(int ndim, const int32_t* counts, const int32
         return o;
     };
     L.o_norms = take(4ull * static_cast<uint64_t>(nvox));
+    L.o_psum = take(4ull * static_cast<uint64_t>(nvox));
+    L.o_mu = take(4ull * static_cast<uint64_t>(n_tiles));
+    L.o_rmu = take(4ull * static_cast<uint64_t>(n_refs));
     L.o_rows = take(4ull * static_cast<uint64_t>(n_refs) * static_cast<uint64_t>(wmax));
     L.o_start = take(4ull * static_cast<uint64_t>(n_tiles + 1));
     L.o_cursor = take(4ull * static_cast<uint64_t>(n_tiles));
@@ -434,6 +472,9 @@ SsdScratchLayout ssd_scratch_layout(int ndim, const int32_t* counts, const int32
 int32_t launch_ssd_screen(SsdScreenArgs a, int64_t nvox, int64_t n_refs, char* base, const SsdScratchLayout& L,
                           cudaStream_t stream) {
     a.norms = reinterpret_cast<float*>(base + L.o_norms);
+    a.sums = reinterpret_cast<float*>(base + L.o_psum);
+    a.mu = reinterpret_cast<float*>(base + L.o_mu);
+    a.ref_mu = reinterpret_cast<float*>(base + L.o_rmu);
     a.out = reinterpret_cast<float*>(base + L.o_rows);
     a.wmax = L.wmax;
     a.err = reinterpret_cast<int*>(base + L.o_err);

@@ -201,6 +201,18 @@ class GaussianModel:
     _ssd: dict = field(default_factory=dict, repr=False)
 
 
+def white_variance(model: GaussianModel) -> float | None:
+    """The noise variance when the noise is white, else None
+    (variance.py:1459-1470): white means no autocovariance lag but 0 above
+    max(1e-12, 1e-6 x the lag-0 variance)."""
+    ac = np.asarray(model.autocovariance, dtype=np.float64)
+    var0 = float(ac.reshape(-1)[0])
+    tol = max(1e-12, 1e-6 * max(var0, 0.0))
+    if np.any(np.abs(ac.reshape(-1)[1:]) > tol):
+        return None
+    return max(var0, 0.0)
+
+
 def build_model(volume_shape: tuple[int, ...], nf, *, sigma=None, sigma_psd=None, volume=None) -> GaussianModel:
     """The noise model for ``bmnd(volume, profile, sigma=..., sigma_psd=...)``;
     with neither given, sigma is estimated from ``volume``."""

@@ -75,7 +75,8 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     ``gauss`` (stationary Gaussian noise) holds the device tables of the stage:
     ``cov`` (float32 CUDA tensor [lag][coefficient]), ``domain`` (its lag
     domain), ``ssd`` (SSD noise bias over the search offsets, or None) and
-    ``gamma``; without it the stage models direct Poisson noise.  ``null_table``
+    ``gamma``, and ``white_variance`` (the noise variance when the noise is
+    white, else None); without it the stage models direct Poisson noise.  ``null_table``
     (float64 CUDA tensor [2, max_count + 1], ``policies.null_moment_table``)
     enables the profile's Poisson HT match policy.  ``fast_transforms`` computes
     the Haar group axis by its sum pyramid (same transform, different rounding)."""
@@ -93,7 +94,7 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     model = getattr(profile, f"{stage}_weight_model")
     domain = getattr(profile, f"{stage}_weight_domain")
     scope = getattr(profile, f"{stage}_weight_scope")
-    _check_stage_weights(stage, model, domain, scope, variance_k)
+    exact_risk = _check_stage_weights(stage, model, domain, scope, variance_k, int(np.prod(block)))
 
     group_kind, spatial = resolve_axes(getattr(profile, f"{stage}_transform"), ndim)
     p = _abi.StageParams()
@@ -116,6 +117,12 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     p.weight_group_scope = int(scope is AggregationWeightScope.GROUP)
     p.fast_group_transform = int(bool(fast_transforms))
     p.windowed_synthesis = int(domain is AggregationWeightDomain.WINDOWED_SYNTHESIS)
+    # exact risk weights under Gaussian noise only when the noise is white
+    # (variance.py:1459-1470); otherwise the reference weighs by the diagonal
+    if exact_risk and (gauss is None or gauss.get("white_variance") is not None):
+        p.exact_risk_weights = 1
+        if gauss is not None:
+            p.exact_source_variance = float(np.float32(gauss["white_variance"]))
     p.match_threshold = float(np.float32(getattr(profile, f"{stage}_match_threshold")))
     p.ht_lambda = float(profile.ht_lambda_threshold)
     p.wiener_scale = float(profile.wiener_variance_scale)
@@ -193,15 +200,18 @@ def stage_params(profile, shape: tuple[int, ...], stage: str, distance: BlockMat
     return p
 
 
-def _check_stage_weights(stage, model, domain, scope, variance_k) -> None:
+def _check_stage_weights(stage, model, domain, scope, variance_k, patch_volume: int) -> bool:
+    """Whether the stage weights its groups by their exact risk: the
+    covariance-aware exact group weighting (bmndalgo.py:363-370, :752-758)."""
     if model is AggregationWeightModel.RISK and stage != "wiener":
         raise unsupported("risk aggregation weights apply to the Wiener stage only")
     exact = (model in (AggregationWeightModel.VARIANCE, AggregationWeightModel.RISK)
              and domain is AggregationWeightDomain.WINDOWED_SYNTHESIS
              and scope is AggregationWeightScope.GROUP and int(variance_k) > 0)
-    if exact:
-        raise unsupported("the covariance-aware exact group weighting (group scope, windowed synthesis, k > 0) "
-                          "is not on the GPU path")
+    if exact and patch_volume > 128:
+        raise unsupported(f"the covariance-aware exact group weighting needs patches of at most 128 voxels, "
+                          f"got {patch_volume}")
+    return exact
 
 
 def check_weight_options(profile, variance_k: int) -> None:
@@ -209,7 +219,8 @@ def check_weight_options(profile, variance_k: int) -> None:
     for stage in ("ht", "wiener"):
         _check_stage_weights(stage, getattr(profile, f"{stage}_weight_model"),
                              getattr(profile, f"{stage}_weight_domain"),
-                             getattr(profile, f"{stage}_weight_scope"), variance_k)
+                             getattr(profile, f"{stage}_weight_scope"), variance_k,
+                             int(np.prod(getattr(profile, f"{stage}_block_size"))))
 
 
 def check_gaussian_options(profile, variance_k: int) -> None:

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define BMND_ABI_VERSION 2
+#define BMND_ABI_VERSION 3
 #define BMND_MAX_DIMS 3
 #define BMND_MAX_EDGE 8       /* largest patch edge per axis */
 #define BMND_MAX_PATCH 512    /* largest patch volume */
@@ -175,11 +175,25 @@ typedef struct BmndStageParams {
     double policy_beta;              /* poisson_ht_match_structure_beta */
     double policy_power;             /* poisson_ht_match_intensity_power */
     /* one aggregation weight per group (weight_scope "group") instead of one
-     * per patch; the covariance-aware exact weighting is not available */
+     * per patch */
     int32_t weight_group_scope;
     /* Haar group axis by its sum pyramid instead of the matrix product (same
      * transform, different rounding; used by the fast path) */
     int32_t fast_group_transform;
+    /* covariance-aware exact group weighting (bmndalgo.py:363-377, :491-503,
+     * :752-758, :913-927; wiener.py:638-822): with weight_group_scope,
+     * windowed_synthesis and variance_k > 0, the group's weight is
+     * 1 / (risk + eps) with the noise risk of the first min(k, n) planes
+     * summed exactly over the group's union voxels,
+     *   sum_u V_u sum_g (a_g o c_u[g])^T SM (a_g o c_u[g]),
+     * c_u[g] the coefficients of plane g that voxel u reaches, a the
+     * attenuation and SM = S_inv^T diag(w^2) S_inv; the other planes and the
+     * bias term use the coefficient-metric diagonal.  Patches of at most 128
+     * voxels. */
+    int32_t exact_risk_weights;
+    /* Gaussian noise with exact_risk_weights: the (white) noise variance of
+     * every union voxel (variance.py:1451-1496) */
+    float exact_source_variance;
 } BmndStageParams;
 
 #define BMND_GAIN_VARIANCE_SCALED 0
@@ -440,6 +454,14 @@ int32_t bmnd_pilotnet_status(const BmndPilotNet* net, const void* d_workspace, u
 #define BMND_CONV_TCGEN05 0
 #define BMND_CONV_MMA_SYNC 1
 int32_t bmnd_pilotnet_set_conv_engine(int32_t engine);
+
+/* Failure-detection test hook (process-wide): with ns > 0 (at most 1e9), every
+ * following tensor-core layer launch first waits up to ns nanoseconds on an
+ * mbarrier that nothing completes.  The wait runs out before any copy or
+ * product is issued; the launch stops as on a real timeout, frees its tensor
+ * memory, and bmnd_pilotnet_status then reports BMND_ERR_TIMEOUT.  0, the
+ * default, turns it off. */
+int32_t bmnd_pilotnet_set_wait_probe(uint64_t ns);
 int32_t bmnd_pilotnet_get_conv_engine(int32_t* engine);
 /* Residual check of a pilot, per tile of edge `edge` (cubes in 3-D, squares in
  * 2-D; shape as in BmndPilotNet): d_out[3 * tile + (0, 1, 2)] = observed Poisson

@@ -14,6 +14,7 @@ Usage (``BMND_REFERENCE_SRC`` names the reference's ``src/`` directory)::
     python tests/golden/make_golden.py sigma bm3d_32 [bm4d_12x16x20 ...]
     python tests/golden/make_golden.py gauss [bm3d_32 ...]
     python tests/golden/make_golden.py option [mass_bm3d_32 ...]
+    python tests/golden/make_golden.py exact_risk
     python tests/golden/make_golden.py list
 
 ``unit`` writes ``unit_*.npz`` (distances, canonical keys, transforms, exact
@@ -294,6 +295,82 @@ def run_unit() -> None:
     print(f"unit fixtures -> {path} ({len(out)} arrays)")
 
 
+def run_exact_risk() -> None:
+    """exact_risk_groups.npz: the covariance-aware exact group weighting on
+    single groups, made by the reference's own functions
+    (build_exact_poisson_group_plan, prepare_noise_std_for_risk,
+    limit_poisson_group_variance_planes, compute_covariance_aware_group_risk_from_plan,
+    invert_aggregation_risks): per case the volume (also the Wiener pilot),
+    member positions, sigma, attenuation, the group risk (float64) and weight."""
+    from bmnd import aggregationweights, poisson, transforms, utils, variance, wiener
+    from bmnd.profiles import BM3DProfile, BM4DProfile
+    from bmnd.enums import AggregationWeightScope
+
+    rng = np.random.default_rng(4321)
+    out = {}
+    cases = [
+        ("ht2d", BM3DProfile(), (8, 8), (4, 9, 16), 19),
+        ("wi2d", BM3DProfile(), (8, 8), (3, 8, 32), 19),
+        ("ht3d", BM4DProfile(), (4, 4, 4), (2, 5, 16), 7),
+        ("wi3d", BM4DProfile(), (5, 5, 5), (4, 7, 32), 7),
+    ]
+    for tag, prof, block, sizes, radius in cases:
+        stage = "ht" if tag.startswith("ht") else "wiener"
+        tlist = getattr(prof, f"{stage}_transform")
+        beta = float(getattr(prof, f"{stage}_kaiser_beta"))
+        vol_shape = tuple(b + 2 * radius + 3 for b in block)
+        vol = rng.poisson(rng.uniform(3.0, 40.0, size=vol_shape)).astype(np.float32)
+        vmodel = variance.build_poisson_variance_model(vol, variance_floor=1e-10, scale=1.0, source_name="observation")
+        counts = tuple(s - b + 1 for s, b in zip(vol_shape, block))
+        w_patch = utils.kaiser_window_nd(block, beta=beta)
+        for n in sizes:
+            # members clustered around a centre, so that many patches overlap
+            centre = np.array([c // 2 for c in counts])
+            pos = set()
+            while len(pos) < n:
+                pos.add(tuple(int(v) for v in np.clip(centre + rng.integers(-3, 4, size=len(block)), 0,
+                                                       np.array(counts) - 1)))
+            abs_pos = np.array(sorted(pos), dtype=np.int64)
+            rng.shuffle(abs_pos)
+            shifted = abs_pos - abs_pos.min(axis=0, keepdims=True)
+            group_shape = (n,) + block
+            fwd, inv = transforms.get_transform_matrix(group_shape, tlist)
+            patches = np.stack([vol[tuple(slice(a, a + b) for a, b in zip(p, block))] for p in abs_pos])
+            vpatches = np.stack([vmodel.variance_volume[tuple(slice(a, a + b) for a, b in zip(p, block))]
+                                 for p in abs_pos])
+            coef = transforms.apply_transform_nd(patches, fwd)
+            for k in (1, 4):
+                plan_ = variance.build_exact_poisson_group_plan(vmodel, abs_pos, shifted, group_shape, fwd)
+                exact = plan_.prepare_noise_std_for_risk(k)
+                if k >= n:
+                    sigma = exact
+                else:
+                    approx = variance.get_direct_poisson_noise_std(vpatches, fwd, k=0)
+                    sigma = variance.limit_poisson_group_variance_planes(exact, approx, k)
+                if stage == "ht":
+                    att = np.asarray(poisson._poisson_hard_threshold_mask(np.abs(coef), np.float32(3.0) * sigma, 1.0),
+                                     dtype=np.float32)
+                    risk = wiener.compute_covariance_aware_group_risk_from_plan(
+                        att, plan_, inv, w_patch, exact_plane_count=k, noise_sigma=sigma)
+                else:
+                    att = wiener.compute_poisson_wiener_gain(coef, sigma, 0.4, eps=1e-10)
+                    spow = wiener.compute_poisson_wiener_signal_power(coef, sigma, 0.4)
+                    risk = wiener.compute_covariance_aware_group_risk_from_plan(
+                        att, plan_, inv, w_patch, exact_plane_count=k, noise_sigma=sigma, signal_power=spow)
+                weights = aggregationweights.invert_aggregation_risks(risk, group_size=n,
+                                                                      scope=AggregationWeightScope.GROUP, eps=1e-10)
+                key = f"{tag}_n{n}_k{k}"
+                out[key + "_vol"] = vol
+                out[key + "_abs"] = abs_pos
+                out[key + "_sigma"] = np.asarray(sigma, dtype=np.float32)
+                out[key + "_att"] = np.asarray(att, dtype=np.float32)
+                out[key + "_risk"] = np.float64(risk)
+                out[key + "_weights"] = np.asarray(weights, dtype=np.float32)
+    path = os.path.join(HERE, "exact_risk_groups.npz")
+    np.savez_compressed(path, **out)
+    print(f"exact risk fixtures -> {path} ({len(out)} arrays)")
+
+
 # Poisson cases with non-default profile fields: name -> (kind, generator, kwargs, profile fields)
 OPTION_CASES = {
     "mass_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=21), dict(poisson_group_mass_conservation="both")),
@@ -325,6 +402,19 @@ OPTION_CASES = {
                                           k=0)),
     "risk_windowed_bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=35),
                                     dict(wiener_weight_model="risk", wiener_weight_domain="windowed_synthesis")),
+    "exact_group_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=38),
+                            dict(ht_weight_scope="group", ht_weight_domain="windowed_synthesis",
+                                 wiener_weight_scope="group", wiener_weight_domain="windowed_synthesis")),
+    "exact_group_risk_bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=39),
+                                       dict(ht_weight_scope="group", ht_weight_domain="windowed_synthesis",
+                                            wiener_weight_model="risk", wiener_weight_scope="group",
+                                            wiener_weight_domain="windowed_synthesis")),
+    "exact_group_mass_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=41),
+                                 dict(ht_weight_scope="group", ht_weight_domain="windowed_synthesis",
+                                      poisson_group_mass_conservation="both")),
+    "exact_group_risk_bm3d_40x24": ("bm3d", "ragged2d", dict(shape=(40, 24), seed=40),
+                                    dict(wiener_weight_model="risk", wiener_weight_scope="group",
+                                         wiener_weight_domain="windowed_synthesis", k=2)),
     "ssd_gamma_bm3d_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=36), dict(blockmatch_distance="ssd")),
     "ssd_gamma_bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=37),
                                 dict(blockmatch_distance="ssd", gamma=2.5)),
@@ -376,6 +466,13 @@ GAUSS_CASES = {
     "bm3d_conv_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=15), 3.0, {}, dict(nf=0)),
     "bm4d_12x16x20": ("bm4d", "ragged3d", dict(shape=(12, 16, 20), seed=16), 1.5, {}, {}),
     "bm3d_soft_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=17), 3.0, {}, dict(ht_use_soft_thresholding=True)),
+    "bm3d_exact_group_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=18), 3.0, {},
+                            dict(ht_weight_scope="group", ht_weight_domain="windowed_synthesis",
+                                 wiener_weight_model="risk", wiener_weight_scope="group",
+                                 wiener_weight_domain="windowed_synthesis")),
+    "bm3d_psd_group_32": ("bm3d", phantoms.shapes_2d, dict(size=32, seed=19), 2.5, dict(psd=True),
+                          dict(ht_weight_scope="group", ht_weight_domain="windowed_synthesis",
+                               wiener_weight_scope="group", wiener_weight_domain="windowed_synthesis")),
 }
 
 
@@ -401,6 +498,8 @@ def _colored_psd(shape, sigma):
 def run_gauss(name: str) -> None:
     """gauss_<case>.npz: the reference on stationary Gaussian noise (both stage
     estimates, both match sets, the sigma maps and the noise model's tables)."""
+    import json
+
     import bmnd as ref
     from bmnd import variance as refvar
 
@@ -434,7 +533,8 @@ def run_gauss(name: str) -> None:
                    sigma_wiener=np.asarray(smap["wiener"], dtype=np.float32), seconds=np.float64(elapsed),
                    sigma=np.float64(-1.0 if "sigma" not in call else sigma),
                    nf=np.array(-1 if "nf" not in extra else extra["nf"]),
-                   soft=np.array(int(bool(extra.get("ht_use_soft_thresholding", False)))))
+                   soft=np.array(int(bool(extra.get("ht_use_soft_thresholding", False)))),
+                   extra_json=np.array(json.dumps(extra)))
     if psd is not None:
         payload["sigma_psd"] = psd
     for stage, (sel, counts, accepted, refs) in matches.items():
@@ -471,6 +571,9 @@ def main(argv: list[str]) -> None:
         return
     if argv[0] == "unit":
         run_unit()
+        return
+    if argv[0] == "exact_risk":
+        run_exact_risk()
         return
     if argv[0] == "sigma":
         for name in argv[1:]:

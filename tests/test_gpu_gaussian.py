@@ -3,7 +3,10 @@
 Cases (``tests/golden/gauss_*.npz``, made by ``make_golden.py gauss``): BM3D
 with a scalar sigma, a ragged 2-D volume, sigma estimated from the data, a
 coloured ``sigma_psd``, conventional mode (``nf=0``: no gamma correction,
-k = 0), soft thresholding, and a ragged BM4D volume.
+k = 0), soft thresholding, a ragged BM4D volume, and group-scope
+windowed-synthesis weights: with white noise the covariance-aware exact group
+weighting (risk weights in the Wiener stage), with a coloured PSD the
+diagonal weighting the reference falls back to (variance.py:1459-1470).
 
 Stated tolerance:
 * stage-1 match sets (SSD with the gamma noise-bias correction) equal the
@@ -32,12 +35,17 @@ CASES = sorted(os.path.basename(p)[6:-4] for p in glob.glob(os.path.join(GOLDEN,
 
 
 def _profile(g):
+    import json
+
     import bmnd_gb300 as bg
 
-    nf = int(g["nf"])
-    extra = {} if nf < 0 else dict(nf=nf)
-    if "soft" in g.files and int(g["soft"]):
-        extra["ht_use_soft_thresholding"] = True
+    if "extra_json" in g.files:
+        extra = json.loads(str(g["extra_json"]))
+    else:
+        nf = int(g["nf"])
+        extra = {} if nf < 0 else dict(nf=nf)
+        if "soft" in g.files and int(g["soft"]):
+            extra["ht_use_soft_thresholding"] = True
     return (bg.BM3DProfile if str(g["kind"]) == "bm3d" else bg.BM4DProfile)(**extra)
 
 

@@ -97,3 +97,33 @@ def test_learned_pilot_through_bmnd(cuda, case):
         bg.bmnd(noisy, prof, pilot="learned", return_sigma_map=True)
     with pytest.raises(ValueError):
         bg.bmnd(noisy, prof, pilot="neural")
+
+
+def test_lowcount_pilot_on_uneven_volume(cuda, native):
+    """The low-count 3-D net (bmnd_gb300/weights/pilot_bm4d_lowcount.npz,
+    trained on 400 volumes of 128^3 at peaks U[2, 5], seeds 3000-3399) on a
+    held-out volume of uneven extents at a peak drawn from the same range:
+    the fast path through bmnd() stays within 0.4 dB of the plain path (the
+    eight 128^3-320^3 evaluation volumes range from -0.36 to +0.28 dB), far
+    above the noisy input, and reports its tile fallback."""
+    import bmnd_gb300 as bg
+    from bmnd_gb300 import phantoms
+    from bmnd_gb300.pilot import PilotNet, bmnd_fast, default_net_path, lowcount_peak
+
+    path = default_net_path("bm4d_lowcount")
+    if not os.path.exists(path):
+        pytest.skip("no trained low-count weights")
+    seed = 6001
+    clean, noisy = phantoms.ellipsoids_3d((72, 96, 120), seed=seed, peak=lowcount_peak(seed))
+    prof = bg.BM4DProfile(noise_model=bg.NoiseModel.POISSON)
+    plain = bg.bmnd(noisy, prof)
+    fast = bg.bmnd(noisy, prof, pilot="learned", pilot_weights=path)
+    details = {}
+    ref = bmnd_fast(cuda.from_numpy(noisy).cuda(), prof, PilotNet.load(path), details=details).cpu().numpy()
+    np.testing.assert_allclose(fast, ref, rtol=0, atol=1e-4 * float(np.max(ref)))
+    p_noisy, p_plain, p_fast = (phantoms.psnr(v, clean) for v in (noisy, plain, fast))
+    print(f"low-count {noisy.shape}: noisy {p_noisy:.3f} dB, plain {p_plain:.3f} dB, fast {p_fast:.3f} dB, "
+          f"fallback tiles {details['fallback_tiles']} of {details['tiles']}")
+    assert p_fast >= p_plain - 0.4, (p_fast, p_plain)
+    assert p_fast > p_noisy + 12.0, (p_fast, p_noisy)
+    assert 0 <= details["fallback_tiles"] <= details["tiles"]

@@ -97,6 +97,42 @@ def test_tensor_memory_engine_matches_warp_mma(cuda, native, ndim, channels, lay
     assert np.linalg.norm(ga - gb) / np.linalg.norm(ga) < 2e-2
 
 
+def test_tensor_core_wait_runs_out_and_recovers(cuda, native):
+    """Failure detection without a GPU fault: with the wait probe set, every
+    tcgen05 layer waits 2 ms on an mbarrier that nothing completes; the wait
+    runs out, the launches stop with their tensor memory freed, and the status
+    call reports BMND_ERR_TIMEOUT.  The next forward pass (probe off) runs and
+    equals the one before the probe bit for bit, which also shows that the
+    tensor memory was given back (an allocation would wait otherwise)."""
+    from bmnd_gb300 import _abi
+    from bmnd_gb300.pilot import get_conv_engine, set_conv_engine
+
+    rng = np.random.default_rng(11)
+    x = cuda.from_numpy(rng.poisson(rng.uniform(1, 20, size=(1, 20, 36, 40))).astype(np.float32)).cuda()
+    net, _ = _net(cuda, 3, 48, 5, seed=12)
+    lib = _abi.lib()
+    old = get_conv_engine()
+    try:
+        set_conv_engine("tcgen05")
+        before = net.forward(x).clone()
+        net.check_status()
+        _abi.check(lib.bmnd_pilotnet_set_wait_probe(2_000_000))
+        try:
+            net.forward(x)
+            with pytest.raises(_abi.BmndError) as info:
+                net.check_status()
+            assert info.value.code == _abi.ERR_TIMEOUT
+        finally:
+            _abi.check(lib.bmnd_pilotnet_set_wait_probe(0))
+        after = net.forward(x)
+        net.check_status()
+        assert cuda.equal(after, before)
+    finally:
+        set_conv_engine(old)
+    with pytest.raises(_abi.BmndError):
+        _abi.check(lib.bmnd_pilotnet_set_wait_probe(2_000_000_000))
+
+
 def test_tile_deviance_matches_numpy(cuda, native):
     from bmnd_gb300.pilot import deviance_table, tile_zscores
 

@@ -175,8 +175,38 @@ def test_unsupported_options_raise_not_implemented():
     vol = np.ones((24, 24), dtype=np.float32)
     with pytest.raises(NotImplementedError):
         bg.bmnd(vol, bg.BM3DProfile(reference_schedule_mode="official"), sigma=1.0)
+    # the covariance-aware exact group weighting is limited to patches of <= 128 voxels
+    vol3 = np.ones((16, 16, 16), dtype=np.float32)
     with pytest.raises(NotImplementedError):
-        bg.bmnd(vol, _poisson(ht_weight_scope="group", ht_weight_domain="windowed_synthesis"))
+        bg.bmnd(vol3, bg.BM4DProfile(noise_model="poisson", ht_block_size=(6, 6, 6), ht_weight_scope="group",
+                                     ht_weight_domain="windowed_synthesis"))
+
+
+def test_exact_risk_weight_planning():
+    """The covariance-aware exact group weighting is planned exactly when the
+    reference takes it (bmndalgo.py:363-370, :752-758): variance or risk
+    weights, windowed synthesis, group scope and k > 0; under Gaussian noise
+    only when the noise is white (variance.py:1459-1470)."""
+    from bmnd_gb300 import gaussian
+    from bmnd_gb300.validation import resolve_profile
+
+    shape = (32, 32)
+    opts = dict(ht_weight_scope="group", ht_weight_domain="windowed_synthesis", wiener_weight_model="risk",
+                wiener_weight_scope="group", wiener_weight_domain="windowed_synthesis")
+    for extra, want in ((opts, (1, 1)), (dict(opts, k=0), (0, 0)),
+                        (dict(opts, wiener_weight_scope="patch"), (1, 0)),
+                        (dict(opts, ht_weight_domain="coefficient"), (0, 1)), ({}, (0, 0))):
+        prof = bg.BM3DProfile(noise_model="poisson", **extra)
+        res = resolve_profile(prof, shape)
+        got = tuple(plan.stage_params(prof, shape, st, res.blockmatch_distance, res.variance_k).exact_risk_weights
+                    for st in ("ht", "wiener"))
+        assert got == want, (extra, got)
+    white = gaussian.build_model(shape, None, sigma=3.0)
+    assert abs(gaussian.white_variance(white) - 9.0) < 1e-4
+    psd = np.ones(shape, dtype=np.float32)
+    psd[0, 1] = 40.0
+    colored = gaussian.build_model(shape, None, sigma_psd=psd)
+    assert gaussian.white_variance(colored) is None
 
 
 def test_stage_params_defaults():
