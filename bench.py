@@ -50,6 +50,8 @@ WORKLOADS = {
                       desc="2048^2 BM3D-Gaussian sigma=5, 40 blobs + 60 rectangles"),
     "gauss256": dict(kind="bm4d", size=256, noise="gaussian", sigma=2.0,
                      desc="256^3 BM4D-Gaussian sigma=2, 30 ellipsoids"),
+    "gauss128": dict(kind="bm4d", size=128, noise="gaussian", sigma=2.0,
+                     desc="128^3 BM4D-Gaussian sigma=2, 30 ellipsoids"),
 }
 
 

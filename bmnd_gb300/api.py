@@ -111,12 +111,18 @@ _REFS_CACHE: dict = {}
 class _Staging:
     """Page-locked host buffers for the NumPy path of :func:`bmnd`, grown on
     demand and reused: the input is copied into one and sent to the device
-    asynchronously, the result comes back through the other.  A lock makes
-    concurrent host threads take turns."""
+    asynchronously, the result comes back through the other.  The host-side
+    copies are split over a few threads (NumPy releases the interpreter lock
+    while it copies), and the upload goes in slices, each slice's transfer
+    overlapping the copy of the next.  A lock makes concurrent host threads
+    take turns."""
+
+    _SLICES = 8
 
     def __init__(self):
         self._lock = threading.Lock()
         self._bufs = {}
+        self._pool = None
 
     def _get(self, key, numel):
         torch = _torch()
@@ -126,25 +132,65 @@ class _Staging:
             self._bufs[key] = buf
         return buf[:numel]
 
+    def _threads(self):
+        if self._pool is None:
+            import os
+            from concurrent.futures import ThreadPoolExecutor
+
+            self._pool = ThreadPoolExecutor(max(1, min(8, os.cpu_count() or 1)), thread_name_prefix="bmnd-copy")
+        return self._pool
+
+    def _copy(self, dst: np.ndarray, src: np.ndarray) -> None:
+        """dst[...] = src over flat float32 arrays, in parallel slices."""
+        n = src.size
+        if n < (1 << 20):
+            np.copyto(dst, src)
+            return
+        parts = self._SLICES
+        step = (n + parts - 1) // parts
+        list(self._threads().map(lambda i: np.copyto(dst[i * step:(i + 1) * step], src[i * step:(i + 1) * step]),
+                                 range(parts)))
+
     def upload(self, arr: np.ndarray):
         torch = _torch()
         with self._lock:
-            host = self._get("in", arr.size)
-            host.numpy().reshape(arr.shape)[...] = arr
+            flat = arr.reshape(-1)
+            host = self._get("in", flat.size)
             dev = torch.empty(arr.shape, dtype=torch.float32, device=torch.cuda.current_device())
-            dev.copy_(host.view(arr.shape), non_blocking=True)
-            # the staging buffer is reused by the next call: wait for the copy
+            dflat = dev.view(-1)
+            n = flat.size
+            parts = self._SLICES if n >= (1 << 22) else 1
+            step = (n + parts - 1) // parts
+            hnp = host.numpy()
+            for i in range(parts):
+                lo, hi = i * step, min(n, (i + 1) * step)
+                if lo >= hi:
+                    break
+                self._copy(hnp[lo:hi], flat[lo:hi])
+                dflat[lo:hi].copy_(host[lo:hi], non_blocking=True)
+            # the staging buffer is reused by the next call: wait for the copies
             torch.cuda.current_stream().synchronize()
         return dev
 
     def download(self, t) -> np.ndarray:
         with self._lock:
-            host = self._get("out", t.numel()).view(t.shape)
-            host.copy_(t)
-            return host.numpy().copy()
+            host = self._get("out", t.numel())
+            host.copy_(t.reshape(-1))
+            out = np.empty(tuple(t.shape), dtype=np.float32)
+            self._copy(out.reshape(-1), host.numpy())
+            return out
 
 
 _STAGING = _Staging()
+_CUDA_READY = None
+
+
+def _cuda_ready() -> bool:
+    """Whether a CUDA device is present (checked once)."""
+    global _CUDA_READY
+    if _CUDA_READY is None:
+        _CUDA_READY = bool(_torch().cuda.is_available())
+    return _CUDA_READY
 
 
 def _host_result(t) -> np.ndarray:
@@ -496,6 +542,7 @@ def bmnd(
     torch_input = type(volume).__module__.startswith("torch")
     shape = tuple(int(s) for s in volume.shape)
     resolved = resolve_profile(profile, shape)
+    uploaded = None  # NumPy float32 input already on the device
     if resolved.is_poisson and sigma_psd is not None:
         raise ValueError(
             "sigma_psd is only supported for stationary additive noise; "
@@ -516,8 +563,14 @@ def bmnd(
         arr = np.asarray(volume)
         if arr.dtype == np.float32 and arr.size:
             # one min and one max pass: NaN propagates through both, so both are
-            # finite exactly when every value is (the same checks, in the same order)
-            lo, hi = float(np.min(arr)), float(np.max(arr))
+            # finite exactly when every value is (the same checks, in the same order).
+            # With a GPU the volume is uploaded first and both are taken there.
+            if _cuda_ready():
+                uploaded = _STAGING.upload(np.ascontiguousarray(arr))
+                mm = _torch().aminmax(uploaded.view(-1))
+                lo, hi = (float(v) for v in _torch().stack([mm.min, mm.max]).cpu())
+            else:
+                lo, hi = float(np.min(arr)), float(np.max(arr))
             if not (np.isfinite(lo) and np.isfinite(hi)):
                 raise ValueError("volume must contain only finite values.")
             vol = arr
@@ -568,6 +621,8 @@ def bmnd(
         dev = dev_vol.contiguous()
         if not dev.is_cuda:
             dev = dev.cuda()
+    elif uploaded is not None:
+        dev = uploaded
     else:
         dev = _STAGING.upload(np.ascontiguousarray(vol))
     maps = None

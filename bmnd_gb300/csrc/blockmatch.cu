@@ -596,8 +596,13 @@ __global__ void __launch_bounds__(kWarps * 32) ssd_select_kernel(MatchArgs a, co
                 bhi = sub_rn(bhi, g);
             }
         };
-        // pass 1: certain accepts and the K-th smallest upper bound among them
-        int acc_size = 0, n_cert = 0;
+        // pass 1: the certain accepts, and V at or above the K-th smallest upper
+        // bound among them: every lane keeps its 4 smallest, and V is the K-th
+        // smallest of the warp's 128 kept values (K <= 32).  At least K certain
+        // accepts have upper bounds <= V, so no candidate whose lower bound
+        // exceeds V can reach the top K.
+        int n_cert = 0;
+        float t0 = INFINITY, t1 = INFINITY, t2 = INFINITY, t3 = INFINITY;
         for (int64_t c = lane; c < window; c += 32) {
             int64_t lin;
             const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
@@ -605,20 +610,61 @@ __global__ void __launch_bounds__(kWarps * 32) ssd_select_kernel(MatchArgs a, co
             bounds(c, origin, blo, bhi);
             if (bhi < thr) {
                 ++n_cert;
-                acc_size = list_insert(my_acc, acc_size, K, composite_key(bhi, static_cast<int32_t>(lin)));
+                if (bhi < t3) {
+                    if (bhi < t2) {
+                        t3 = t2;
+                        if (bhi < t1) {
+                            t2 = t1;
+                            if (bhi < t0) {
+                                t1 = t0;
+                                t0 = bhi;
+                            } else {
+                                t1 = bhi;
+                            }
+                        } else {
+                            t2 = bhi;
+                        }
+                    } else {
+                        t3 = bhi;
+                    }
+                }
             }
         }
-        __syncwarp();
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) n_cert += __shfl_xor_sync(0xffffffffu, n_cert, o);
-        const int n_top = warp_merge(my_acc, acc_size, K, merged, lane);
-        __syncwarp();
         if (n_cert < R) {
             if (lane == 0) a.count[r] = -1;  // may need rejected candidates: the exact kernel redoes it
             __syncwarp();
             continue;
         }
-        const float vkey = n_top >= K ? ordered_float(static_cast<uint32_t>(merged[K - 1] >> 32)) : thr;
+        float vkey = thr;
+        if (n_cert >= K) {
+            // rank of each kept value among all 128, ties ordered by (lane, slot)
+            const float mine[4] = {t0, t1, t2, t3};
+            int rank[4] = {0, 0, 0, 0};
+            for (int sl = 0; sl < 32; ++sl) {
+                float other[4];
+#pragma unroll
+                for (int p = 0; p < 4; ++p) other[p] = __shfl_sync(0xffffffffu, mine[p], sl);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int p = 0; p < 4; ++p)
+                        rank[q] += (other[p] < mine[q] || (other[p] == mine[q] && (sl < lane || (sl == lane && p < q))))
+                                       ? 1 : 0;
+            }
+            float pick = 0.0f;
+            bool has = false;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (rank[q] == K - 1) {
+                    pick = mine[q];
+                    has = true;
+                }
+            const unsigned who = __ballot_sync(0xffffffffu, has);
+            vkey = __shfl_sync(0xffffffffu, pick, __ffs(who) - 1);
+        }
+        int acc_size = 0;
         __syncwarp();
         // pass 2: exact rescoring of every candidate that can matter
         acc_size = 0;

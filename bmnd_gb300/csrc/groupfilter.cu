@@ -47,8 +47,8 @@ constexpr int kThreads = 256;      // threads per group (CTA)
 // shrinkage, so they get a region of their own after the group buffers.
 struct Layout {
     // byte offsets into dynamic shared memory
-    int64_t g, gt, fw, fi, fit, dir, win, mdiag, pos, shf, shl, sg, ex, lag, uni, s, x, r, v, grid, lval, lstart,
-        lent, scan, plane, wts, misc, risk, total;
+    int64_t g, gt, fw, fi, fit, dir, win, mdiag, pos, shf, shl, sg, ex, part, lag, uni, s, x, r, v, grid, lval,
+        lstart, lent, scan, plane, wts, misc, risk, total;
 };
 
 struct FilterArgs {
@@ -108,6 +108,7 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     // hard thresholding with a sigma map keeps each coefficient's sigma until the scatter
     L.sg = take(sigma && !wiener ? 4 * np : 16);
     L.ex = take(4 * static_cast<int64_t>(kmax) * P);
+
     // Gaussian noise: lag index of every member pair (i >= j)
     const bool gauss = sp.noise_model == BMND_NOISE_GAUSSIAN;
     L.lag = take(gauss && kmax > 0 ? 4 * static_cast<int64_t>(nmax) * (nmax + 1) / 2 : 16);
@@ -136,6 +137,15 @@ __host__ Layout make_layout(const BmndStageParams& sp, int P, int nmax, int kmax
     L.lent = L.lstart + round16(4 * (umax + 1));
     const int64_t list_end = L.lent + round16(kl > 0 ? 4 * np : 0);
     off = keep ? list_end : L.uni + (group_bytes > list_end - L.uni ? group_bytes : list_end - L.uni);
+    // exact variance: per-warp partial sums of one tile of 4 planes x 32 JR
+    // coefficients (64 for the half-warp form), added in warp order afterwards;
+    // they take the occupancy grid's place (free once the lists are built) when
+    // it is large enough
+    const int tile_w = kron_jr(P) == 2 ? 64 : 32 * kron_jr(P);
+    const int64_t part_bytes = 4 * (kThreads / 32) * 4 * static_cast<int64_t>(tile_w);
+    if (gauss || kmax <= 0) L.part = L.grid;
+    else if (4 * ucells >= part_bytes) L.part = L.grid;
+    else L.part = take(part_bytes);
     L.total = off;
     return L;
 }
@@ -597,14 +607,76 @@ __device__ void exact_tile(const float* __restrict__ lval, const int* __restrict
     }
 }
 
-// all tiles of (NQ planes) x (32 * JR coefficients); EX[i * P + j] receives the
+// Patches of 33-64 voxels (JR = 2): the two half-warps take alternate voxels
+// of the warp's range and each lane holds 4 coefficients, j = 4 (lane % 16) + r,
+// so an entry costs the same three loads for 4 NQ fused multiply-adds instead of
+// 2 NQ.  The halves' sums are added at the end (lanes l and l + 16 hold the
+// same coefficients).
+template <int NQ>
+__device__ void exact_tile_hw(const float* __restrict__ lval, const int* __restrict__ lstart,
+                              const uint32_t* __restrict__ lent, int u_lo, int u_hi,
+                              const float* __restrict__ GT, int kpad, int i0,
+                              const float* __restrict__ st, float (&var)[4][NQ]) {
+    const int lane = threadIdx.x & 31;
+    const int half = lane >> 4;
+    const float* stl = st + 4 * (lane & 15);
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) var[r][q] = 0.0f;
+    const float* gt0 = GT + i0;
+    for (int u = u_lo + half; u < u_hi; u += 2) {
+        int e = lstart[u];
+        const int e1 = lstart[u + 1];
+        float c[4][NQ];
+        {
+            const uint32_t ent = lent[e];
+            PlaneVec<NQ> gv;
+            gv.load(gt0 + (ent & 0xffu) * kpad);
+            KronVec<4> sv;
+            sv.load(stl + (ent >> 8));
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) c[r][q] = mul_rn(gv.v[q], sv.v[r]);
+        }
+#pragma unroll 2
+        for (++e; e < e1; ++e) {
+            const uint32_t ent = lent[e];
+            PlaneVec<NQ> gv;
+            gv.load(gt0 + (ent & 0xffu) * kpad);
+            KronVec<4> sv;
+            sv.load(stl + (ent >> 8));
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) c[r][q] = fmaf(gv.v[q], sv.v[r], c[r][q]);
+        }
+        const float v = lval[u];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) var[r][q] = fmaf(mul_rn(v, c[r][q]), c[r][q], var[r][q]);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) var[r][q] = add_rn(var[r][q], __shfl_xor_sync(0xffffffffu, var[r][q], 16));
+}
+
+// all tiles of (NQ planes) x (TW coefficients); EX[i * P + j] receives the
 // standard deviation sqrt(max(var, 0)) of planes i < kk.  NQ = 4 in general;
-// groups with fewer exact planes (k < 4, or fewer members) use NQ = kk.
+// groups with fewer exact planes (k < 4, or fewer members) use NQ = kk.  Each
+// warp leaves its partial sums in `part`; after one barrier every thread adds
+// the warps' partials of its (plane, coefficient) pairs in warp order.
 template <int JR, int NQ>
 __device__ void exact_planes(const float* __restrict__ lval, const int* __restrict__ lstart,
                              const uint32_t* __restrict__ lent, int U, const float* __restrict__ GT,
                              int kpad, int kk, const float* __restrict__ st, int P,
-                             float* __restrict__ EX) {
+                             float* __restrict__ EX, float* __restrict__ part) {
+    constexpr bool kHalf = JR == 2;
+    constexpr int RL = kHalf ? 4 : JR;       // coefficients per lane
+    constexpr int TW = kHalf ? 64 : 32 * JR;  // coefficients per tile
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nw = blockDim.x >> 5;
     // voxel range of this warp: voxels whose first entry lies in its entry share
@@ -620,28 +692,30 @@ __device__ void exact_planes(const float* __restrict__ lval, const int* __restri
     };
     const int u_lo = first_voxel(static_cast<int>(static_cast<int64_t>(E) * warp / nw));
     const int u_hi = warp == nw - 1 ? U : first_voxel(static_cast<int>(static_cast<int64_t>(E) * (warp + 1) / nw));
+    const int jl = kHalf ? 4 * (lane & 15) : JR * lane;
+    const bool writer = !kHalf || lane < 16;
     for (int i0 = 0; i0 < kk; i0 += NQ) {
-        for (int j0 = 0; j0 < P; j0 += 32 * JR) {
-            float var[JR][NQ];
-            exact_tile<JR, NQ>(lval, lstart, lent, u_lo, u_hi, GT, kpad, i0, st, j0, var);
-            for (int w = 0; w < nw; ++w) {
-                if (warp == w) {
+        for (int j0 = 0; j0 < P; j0 += TW) {
+            float var[RL][NQ];
+            if constexpr (kHalf) exact_tile_hw<NQ>(lval, lstart, lent, u_lo, u_hi, GT, kpad, i0, st, var);
+            else exact_tile<JR, NQ>(lval, lstart, lent, u_lo, u_hi, GT, kpad, i0, st, j0, var);
+            if (writer) {
 #pragma unroll
-                    for (int r = 0; r < JR; ++r) {
-                        const int j = j0 + JR * lane + r;
+                for (int q = 0; q < NQ; ++q)
 #pragma unroll
-                        for (int q = 0; q < NQ; ++q) {
-                            const int i = i0 + q;
-                            if (j < P && i < kk) {
-                                float t = w == 0 ? var[r][q] : add_rn(EX[i * P + j], var[r][q]);
-                                if (w == nw - 1) t = sqrtf(t > 0.0f ? t : 0.0f);
-                                EX[i * P + j] = t;
-                            }
-                        }
-                    }
-                }
-                __syncthreads();
+                    for (int r = 0; r < RL; ++r) part[(warp * NQ + q) * TW + jl + r] = var[r][q];
             }
+            __syncthreads();
+            for (int t = threadIdx.x; t < NQ * TW; t += blockDim.x) {
+                const int q = t / TW, jj = t - q * TW;
+                const int i = i0 + q, j = j0 + jj;
+                if (i < kk && j < P) {
+                    float v = part[q * TW + jj];
+                    for (int w = 1; w < nw; ++w) v = add_rn(v, part[(w * NQ + q) * TW + jj]);
+                    EX[i * P + j] = sqrtf(v > 0.0f ? v : 0.0f);
+                }
+            }
+            __syncthreads();
         }
     }
 }
@@ -650,10 +724,10 @@ template <int JR>
 __device__ void exact_planes_any(const float* __restrict__ lval, const int* __restrict__ lstart,
                                  const uint32_t* __restrict__ lent, int U, const float* __restrict__ GT,
                                  int kpad, int kk, const float* __restrict__ st, int P,
-                                 float* __restrict__ EX) {
-    if (kk == 1) exact_planes<JR, 1>(lval, lstart, lent, U, GT, kpad, kk, st, P, EX);
-    else if (kk == 2) exact_planes<JR, 2>(lval, lstart, lent, U, GT, kpad, kk, st, P, EX);
-    else exact_planes<JR, 4>(lval, lstart, lent, U, GT, kpad, kk, st, P, EX);
+                                 float* __restrict__ EX, float* __restrict__ part) {
+    if (kk == 1) exact_planes<JR, 1>(lval, lstart, lent, U, GT, kpad, kk, st, P, EX, part);
+    else if (kk == 2) exact_planes<JR, 2>(lval, lstart, lent, U, GT, kpad, kk, st, P, EX, part);
+    else exact_planes<JR, 4>(lval, lstart, lent, U, GT, kpad, kk, st, P, EX, part);
 }
 
 // Exact noise risk of the first kk planes (wiener.py:638-711, :505-535; the
@@ -792,7 +866,7 @@ __device__ void exact_risk_any(const float* __restrict__ lval, const int* __rest
 }
 
 template <int ND, int B0, int B1, int B2, int NT>
-__global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) group_filter_kernel(FilterArgs a) {
+__global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) group_filter_kernel(FilterArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     using GM = Geom<ND, B0, B1, B2>;
     const BmndStageParams& sp = a.sp;
@@ -1107,12 +1181,14 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND == 3 ? 3 : 2) : 1) gr
         if (gauss) {
             // sigma comes from the covariance maps
         } else if constexpr (ND > 0) {
-            exact_planes_any<kron_jr(B0 * B1 * B2)>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
+            exact_planes_any<kron_jr(B0 * B1 * B2)>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX,
+                                                    sm<float>(smem, a.L.part));
         } else {
             const int jr = kron_jr(P);
-            if (jr == 1) exact_planes_any<1>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
-            else if (jr == 2) exact_planes_any<2>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
-            else exact_planes_any<4>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX);
+            float* part = sm<float>(smem, a.L.part);
+            if (jr == 1) exact_planes_any<1>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX, part);
+            else if (jr == 2) exact_planes_any<2>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX, part);
+            else exact_planes_any<4>(lval, lstart, lent, U, GT, kpad, kk, a.st, P, EX, part);
         }
     }
 

@@ -79,6 +79,36 @@ def blobs_2d(size: int = 2048, seed: int = 0, n_blobs: int = 40, n_rects: int = 
     return clean, poisson_noise(clean, seed)
 
 
+def blobs_2d_window(size: int = 256, seed: int = 0, full: int = 2048, n_blobs: int = 40, n_rects: int = 60):
+    """A ``size`` x ``size`` window of a ``full`` x ``full`` phantom of the
+    ``blobs_2d`` kind (the same object sizes and counts), at a random offset,
+    scaled so that the window's peak is log-uniform in [1, 100] counts.  Only
+    the window is evaluated, so thousands of them are cheap."""
+    rng = np.random.default_rng(seed)
+    oy, ox = rng.integers(0, full - size + 1, size=2)
+    ys = np.arange(oy, oy + size, dtype=np.float64)
+    xs = np.arange(ox, ox + size, dtype=np.float64)
+    clean = np.zeros((size, size), dtype=np.float64)
+    for _ in range(n_blobs):
+        cy, cx = rng.uniform(0, full, size=2)
+        sigma = rng.uniform(10.0, 80.0)
+        amp = rng.uniform(0.2, 1.0)
+        clean += amp * np.outer(np.exp(-0.5 * ((ys - cy) / sigma) ** 2), np.exp(-0.5 * ((xs - cx) / sigma) ** 2))
+    for _ in range(n_rects):
+        cy, cx = rng.uniform(0, full, size=2)
+        hy, hx = rng.uniform(4.0, 96.0, size=2)
+        amp = rng.uniform(0.1, 0.6)
+        y0, y1 = int(max(cy - hy - oy, 0)), int(min(cy + hy - oy, size))
+        x0, x1 = int(max(cx - hx - ox, 0)), int(min(cx + hx - ox, size))
+        if y1 > y0 and x1 > x0:
+            clean[y0:y1, x0:x1] += amp
+    clean += 1e-3  # a window that misses every object is a flat low-count field
+    peak = float(np.exp(rng.uniform(np.log(1.0), np.log(100.0))))
+    clean *= peak / float(clean.max())
+    clean = clean.astype(np.float32)
+    return clean, poisson_noise(clean, seed)
+
+
 def ellipsoids_3d(
     size: int | tuple[int, int, int] = 256,
     seed: int = 0,

@@ -267,15 +267,18 @@ def training_pairs(kind: str = "bm4d", size: int = 128, count: int = 8, seed0: i
     """(noisy, plain stage-1 estimate) CUDA pairs on seeded phantoms (seeds
     seed0 .. seed0 + count - 1, disjoint from the benchmark's).  ``kind``
     "bm4d_lowcount" scales each ellipsoid volume to a peak of
-    ``lowcount_peak(seed)`` counts."""
+    ``lowcount_peak(seed)`` counts; "bm3d_windows" takes ``size``-square
+    windows of 2048^2 blob phantoms (``phantoms.blobs_2d_window``)."""
     torch = _torch()
     import bmnd_gb300 as bg
 
     if profile is None:
-        profile = (bg.BM3DProfile if kind == "bm3d" else bg.BM4DProfile)(noise_model=bg.NoiseModel.POISSON)
+        profile = (bg.BM3DProfile if kind.startswith("bm3d") else bg.BM4DProfile)(noise_model=bg.NoiseModel.POISSON)
     pairs = []
     for i in range(count):
-        if kind == "bm4d_lowcount":
+        if kind == "bm3d_windows":
+            _, noisy = phantoms.blobs_2d_window(size, seed=seed0 + i)
+        elif kind == "bm4d_lowcount":
             _, noisy = phantoms.ellipsoids_3d(size, seed=seed0 + i, peak=lowcount_peak(seed0 + i))
         elif kind == "bm4d":
             _, noisy = phantoms.ellipsoids_3d(size, seed=seed0 + i)

@@ -18,10 +18,12 @@ import time
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kind", default="bm4d", choices=["bm4d", "bm3d", "bm4d_lowcount"])
+    ap.add_argument("--kind", default="bm4d", choices=["bm4d", "bm3d", "bm4d_lowcount", "bm3d_windows"])
     ap.add_argument("--seed0", type=int, default=1000, help="first training phantom seed")
     ap.add_argument("--eval-uneven", action="store_true",
                     help="only evaluate the saved net on eight uneven volumes (128^3 .. 320^3)")
+    ap.add_argument("--eval-images", type=int, default=0, metavar="N",
+                    help="only evaluate the saved 2-D net on the 2048^2 benchmark images of seeds 0 .. N-1")
     ap.add_argument("--size", type=int, default=None)
     ap.add_argument("--count", type=int, default=8)
     ap.add_argument("--steps", type=int, default=3000)
@@ -44,9 +46,12 @@ def main(argv=None):
                                   lowcount_peak, training_pairs)
 
     torch.cuda.set_device(0)
-    nd = 2 if args.kind == "bm3d" else 3
+    nd = 2 if args.kind.startswith("bm3d") else 3
     if args.eval_uneven:
         evaluate_uneven(args.kind, args.out or default_net_path(args.kind))
+        return
+    if args.eval_images:
+        evaluate_images(args.out or default_net_path(args.kind), args.eval_images)
         return
     channels = args.channels or (48 if nd == 3 else 32)
     layers = args.layers or (8 if nd == 3 else 10)
@@ -78,6 +83,8 @@ def main(argv=None):
     prof = (bg.BM4DProfile if nd == 3 else bg.BM3DProfile)(noise_model=bg.NoiseModel.POISSON)
     if args.kind == "bm4d_lowcount":
         clean, noisy = phantoms.ellipsoids_3d(args.size, seed=2000, peak=lowcount_peak(2000))
+    elif args.kind == "bm3d_windows":
+        clean, noisy = phantoms.blobs_2d(2048, seed=2000)  # trained on windows, evaluated on a full image
     elif nd == 3:
         clean, noisy = phantoms.ellipsoids_3d(args.size, seed=2000)
     elif args.size >= 1024:
@@ -177,6 +184,50 @@ def evaluate_uneven(kind: str, weights: str) -> list:
         print(json.dumps(row), flush=True)
         del x, plain, fast
         torch.cuda.empty_cache()
+    return rows
+
+
+def evaluate_images(weights: str, count: int, size: int = 2048) -> list:
+    """The 2-D fast path with the net in ``weights`` against the plain path on
+    the benchmark's blob images (seeds 0 .. count-1): PSNR of both against the
+    clean image, the tiles that fell back, and the time of each (CUDA events,
+    one warm-up call, the best of three).  One JSON line per image."""
+    import torch
+
+    import bmnd_gb300 as bg
+    from bmnd_gb300 import phantoms
+    from bmnd_gb300.pilot import PilotNet, bmnd_fast
+
+    net = PilotNet.load(weights)
+    prof = bg.BM3DProfile(noise_model=bg.NoiseModel.POISSON)
+    rows = []
+
+    def timed(fn):
+        r = fn()
+        best = float("inf")
+        for _ in range(3):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return r, best
+
+    for seed in range(count):
+        clean, noisy = phantoms.blobs_2d(size, seed=seed)
+        x = torch.from_numpy(noisy).cuda()
+        plain, ms_plain = timed(lambda: bg.bmnd_device(x, prof))
+        d = {}
+        fast, ms_fast = timed(lambda: bmnd_fast(x, prof, net, details=d))
+        p_plain = phantoms.psnr(plain.cpu().numpy(), clean)
+        p_fast = phantoms.psnr(fast.cpu().numpy(), clean)
+        row = dict(seed=seed, psnr_noisy=phantoms.psnr(noisy, clean), psnr_plain=p_plain, psnr_fast=p_fast,
+                   fast_minus_plain_db=p_fast - p_plain, fallback_tiles=d["fallback_tiles"], tiles=d["tiles"],
+                   ms_plain=ms_plain, ms_fast=ms_fast, speedup=ms_plain / ms_fast)
+        rows.append(row)
+        print(json.dumps(row), flush=True)
     return rows
 
 

@@ -89,14 +89,26 @@ def _stage_setup(kind, shape, stage):
 def _isolated_filtering(oracle_lib, tag, p, noisy, pilot, refs, sel, cnt, gpu_est):
     """The oracle's filtering on the GPU's match sets: max abs error against the
     float32 restatement, and the float64 per-stage error."""
-    o32 = oracle_lib.stage(p, noisy, pilot, refs, sel=sel, count=cnt)[0]
+    o32, _, _, _, marg = oracle_lib.stage(p, noisy, pilot, refs, sel=sel, count=cnt, margins=True)
     o64 = oracle_lib.stage(p, noisy, pilot, refs, sel=sel, count=cnt, f64=True)[0]
     err32 = max_abs_outside(gpu_est, o32)
     err_gpu64 = max_abs_outside(gpu_est, o64)
     err_ref64 = max_abs_outside(o32, o64)
     print(f"{tag}: max|gpu-oracle32|={err32:.3e} max|gpu-oracle64|={err_gpu64:.3e} "
           f"max|oracle32-oracle64|={err_ref64:.3e}")
-    assert err32 <= TOL, (tag, err32)
+    if err32 > TOL:
+        # a hard-threshold decision within float32 rounding of its boundary
+        # (relative margin <= 1e-5) may go either way in two float32
+        # evaluations: outside those groups' footprint the bar holds, and
+        # everywhere the GPU must stay within it of the float64 oracle
+        block = tuple(int(p.block[a]) for a in range(p.ndim))
+        near = np.flatnonzero(marg <= 1e-5)
+        foot = group_footprint(noisy.shape, block, sel, cnt, near)
+        err32_out = max_abs_outside(gpu_est, o32, foot)
+        print(f"{tag}: {near.size} groups with a decision at its threshold; outside them "
+              f"max|gpu-oracle32|={err32_out:.3e}")
+        assert err32_out <= TOL, (tag, err32_out)
+        assert err_gpu64 <= TOL, (tag, err_gpu64)
     assert err_gpu64 <= max(2.0 * err_ref64, 1e-5), (tag, err_gpu64, err_ref64)
     return o32
 
