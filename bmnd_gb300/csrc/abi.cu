@@ -347,7 +347,10 @@ int32_t run_stage(const BmndStageParams& sp, const float* noisy, const float* pi
     BmndMatchParams mp = match_params_of(sp);
     const bool on_pilot = sp.filter == BMND_FILTER_WIENER && sp.wiener_match_source == BMND_SOURCE_PILOT;
     const float* match_src = on_pilot ? pilot : noisy;
-    if (on_pilot && sp.match_precision == BMND_MATCH_EXACT) mp.precision = BMND_MATCH_REAL_VALUED;
+    // the real-valued pilot: the bounded screening of the Poisson deviance
+    // (SSD matching keeps its tensor-core screening, which any values suit)
+    if (on_pilot && sp.match_precision == BMND_MATCH_EXACT && sp.distance != BMND_DIST_SSD)
+        mp.precision = BMND_MATCH_REAL_VALUED;
     const float* thr_dev = nullptr;
     if (sp.distance == BMND_DIST_SSD) {
         rc = launch_ssd_threshold(match_src, static_cast<int64_t>(vox), sp.ssd_threshold, w.mm, w.thr, stream);

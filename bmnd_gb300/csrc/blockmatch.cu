@@ -311,6 +311,48 @@ __device__ __forceinline__ int64_t window_origin(const MatchArgs& a, const int* 
     return origin;
 }
 
+// window_origin, plus the index of the candidate's offset in a table over the
+// search offsets (C order over 2 radius + 1 per axis), from the reference's
+// patch-grid coordinates rc
+__device__ __forceinline__ int64_t window_origin_offset(const MatchArgs& a, const int* lo, const int* ext,
+                                                        const float* inv_ext, bool small_window, int64_t c,
+                                                        const int* rc, int64_t* lin_out, int* gidx_out) {
+    int coord[BMND_MAX_DIMS] = {0, 0, 0};
+    if (small_window) {
+        int rem = static_cast<int>(c);
+#pragma unroll
+        for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+            if (d < a.ndim) {
+                const int q = d > 0 ? small_div(rem, inv_ext[d]) : 0;
+                coord[d] = lo[d] + rem - q * ext[d];
+                rem = q;
+            }
+        }
+    } else {
+        int64_t rem = c;
+#pragma unroll
+        for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+            if (d < a.ndim) {
+                coord[d] = lo[d] + static_cast<int>(rem % ext[d]);
+                rem /= ext[d];
+            }
+        }
+    }
+    int64_t lin = 0, origin = 0;
+    int gidx = 0;
+#pragma unroll
+    for (int d = 0; d < BMND_MAX_DIMS; ++d) {
+        if (d < a.ndim) {
+            lin = lin * a.counts[d] + coord[d];
+            origin += static_cast<int64_t>(coord[d]) * a.grid_stride[d];
+            gidx = gidx * (2 * a.radius[d] + 1) + (coord[d] - rc[d] + a.radius[d]);
+        }
+    }
+    *lin_out = lin;
+    *gidx_out = gidx;
+    return origin;
+}
+
 template <int CODE>
 __global__ void __launch_bounds__(kWarps * 32) blockmatch_kernel(MatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -546,10 +588,12 @@ __global__ void __launch_bounds__(kWarps * 32) ssd_select_kernel(MatchArgs a, co
         int lo[BMND_MAX_DIMS] = {0, 0, 0}, ext[BMND_MAX_DIMS] = {1, 1, 1};
         float inv_ext[BMND_MAX_DIMS] = {1.0f, 1.0f, 1.0f};
         int64_t center_lin = 0, center_origin = 0, window = 1;
+        int rc[BMND_MAX_DIMS] = {0, 0, 0};
 #pragma unroll
         for (int d = 0; d < BMND_MAX_DIMS; ++d) {
             if (d < a.ndim) {
                 const int cd = a.refs[r * a.ndim + d];
+                rc[d] = cd;
                 center_lin = center_lin * a.counts[d] + cd;
                 center_origin += static_cast<int64_t>(cd) * a.grid_stride[d];
                 const int l = max(cd - a.radius[d], 0);
@@ -573,7 +617,7 @@ __global__ void __launch_bounds__(kWarps * 32) ssd_select_kernel(MatchArgs a, co
         // the bounds of candidate c, with the noise-bias correction of its offset:
         // the products' error scales with the centred norms, the cancellation in
         // the centred norms with the raw sums of squares
-        auto bounds = [&](int64_t c, int64_t origin, float& blo, float& bhi) {
+        auto bounds = [&](int64_t c, int64_t origin, int gidx, float& blo, float& bhi) {
             const float nb2 = __ldg(norms + origin);
             const float nb = centred_norm(nb2, __ldg(sums + origin), mu, P);
             const float del = fmaf(kSsdBoundRel, na + nb, fmaf(kSsdBoundCancel, na2 + nb2 + pmu2, kSsdBoundAbs));
@@ -581,16 +625,6 @@ __global__ void __launch_bounds__(kWarps * 32) ssd_select_kernel(MatchArgs a, co
             blo = dv - del;
             bhi = dv + del;
             if (a.noise_ssd) {
-                int64_t rem = c, gidx = 0, mul = 1;
-#pragma unroll
-                for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
-                    if (d < a.ndim) {
-                        const int cd = lo[d] + static_cast<int>(rem % ext[d]);
-                        rem /= ext[d];
-                        gidx += (cd - a.refs[r * a.ndim + d] + a.radius[d]) * mul;
-                        mul *= 2 * a.radius[d] + 1;
-                    }
-                }
                 const float g = mul_rn(a.gamma, __ldg(a.noise_ssd + gidx));
                 blo = sub_rn(blo, g);  // rounding is monotone: the bounds stay bounds
                 bhi = sub_rn(bhi, g);
@@ -605,9 +639,10 @@ __global__ void __launch_bounds__(kWarps * 32) ssd_select_kernel(MatchArgs a, co
         float t0 = INFINITY, t1 = INFINITY, t2 = INFINITY, t3 = INFINITY;
         for (int64_t c = lane; c < window; c += 32) {
             int64_t lin;
-            const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
+            int gidx;
+            const int64_t origin = window_origin_offset(a, lo, ext, inv_ext, small_window, c, rc, &lin, &gidx);
             float blo, bhi;
-            bounds(c, origin, blo, bhi);
+            bounds(c, origin, gidx, blo, bhi);
             if (bhi < thr) {
                 ++n_cert;
                 if (bhi < t3) {
@@ -671,25 +706,14 @@ __global__ void __launch_bounds__(kWarps * 32) ssd_select_kernel(MatchArgs a, co
         int acc_open = 0;
         for (int64_t c = lane; c < window; c += 32) {
             int64_t lin;
-            const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, c, &lin);
+            int gidx;
+            const int64_t origin = window_origin_offset(a, lo, ext, inv_ext, small_window, c, rc, &lin, &gidx);
             float blo, bhi;
-            bounds(c, origin, blo, bhi);
+            bounds(c, origin, gidx, blo, bhi);
             const bool certain = bhi < thr;
             if (!(blo < thr) || (certain && blo > vkey)) continue;
             float dist = patch_distance<BMND_DIST_SSD>(ref_s, a.src, origin, poff_s, P, 1.0f);
-            if (a.noise_ssd) {
-                int64_t rem = c, gidx = 0, mul = 1;
-#pragma unroll
-                for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
-                    if (d < a.ndim) {
-                        const int cd = lo[d] + static_cast<int>(rem % ext[d]);
-                        rem /= ext[d];
-                        gidx += (cd - a.refs[r * a.ndim + d] + a.radius[d]) * mul;
-                        mul *= 2 * a.radius[d] + 1;
-                    }
-                }
-                dist = sub_rn(dist, mul_rn(a.gamma, __ldg(a.noise_ssd + gidx)));
-            }
+            if (a.noise_ssd) dist = sub_rn(dist, mul_rn(a.gamma, __ldg(a.noise_ssd + gidx)));
             if (dist < thr) {
                 if (!certain) ++acc_open;
                 acc_size = list_insert(my_acc, acc_size, K, composite_key(dist, static_cast<int32_t>(lin)));

@@ -558,6 +558,73 @@ struct PlaneVec {
     }
 };
 
+// The warp's (or half-warp's) voxels [u_lo, u_hi) are walked as one stream of
+// entries: an entry adds G[i, g] S[j, p] to the running c of its voxel, and the
+// first entry of the next voxel first folds V_u c^2 into var.  The loads of
+// entry e + 1 are issued before the multiply-adds of entry e, and its entry
+// word one step earlier, so the shared-memory and L1 latencies overlap the
+// arithmetic across voxel boundaries.  Lane l holds RL coefficients starting
+// at j0 + jl (jl = RL l, or RL (l % 16) for the half-warp form).
+template <int RL, int NQ>
+__device__ __forceinline__ void exact_stream(const float* __restrict__ lval, const int* __restrict__ lstart,
+                                             const uint32_t* __restrict__ lent, int u_lo, int u_hi,
+                                             const float* __restrict__ gt0, int kpad,
+                                             const float* __restrict__ stl, float (&var)[RL][NQ]) {
+#pragma unroll
+    for (int r = 0; r < RL; ++r)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) var[r][q] = 0.0f;
+    if (u_lo >= u_hi) return;
+    int e = lstart[u_lo];
+    const int e_end = lstart[u_hi];
+    int u = u_lo;
+    int next_start = lstart[u + 1];
+    float v = lval[u];
+    float c[RL][NQ];
+#pragma unroll
+    for (int r = 0; r < RL; ++r)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) c[r][q] = 0.0f;
+    uint32_t ent1 = lent[e];
+    PlaneVec<NQ> g0;
+    KronVec<RL> s0;
+    g0.load(gt0 + (ent1 & 0xffu) * kpad);
+    s0.load(stl + (ent1 >> 8));
+    ent1 = lent[e + 1 < e_end ? e + 1 : e];
+    for (; e < e_end; ++e) {
+        // loads of entry e + 1 (harmless repeats of the last entry at the end)
+        PlaneVec<NQ> g1;
+        KronVec<RL> s1;
+        g1.load(gt0 + (ent1 & 0xffu) * kpad);
+        s1.load(stl + (ent1 >> 8));
+        const uint32_t ent2 = lent[e + 2 < e_end ? e + 2 : e_end - 1];
+        if (e == next_start) {
+#pragma unroll
+            for (int r = 0; r < RL; ++r)
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) {
+                    var[r][q] = fmaf(mul_rn(v, c[r][q]), c[r][q], var[r][q]);
+                    c[r][q] = 0.0f;
+                }
+            ++u;
+            v = lval[u];
+            next_start = lstart[u + 1];
+        }
+        // the voxel's first entry: fma(g, s, 0) is the rounded product
+#pragma unroll
+        for (int r = 0; r < RL; ++r)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) c[r][q] = fmaf(g0.v[q], s0.v[r], c[r][q]);
+        g0 = g1;
+        s0 = s1;
+        ent1 = ent2;
+    }
+#pragma unroll
+    for (int r = 0; r < RL; ++r)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) var[r][q] = fmaf(mul_rn(v, c[r][q]), c[r][q], var[r][q]);
+}
+
 // one tile of NQ planes x 32 JR coefficients over the warp's voxels
 template <int JR, int NQ>
 __device__ void exact_tile(const float* __restrict__ lval, const int* __restrict__ lstart,
@@ -565,52 +632,13 @@ __device__ void exact_tile(const float* __restrict__ lval, const int* __restrict
                            const float* __restrict__ GT, int kpad, int i0,
                            const float* __restrict__ st, int j0, float (&var)[JR][NQ]) {
     const int lane = threadIdx.x & 31;
-    const float* stl = st + j0 + JR * lane;
-#pragma unroll
-    for (int r = 0; r < JR; ++r)
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) var[r][q] = 0.0f;
-    const float* gt0 = GT + i0;
-    for (int u = u_lo; u < u_hi; ++u) {
-        int e = lstart[u];
-        const int e1 = lstart[u + 1];
-        float c[JR][NQ];
-        {
-            // first entry: the product itself (every voxel has at least one)
-            const uint32_t ent = lent[e];
-            PlaneVec<NQ> gv;
-            gv.load(gt0 + (ent & 0xffu) * kpad);
-            KronVec<JR> sv;
-            sv.load(stl + (ent >> 8));
-#pragma unroll
-            for (int r = 0; r < JR; ++r)
-#pragma unroll
-                for (int q = 0; q < NQ; ++q) c[r][q] = mul_rn(gv.v[q], sv.v[r]);
-        }
-#pragma unroll 2
-        for (++e; e < e1; ++e) {
-            const uint32_t ent = lent[e];
-            PlaneVec<NQ> gv;
-            gv.load(gt0 + (ent & 0xffu) * kpad);
-            KronVec<JR> sv;
-            sv.load(stl + (ent >> 8));
-#pragma unroll
-            for (int r = 0; r < JR; ++r)
-#pragma unroll
-                for (int q = 0; q < NQ; ++q) c[r][q] = fmaf(gv.v[q], sv.v[r], c[r][q]);
-        }
-        const float v = lval[u];
-#pragma unroll
-        for (int r = 0; r < JR; ++r)
-#pragma unroll
-            for (int q = 0; q < NQ; ++q) var[r][q] = fmaf(mul_rn(v, c[r][q]), c[r][q], var[r][q]);
-    }
+    exact_stream<JR, NQ>(lval, lstart, lent, u_lo, u_hi, GT + i0, kpad, st + j0 + JR * lane, var);
 }
 
-// Patches of 33-64 voxels (JR = 2): the two half-warps take alternate voxels
-// of the warp's range and each lane holds 4 coefficients, j = 4 (lane % 16) + r,
-// so an entry costs the same three loads for 4 NQ fused multiply-adds instead of
-// 2 NQ.  The halves' sums are added at the end (lanes l and l + 16 hold the
+// Patches of 33-64 voxels (JR = 2): the two half-warps take the two halves of
+// the warp's voxels and each lane holds 4 coefficients, j = 4 (lane % 16) + r,
+// so an entry costs the same three loads for 4 NQ fused multiply-adds instead
+// of 2 NQ.  The halves' sums are added at the end (lanes l and l + 16 hold the
 // same coefficients).
 template <int NQ>
 __device__ void exact_tile_hw(const float* __restrict__ lval, const int* __restrict__ lstart,
@@ -619,45 +647,17 @@ __device__ void exact_tile_hw(const float* __restrict__ lval, const int* __restr
                               const float* __restrict__ st, float (&var)[4][NQ]) {
     const int lane = threadIdx.x & 31;
     const int half = lane >> 4;
-    const float* stl = st + 4 * (lane & 15);
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) var[r][q] = 0.0f;
-    const float* gt0 = GT + i0;
-    for (int u = u_lo + half; u < u_hi; u += 2) {
-        int e = lstart[u];
-        const int e1 = lstart[u + 1];
-        float c[4][NQ];
-        {
-            const uint32_t ent = lent[e];
-            PlaneVec<NQ> gv;
-            gv.load(gt0 + (ent & 0xffu) * kpad);
-            KronVec<4> sv;
-            sv.load(stl + (ent >> 8));
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int q = 0; q < NQ; ++q) c[r][q] = mul_rn(gv.v[q], sv.v[r]);
-        }
-#pragma unroll 2
-        for (++e; e < e1; ++e) {
-            const uint32_t ent = lent[e];
-            PlaneVec<NQ> gv;
-            gv.load(gt0 + (ent & 0xffu) * kpad);
-            KronVec<4> sv;
-            sv.load(stl + (ent >> 8));
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int q = 0; q < NQ; ++q) c[r][q] = fmaf(gv.v[q], sv.v[r], c[r][q]);
-        }
-        const float v = lval[u];
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-            for (int q = 0; q < NQ; ++q) var[r][q] = fmaf(mul_rn(v, c[r][q]), c[r][q], var[r][q]);
+    // split at the first voxel whose entries start in the second half of the entries
+    const int e_mid = (lstart[u_lo] + lstart[u_hi]) >> 1;
+    int lo = u_lo, hi = u_hi;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (lstart[mid] < e_mid) lo = mid + 1;
+        else hi = mid;
     }
+    const int u_mid = lo;
+    exact_stream<4, NQ>(lval, lstart, lent, half ? u_mid : u_lo, half ? u_hi : u_mid, GT + i0, kpad,
+                        st + 4 * (lane & 15), var);
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
