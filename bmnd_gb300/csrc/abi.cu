@@ -255,8 +255,8 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
     uint64_t o_cnt = take(4ull * n_refs);
     uint64_t o_acc = take(4ull * n_refs);
     const uint64_t P = static_cast<uint64_t>(patch_volume(sp));
-    // the Kronecker table, then the risk metric SM (exact risk weights)
-    uint64_t o_st = take(8ull * P * static_cast<uint64_t>(kron_stride(static_cast<int>(P))));
+    // the Kronecker table, the risk metric SM (exact risk weights), the group matrices
+    uint64_t o_st = take(4ull * stage_table_floats(static_cast<int>(P)));
     uint64_t o_mm = take(16);
     uint64_t o_tr = take(sp.match_policy == BMND_POLICY_REFERENCE_FINITE_COUNT ? 4ull * n_refs : 16);
     const BmndMatchParams mp = match_params_of(sp);
@@ -656,8 +656,8 @@ int32_t bmnd_group_probe_workspace_bytes(const BmndStageParams* params, uint64_t
     if (!params || !out_bytes) return fail(BMND_ERR_INVALID_ARG, "null argument");
     if (int32_t rc = validate_stage(*params)) return rc;
     const uint64_t P = static_cast<uint64_t>(patch_volume(*params));
-    // the Kronecker table and the risk metric, then the status word
-    *out_bytes = align256(8ull * P * static_cast<uint64_t>(kron_stride(static_cast<int>(P)))) + 256;
+    // the Kronecker table, the risk metric and the group matrices, then the status word
+    *out_bytes = align256(4ull * stage_table_floats(static_cast<int>(P))) + 256;
     return BMND_OK;
 }
 

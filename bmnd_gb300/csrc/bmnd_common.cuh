@@ -153,6 +153,12 @@ __host__ __device__ inline float group_entry(int kind, int n, int i, int g) {
     return dct_entry(n, i, g);
 }
 
+// the n x n group matrices of every group size n = 1 .. BMND_MAX_STACK, one
+// after another (group n starts at group_table_offset(n)), as a table the
+// filter copies instead of evaluating group_entry per CTA
+__host__ __device__ constexpr int group_table_offset(int n) { return (n - 1) * n * (2 * n - 1) / 6; }
+constexpr int kGroupTableFloats = group_table_offset(BMND_MAX_STACK + 1);
+
 // exact float32 operations that the compiler must not contract into FMAs
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
@@ -185,6 +191,10 @@ inline int patch_volume(const BmndStageParams& p) {
 __host__ __device__ constexpr int kron_jr(int P) { return P <= 32 ? 1 : (P <= 64 ? 2 : 4); }
 __host__ __device__ constexpr int kron_stride(int P) {
     return (P + 32 * kron_jr(P) - 1) / (32 * kron_jr(P)) * (32 * kron_jr(P));
+}
+// floats of the per-stage table region: Kronecker table, risk metric, group matrices
+inline uint64_t stage_table_floats(int P) {
+    return 2ull * static_cast<uint64_t>(P) * static_cast<uint64_t>(kron_stride(P)) + kGroupTableFloats;
 }
 
 // Launch shape of `fn` with `threads` threads and `smem` bytes of dynamic

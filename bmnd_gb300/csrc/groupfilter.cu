@@ -923,7 +923,10 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
         if (tid == 0 && a.err) atomicExch(a.err, 2);
         return;
     }
-    for (int e = tid; e < n * n; e += blockDim.x) G[e] = group_entry(sp.group_transform, n, e / n, e % n);
+    {
+        const float* gtab = a.st + 2 * static_cast<int64_t>(P) * kron_stride(P) + group_table_offset(n);
+        for (int e = tid; e < n * n; e += blockDim.x) G[e] = __ldg(gtab + e);
+    }
     for (int e = tid; e < BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE; e += blockDim.x) {
         Fw[e] = sp.spatial_fwd[e / (BMND_MAX_EDGE * BMND_MAX_EDGE)][e % (BMND_MAX_EDGE * BMND_MAX_EDGE)];
         Fi[e] = sp.spatial_inv[e / (BMND_MAX_EDGE * BMND_MAX_EDGE)][e % (BMND_MAX_EDGE * BMND_MAX_EDGE)];
@@ -1215,30 +1218,43 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
     } else if (k > 0 && kk == n) {
         for (int e = tid; e < total; e += blockDim.x) S[e] = EX[e];
     } else if (k > 0) {
-        for (int j = tid; j < P; j += blockDim.x) {
+        // TPJ threads per coefficient j (neighbouring lanes), each summing the
+        // planes i = sub (mod TPJ); the partial sums are added by shuffles in
+        // a fixed order, and each thread rescales its own planes
+        const int TPJ = P <= 64 ? 4 : (P <= 128 ? 2 : 1);
+        for (int base = 0; base < P * TPJ; base += blockDim.x) {
+            const int t = base + tid;
+            const int j = t / TPJ, sub = t - j * TPJ;
+            const bool live = j < P;
             float sum_a = 0.0f, sum_e = 0.0f, rem_a = 0.0f;
-            for (int i = 0; i < n; ++i) {
-                float sa = fmaxf(S[i * P + j], 0.0f);
-                sum_a = add_rn(sum_a, mul_rn(sa, sa));
+            if (live) {
+                for (int i = sub; i < n; i += TPJ) {
+                    const float sa = fmaxf(S[i * P + j], 0.0f);
+                    const float va = mul_rn(sa, sa);
+                    sum_a = add_rn(sum_a, va);
+                    if (i >= kk) rem_a = add_rn(rem_a, va);
+                }
+                for (int i = sub; i < kk; i += TPJ) {
+                    const float se = fmaxf(EX[i * P + j], 0.0f);
+                    sum_e = add_rn(sum_e, mul_rn(se, se));
+                }
             }
-            for (int i = 0; i < kk; ++i) {
-                float se = fmaxf(EX[i * P + j], 0.0f);
-                sum_e = add_rn(sum_e, mul_rn(se, se));
+            for (int o = 1; o < TPJ; o <<= 1) {
+                sum_a = add_rn(sum_a, __shfl_xor_sync(0xffffffffu, sum_a, o));
+                sum_e = add_rn(sum_e, __shfl_xor_sync(0xffffffffu, sum_e, o));
+                rem_a = add_rn(rem_a, __shfl_xor_sync(0xffffffffu, rem_a, o));
             }
-            for (int i = kk; i < n; ++i) {
-                float sa = fmaxf(S[i * P + j], 0.0f);
-                rem_a = add_rn(rem_a, mul_rn(sa, sa));
-            }
+            if (!live) continue;
             float target = sub_rn(sum_a, sum_e);
             if (target < 0.0f) target = 0.0f;
-            float scl = rem_a > 0.0f ? div_rn(target, rem_a) : 0.0f;
-            for (int i = 0; i < n; ++i) {
+            const float scl = rem_a > 0.0f ? div_rn(target, rem_a) : 0.0f;
+            for (int i = sub; i < n; i += TPJ) {
                 float v;
                 if (i < kk) {
-                    float se = fmaxf(EX[i * P + j], 0.0f);
+                    const float se = fmaxf(EX[i * P + j], 0.0f);
                     v = mul_rn(se, se);
                 } else if (rem_a > 0.0f) {
-                    float sa = fmaxf(S[i * P + j], 0.0f);
+                    const float sa = fmaxf(S[i * P + j], 0.0f);
                     v = mul_rn(mul_rn(sa, sa), scl);
                 } else {
                     v = div_rn(target, static_cast<float>(n - kk));
@@ -1627,6 +1643,16 @@ __global__ void risk_metric_kernel(BmndStageParams sp, int P, int stride, float*
     }
 }
 
+// every group size's group matrix, n = 1 .. BMND_MAX_STACK (group_table_offset)
+__global__ void group_table_kernel(int kind, float* __restrict__ gtab) {
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < kGroupTableFloats; idx += gridDim.x * blockDim.x) {
+        int n = 1;
+        while (group_table_offset(n + 1) <= idx) ++n;
+        const int e = idx - group_table_offset(n);
+        gtab[idx] = group_entry(kind, n, e / n, e % n);
+    }
+}
+
 __global__ void finalize_kernel(const double* __restrict__ num, const double* __restrict__ den,
                                 const float* __restrict__ noisy, float* __restrict__ out,
                                 int64_t n, float eps_f, int no_eps) {
@@ -1684,6 +1710,9 @@ int32_t launch_group_filter(const BmndStageParams& sp, const float* noisy, const
                                                                             st + static_cast<int64_t>(P) * stride);
             BMND_LAUNCH_CHECK("risk_metric_kernel");
         }
+        group_table_kernel<<<(kGroupTableFloats + 255) / 256, 256, 0, stream>>>(
+            sp.group_transform, st + 2 * static_cast<int64_t>(P) * stride);
+        BMND_LAUNCH_CHECK("group_table_kernel");
     }
     FilterArgs a{};
     a.st = st;
