@@ -1085,60 +1085,67 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
             atomicOr(grid + cell, 1u << g);
         }
         __syncthreads();
-        // compact occupied cells (ascending) and their entries (ascending member)
-        const int per = (ucells + blockDim.x - 1) / blockDim.x;
-        const int c0 = tid * per, c1 = min(ucells, c0 + per);
-        int nvox = 0, nent = 0;
-        for (int c = c0; c < c1; ++c) {
-            uint32_t m = grid[c];
-            nvox += m != 0u;
-            nent += __popc(m);
-        }
-        scan[tid] = make_int2(nvox, nent);
-        __syncthreads();
-        if (tid < 32) {
-            // warp-cooperative exclusive scan over blockDim.x partial counts
-            int carry_v = 0, carry_e = 0;
-            for (int base = 0; base < static_cast<int>(blockDim.x); base += 32) {
-                int2 v = scan[base + tid];
-                int iv = v.x, ie = v.y;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    int tv = __shfl_up_sync(0xffffffffu, iv, o);
-                    int te = __shfl_up_sync(0xffffffffu, ie, o);
-                    if (tid >= o) {
-                        iv += tv;
-                        ie += te;
-                    }
-                }
-                scan[base + tid] = make_int2(carry_v + iv - v.x, carry_e + ie - v.y);
-                carry_v += __shfl_sync(0xffffffffu, iv, 31);
-                carry_e += __shfl_sync(0xffffffffu, ie, 31);
-            }
-            if (tid == 0) scan[blockDim.x] = make_int2(carry_v, carry_e);
-        }
-        __syncthreads();
-        // compaction: this thread's cells c0..c1 in order, the cell index parked
-        // in lval until the variance pass below
+        // compact occupied cells (ascending) and their entries (ascending
+        // member): warp w takes a contiguous 1/nw of the cells, 32 at a time,
+        // one cell per lane; voxel ranks come from ballots and entry offsets
+        // from a warp scan of the cells' member counts, after the warps'
+        // totals are added up in warp order.  The cell index is parked in lval
+        // until the variance pass below.
         {
+            const int nw = blockDim.x >> 5, warp = tid >> 5, lane = tid & 31;
+            const int cpw = (ucells + nw - 1) / nw;
+            const int wc0 = min(ucells, warp * cpw), wc1 = min(ucells, wc0 + cpw);
+            int wv = 0, wsum = 0;
+            for (int base = wc0; base < wc1; base += 32) {
+                const int c = base + lane;
+                const uint32_t m = c < wc1 ? grid[c] : 0u;
+                wv += __popc(__ballot_sync(0xffffffffu, m != 0u));
+                wsum += __popc(m);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
+            if (lane == 0) scan[warp] = make_int2(wv, wsum);
+            __syncthreads();
+            int vbase = 0, ebase = 0, vtot = 0, etot = 0;
+            for (int w = 0; w < nw; ++w) {
+                const int2 t = scan[w];
+                if (w < warp) {
+                    vbase += t.x;
+                    ebase += t.y;
+                }
+                vtot += t.x;
+                etot += t.y;
+            }
             const int* shl = sm<int>(smem, a.L.shl);
             const int kstride = kron_stride(P);
-            int w = scan[tid].x, we = scan[tid].y;
-            int cc[BMND_MAX_DIMS] = {0, 0, 0};
-            {
-                int rem = c0;
+            float inv_ush[BMND_MAX_DIMS];
 #pragma unroll
-                for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
-                    if (d < geo.nd()) {
-                        cc[d] = rem % ush[d];
-                        rem /= ush[d];
-                    }
+            for (int d = 0; d < BMND_MAX_DIMS; ++d) inv_ush[d] = 1.0f / static_cast<float>(ush[d]);
+            const uint32_t below = (1u << lane) - 1u;
+            for (int base = wc0; base < wc1; base += 32) {
+                const int c = base + lane;
+                uint32_t m = c < wc1 ? grid[c] : 0u;
+                const uint32_t occ = __ballot_sync(0xffffffffu, m != 0u);
+                const int cnt = __popc(m);
+                int incl = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
                 }
-            }
-            for (int c = c0; c < c1; ++c) {
-                uint32_t m = grid[c];
                 if (m) {
-                    int lin = 0;
+                    const int w = vbase + __popc(occ & below);
+                    int we = ebase + incl - cnt;
+                    // cell -> union-box coordinates -> patch-linear offset
+                    int rem = c, lin = 0, cc[BMND_MAX_DIMS] = {0, 0, 0};
+#pragma unroll
+                    for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
+                        if (d < geo.nd()) {
+                            const int q = d > 0 ? small_div(rem, inv_ush[d]) : 0;
+                            cc[d] = rem - q * ush[d];
+                            rem = q;
+                        }
+                    }
 #pragma unroll
                     for (int d = 0; d < BMND_MAX_DIMS; ++d)
                         if (d < geo.nd()) lin += cc[d] * geo.inner(d);
@@ -1149,17 +1156,13 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
                         m &= m - 1;
                         lent[we++] = static_cast<uint32_t>(g) | (static_cast<uint32_t>((lin - shl[g]) * kstride) << 8);
                     }
-                    ++w;
                 }
-#pragma unroll
-                for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
-                    if (d < geo.nd()) {
-                        if (++cc[d] < ush[d]) break;
-                        cc[d] = 0;
-                    }
-                }
+                vbase += __popc(occ);
+                ebase += __shfl_sync(0xffffffffu, incl, 31);
             }
+            if (tid == 0) scan[blockDim.x] = make_int2(vtot, etot);
         }
+        __syncthreads();
         U = scan[blockDim.x].x;
         if (tid == 0) lstart[U] = scan[blockDim.x].y;
         __syncthreads();
@@ -1197,12 +1200,19 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
 
     // ---- approximate sigma from the variance group (squared transforms) ----
     // (after the exact phase: S shares the union region with its lists)
+    // The observation (and the pilot) are gathered here too, so the volume the
+    // variance comes from is read once (its lists are no longer needed).
+    bool gathered = false;
     if (!gauss && need_approx) {
         for (int e = tid; e < total; e += blockDim.x) {
             const int g = e / P;
-            S[e] = variance_of(__ldg(varsrc + geo.offset(pos + g * BMND_MAX_DIMS, e - g * P, a.vstride)),
-                               scale_f, floor_f);
+            const int64_t off = geo.offset(pos + g * BMND_MAX_DIMS, e - g * P, a.vstride);
+            const float vs = __ldg(varsrc + off);
+            S[e] = variance_of(vs, scale_f, floor_f);
+            X[e] = varsrc == a.noisy ? vs : __ldg(a.noisy + off);
+            if (wiener) R[e] = varsrc == a.pilot ? vs : __ldg(a.pilot + off);
         }
+        gathered = true;
         __syncthreads();
         transform_group<ND, B0, B1, B2>(geo, a, smem, n, S, 2);
         for (int e = tid; e < total; e += blockDim.x) {
@@ -1266,13 +1276,15 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
     __syncthreads();
 
     // ---- gather and forward-transform the observation (and the pilot) ----
-    for (int e = tid; e < total; e += blockDim.x) {
-        const int g = e / P;
-        const int64_t off = geo.offset(pos + g * BMND_MAX_DIMS, e - g * P, a.vstride);
-        X[e] = __ldg(a.noisy + off);
-        if (wiener) R[e] = __ldg(a.pilot + off);
+    if (!gathered) {
+        for (int e = tid; e < total; e += blockDim.x) {
+            const int g = e / P;
+            const int64_t off = geo.offset(pos + g * BMND_MAX_DIMS, e - g * P, a.vstride);
+            X[e] = __ldg(a.noisy + off);
+            if (wiener) R[e] = __ldg(a.pilot + off);
+        }
+        __syncthreads();
     }
-    __syncthreads();
     transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, 0);
     if (wiener) transform_group<ND, B0, B1, B2>(geo, a, smem, n, R, 0);
     const int64_t probe_base = gid * static_cast<int64_t>(a.nmax) * P;
