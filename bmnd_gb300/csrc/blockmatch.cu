@@ -1272,27 +1272,38 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                 // the prescreened candidates in window order (ballots and warp
                 // counts, no atomics), so that when ties at the cut fill the
                 // queue the same candidates are kept on every run
-                int nq = 0;
+                // (warp w takes a contiguous 1/nwarps of the window: it counts
+                // its candidates, the warps' counts are added in warp order, and
+                // it writes them; two barriers in all)
                 const int nwarps = static_cast<int>(blockDim.x >> 5);
-                for (int64_t c0 = 0; c0 < window; c0 += blockDim.x) {
-                    const int64_t c = c0 + tid;
-                    const bool take = c < window && canonical_key(cand[c]) <= vskey;
+                const int64_t span = ((window + nwarps - 1) / nwarps + 31) / 32 * 32;
+                const int64_t w0 = min(window, static_cast<int64_t>(warp) * span);
+                const int64_t w1 = min(window, w0 + span);
+                int mine = 0;
+                for (int64_t c0 = w0; c0 < w1; c0 += 32) {
+                    const int64_t c = c0 + lane;
+                    const bool take = c < w1 && canonical_key(cand[c]) <= vskey;
+                    mine += __popc(__ballot_sync(0xffffffffu, take));
+                }
+                if (lane == 0) hist[warp] = static_cast<uint32_t>(mine);
+                __syncthreads();
+                int before = 0, nq = 0;
+                for (int w = 0; w < nwarps; ++w) {
+                    const int cw = static_cast<int>(hist[w]);
+                    if (w < warp) before += cw;
+                    nq += cw;
+                }
+                for (int64_t c0 = w0; c0 < w1; c0 += 32) {
+                    const int64_t c = c0 + lane;
+                    const bool take = c < w1 && canonical_key(cand[c]) <= vskey;
                     const unsigned m = __ballot_sync(0xffffffffu, take);
-                    if (lane == 0) hist[warp] = static_cast<uint32_t>(__popc(m));
-                    __syncthreads();
-                    int before = nq, chunk = 0;
-                    for (int w = 0; w < nwarps; ++w) {
-                        const int cw = static_cast<int>(hist[w]);
-                        if (w < warp) before += cw;
-                        chunk += cw;
-                    }
                     if (take) {
                         const int slot = before + __popc(m & ((1u << lane) - 1u));
                         if (slot < kSQueue) qidx[slot] = static_cast<int32_t>(c);
                     }
-                    nq += chunk;
-                    __syncthreads();
+                    before += __popc(m);
                 }
+                __syncthreads();
                 const int nsel = min(nq, kSQueue);
                 const float sum_a = redf[4] + redf[5] + redf[6] + redf[7];
                 for (int i = tid; i < nsel; i += blockDim.x) {
