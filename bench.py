@@ -253,7 +253,12 @@ def time_kernels(torch, noisy_t, profile, reps: int = 2, stages=("ht", "wiener")
     stream = torch.cuda.current_stream()
     res = {}
     if precision is None:
-        precision = {"ht": _abi.MATCH_EXACT, "wiener": _abi.MATCH_FAST}
+        if gauss is not None:
+            # SSD: the pipeline's choice (tensor-core screening in 2-D, the exact kernel in 3-D)
+            ssd = _abi.MATCH_FAST if len(shape) == 2 else _abi.MATCH_EXACT
+            precision = {"ht": ssd, "wiener": ssd}
+        else:
+            precision = {"ht": _abi.MATCH_EXACT, "wiener": _abi.MATCH_FAST}
     for stage in stages:
         stage_prec = precision[stage]
         p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k,

@@ -285,9 +285,13 @@ StageWorkspace carve(const BmndStageParams& sp, int64_t n_refs, void* base) {
 
 BmndMatchParams match_params_of(const BmndStageParams& sp) {
     BmndMatchParams mp{};
-    // SSD matching of a volume: the tensor-core screening with exact rescoring
-    // gives the exact kernel's match sets (see ssd_select_kernel), so exact
-    // requests take it
+    // SSD matching of a 2-D image: the tensor-core screening with exact
+    // rescoring gives the exact kernel's match sets (see ssd_select_kernel), so
+    // exact requests take it.  In 3-D the exact kernel stays: a tile's union box
+    // of candidates is 8x a reference's window (about 6 % of the tensor
+    // products are used), and on a denoised pilot the screening bound leaves
+    // most of the window to rescore; measured at 256^3 the whole Gaussian call
+    // took 810 ms with the screening and 780 ms without.
     mp.ndim = sp.ndim;
     for (int d = 0; d < sp.ndim; ++d) {
         mp.counts[d] = sp.shape[d] - sp.block[d] + 1;
@@ -299,7 +303,8 @@ BmndMatchParams match_params_of(const BmndStageParams& sp) {
     mp.distance = sp.distance;
     mp.stabilize_ties = sp.stabilize_ties;
     mp.precision = sp.match_precision;
-    if (sp.distance == BMND_DIST_SSD && sp.match_precision == BMND_MATCH_EXACT && !sp.ssd_poisson_bias)
+    if (sp.distance == BMND_DIST_SSD && sp.match_precision == BMND_MATCH_EXACT && !sp.ssd_poisson_bias &&
+        sp.ndim == 2)
         mp.precision = BMND_MATCH_FAST;
     mp.count_scale = sp.count_scale;
     return mp;
