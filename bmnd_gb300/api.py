@@ -173,11 +173,31 @@ class _Staging:
         return dev
 
     def download(self, t) -> np.ndarray:
+        torch = _torch()
         with self._lock:
-            host = self._get("out", t.numel())
-            host.copy_(t.reshape(-1))
+            flat = t.reshape(-1)
+            n = flat.numel()
+            host = self._get("out", n)
             out = np.empty(tuple(t.shape), dtype=np.float32)
-            self._copy(out.reshape(-1), host.numpy())
+            oflat = out.reshape(-1)
+            hnp = host.numpy()
+            parts = self._SLICES if n >= (1 << 22) else 1
+            step = (n + parts - 1) // parts
+            # every slice's transfer is queued behind an event, and each slice
+            # is copied out on the host while the later ones are still in flight
+            stream = torch.cuda.current_stream()
+            events = []
+            for i in range(parts):
+                lo, hi = i * step, min(n, (i + 1) * step)
+                if lo >= hi:
+                    break
+                host[lo:hi].copy_(flat[lo:hi], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(stream)
+                events.append((lo, hi, ev))
+            for lo, hi, ev in events:
+                ev.synchronize()
+                self._copy(oflat[lo:hi], hnp[lo:hi])
             return out
 
 

@@ -912,11 +912,15 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
     // a member outside the patch grid skips the group (matching never makes one)
     bool bad_member = false;
     if (tid < n) {
-        int64_t rem = a.sel[gid * sp.max_stack + tid];
-        bad_member = rem < 0 || rem >= a.n_lins;
+        const int32_t lin = a.sel[gid * sp.max_stack + tid];
+        bad_member = lin < 0 || lin >= a.n_lins;
+        // lins fit in 31 bits (volumes are limited to 2^31 voxels): 32-bit division
+        uint32_t rem = static_cast<uint32_t>(lin);
         for (int d = geo.nd() - 1; d >= 0 && !bad_member; --d) {
-            pos[tid * BMND_MAX_DIMS + d] = static_cast<int>(rem % a.counts[d]);
-            rem /= a.counts[d];
+            const uint32_t c = static_cast<uint32_t>(a.counts[d]);
+            const uint32_t q = rem / c;
+            pos[tid * BMND_MAX_DIMS + d] = static_cast<int>(rem - q * c);
+            rem = q;
         }
     }
     if (__syncthreads_or(bad_member)) {
@@ -1177,8 +1181,9 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
 #pragma unroll
             for (int d = BMND_MAX_DIMS - 1; d >= 0; --d) {
                 if (d < geo.nd()) {
-                    vox += static_cast<int64_t>(rem % ush[d] + org[d]) * a.vstride[d];
-                    rem /= ush[d];
+                    const int q = d > 0 ? small_div(rem, 1.0f / static_cast<float>(ush[d])) : 0;
+                    vox += static_cast<int64_t>(rem - q * ush[d] + org[d]) * a.vstride[d];
+                    rem = q;
                 }
             }
             lval[u] = variance_of(__ldg(varsrc + vox), scale_f, floor_f);
