@@ -454,11 +454,25 @@ def stage_device(noisy, profile, stage: str, pilot=None, *, resolved=None, match
         raise ValueError(f"stage must be 'ht' or 'wiener', got {stage!r}")
     if (stage == "wiener") != (pilot is not None):
         raise ValueError("the Wiener stage needs a pilot and the hard-thresholding stage takes none")
+    prep = stage_prepare(noisy, profile, stage, resolved=resolved, match_precision=match_precision, gauss=gauss,
+                         fast_transforms=fast_transforms)
+    return stage_launch(prep, noisy, pilot, stream=stream)
+
+
+def stage_prepare(noisy, profile, stage: str, *, resolved=None, match_precision: str = "exact",
+                  gauss: dict | None = None, fast_transforms: bool = False) -> dict:
+    """The host-side part of :func:`stage_device` (stage parameters, reference
+    schedule, workspace, output tensor), so that a caller can do it while the
+    device is still busy with earlier work; :func:`stage_launch` runs it."""
+    torch = _torch()
+    shape = tuple(int(s) for s in noisy.shape)
+    if resolved is None:
+        resolved = resolve_profile(profile, shape)
+    if stage not in ("ht", "wiener"):
+        raise ValueError(f"stage must be 'ht' or 'wiener', got {stage!r}")
     precision = _MATCH_PRECISIONS[match_precision]
     device = noisy.device
     L = _abi.lib()
-    if stream is None:
-        stream = torch.cuda.current_stream(device)
     p = plan.stage_params(profile, shape, stage, resolved.blockmatch_distance, resolved.variance_k, precision,
                           None if gauss is None else gauss[stage], null_table_device(profile, resolved, device),
                           fast_transforms)
@@ -468,11 +482,24 @@ def stage_device(noisy, profile, stage: str, pilot=None, *, resolved=None, match
     nbytes = ctypes.c_uint64(0)
     _abi.check(L.bmnd_stage_workspace_bytes(ctypes.byref(p), len(sched), ctypes.byref(nbytes)))
     ws = _WORKSPACE.get(device, nbytes.value)
-    out = torch.empty_like(noisy)
-    refs = _device_refs(sched, device)
-    _abi.check(L.bmnd_stage(
-        ctypes.byref(p), noisy.data_ptr(), None if pilot is None else pilot.data_ptr(), refs.data_ptr(),
-        len(sched), out.data_ptr(), None, None, None, ws.data_ptr(), ws.numel(), int(stream.cuda_stream)))
+    return dict(stage=stage, params=p, n_refs=len(sched), refs=_device_refs(sched, device), ws=ws,
+                out=torch.empty_like(noisy), shape=shape)
+
+
+def stage_launch(prep: dict, noisy, pilot=None, stream=None):
+    """Launch a stage prepared by :func:`stage_prepare`; returns its output tensor."""
+    torch = _torch()
+    if (prep["stage"] == "wiener") != (pilot is not None):
+        raise ValueError("the Wiener stage needs a pilot and the hard-thresholding stage takes none")
+    if tuple(int(s) for s in noisy.shape) != prep["shape"]:
+        raise ValueError("the volume's shape differs from the prepared stage's")
+    if stream is None:
+        stream = torch.cuda.current_stream(noisy.device)
+    out, ws, refs = prep["out"], prep["ws"], prep["refs"]
+    _abi.check(_abi.lib().bmnd_stage(
+        ctypes.byref(prep["params"]), noisy.data_ptr(), None if pilot is None else pilot.data_ptr(),
+        refs.data_ptr(), prep["n_refs"], out.data_ptr(), None, None, None, ws.data_ptr(), ws.numel(),
+        int(stream.cuda_stream)))
     return out
 
 
@@ -542,9 +569,9 @@ def bmnd(
     * ``match_precision`` -- "exact" (the default of the plain pilot): float32
       per-term distances for every candidate; "fast": screening plus exact
       rescoring near the selection boundary (same match sets); "approx":
-      selection by the screening distances with exact rescoring of the
-      selected candidates only (the match sets may differ where the two orders
-      disagree); "subsampled" (the default of the learned pilot's Wiener
+      selection by the screening distances, the selected candidates rescored
+      with the ratio form of the deviance (within 4e-6 per unit of r + c of the
+      float32 terms; the match sets may differ where the orders disagree); "subsampled" (the default of the learned pilot's Wiener
       stage): "approx" after a prescreen on the patch's even sub-lattice.
     """
     if sigma is not None and sigma_psd is not None:

@@ -1366,24 +1366,29 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
         const int qn = overflow ? 0 : qn_all;
         // rescoring of the queue.  Fast mode: the exact float32 distance, one
         // thread per candidate, bit-identical to the exact kernel.  Approx mode:
-        // the same terms, one warp per candidate (lanes over patch elements,
-        // tree-ordered sum), so the whole CTA works on the queue.
+        // the ratio form of the screened mode (one SFU reciprocal and two log2
+        // per term, free of cancellation, within 4e-6 per unit of r + c of the
+        // exact terms) over the full patch, one warp per candidate (lanes over
+        // patch elements, tree-ordered sum), so the whole CTA works on the queue;
+        // the IEEE division and two full logarithms of the exact term cost
+        // about eight times as many instructions.
         if (a.approx) {
             const int nwarps = static_cast<int>(blockDim.x >> 5);
             for (int i = warp; i < qn; i += nwarps) {
                 const int32_t q = qidx[i];
                 int64_t lin;
                 const int64_t origin = window_origin(a, lo, ext, inv_ext, small_window, q & 0x7fffffff, &lin);
-                float d = 0.0f;
+                float d = 0.0f, ss = 0.0f;
                 for (int p = lane; p < P; p += 32) {
                     float c = mul_rn(__ldg(a.src + origin + poff_s[p]), a.inv_scale);
                     if (c < 0.0f) c = 0.0f;
-                    d += deviance_term(ref[p].x, c);
+                    const float r = ref[p].x;
+                    d += ratio_term(r, r + r, c, ss);
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
                 if (lane == 0) {
-                    const float key = canonical_key(div_rn(fmaxf(d, 0.0f), static_cast<float>(P)));
+                    const float key = canonical_key(fmaxf(1.38629436f * d, 0.0f) / static_cast<float>(P));
                     const bool accepted = key < tkey;
                     if (accepted && q >= 0) ++acc_t;
                     qkey[i] = accepted ? composite_key(key, static_cast<int32_t>(lin)) : ~0ull;
