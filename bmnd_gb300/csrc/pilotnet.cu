@@ -778,7 +778,6 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
                     "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(afull(s))
                     : "memory");
             }
-            committed = it + 1;
             __syncwarp();
         }
         if (lane == 0 && *abort_v && committed > 0) {
@@ -852,6 +851,314 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
     if (warp == 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TT::tmem_cols)
                      : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Weight gradients of the C -> C layers on the tensor cores.  For tap t,
+//   dW_t[ci][co] = sum_v X[v + off_t][ci] dY[v][co],
+// a GEMM with M = ci, N = co and K = the voxels: A is the input halo of a tile
+// and B its output-gradient tile, both in shared memory exactly as TMA lands
+// them from the chunk-planar tensors, where the 8 channels of a voxel are 16
+// contiguous bytes and a tile row holds 8 voxels.  That is the MN-major
+// core-matrix layout: 8 K-rows (voxels, 16 bytes apart) of 8 MN elements
+// (channels); the MN stride between core matrices is one chunk plane, the K
+// stride one tile row (the halo's row pitch for A, 128 bytes for B).  A tap is
+// a shift of A's start address, as in the forward kernel.  M is 128 (the
+// smallest single-CTA shape): rows C .. 127 read the memory after the C / 8
+// chunk planes of the stage, which the layout keeps inside the allocation, and
+// are discarded.  The CTAs split the taps into groups of 9, so one group's
+// accumulators (9 x C columns) fit the 512 columns of tensor memory, and each
+// CTA accumulates its share of the tiles for the whole launch; the per-CTA
+// sums are added by reduce_partials_kernel.  Roles: warp 0 issues the TMA
+// loads (two stages), one thread of warp 1 the MMAs; at the end warps 0-1 read
+// tensor-memory lanes 0-63.  Every mbarrier wait is bounded.
+// ---------------------------------------------------------------------------
+template <int ND, int C>
+struct WgTile {
+    using TT = TcTile<ND, C>;
+    static constexpr int taps_per_cta = 9;
+    static constexpr int groups = TT::taps / taps_per_cta;
+    static constexpr uint32_t xbytes = TT::tbytes;                                   // one input-halo stage
+    static constexpr uint32_t ybytes = TT::chunks * TT::tx * TT::ty * 16;            // one output-gradient stage
+    // A of stage 1 reads 16 chunk planes from its start (M = 128)
+    static constexpr uint32_t bytes = xbytes + 16 * TT::cbytes > 2 * (xbytes + ybytes)
+                                          ? xbytes + 16 * TT::cbytes
+                                          : 2 * (xbytes + ybytes);
+    static constexpr uint32_t acc_cols = taps_per_cta * C;
+    static constexpr int threads = 128;
+};
+
+template <int ND, int C>
+__global__ void __launch_bounds__(128, 1) wgrad_tc_kernel(const __grid_constant__ TcMaps xmaps,
+                                                          const __grid_constant__ TcMaps ymaps,
+                                                          float* __restrict__ partial, int64_t nparams, NetGeo g,
+                                                          int* __restrict__ err, uint64_t probe_ns) {
+    using TT = TcTile<ND, C>;
+    using WT = WgTile<ND, C>;
+    extern __shared__ __align__(128) unsigned char wg_smem[];
+    __shared__ __align__(8) uint64_t bars[6];  // full[2], empty[2], done, never
+    __shared__ uint32_t tmem_slot;
+    __shared__ int abort_flag;
+    volatile int* abort_v = &abort_flag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(wg_smem));
+    // stage s: the input halo at xs(s), the output gradient at ys(s)
+    auto xs = [&](int st) { return sbase + static_cast<uint32_t>(st) * WT::xbytes; };
+    auto ys = [&](int st) { return sbase + 2 * WT::xbytes + static_cast<uint32_t>(st) * WT::ybytes; };
+    const uint32_t bar0 = static_cast<uint32_t>(__cvta_generic_to_shared(bars));
+    auto full = [&](int st) { return bar0 + 8u * st; };
+    auto empty = [&](int st) { return bar0 + 16u + 8u * st; };
+    const uint32_t done = bar0 + 32u, never = bar0 + 40u;
+    constexpr uint64_t kWaitNs = 1000000000ull;
+    const int cpg = static_cast<int>(gridDim.x) / WT::groups;  // CTAs per tap group
+    const int group = static_cast<int>(blockIdx.x) / cpg;
+    const int gidx = static_cast<int>(blockIdx.x) - group * cpg;
+
+    if (tid == 0) {
+        for (int st = 0; st < 2; ++st) {
+            mbar_init(full(st), 1);
+            mbar_init(empty(st), 1);
+        }
+        mbar_init(done, 1);
+        mbar_init(never, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        abort_flag = ((sbase & 127u) != 0u || group >= WT::groups) ? 1 : 0;
+        if ((sbase & 127u) != 0u) atomicExch(err, 2);
+    }
+    if (warp == 1) {
+        const uint32_t slot = static_cast<uint32_t>(__cvta_generic_to_shared(&tmem_slot));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(slot), "r"(512)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    if (probe_ns) {
+        if (tid == 0 && !mbar_wait(never, 0, probe_ns)) {
+            abort_flag = 1;
+            atomicExch(err, 1);
+        }
+        __syncthreads();
+    }
+
+    const int tiles_x = (g.W + TT::tx - 1) / TT::tx;
+    const int tiles_y = (g.H + TT::ty - 1) / TT::ty;
+    const int64_t ntiles = static_cast<int64_t>(tiles_x) * tiles_y * g.D * g.nb;
+    auto decode = [&](int64_t tl, int& b, int& z0, int& y0, int& x0) {
+        int64_t r = tl;
+        x0 = static_cast<int>(r % tiles_x) * TT::tx;
+        r /= tiles_x;
+        y0 = static_cast<int>(r % tiles_y) * TT::ty;
+        r /= tiles_y;
+        z0 = static_cast<int>(r % g.D);
+        b = static_cast<int>(r / g.D);
+    };
+    auto fail = [&](int code) {
+        *abort_v = 1;
+        atomicExch(err, code);
+    };
+    if (warp == 0) {
+        // ---- producer: one input halo and one output-gradient tile per stage ----
+        int issued = 0;
+        if (lane == 0 && !*abort_v) {
+            int it = 0;
+            for (int64_t tl = gidx; tl < ntiles; tl += cpg, ++it) {
+                const int st = it & 1;
+                if (!mbar_wait(empty(st), ((it >> 1) & 1) ^ 1, kWaitNs)) {
+                    fail(1);
+                    break;
+                }
+                if (*abort_v) break;
+                int b, z0, y0, x0;
+                decode(tl, b, z0, y0, x0);
+                mbar_expect_tx(full(st), TT::chunks * (TT::box_bytes + TT::tx * TT::ty * 16));
+#pragma unroll
+                for (int ch = 0; ch < TT::chunks; ++ch) {
+                    tma_load_4d(xs(st) + ch * TT::cbytes, &xmaps.m[ch], 0, x0 - 1, y0 - 1,
+                                ND == 3 ? b * g.D + z0 - 1 : b, full(st));
+                    tma_load_4d(ys(st) + ch * (TT::tx * TT::ty * 16), &ymaps.m[ch], 0, x0, y0,
+                                ND == 3 ? b * g.D + z0 : b, full(st));
+                }
+                issued = it + 1;
+            }
+            if (*abort_v) {
+                // copies in flight: wait (bounded) for the last two stages
+                for (int j = issued - 2; j < issued; ++j)
+                    if (j >= 0) (void)mbar_wait(full(j & 1), (j >> 1) & 1, kWaitNs);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---- MMA issuer; the warp zeroes batch-boundary planes ----
+        constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+                                   (static_cast<uint32_t>(C >> 3) << 17) | (static_cast<uint32_t>(128 >> 4) << 24);
+        int it = 0;
+        for (int64_t tl = gidx; !*abort_v && tl < ntiles; tl += cpg, ++it) {
+            const int st = it & 1;
+            bool got = true;
+            if (lane == 0) got = mbar_wait(full(st), (it >> 1) & 1, kWaitNs);
+            got = __shfl_sync(0xffffffffu, got ? 1 : 0, 0) != 0;
+            if (!got || *abort_v) {
+                if (lane == 0 && !got) fail(1);
+                break;
+            }
+            if (ND == 3 && g.nb > 1) {
+                // planes of the neighbouring volume in the batch read as zero padding
+                int b, z0, y0, x0;
+                decode(tl, b, z0, y0, x0);
+                const bool below = z0 == 0 && b > 0, above = z0 == g.D - 1 && b < g.nb - 1;
+                if (below || above) {
+                    constexpr int pv = TT::hx * TT::hy;
+                    for (int plane = 0; plane < 3; plane += 2) {
+                        if (plane == 0 ? !below : !above) continue;
+                        for (int i = lane; i < TT::chunks * pv; i += 32) {
+                            const int ch = i / pv, v = plane * pv + i % pv;
+                            const uint32_t a = xs(st) + ch * TT::cbytes + static_cast<uint32_t>(v) * 16u;
+                            asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};\n" ::"r"(a), "r"(0) : "memory");
+                        }
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                    __syncwarp();
+                }
+            }
+            tc_fence_after();
+            if (lane == 0) {
+                // A: MN-major, SBO = chunk plane (next 8 input channels), LBO = halo row (next 8 voxels)
+                const uint64_t a_base = umma_desc(xs(st), TT::hx * 16, TT::cbytes);
+                // B: MN-major, SBO = chunk plane of the gradient tile, LBO = one tile row (128 bytes)
+                const uint64_t b_base = umma_desc(ys(st), 128, TT::tx * TT::ty * 16);
+#pragma unroll 1
+                for (int tt = 0; tt < WT::taps_per_cta; ++tt) {
+                    const int t = group * WT::taps_per_cta + tt;
+                    const int dz = ND == 3 ? t / 9 : 0;
+                    const int dy = ND == 3 ? (t / 3) % 3 : t / 3;
+                    const int dx = t % 3;
+                    const int vox0 = (dz * TT::hy + dy) * TT::hx + dx;
+                    const uint32_t d_tmem = tmem + static_cast<uint32_t>(tt * C);
+#pragma unroll
+                    for (int ks = 0; ks < TT::ty / 2; ++ks) {
+                        // K step ks: tile rows 2 ks and 2 ks + 1 (16 voxels)
+                        const uint64_t ad = a_base + static_cast<uint64_t>(vox0 + 2 * ks * TT::hx);
+                        const uint64_t bd = b_base + static_cast<uint64_t>(2 * ks * TT::tx);
+                        const uint32_t acc = (it > 0 || ks > 0) ? 1u : 0u;
+                        asm volatile(
+                            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+                            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                            : "memory");
+                    }
+                }
+                asm volatile(
+                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(empty(st))
+                    : "memory");
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            // everything issued (or nothing): the done barrier completes when the products have
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(done)
+                         : "memory");
+        }
+        __syncwarp();
+    }
+    // ---- read the accumulators out: warp w holds tensor-memory lanes 32 w .. 32 w + 31 ----
+    __syncthreads();
+    bool got = true;
+    if (lane == 0) got = mbar_wait(done, 0, kWaitNs);
+    got = __shfl_sync(0xffffffffu, got ? 1 : 0, 0) != 0;
+    if (!got && lane == 0) fail(1);
+    tc_fence_after();
+    if (warp < 2 && got && !*abort_v) {
+        const int ci = 32 * warp + lane;
+        float* out = partial + static_cast<int64_t>(blockIdx.x) * nparams;
+        for (int c0 = 0; c0 < static_cast<int>(WT::acc_cols); c0 += 16) {
+            uint32_t r[16];
+            const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * warp) << 16) + static_cast<uint32_t>(c0);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                "%12, %13, %14, %15}, [%16];\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (ci < C) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int col = c0 + j;
+                    const int t = group * WT::taps_per_cta + col / C;
+                    const int co = col % C;
+                    out[(static_cast<int64_t>(t) * C + ci) * C + co] = __uint_as_float(r[j]);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(512) : "memory");
+}
+
+// bias gradient of a C-channel layer: per-CTA partial sums of the output
+// gradient over a contiguous share of the voxels, into the bias slots of the
+// partial records; a thread reads the 8 channels of a voxel as 16 bytes
+template <int C>
+__global__ void __launch_bounds__(256) bias_partial_kernel(const bf16* __restrict__ gout, int64_t nv,
+                                                           float* __restrict__ partial, int64_t nparams,
+                                                           int64_t wparams) {
+    __shared__ float red[8][8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t per = (nv + gridDim.x - 1) / gridDim.x;
+    const int64_t v0 = static_cast<int64_t>(blockIdx.x) * per, v1 = min(nv, v0 + per);
+    for (int ch = 0; ch < C / 8; ++ch) {
+        const uint4* src = reinterpret_cast<const uint4*>(gout + static_cast<int64_t>(ch) * nv * 8);
+        float s[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[e] = 0.0f;
+        for (int64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
+            const uint4 q = src[v];
+            const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                s[2 * e] += __uint_as_float(w[e] << 16);
+                s[2 * e + 1] += __uint_as_float(w[e] & 0xffff0000u);
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s[e] += __shfl_xor_sync(0xffffffffu, s[e], o);
+        if (lane == 0)
+#pragma unroll
+            for (int e = 0; e < 8; ++e) red[warp][e] = s[e];
+        __syncthreads();
+        if (threadIdx.x < 8) {
+            float t = 0.0f;
+            for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) t += red[w][threadIdx.x];
+            partial[static_cast<int64_t>(blockIdx.x) * nparams + wparams + ch * 8 + threadIdx.x] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// sums the partial records of the tensor-core weight gradient: tap t's
+// weights from the cpg records of its tap group, the bias from all of them
+__global__ void reduce_wgrad_tc_kernel(const float* __restrict__ partial, int cpg, int groups, int64_t group_params,
+                                       int64_t wparams, int64_t nparams, float* __restrict__ grad) {
+    for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < nparams;
+         p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t c0 = 0, c1 = static_cast<int64_t>(cpg) * groups;
+        if (p < wparams) {
+            c0 = (p / group_params) * cpg;
+            c1 = c0 + cpg;
+        }
+        float s = 0.0f;
+        for (int64_t c = c0; c < c1; ++c) s += partial[c * nparams + p];
+        grad[p] = s;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1233,6 +1540,36 @@ int32_t run_mid(const bf16* in, const uint2* wpk, const float* bias, const bf16*
 int g_conv_engine = BMND_CONV_TCGEN05;
 uint64_t g_wait_probe_ns = 0;  // see bmnd_pilotnet_set_wait_probe
 
+// One 4-D tensor map per 8-channel chunk plane of a chunk-planar BF16 tensor
+// (8 channels, x, y, z * batch) with the given box; out-of-range elements read
+// as zero.  The CUDA driver API's tensor-map encoder is fetched through the
+// runtime (no link-time dependency on libcuda).
+int32_t encode_chunk_maps(const bf16* base, NetGeo g, int C, const uint32_t box_in[4], TcMaps& maps) {
+    memset(&maps, 0, sizeof(maps));
+    const cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(g.W), static_cast<cuuint64_t>(g.H),
+                                static_cast<cuuint64_t>(g.D) * static_cast<cuuint64_t>(g.nb)};
+    const cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(g.W) * 16, static_cast<cuuint64_t>(g.H) * g.W * 16};
+    const cuuint32_t box[4] = {box_in[0], box_in[1], box_in[2], box_in[3]};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        void* fn = nullptr;
+        BMND_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !fn) return fail(BMND_ERR_CUDA, "cuTensorMapEncodeTiled not available");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const int64_t nv = g.voxels();
+    for (int ch = 0; ch < C / 8; ++ch) {
+        const CUresult rc = encode(&maps.m[ch], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
+                                   const_cast<bf16*>(base) + static_cast<int64_t>(ch) * nv * 8, dims, strides, box,
+                                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (rc != CUDA_SUCCESS) return fail(BMND_ERR_CUDA, "cuTensorMapEncodeTiled failed for a pilot net tensor");
+    }
+    return BMND_OK;
+}
+
 template <int ND, int C>
 int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf16* mask, bf16* out, NetGeo g,
                    int* err, cudaStream_t stream) {
@@ -1248,29 +1585,8 @@ int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf1
     // box of (8, hx, hy, hz) voxels whose rows are 16 * hx contiguous bytes;
     // out-of-range elements read as zero
     TcMaps maps;
-    memset(&maps, 0, sizeof(maps));
-    const cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(g.W), static_cast<cuuint64_t>(g.H),
-                                static_cast<cuuint64_t>(g.D) * static_cast<cuuint64_t>(g.nb)};
-    const cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(g.W) * 16, static_cast<cuuint64_t>(g.H) * g.W * 16};
-    const cuuint32_t box[4] = {8, TT::hx, TT::hy, TT::hz};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    // the CUDA driver API's tensor-map encoder, fetched through the runtime (no link-time dependency on libcuda)
-    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    if (!encode) {
-        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-        void* fn = nullptr;
-        BMND_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
-        if (q != cudaDriverEntryPointSuccess || !fn) return fail(BMND_ERR_CUDA, "cuTensorMapEncodeTiled not available");
-        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-    }
-    for (int ch = 0; ch < TT::chunks; ++ch) {
-        const CUresult rc = encode(
-            &maps.m[ch], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(in) + hid<C>(0, ch * 8, g.voxels()),
-            dims, strides, box,
-            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (rc != CUDA_SUCCESS) return fail(BMND_ERR_CUDA, "cuTensorMapEncodeTiled failed for the pilot net input");
-    }
+    const uint32_t box[4] = {8, TT::hx, TT::hy, TT::hz};
+    if (int32_t rc = encode_chunk_maps(in, g, C, box, maps)) return rc;
     const int64_t ntiles = static_cast<int64_t>((g.W + TT::tx - 1) / TT::tx) * ((g.H + TT::ty - 1) / TT::ty) * g.D *
                            g.nb;
     // one persistent CTA per SM: the weights fill most of the shared memory
@@ -1346,6 +1662,46 @@ int32_t run_wgrad(const TI* in, const TG* gout, float* partial, float* grad, int
     return BMND_OK;
 }
 
+// the C -> C weight gradient on the tensor cores; returns BMND_ERR_UNSUPPORTED
+// (nothing launched) when the partial records do not fit the workspace
+template <int ND, int C>
+int32_t run_wgrad_tc(const bf16* in, const bf16* gout, float* partial, int64_t capacity, float* grad, NetGeo g,
+                     int* err, cudaStream_t stream) {
+    using TT = TcTile<ND, C>;
+    using WT = WgTile<ND, C>;
+    auto kernel = wgrad_tc_kernel<ND, C>;
+    int sms = 0, per_sm = 0;
+    if (int32_t rc = kernel_residency(reinterpret_cast<const void*>(kernel), WT::threads, WT::bytes, false, &per_sm,
+                                      &sms))
+        return rc;
+    if (per_sm < 1) return BMND_ERR_UNSUPPORTED;
+    if ((reinterpret_cast<uintptr_t>(in) & 15u) != 0 || (reinterpret_cast<uintptr_t>(gout) & 15u) != 0)
+        return fail(BMND_ERR_INVALID_ARG, "pilot net buffers must be 16-byte aligned");
+    const int64_t ntiles = static_cast<int64_t>((g.W + TT::tx - 1) / TT::tx) * ((g.H + TT::ty - 1) / TT::ty) *
+                           g.D * g.nb;
+    int64_t cpg = sms / WT::groups;
+    if (cpg > ntiles) cpg = ntiles;
+    if (cpg * WT::groups > capacity) cpg = capacity / WT::groups;
+    if (cpg < 1) return BMND_ERR_UNSUPPORTED;
+    TcMaps xmaps, ymaps;
+    const uint32_t xbox[4] = {8, TT::hx, TT::hy, TT::hz};
+    const uint32_t ybox[4] = {8, TT::tx, TT::ty, 1};
+    if (int32_t rc = encode_chunk_maps(in, g, C, xbox, xmaps)) return rc;
+    if (int32_t rc = encode_chunk_maps(gout, g, C, ybox, ymaps)) return rc;
+    constexpr int64_t wparams = static_cast<int64_t>(TT::taps) * C * C;
+    constexpr int64_t np = wparams + C;
+    const int64_t nparts = cpg * WT::groups;
+    kernel<<<static_cast<unsigned>(nparts), WT::threads, WT::bytes, stream>>>(xmaps, ymaps, partial, np, g, err,
+                                                                             g_wait_probe_ns);
+    BMND_LAUNCH_CHECK("wgrad_tc_kernel");
+    bias_partial_kernel<C><<<static_cast<unsigned>(nparts), 256, 0, stream>>>(gout, g.voxels(), partial, np, wparams);
+    BMND_LAUNCH_CHECK("bias_partial_kernel");
+    reduce_wgrad_tc_kernel<<<launch_blocks(np, 256), 256, 0, stream>>>(
+        partial, static_cast<int>(cpg), WT::groups, static_cast<int64_t>(WT::taps_per_cta) * C * C, wparams, np, grad);
+    BMND_LAUNCH_CHECK("reduce_wgrad_tc_kernel");
+    return BMND_OK;
+}
+
 template <int ND, int C>
 int32_t gradient_impl(const NetPlan& P, const unsigned char* packed, const float* noisy, const float* target,
                       float* grad, double* loss, Bufs& B, cudaStream_t stream) {
@@ -1364,6 +1720,7 @@ int32_t gradient_impl(const NetPlan& P, const unsigned char* packed, const float
     const int64_t stride = nv * C;
     auto act = [&](int l) -> bf16* { return B.act + l * stride; };
     const int L = P.L;
+    constexpr int64_t wg_params = static_cast<int64_t>(TL::taps) * C * C + C;  // one C -> C layer
     // last layer: weight gradient from h_{L-1} and gy, data gradient into h_{L-1}
     rc = run_wgrad<ND, C, 1, bf16, float>(act(L - 2), B.gy, B.partial, grad + P.w_off[L - 1], tiles, g, stream);
     if (rc) return rc;
@@ -1372,7 +1729,13 @@ int32_t gradient_impl(const NetPlan& P, const unsigned char* packed, const float
     BMND_LAUNCH_CHECK("conv_out_dgrad_kernel");
     // mid layers, last to first: B.grad[cur] is the gradient of layer l's output
     for (int l = L - 2; l >= 1; --l) {
-        rc = run_wgrad<ND, C, C, bf16, bf16>(act(l - 1), B.grad[cur], B.partial, grad + P.w_off[l], tiles, g, stream);
+        rc = BMND_ERR_UNSUPPORTED;
+        if (g_conv_engine == BMND_CONV_TCGEN05)
+            rc = run_wgrad_tc<ND, C>(act(l - 1), B.grad[cur], B.partial, tiles * P.max_layer_params / wg_params,
+                                     grad + P.w_off[l], g, B.err, stream);
+        if (rc == BMND_ERR_UNSUPPORTED)
+            rc = run_wgrad<ND, C, C, bf16, bf16>(act(l - 1), B.grad[cur], B.partial, grad + P.w_off[l], tiles, g,
+                                                 stream);
         if (rc) return rc;
         rc = run_layer<ND, C>(P, packed, l, true, B.grad[cur], nullptr, act(l - 1), B.grad[cur ^ 1], B, stream);
         if (rc) return rc;
