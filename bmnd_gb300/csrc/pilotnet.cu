@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(256, 1) conv_mid_kernel(const bf16* __restrict
 // Output tile: one z plane of 16 rows x 8 voxels = the M = 128 rows of one
 // tcgen05.mma (kind::f16, BF16 in, FP32 accumulate, N = C, K = 16).  The
 // input halo of the tile (10 x 18 voxels, x 3 planes in 3-D) arrives by TMA,
-// one 4-D box per 8-channel chunk plane of the chunk-planar activations (each
+// one 3-D box per 8-channel chunk plane of the chunk-planar activations (each
 // box row is 16 * hx contiguous bytes), so shared memory holds it chunk-major:
 // [chunk][halo voxel][16 bytes], chunks 128-byte aligned.  For every tap the A
 // operand is then a no-swizzle K-major matrix: a core matrix is 8 consecutive
@@ -526,12 +526,16 @@ __global__ void __launch_bounds__(256, 1) conv_mid_kernel(const bf16* __restrict
 // convolution's zero padding.  The weights stay in shared memory for the whole
 // launch as B = W_t[ci][co] in the same K-major core-matrix layout.
 //
-// Warp roles (192 threads, one CTA per SM): warp 0 issues the TMA loads into
-// two halo stages; one thread of warp 1 issues the 27 x C/16 MMAs of a tile
-// into one of two accumulators in tensor memory and commits them to mbarriers
-// (stage free, accumulator full); warps 2-5 read the accumulator rows they may
-// access (tcgen05.ld 32x32b), release it, and apply the epilogue.  Loads, MMAs
-// and epilogues of neighbouring tiles overlap.  Every mbarrier wait is
+// Warp roles (224 threads, one CTA per SM): warp 0 issues the TMA loads into
+// two halo stages; one thread each of warps 1 and 6 issues the MMAs of a tile,
+// the first half of the taps and the second, into two partial accumulators in
+// tensor memory (one pair per stage), and commits them to mbarriers (stage
+// free, accumulator full); warps 2-5 read the accumulator rows they may access
+// (tcgen05.ld 32x32b), add the two partials, release them, and apply the
+// epilogue.  Loads, MMAs and epilogues of neighbouring tiles overlap.  Two
+// issuing threads, because one thread issues a 128 x 48 x 16 MMA about every
+// 64 clocks, while the tensor core reads its operands (4 KB of A, 1.5 KB of B
+// at 128 bytes per clock) in 44.  Every mbarrier wait is
 // bounded: on timeout the kernel records an error, stops issuing work, waits
 // (bounded) for its copies and MMAs in flight, and frees its tensor memory.
 // ---------------------------------------------------------------------------
@@ -549,9 +553,10 @@ struct TcTile {
     static constexpr uint32_t tbytes = chunks * cbytes;                                 // one halo stage
     static constexpr uint32_t wbytes = static_cast<uint32_t>(taps) * kc * 2 * C * 16;  // B core matrices
     static constexpr uint32_t bytes = 2 * tbytes + wbytes;
+    static constexpr int tsplit = (taps + 1) / 2;  // taps of the first issuing thread
     static constexpr uint32_t acc_cols = C <= 32 ? 32 : 64;
-    static constexpr uint32_t tmem_cols = 2 * acc_cols;
-    static constexpr int threads = 192;
+    static constexpr uint32_t tmem_cols = 4 * acc_cols;  // (stage, half) partial accumulators
+    static constexpr int threads = 224;
 };
 
 struct TcMaps {
@@ -582,17 +587,46 @@ __global__ void pack_tc_kernel(const float* __restrict__ W, bf16* __restrict__ o
     }
 }
 
-__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+// c0 is the element offset along a row of the chunk plane (8 per voxel), so
+// c0 * 2 bytes is a multiple of 16 for every voxel offset, negative included
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2,
                                             uint32_t mbar) {
     asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
-        "%5}], [%6];\n" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(mbar)
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+        "%4}], [%5];\n" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(mbar)
         : "memory");
 }
 
+// the MMAs of taps T0 .. T1 - 1 of one tile into the accumulator at d_tmem
+template <int ND, int C, int T0, int T1>
+__device__ __forceinline__ void issue_conv_taps(uint64_t a_base, uint64_t b_base, uint32_t d_tmem) {
+    using TT = TcTile<ND, C>;
+    constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(C >> 3) << 17) |
+                               (static_cast<uint32_t>(128 >> 4) << 24);
+#pragma unroll
+    for (int t = T0; t < T1; ++t) {
+        const int dz = ND == 3 ? t / 9 : 0;
+        const int dy = ND == 3 ? (t / 3) % 3 : t / 3;
+        const int dx = t % 3;
+        const int vox0 = (dz * TT::hy + dy) * TT::hx + dx;
+#pragma unroll
+        for (int k = 0; k < TT::kc; ++k) {
+            // start-address field += offset / 16 (stays below 2^14: no carry)
+            const uint64_t ad = a_base + static_cast<uint64_t>(2 * k * TT::halo_pad + vox0);
+            const uint64_t bd = b_base + static_cast<uint64_t>((t * TT::kc + k) * 2 * C);
+            const uint32_t acc = (t != T0 || k != 0) ? 1u : 0u;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                : "memory");
+        }
+    }
+}
+
 template <int ND, int C>
-__global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_constant__ TcMaps maps,
+__global__ void __launch_bounds__(224, 1) conv_mid_tc_kernel(const __grid_constant__ TcMaps maps,
                                                              const bf16* __restrict__ wtc,
                                                              const float* __restrict__ bias,
                                                              const bf16* __restrict__ mask, bf16* __restrict__ out,
@@ -600,9 +634,10 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
     using TT = TcTile<ND, C>;
     extern __shared__ __align__(128) unsigned char tc_smem[];
     // full[2] (halo stage landed), empty[2] (stage read by the MMAs), afull[2]
-    // (accumulator complete), aempty[2] (accumulator read out), weights, and
-    // one barrier that nothing completes (the wait probe)
-    __shared__ __align__(8) uint64_t bars[10];
+    // (accumulator complete), aempty[2] (accumulator read out), weights, one
+    // barrier that nothing completes (the wait probe), drain[2] (an issuing
+    // thread's MMAs all done)
+    __shared__ __align__(8) uint64_t bars[12];
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
     volatile int* abort_v = &abort_flag;
@@ -616,14 +651,16 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
     auto aempty = [&](int s) { return bar0 + 48u + 8u * s; };
     const uint32_t wbar = bar0 + 64u;
     const uint32_t never = bar0 + 72u;
+    auto drain = [&](int k) { return bar0 + 80u + 8u * k; };
     constexpr uint64_t kWaitNs = 1000000000ull;  // one tile takes microseconds
 
     if (tid == 0) {
         for (int s = 0; s < 2; ++s) {
             mbar_init(full(s), 1);
-            mbar_init(empty(s), 1);
-            mbar_init(afull(s), 1);
+            mbar_init(empty(s), 2);   // one commit per issuing thread
+            mbar_init(afull(s), 2);
             mbar_init(aempty(s), 4);  // one arrival per epilogue warp
+            mbar_init(drain(s), 1);
         }
         mbar_init(wbar, 1);
         mbar_init(never, 1);
@@ -695,7 +732,7 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
                 const uint32_t dst = sbase + static_cast<uint32_t>(s) * TT::tbytes;
 #pragma unroll
                 for (int ch = 0; ch < TT::chunks; ++ch)
-                    tma_load_4d(dst + ch * TT::cbytes, &maps.m[ch], 0, x0 - 1, y0 - 1, zc, full(s));
+                    tma_load_3d(dst + ch * TT::cbytes, &maps.m[ch], 8 * (x0 - 1), y0 - 1, zc, full(s));
                 issued = it + 1;
             }
             if (*abort_v) {
@@ -706,11 +743,11 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
             }
         }
         __syncwarp();
-    } else if (warp == 1) {
-        // ---- MMA issuer (lane 0); the warp zeroes batch-boundary planes ----
-        constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(C >> 3) << 17) |
-                                   (static_cast<uint32_t>(128 >> 4) << 24);
-        int committed = 0;
+    } else if (warp == 1 || warp == 6) {
+        // ---- MMA issuers (lane 0): warp 1 the first TT::tsplit taps, warp 6 the
+        // rest; each warp zeroes the batch-boundary planes of the stage before
+        // its own MMAs (both write the same zeros) ----
+        const int k = warp == 6 ? 1 : 0;
         bool ok = !*abort_v;
         if (ok && !mbar_wait(wbar, 0, kWaitNs)) {
             fail(1);
@@ -751,26 +788,11 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
             if (lane == 0) {
                 const uint64_t a_base = umma_desc(stage, TT::cbytes, TT::hx * 16);
                 const uint64_t b_base = umma_desc(wsm, C * 16, 128);
-                const uint32_t d_tmem = tmem + static_cast<uint32_t>(s) * TT::acc_cols;
-#pragma unroll
-                for (int t = 0; t < TT::taps; ++t) {
-                    const int dz = ND == 3 ? t / 9 : 0;
-                    const int dy = ND == 3 ? (t / 3) % 3 : t / 3;
-                    const int dx = t % 3;
-                    const int vox0 = (dz * TT::hy + dy) * TT::hx + dx;
-#pragma unroll
-                    for (int k = 0; k < TT::kc; ++k) {
-                        // start-address field += offset / 16 (stays below 2^14: no carry)
-                        const uint64_t ad = a_base + static_cast<uint64_t>(2 * k * TT::halo_pad + vox0);
-                        const uint64_t bd = b_base + static_cast<uint64_t>((t * TT::kc + k) * 2 * C);
-                        const uint32_t acc = (t | k) != 0 ? 1u : 0u;
-                        asm volatile(
-                            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-                            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-                            : "memory");
-                    }
-                }
+                const uint32_t d_tmem = tmem + static_cast<uint32_t>(2 * s + k) * TT::acc_cols;
+                if (k == 0)
+                    issue_conv_taps<ND, C, 0, TT::tsplit>(a_base, b_base, d_tmem);
+                else
+                    issue_conv_taps<ND, C, TT::tsplit, TT::taps>(a_base, b_base, d_tmem);
                 asm volatile(
                     "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(empty(s))
                     : "memory");
@@ -780,9 +802,12 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
             }
             __syncwarp();
         }
-        if (lane == 0 && *abort_v && committed > 0) {
-            const int j = committed - 1;  // MMAs in flight: wait (bounded) for the last commit
-            (void)mbar_wait(afull(j & 1), (j >> 1) & 1, kWaitNs);
+        if (lane == 0) {
+            // every MMA of this thread done (bounded) before the tensor memory is freed
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             drain(k))
+                         : "memory");
+            if (!mbar_wait(drain(k), 0, kWaitNs)) fail(1);
         }
         __syncwarp();
     } else {
@@ -802,21 +827,27 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
                 break;
             }
             tc_fence_after();
-            uint32_t r[C];
+            uint32_t r[C], r2[C];
 #pragma unroll
-            for (int c0 = 0; c0 < C; c0 += 16) {
-                const uint32_t taddr =
-                    tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(s) * TT::acc_cols + c0;
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-                    "%12, %13, %14, %15}, [%16];\n"
-                    : "=r"(r[c0 + 0]), "=r"(r[c0 + 1]), "=r"(r[c0 + 2]), "=r"(r[c0 + 3]), "=r"(r[c0 + 4]),
-                      "=r"(r[c0 + 5]), "=r"(r[c0 + 6]), "=r"(r[c0 + 7]), "=r"(r[c0 + 8]), "=r"(r[c0 + 9]),
-                      "=r"(r[c0 + 10]), "=r"(r[c0 + 11]), "=r"(r[c0 + 12]), "=r"(r[c0 + 13]), "=r"(r[c0 + 14]),
-                      "=r"(r[c0 + 15])
-                    : "r"(taddr));
+            for (int h = 0; h < 2; ++h) {
+                uint32_t* d = h == 0 ? r : r2;
+#pragma unroll
+                for (int c0 = 0; c0 < C; c0 += 16) {
+                    const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * q) << 16) +
+                                           static_cast<uint32_t>(2 * s + h) * TT::acc_cols + c0;
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                        "%12, %13, %14, %15}, [%16];\n"
+                        : "=r"(d[c0 + 0]), "=r"(d[c0 + 1]), "=r"(d[c0 + 2]), "=r"(d[c0 + 3]), "=r"(d[c0 + 4]),
+                          "=r"(d[c0 + 5]), "=r"(d[c0 + 6]), "=r"(d[c0 + 7]), "=r"(d[c0 + 8]), "=r"(d[c0 + 9]),
+                          "=r"(d[c0 + 10]), "=r"(d[c0 + 11]), "=r"(d[c0 + 12]), "=r"(d[c0 + 13]), "=r"(d[c0 + 14]),
+                          "=r"(d[c0 + 15])
+                        : "r"(taddr));
+                }
             }
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+            for (int c = 0; c < C; ++c) r[c] = __float_as_uint(__uint_as_float(r[c]) + __uint_as_float(r2[c]));
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(aempty(s));
@@ -870,13 +901,16 @@ __global__ void __launch_bounds__(192, 1) conv_mid_tc_kernel(const __grid_consta
 // accumulators (9 x C columns) fit the 512 columns of tensor memory, and each
 // CTA accumulates its share of the tiles for the whole launch; the per-CTA
 // sums are added by reduce_partials_kernel.  Roles: warp 0 issues the TMA
-// loads (two stages), one thread of warp 1 the MMAs; at the end warps 0-1 read
+// loads (two stages); one thread each of warps 1 and 2 issues the MMAs of the
+// first 5 taps of the group and of the other 4 (one issuing thread cannot keep
+// the tensor core busy with MMAs this small); at the end warps 0-1 read
 // tensor-memory lanes 0-63.  Every mbarrier wait is bounded.
 // ---------------------------------------------------------------------------
 template <int ND, int C>
 struct WgTile {
     using TT = TcTile<ND, C>;
     static constexpr int taps_per_cta = 9;
+    static constexpr int tsplit = 5;  // taps of the first issuing thread
     static constexpr int groups = TT::taps / taps_per_cta;
     static constexpr uint32_t xbytes = TT::tbytes;                                   // one input-halo stage
     static constexpr uint32_t ybytes = TT::chunks * TT::tx * TT::ty * 16;            // one output-gradient stage
@@ -917,9 +951,9 @@ __global__ void __launch_bounds__(128, 1) wgrad_tc_kernel(const __grid_constant_
     if (tid == 0) {
         for (int st = 0; st < 2; ++st) {
             mbar_init(full(st), 1);
-            mbar_init(empty(st), 1);
+            mbar_init(empty(st), 2);  // one commit per issuing thread
         }
-        mbar_init(done, 1);
+        mbar_init(done, 2);
         mbar_init(never, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         abort_flag = ((sbase & 127u) != 0u || group >= WT::groups) ? 1 : 0;
@@ -976,9 +1010,9 @@ __global__ void __launch_bounds__(128, 1) wgrad_tc_kernel(const __grid_constant_
                 mbar_expect_tx(full(st), TT::chunks * (TT::box_bytes + TT::tx * TT::ty * 16));
 #pragma unroll
                 for (int ch = 0; ch < TT::chunks; ++ch) {
-                    tma_load_4d(xs(st) + ch * TT::cbytes, &xmaps.m[ch], 0, x0 - 1, y0 - 1,
+                    tma_load_3d(xs(st) + ch * TT::cbytes, &xmaps.m[ch], 8 * (x0 - 1), y0 - 1,
                                 ND == 3 ? b * g.D + z0 - 1 : b, full(st));
-                    tma_load_4d(ys(st) + ch * (TT::tx * TT::ty * 16), &ymaps.m[ch], 0, x0, y0,
+                    tma_load_3d(ys(st) + ch * (TT::tx * TT::ty * 16), &ymaps.m[ch], 8 * x0, y0,
                                 ND == 3 ? b * g.D + z0 : b, full(st));
                 }
                 issued = it + 1;
@@ -990,8 +1024,10 @@ __global__ void __launch_bounds__(128, 1) wgrad_tc_kernel(const __grid_constant_
             }
         }
         __syncwarp();
-    } else if (warp == 1) {
-        // ---- MMA issuer; the warp zeroes batch-boundary planes ----
+    } else if (warp == 1 || warp == 2) {
+        // ---- MMA issuers; each warp zeroes the batch-boundary planes before
+        // its own MMAs (both write the same zeros) ----
+        const int t_lo = warp == 1 ? 0 : WT::tsplit, t_hi = warp == 1 ? WT::tsplit : WT::taps_per_cta;
         constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
                                    (static_cast<uint32_t>(C >> 3) << 17) | (static_cast<uint32_t>(128 >> 4) << 24);
         int it = 0;
@@ -1030,7 +1066,7 @@ __global__ void __launch_bounds__(128, 1) wgrad_tc_kernel(const __grid_constant_
                 // B: MN-major, SBO = chunk plane of the gradient tile, LBO = one tile row (128 bytes)
                 const uint64_t b_base = umma_desc(ys(st), 128, TT::tx * TT::ty * 16);
 #pragma unroll 1
-                for (int tt = 0; tt < WT::taps_per_cta; ++tt) {
+                for (int tt = t_lo; tt < t_hi; ++tt) {
                     const int t = group * WT::taps_per_cta + tt;
                     const int dz = ND == 3 ? t / 9 : 0;
                     const int dy = ND == 3 ? (t / 3) % 3 : t / 3;
@@ -1144,23 +1180,6 @@ __global__ void __launch_bounds__(256) bias_partial_kernel(const bf16* __restric
     }
 }
 
-// sums the partial records of the tensor-core weight gradient: tap t's
-// weights from the cpg records of its tap group, the bias from all of them
-__global__ void reduce_wgrad_tc_kernel(const float* __restrict__ partial, int cpg, int groups, int64_t group_params,
-                                       int64_t wparams, int64_t nparams, float* __restrict__ grad) {
-    for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < nparams;
-         p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        int64_t c0 = 0, c1 = static_cast<int64_t>(cpg) * groups;
-        if (p < wparams) {
-            c0 = (p / group_params) * cpg;
-            c1 = c0 + cpg;
-        }
-        float s = 0.0f;
-        for (int64_t c = c0; c < c1; ++c) s += partial[c * nparams + p];
-        grad[p] = s;
-    }
-}
-
 // ---------------------------------------------------------------------------
 // weight gradients (CUDA cores): per-CTA partial sums over a tile of 256
 // voxels, summed over CTAs by reduce_partials_kernel
@@ -1265,13 +1284,43 @@ __global__ void __launch_bounds__(256) wgrad_kernel(const TI* __restrict__ in, c
     }
 }
 
-__global__ void reduce_partials_kernel(const float* __restrict__ partial, int64_t nparts, int64_t nparams,
-                                       float* __restrict__ grad) {
-    for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < nparams;
-         p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        float s = 0.0f;
-        for (int64_t c = 0; c < nparts; ++c) s += partial[c * nparams + p];
-        grad[p] = s;
+// Sums the per-CTA partial records into the gradient.  Block b owns the 32
+// parameters 32 b .. 32 b + 31 (lane = parameter, coalesced 128-byte rows);
+// warp w adds the records w, w + 32, ... of the range, and the warps' sums are
+// added in warp order, so the result does not depend on timing.  With cpg > 0
+// (tensor-core weight gradients) parameter p < wparams is summed over the cpg
+// records of its tap group, p / group_params; otherwise over all records.
+__global__ void __launch_bounds__(1024) reduce_partials_kernel(const float* __restrict__ partial, int64_t nparts,
+                                                               int64_t nparams, float* __restrict__ grad, int cpg,
+                                                               int64_t group_params, int64_t wparams) {
+    __shared__ float red[32][33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t p0 = static_cast<int64_t>(blockIdx.x) * 32;
+    const int64_t p = p0 + lane;
+    int64_t c0 = 0, c1 = nparts;
+    if (cpg > 0 && p0 < wparams) {  // group_params and wparams are multiples of 32
+        c0 = (p0 / group_params) * cpg;
+        c1 = c0 + cpg;
+    }
+    float s = 0.0f;
+    if (p < nparams) {
+        int64_t c = c0 + warp;
+        for (; c + 96 < c1; c += 128) {
+            const float a0 = partial[c * nparams + p], a1 = partial[(c + 32) * nparams + p];
+            const float a2 = partial[(c + 64) * nparams + p], a3 = partial[(c + 96) * nparams + p];
+            s += a0;
+            s += a1;
+            s += a2;
+            s += a3;
+        }
+        for (; c < c1; c += 32) s += partial[c * nparams + p];
+    }
+    red[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0) {
+        float t = 0.0f;
+        for (int w = 0; w < 32; ++w) t += red[w][lane];
+        if (p < nparams) grad[p] = t;
     }
 }
 
@@ -1540,17 +1589,19 @@ int32_t run_mid(const bf16* in, const uint2* wpk, const float* bias, const bf16*
 int g_conv_engine = BMND_CONV_TCGEN05;
 uint64_t g_wait_probe_ns = 0;  // see bmnd_pilotnet_set_wait_probe
 
-// One 4-D tensor map per 8-channel chunk plane of a chunk-planar BF16 tensor
-// (8 channels, x, y, z * batch) with the given box; out-of-range elements read
-// as zero.  The CUDA driver API's tensor-map encoder is fetched through the
-// runtime (no link-time dependency on libcuda).
-int32_t encode_chunk_maps(const bf16* base, NetGeo g, int C, const uint32_t box_in[4], TcMaps& maps) {
+// One 3-D tensor map per 8-channel chunk plane of a chunk-planar BF16 tensor:
+// (8 channels x W voxels as one row of elements, y, z * batch), with a box of
+// box_vox = (x, y, z) voxels, so a box row is 16 x bytes contiguous in memory
+// and arrives as whole 32-byte sectors; out-of-range elements read as zero.
+// The CUDA driver API's tensor-map encoder is fetched through the runtime (no
+// link-time dependency on libcuda).
+int32_t encode_chunk_maps(const bf16* base, NetGeo g, int C, const uint32_t box_vox[3], TcMaps& maps) {
     memset(&maps, 0, sizeof(maps));
-    const cuuint64_t dims[4] = {8, static_cast<cuuint64_t>(g.W), static_cast<cuuint64_t>(g.H),
+    const cuuint64_t dims[3] = {static_cast<cuuint64_t>(g.W) * 8, static_cast<cuuint64_t>(g.H),
                                 static_cast<cuuint64_t>(g.D) * static_cast<cuuint64_t>(g.nb)};
-    const cuuint64_t strides[3] = {16, static_cast<cuuint64_t>(g.W) * 16, static_cast<cuuint64_t>(g.H) * g.W * 16};
-    const cuuint32_t box[4] = {box_in[0], box_in[1], box_in[2], box_in[3]};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const cuuint64_t strides[2] = {static_cast<cuuint64_t>(g.W) * 16, static_cast<cuuint64_t>(g.H) * g.W * 16};
+    const cuuint32_t box[3] = {box_vox[0] * 8, box_vox[1], box_vox[2]};
+    const cuuint32_t estr[3] = {1, 1, 1};
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
         cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
@@ -1561,7 +1612,7 @@ int32_t encode_chunk_maps(const bf16* base, NetGeo g, int C, const uint32_t box_
     }
     const int64_t nv = g.voxels();
     for (int ch = 0; ch < C / 8; ++ch) {
-        const CUresult rc = encode(&maps.m[ch], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
+        const CUresult rc = encode(&maps.m[ch], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
                                    const_cast<bf16*>(base) + static_cast<int64_t>(ch) * nv * 8, dims, strides, box,
                                    estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -1581,11 +1632,10 @@ int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf1
         return rc;
     if ((reinterpret_cast<uintptr_t>(in) & 15u) != 0 || (reinterpret_cast<uintptr_t>(wtc) & 15u) != 0)
         return fail(BMND_ERR_INVALID_ARG, "pilot net buffers must be 16-byte aligned");
-    // one 4-D map per 8-channel chunk plane: (8 channels, x, y, z * batch), a
-    // box of (8, hx, hy, hz) voxels whose rows are 16 * hx contiguous bytes;
-    // out-of-range elements read as zero
+    // one map per 8-channel chunk plane, a box of (hx, hy, hz) voxels whose
+    // rows are 16 * hx contiguous bytes; out-of-range elements read as zero
     TcMaps maps;
-    const uint32_t box[4] = {8, TT::hx, TT::hy, TT::hz};
+    const uint32_t box[3] = {TT::hx, TT::hy, TT::hz};
     if (int32_t rc = encode_chunk_maps(in, g, C, box, maps)) return rc;
     const int64_t ntiles = static_cast<int64_t>((g.W + TT::tx - 1) / TT::tx) * ((g.H + TT::ty - 1) / TT::ty) * g.D *
                            g.nb;
@@ -1657,7 +1707,8 @@ int32_t run_wgrad(const TI* in, const TG* gout, float* partial, float* grad, int
     kernel<<<static_cast<unsigned>(tiles), 256, S::bytes, stream>>>(in, gout, partial, g);
     BMND_LAUNCH_CHECK("wgrad_kernel");
     constexpr int64_t np = static_cast<int64_t>(Tile<ND>::taps) * CIN * COUT + COUT;
-    reduce_partials_kernel<<<launch_blocks(np, 256), 256, 0, stream>>>(partial, tiles, np, grad);
+    reduce_partials_kernel<<<static_cast<unsigned>((np + 31) / 32), 1024, 0, stream>>>(partial, tiles, np, grad, 0,
+                                                                                      np, np);
     BMND_LAUNCH_CHECK("reduce_partials_kernel");
     return BMND_OK;
 }
@@ -1684,8 +1735,8 @@ int32_t run_wgrad_tc(const bf16* in, const bf16* gout, float* partial, int64_t c
     if (cpg * WT::groups > capacity) cpg = capacity / WT::groups;
     if (cpg < 1) return BMND_ERR_UNSUPPORTED;
     TcMaps xmaps, ymaps;
-    const uint32_t xbox[4] = {8, TT::hx, TT::hy, TT::hz};
-    const uint32_t ybox[4] = {8, TT::tx, TT::ty, 1};
+    const uint32_t xbox[3] = {TT::hx, TT::hy, TT::hz};
+    const uint32_t ybox[3] = {TT::tx, TT::ty, 1};
     if (int32_t rc = encode_chunk_maps(in, g, C, xbox, xmaps)) return rc;
     if (int32_t rc = encode_chunk_maps(gout, g, C, ybox, ymaps)) return rc;
     constexpr int64_t wparams = static_cast<int64_t>(TT::taps) * C * C;
@@ -1696,9 +1747,9 @@ int32_t run_wgrad_tc(const bf16* in, const bf16* gout, float* partial, int64_t c
     BMND_LAUNCH_CHECK("wgrad_tc_kernel");
     bias_partial_kernel<C><<<static_cast<unsigned>(nparts), 256, 0, stream>>>(gout, g.voxels(), partial, np, wparams);
     BMND_LAUNCH_CHECK("bias_partial_kernel");
-    reduce_wgrad_tc_kernel<<<launch_blocks(np, 256), 256, 0, stream>>>(
-        partial, static_cast<int>(cpg), WT::groups, static_cast<int64_t>(WT::taps_per_cta) * C * C, wparams, np, grad);
-    BMND_LAUNCH_CHECK("reduce_wgrad_tc_kernel");
+    reduce_partials_kernel<<<static_cast<unsigned>((np + 31) / 32), 1024, 0, stream>>>(
+        partial, nparts, np, grad, static_cast<int>(cpg), static_cast<int64_t>(WT::taps_per_cta) * C * C, wparams);
+    BMND_LAUNCH_CHECK("reduce_partials_kernel");
     return BMND_OK;
 }
 
