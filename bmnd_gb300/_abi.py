@@ -204,6 +204,8 @@ SIGNATURES = {
         [ctypes.POINTER(StageParams), _VP, _VP, _VP, _VP, _I64, _VP, _VP, _VP, _VP, _VP, _VP, _U64, _U64],
     ),
     "bmnd_unit_rates": (_I32, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _VP, _U64]),
+    "bmnd_mma_rates": (_I32, [ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                              ctypes.POINTER(ctypes.c_double), _VP, _U64]),
     "bmnd_pilotnet_param_count": (_I32, [_PNP, _I64P]),
     "bmnd_pilotnet_packed_bytes": (_I32, [_PNP, _U64P]),
     "bmnd_pilotnet_workspace_bytes": (_I32, [_PNP, _I32, _U64P]),
@@ -287,6 +289,24 @@ def unit_rates(stream=None) -> dict:
     lg2, ffma = ctypes.c_double(0.0), ctypes.c_double(0.0)
     check(lib().bmnd_unit_rates(ctypes.byref(lg2), ctypes.byref(ffma), sink.data_ptr(), int(stream.cuda_stream)))
     return {"lg2_per_s": lg2.value, "ffma_per_s": ffma.value}
+
+
+def mma_rates(configs=((16, 2), (48, 1), (48, 2), (96, 2), (128, 2), (256, 2)), stream=None) -> list:
+    """Measured clocks per 128 x N x 16 BF16 tcgen05 MMA when `issuers` threads
+    of a CTA issue them back to back, for each (N, issuers) in `configs`
+    (``bmnd_mma_rates``).  Returns [(N, issuers, clocks), ...]."""
+    import torch
+
+    n = len(configs)
+    cols = (ctypes.c_int32 * n)(*[int(c[0]) for c in configs])
+    iss = (ctypes.c_int32 * n)(*[int(c[1]) for c in configs])
+    out = (ctypes.c_double * n)()
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    scratch = torch.zeros(sms + 1, dtype=torch.int64, device=torch.cuda.current_device())
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    check(lib().bmnd_mma_rates(n, cols, iss, out, scratch.data_ptr(), int(stream.cuda_stream)))
+    return [(int(c[0]), int(c[1]), float(out[i])) for i, c in enumerate(configs)]
 
 
 def launch_count() -> int:

@@ -539,7 +539,9 @@ __global__ void __launch_bounds__(256, 1) conv_mid_kernel(const bf16* __restrict
 // bounded: on timeout the kernel records an error, stops issuing work, waits
 // (bounded) for its copies and MMAs in flight, and frees its tensor memory.
 // ---------------------------------------------------------------------------
-template <int ND, int C>
+// NO: output columns of the MMA, C for the C -> C layers, 16 for the output
+// layer (one channel, B padded with zero columns to the smallest N)
+template <int ND, int C, int NO = C>
 struct TcTile {
     static constexpr int tx = 8, ty = 16;
     static constexpr int hx = tx + 2, hy = ty + 2, hz = ND == 3 ? 3 : 1;
@@ -551,10 +553,10 @@ struct TcTile {
     static constexpr uint32_t cbytes = static_cast<uint32_t>(halo_pad) * 16;           // one chunk in shared memory
     static constexpr uint32_t box_bytes = static_cast<uint32_t>(halo) * 16;            // one chunk by TMA
     static constexpr uint32_t tbytes = chunks * cbytes;                                 // one halo stage
-    static constexpr uint32_t wbytes = static_cast<uint32_t>(taps) * kc * 2 * C * 16;  // B core matrices
+    static constexpr uint32_t wbytes = static_cast<uint32_t>(taps) * kc * 2 * NO * 16;  // B core matrices
     static constexpr uint32_t bytes = 2 * tbytes + wbytes;
     static constexpr int tsplit = (taps + 1) / 2;  // taps of the first issuing thread
-    static constexpr uint32_t acc_cols = C <= 32 ? 32 : 64;
+    static constexpr uint32_t acc_cols = NO <= 32 ? 32 : 64;
     static constexpr uint32_t tmem_cols = 4 * acc_cols;  // (stage, half) partial accumulators
     static constexpr int threads = 224;
 };
@@ -589,6 +591,28 @@ __global__ void pack_tc_kernel(const float* __restrict__ W, bf16* __restrict__ o
 
 // c0 is the element offset along a row of the chunk plane (8 per voxel), so
 // c0 * 2 bytes is a multiple of 16 for every voxel offset, negative included
+// B of the output layer (one output channel) for tcgen05 with N = 16:
+// element (t, kc, kk, n, e) = W[t][ci = 16 kc + 8 kk + e] for n = 0, else 0
+template <int ND, int C>
+__global__ void pack_tc_out_kernel(const float* __restrict__ W, bf16* __restrict__ out) {
+    constexpr int T = Tile<ND>::taps;
+    const int64_t total = static_cast<int64_t>(T) * (C / 16) * 2 * 16 * 8;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t r = i;
+        const int e = static_cast<int>(r % 8);
+        r /= 8;
+        const int n = static_cast<int>(r % 16);
+        r /= 16;
+        const int kk = static_cast<int>(r % 2);
+        r /= 2;
+        const int kc = static_cast<int>(r % (C / 16));
+        const int t = static_cast<int>(r / (C / 16));
+        const int k = 16 * kc + 8 * kk + e;
+        out[i] = __float2bfloat16_rn(n == 0 ? W[static_cast<int64_t>(t) * C + k] : 0.0f);
+    }
+}
+
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2,
                                             uint32_t mbar) {
     asm volatile(
@@ -599,10 +623,10 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
 }
 
 // the MMAs of taps T0 .. T1 - 1 of one tile into the accumulator at d_tmem
-template <int ND, int C, int T0, int T1>
+template <int ND, int C, int NO, int T0, int T1>
 __device__ __forceinline__ void issue_conv_taps(uint64_t a_base, uint64_t b_base, uint32_t d_tmem) {
-    using TT = TcTile<ND, C>;
-    constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(C >> 3) << 17) |
+    using TT = TcTile<ND, C, NO>;
+    constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(NO >> 3) << 17) |
                                (static_cast<uint32_t>(128 >> 4) << 24);
 #pragma unroll
     for (int t = T0; t < T1; ++t) {
@@ -614,7 +638,7 @@ __device__ __forceinline__ void issue_conv_taps(uint64_t a_base, uint64_t b_base
         for (int k = 0; k < TT::kc; ++k) {
             // start-address field += offset / 16 (stays below 2^14: no carry)
             const uint64_t ad = a_base + static_cast<uint64_t>(2 * k * TT::halo_pad + vox0);
-            const uint64_t bd = b_base + static_cast<uint64_t>((t * TT::kc + k) * 2 * C);
+            const uint64_t bd = b_base + static_cast<uint64_t>((t * TT::kc + k) * 2 * NO);
             const uint32_t acc = (t != T0 || k != 0) ? 1u : 0u;
             asm volatile(
                 "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -625,13 +649,19 @@ __device__ __forceinline__ void issue_conv_taps(uint64_t a_base, uint64_t b_base
     }
 }
 
-template <int ND, int C>
+// NO == C: a C -> C layer (bias, ReLU or ReLU mask, BF16 out).  NO == 16: the
+// output layer, y = a + b + sum (column 0 of the accumulator), written to y
+// and, as the inverse Anscombe transform, to pilot (either may be null).
+template <int ND, int C, int NO = C>
 __global__ void __launch_bounds__(224, 1) conv_mid_tc_kernel(const __grid_constant__ TcMaps maps,
                                                              const bf16* __restrict__ wtc,
                                                              const float* __restrict__ bias,
                                                              const bf16* __restrict__ mask, bf16* __restrict__ out,
-                                                             NetGeo g, int* __restrict__ err, uint64_t probe_ns) {
-    using TT = TcTile<ND, C>;
+                                                             const float* __restrict__ a_in, float* __restrict__ y_out,
+                                                             float* __restrict__ pilot_out, NetGeo g,
+                                                             int* __restrict__ err, uint64_t probe_ns) {
+    using TT = TcTile<ND, C, NO>;
+    constexpr bool kOut = NO != C;
     extern __shared__ __align__(128) unsigned char tc_smem[];
     // full[2] (halo stage landed), empty[2] (stage read by the MMAs), afull[2]
     // (accumulator complete), aempty[2] (accumulator read out), weights, one
@@ -787,12 +817,12 @@ __global__ void __launch_bounds__(224, 1) conv_mid_tc_kernel(const __grid_consta
             tc_fence_after();
             if (lane == 0) {
                 const uint64_t a_base = umma_desc(stage, TT::cbytes, TT::hx * 16);
-                const uint64_t b_base = umma_desc(wsm, C * 16, 128);
+                const uint64_t b_base = umma_desc(wsm, NO * 16, 128);
                 const uint32_t d_tmem = tmem + static_cast<uint32_t>(2 * s + k) * TT::acc_cols;
                 if (k == 0)
-                    issue_conv_taps<ND, C, 0, TT::tsplit>(a_base, b_base, d_tmem);
+                    issue_conv_taps<ND, C, NO, 0, TT::tsplit>(a_base, b_base, d_tmem);
                 else
-                    issue_conv_taps<ND, C, TT::tsplit, TT::taps>(a_base, b_base, d_tmem);
+                    issue_conv_taps<ND, C, NO, TT::tsplit, TT::taps>(a_base, b_base, d_tmem);
                 asm volatile(
                     "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(empty(s))
                     : "memory");
@@ -827,51 +857,80 @@ __global__ void __launch_bounds__(224, 1) conv_mid_tc_kernel(const __grid_consta
                 break;
             }
             tc_fence_after();
-            uint32_t r[C], r2[C];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                uint32_t* d = h == 0 ? r : r2;
-#pragma unroll
-                for (int c0 = 0; c0 < C; c0 += 16) {
-                    const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * q) << 16) +
-                                           static_cast<uint32_t>(2 * s + h) * TT::acc_cols + c0;
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-                        "%12, %13, %14, %15}, [%16];\n"
-                        : "=r"(d[c0 + 0]), "=r"(d[c0 + 1]), "=r"(d[c0 + 2]), "=r"(d[c0 + 3]), "=r"(d[c0 + 4]),
-                          "=r"(d[c0 + 5]), "=r"(d[c0 + 6]), "=r"(d[c0 + 7]), "=r"(d[c0 + 8]), "=r"(d[c0 + 9]),
-                          "=r"(d[c0 + 10]), "=r"(d[c0 + 11]), "=r"(d[c0 + 12]), "=r"(d[c0 + 13]), "=r"(d[c0 + 14]),
-                          "=r"(d[c0 + 15])
-                        : "r"(taddr));
-                }
-            }
-            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-            for (int c = 0; c < C; ++c) r[c] = __float_as_uint(__uint_as_float(r[c]) + __uint_as_float(r2[c]));
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(aempty(s));
-            int b, z0, y0, x0;
-            decode(tl, b, z0, y0, x0);
-            const int xx = x0 + (m % TT::tx), yy = y0 + m / TT::tx;
-            if (xx < g.W && yy < g.H) {
-                const int64_t v = vox_index(g, b, z0, yy, xx);
-#pragma unroll
-                for (int c0 = 0; c0 < C; c0 += 8) {
-                    __align__(16) bf16 o[8];
-                    if (mask) {
-                        __align__(16) bf16 mk[8];
-                        *reinterpret_cast<uint4*>(mk) = *reinterpret_cast<const uint4*>(mask + hid<C>(v, c0, nv));
-#pragma unroll
-                        for (int j = 0; j < 8; ++j)
-                            o[j] = __float2bfloat16_rn(__bfloat162float(mk[j]) > 0.0f ? __uint_as_float(r[c0 + j])
-                                                                                     : 0.0f);
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 8; ++j)
-                            o[j] = __float2bfloat16_rn(fmaxf(__uint_as_float(r[c0 + j]) + __ldg(bias + c0 + j), 0.0f));
+            if constexpr (kOut) {
+                // output layer: column 0 of both partial accumulators
+                uint32_t p0, p1;
+                const uint32_t tbase = tmem + (static_cast<uint32_t>(32 * q) << 16);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];\n"
+                             : "=r"(p0)
+                             : "r"(tbase + static_cast<uint32_t>(2 * s) * TT::acc_cols));
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];\n"
+                             : "=r"(p1)
+                             : "r"(tbase + static_cast<uint32_t>(2 * s + 1) * TT::acc_cols));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(aempty(s));
+                int b, z0, y0, x0;
+                decode(tl, b, z0, y0, x0);
+                const int xx = x0 + (m % TT::tx), yy = y0 + m / TT::tx;
+                if (xx < g.W && yy < g.H) {
+                    const int64_t v = vox_index(g, b, z0, yy, xx);
+                    const float yv = a_in[v] + (__ldg(bias) + (__uint_as_float(p0) + __uint_as_float(p1)));
+                    if (y_out) y_out[v] = yv;
+                    if (pilot_out) {
+                        const float hh = 0.5f * yv;
+                        pilot_out[v] = fmaxf(hh * hh - 0.375f, 0.0f);
                     }
-                    *reinterpret_cast<uint4*>(out + hid<C>(v, c0, nv)) = *reinterpret_cast<const uint4*>(o);
+                }
+            } else {
+                uint32_t r[C], r2[C];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    uint32_t* d = h == 0 ? r : r2;
+#pragma unroll
+                    for (int c0 = 0; c0 < C; c0 += 16) {
+                        const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * q) << 16) +
+                                               static_cast<uint32_t>(2 * s + h) * TT::acc_cols + c0;
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                            "%12, %13, %14, %15}, [%16];\n"
+                            : "=r"(d[c0 + 0]), "=r"(d[c0 + 1]), "=r"(d[c0 + 2]), "=r"(d[c0 + 3]), "=r"(d[c0 + 4]),
+                              "=r"(d[c0 + 5]), "=r"(d[c0 + 6]), "=r"(d[c0 + 7]), "=r"(d[c0 + 8]), "=r"(d[c0 + 9]),
+                              "=r"(d[c0 + 10]), "=r"(d[c0 + 11]), "=r"(d[c0 + 12]), "=r"(d[c0 + 13]), "=r"(d[c0 + 14]),
+                              "=r"(d[c0 + 15])
+                            : "r"(taddr));
+                    }
+                }
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                for (int c = 0; c < C; ++c) r[c] = __float_as_uint(__uint_as_float(r[c]) + __uint_as_float(r2[c]));
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(aempty(s));
+                int b, z0, y0, x0;
+                decode(tl, b, z0, y0, x0);
+                const int xx = x0 + (m % TT::tx), yy = y0 + m / TT::tx;
+                if (xx < g.W && yy < g.H) {
+                    const int64_t v = vox_index(g, b, z0, yy, xx);
+#pragma unroll
+                    for (int c0 = 0; c0 < C; c0 += 8) {
+                        __align__(16) bf16 o[8];
+                        if (mask) {
+                            __align__(16) bf16 mk[8];
+                            *reinterpret_cast<uint4*>(mk) = *reinterpret_cast<const uint4*>(mask + hid<C>(v, c0, nv));
+#pragma unroll
+                            for (int j = 0; j < 8; ++j)
+                                o[j] = __float2bfloat16_rn(__bfloat162float(mk[j]) > 0.0f ? __uint_as_float(r[c0 + j])
+                                                                                         : 0.0f);
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 8; ++j)
+                                o[j] = __float2bfloat16_rn(
+                                    fmaxf(__uint_as_float(r[c0 + j]) + __ldg(bias + c0 + j), 0.0f));
+                        }
+                        *reinterpret_cast<uint4*>(out + hid<C>(v, c0, nv)) = *reinterpret_cast<const uint4*>(o);
+                    }
                 }
             }
         }
@@ -1447,9 +1506,10 @@ struct NetPlan {
     uint64_t p_in_w, packed_bytes;
     std::vector<uint64_t> p_mid_fwd, p_mid_bwd;
     uint64_t mid_frag_bytes;
-    // the same layers as tcgen05 B operands (forward and data gradient)
+    // the same layers as tcgen05 B operands (forward and data gradient), and
+    // the output layer's weights as a B operand of 16 columns
     std::vector<uint64_t> p_tc_fwd, p_tc_bwd;
-    uint64_t tc_bytes;
+    uint64_t tc_bytes, p_tc_out, tc_out_bytes;
     int64_t max_layer_params;
 };
 
@@ -1507,6 +1567,9 @@ int32_t make_plan(const BmndPilotNet* net, NetPlan& P) {
         P.p_tc_bwd.push_back(po);
         po = a256(po + P.tc_bytes);
     }
+    P.tc_out_bytes = static_cast<uint64_t>(P.taps) * (P.C / 16) * 2 * 16 * 16;
+    P.p_tc_out = po;
+    po = a256(po + P.tc_out_bytes);
     P.packed_bytes = po;
     return BMND_OK;
 }
@@ -1642,8 +1705,33 @@ int32_t run_mid_tc(const bf16* in, const bf16* wtc, const float* bias, const bf1
     // one persistent CTA per SM: the weights fill most of the shared memory
     int64_t blocks = sms;
     if (blocks > ntiles) blocks = ntiles;
-    kernel<<<static_cast<unsigned>(blocks), TT::threads, TT::bytes, stream>>>(maps, wtc, bias, mask, out, g, err,
-                                                                             g_wait_probe_ns);
+    kernel<<<static_cast<unsigned>(blocks), TT::threads, TT::bytes, stream>>>(
+        maps, wtc, bias, mask, out, nullptr, nullptr, nullptr, g, err, g_wait_probe_ns);
+    BMND_LAUNCH_CHECK("conv_mid_tc_kernel");
+    return BMND_OK;
+}
+
+// the output layer (C -> 1) on the tensor cores: N = 16 columns, column 0 used
+template <int ND, int C>
+int32_t run_out_tc(const bf16* in, const bf16* wtc, const float* bias, const float* a, float* y, float* pilot,
+                   NetGeo g, int* err, cudaStream_t stream) {
+    using TT = TcTile<ND, C, 16>;
+    auto kernel = conv_mid_tc_kernel<ND, C, 16>;
+    int sms = 0, per_sm = 0;
+    if (int32_t rc = kernel_residency(reinterpret_cast<const void*>(kernel), TT::threads, TT::bytes, false, &per_sm,
+                                      &sms))
+        return rc;
+    if ((reinterpret_cast<uintptr_t>(in) & 15u) != 0 || (reinterpret_cast<uintptr_t>(wtc) & 15u) != 0)
+        return fail(BMND_ERR_INVALID_ARG, "pilot net buffers must be 16-byte aligned");
+    TcMaps maps;
+    const uint32_t box[3] = {TT::hx, TT::hy, TT::hz};
+    if (int32_t rc = encode_chunk_maps(in, g, C, box, maps)) return rc;
+    const int64_t ntiles = static_cast<int64_t>((g.W + TT::tx - 1) / TT::tx) * ((g.H + TT::ty - 1) / TT::ty) * g.D *
+                           g.nb;
+    int64_t blocks = sms;
+    if (blocks > ntiles) blocks = ntiles;
+    kernel<<<static_cast<unsigned>(blocks), TT::threads, TT::bytes, stream>>>(
+        maps, wtc, bias, nullptr, nullptr, a, y, pilot, g, err, g_wait_probe_ns);
     BMND_LAUNCH_CHECK("conv_mid_tc_kernel");
     return BMND_OK;
 }
@@ -1679,6 +1767,10 @@ int32_t forward_impl(const NetPlan& P, const unsigned char* packed, const float*
     for (int l = 1; l < P.L - 1; ++l) {
         int32_t rc = run_layer<ND, C>(P, packed, l, false, act(l - 1), wr + P.b_off[l], nullptr, act(l), B, stream);
         if (rc) return rc;
+    }
+    if (g_conv_engine == BMND_CONV_TCGEN05) {
+        return run_out_tc<ND, C>(act(P.L - 2), reinterpret_cast<const bf16*>(packed + P.p_tc_out),
+                                 wr + P.b_off[P.L - 1], B.a, y_out, pilot, g, B.err, stream);
     }
     {
         using OT = OutTile<ND>;
@@ -1901,6 +1993,10 @@ int32_t bmnd_pilotnet_pack(const BmndPilotNet* net, const float* d_params, void*
                 BMND_LAUNCH_CHECK("pack_tc_kernel");
             }
         }
+        const int64_t nout = static_cast<int64_t>(P.tc_out_bytes / 2);
+        pack_tc_out_kernel<ND, C><<<launch_blocks(nout, 256), 256, 0, stream>>>(
+            d_params + P.w_off[P.L - 1], reinterpret_cast<bf16*>(pk + P.p_tc_out));
+        BMND_LAUNCH_CHECK("pack_tc_out_kernel");
         return BMND_OK;
     });
 }

@@ -408,6 +408,18 @@ int32_t bmnd_stage_noalloc(const BmndStageParams* params, const float* d_noisy,
  */
 int32_t bmnd_unit_rates(double* lg2_per_s, double* ffma_per_s, void* d_sink, uint64_t stream);
 
+/*
+ * Measurement support (no counterpart in the reference): for each of `count`
+ * configurations, the mean clocks one tcgen05.mma kind::f16 (BF16 in, FP32
+ * accumulate, M = 128, N = n_cols[i], K = 16, operands in shared memory) takes
+ * on every SM when issuers[i] threads of a CTA (1..4, one per warp) issue them
+ * back to back into accumulators of their own.  n_cols[i] is 16..256 in steps
+ * of 16 and n_cols[i] x issuers[i] <= 512.  d_scratch: device memory of at
+ * least 8 x (SM count + 1) bytes.  Synchronises the stream.
+ */
+int32_t bmnd_mma_rates(int32_t count, const int32_t* n_cols, const int32_t* issuers, double* clocks_per_mma,
+                       void* d_scratch, uint64_t stream);
+
 /* ------------------------------------------------------------------------
  * Learned stage-1 pilot (fast path).  No counterpart in the reference: a
  * residual 3x3 (2-D) or 3x3x3 (3-D) convolution net in the Anscombe domain,

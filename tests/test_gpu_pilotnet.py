@@ -191,3 +191,14 @@ def test_fallback_replaces_failing_tiles(cuda, native):
     fb = d["pilot"].cpu().numpy()
     assert abs(phantoms.psnr(fb, clean) - phantoms.psnr(plain_pilot, clean)) < 0.3
     assert bool(cuda.isfinite(out).all())
+
+
+def test_mma_rates_measured(cuda, native):
+    """bmnd_mma_rates: clocks per 128 x N x 16 BF16 MMA on every SM, finite and
+    ordered as the operand reads predict (a wider N never costs less)."""
+    from bmnd_gb300 import _abi
+
+    r = _abi.mma_rates(((48, 2), (128, 2), (256, 2), (48, 1)))
+    clk = [c for _, _, c in r]
+    assert all(10.0 < c < 2000.0 for c in clk), r
+    assert clk[0] <= 1.05 * clk[1] and clk[1] <= 1.05 * clk[2], r
