@@ -309,6 +309,82 @@ __global__ void __launch_bounds__(256) gather_finalize_kernel(const float* __res
     }
 }
 
+// step 4 for compile-time patch extents, tiled: a CTA of 256 threads takes 32 x 8
+// voxels of one plane (one voxel per thread) and first copies the weight sums
+// W of every origin its voxels read (the tile grown by the patch extent minus
+// one on the low side of each axis) into shared memory, so the 125 reads of W
+// per voxel come from there instead of L2.  Same terms, same order and the same
+// compensated sums as gather_finalize_kernel: the results are bit-identical.
+constexpr int kGatherTX = 32, kGatherTY = 8;
+
+template <int BB0, int BB1, int BB2>
+__global__ void __launch_bounds__(256, 4) gather_finalize_tiled_kernel(const float* __restrict__ planes,
+                                                                    const float* __restrict__ wsum,
+                                                                    BmndStageParams sp,
+                                                                    const float* __restrict__ noisy,
+                                                                    float* __restrict__ out) {
+    constexpr int SX = kGatherTX + BB2 - 1, SY = kGatherTY + BB1 - 1, SZ = BB0;
+    __shared__ float win[BB0 * BB1 * BB2];
+    __shared__ float wt[SZ * SY * SX];
+    const Vol3 g(sp);
+    const float eps_f = static_cast<float>(sp.eps);
+    const int no_eps = sp.mass_conserve ? 1 : 0;
+    for (int p = threadIdx.x; p < BB0 * BB1 * BB2; p += blockDim.x) win[p] = sp.window[p];
+    const int c0 = g.counts[0], c1 = g.counts[1], c2 = g.counts[2];
+    const int tiles_x = (g.shape[2] + kGatherTX - 1) / kGatherTX;
+    const int tiles_y = (g.shape[1] + kGatherTY - 1) / kGatherTY;
+    const int64_t ntiles = static_cast<int64_t>(tiles_x) * tiles_y * g.shape[0];
+    const int tx = static_cast<int>(threadIdx.x) % kGatherTX, ty = static_cast<int>(threadIdx.x) / kGatherTX;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int bx = static_cast<int>(t % tiles_x);
+        const int by = static_cast<int>((t / tiles_x) % tiles_y);
+        const int x0 = static_cast<int>(t / (static_cast<int64_t>(tiles_x) * tiles_y));
+        const int y1 = by * kGatherTY, y2 = bx * kGatherTX;
+        __syncthreads();  // the previous tile's weight sums are no longer read
+        for (int i = threadIdx.x; i < SZ * SY * SX; i += blockDim.x) {
+            const int iz = i / (SY * SX), iy = (i / SX) % SY, ix = i % SX;
+            const int o0 = x0 - (BB0 - 1) + iz, o1 = y1 - (BB1 - 1) + iy, o2 = y2 - (BB2 - 1) + ix;
+            float w = 0.0f;
+            if (o0 >= 0 && o0 < c0 && o1 >= 0 && o1 < c1 && o2 >= 0 && o2 < c2)
+                w = __ldg(wsum + (static_cast<int64_t>(o0) * c1 + o1) * c2 + o2);
+            wt[i] = w;
+        }
+        __syncthreads();
+        const int x1 = y1 + ty, x2 = y2 + tx;
+        if (x1 >= g.shape[1] || x2 >= g.shape[2]) continue;
+        const int64_t v = (static_cast<int64_t>(x0) * g.shape[1] + x1) * g.shape[2] + x2;
+        Sum2 num, den;
+        // origin x - d for offset d; terms of offsets whose origin lies off
+        // the patch grid add zero, which leaves the compensated pair unchanged
+        const int64_t ox = (static_cast<int64_t>(x0) * c1 + x1) * c2 + x2;
+#pragma unroll
+        for (int d0 = 0; d0 < BB0; ++d0) {
+            const bool v0 = d0 <= x0 && x0 - d0 < c0;
+#pragma unroll
+            for (int d1 = 0; d1 < BB1; ++d1) {
+                const bool v1 = v0 && d1 <= x1 && x1 - d1 < c1;
+                float pv[BB2], wv[BB2];
+#pragma unroll
+                for (int d2 = 0; d2 < BB2; ++d2) {
+                    const bool ok = v1 && d2 <= x2 && x2 - d2 < c2;
+                    const int p = (d0 * BB1 + d1) * BB2 + d2;
+                    const int64_t o = ox - ((static_cast<int64_t>(d0) * c1 + d1) * c2 + d2);
+                    const int si = ((BB0 - 1 - d0) * SY + (ty + BB1 - 1 - d1)) * SX + (tx + BB2 - 1 - d2);
+                    pv[d2] = ok ? __ldg(planes + static_cast<int64_t>(p) * g.n_lins + o) : 0.0f;
+                    wv[d2] = ok ? mul_rn(win[p], wt[si]) : 0.0f;
+                }
+#pragma unroll
+                for (int d2 = 0; d2 < BB2; ++d2) {
+                    num.add(pv[d2]);
+                    den.add(wv[d2]);
+                }
+            }
+        }
+        const float d = den.value();
+        out[v] = d > 0.0f ? div_rn(num.value(), no_eps ? d : add_rn(d, eps_f)) : noisy[v];
+    }
+}
+
 int64_t grid_for(int64_t n, int threads, int64_t cap = 152 * 32) {
     int64_t b = (n + threads - 1) / threads;
     if (b < 1) b = 1;
@@ -413,12 +489,21 @@ int32_t launch_gather(const BmndStageParams& sp, const float* noisy, float* out,
     const int64_t nvox = volume_voxels(sp);
     const unsigned gb = static_cast<unsigned>(grid_for(nvox, 256, 152 * 16));
     const int* b = sp.block;
+    // tiles of 32 x 8 voxels of one plane (padded geometry: z, y, x)
+    int64_t ntiles = 1;
+    {
+        int sh[3] = {1, 1, 1};
+        for (int d = 0; d < sp.ndim; ++d) sh[3 - sp.ndim + d] = sp.shape[d];
+        ntiles = static_cast<int64_t>((sh[2] + kGatherTX - 1) / kGatherTX) * ((sh[1] + kGatherTY - 1) / kGatherTY) *
+                 sh[0];
+    }
+    const unsigned tb = static_cast<unsigned>(ntiles < 152 * 16 ? ntiles : 152 * 16);
     if (sp.ndim == 3 && b[0] == 5 && b[1] == 5 && b[2] == 5)
-        gather_finalize_kernel<5, 5, 5><<<gb, 256, 0, stream>>>(planes, wsum, sp, noisy, out);
+        gather_finalize_tiled_kernel<5, 5, 5><<<tb, 256, 0, stream>>>(planes, wsum, sp, noisy, out);
     else if (sp.ndim == 3 && b[0] == 4 && b[1] == 4 && b[2] == 4)
-        gather_finalize_kernel<4, 4, 4><<<gb, 256, 0, stream>>>(planes, wsum, sp, noisy, out);
+        gather_finalize_tiled_kernel<4, 4, 4><<<tb, 256, 0, stream>>>(planes, wsum, sp, noisy, out);
     else if (sp.ndim == 2 && b[0] == 8 && b[1] == 8)
-        gather_finalize_kernel<1, 8, 8><<<gb, 256, 0, stream>>>(planes, wsum, sp, noisy, out);
+        gather_finalize_tiled_kernel<1, 8, 8><<<tb, 256, 0, stream>>>(planes, wsum, sp, noisy, out);
     else
         gather_finalize_kernel<0, 0, 0><<<gb, 256, 0, stream>>>(planes, wsum, sp, noisy, out);
     BMND_LAUNCH_CHECK("gather_finalize_kernel");
