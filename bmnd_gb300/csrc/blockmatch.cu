@@ -1092,13 +1092,17 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
         bool compact = false;
         // radix select over the upper bounds d + D of the certainly accepted
         // (of every candidate with `all`): the smallest v with >= need of them
-        // bounded by it, or infinity when there are fewer
-        auto select_kth = [&](int need, bool all) -> float {
+        // bounded by it, or infinity when there are fewer.  `passes` 8-bit
+        // digits are resolved; with 2 the result is the top of its 16-bit bin,
+        // so the candidates bounded by it are a superset of those bounded by
+        // the 3-pass result (the approximate modes, whose selections are
+        // heuristic anyway, take the pass and its barriers off)
+        auto select_kth = [&](int need, bool all, int passes) -> float {
             uint32_t prefix = 0;
             bool found = true;
             for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0u;
             __syncthreads();
-            for (int pass = 0; pass < 3 && found; ++pass) {
+            for (int pass = 0; pass < passes && found; ++pass) {
                 const int shift = 24 - 8 * pass;
                 if (pass > 0) {
                     for (int i = tid; i < 256; i += blockDim.x) hist[i] = 0u;
@@ -1178,7 +1182,8 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                 }
                 __syncthreads();
             }
-            return found ? __uint_as_float((prefix << 8) | 0xffu) : INFINITY;
+            if (!found) return INFINITY;
+            return passes == 3 ? __uint_as_float((prefix << 8) | 0xffu) : __uint_as_float((prefix << 16) | 0xffffu);
         };
 
         // pass A: screening distances and the reference-wide absolute bound
@@ -1267,7 +1272,7 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
                     }
                 }
                 __syncthreads();
-                const float vs = select_kth(a.presel, true);
+                const float vs = select_kth(a.presel, true, 2);
                 const float vskey = canonical_key(vs);
                 // the prescreened candidates in window order (ballots and warp
                 // counts, no atomics), so that when ties at the cut fill the
@@ -1340,7 +1345,7 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
         for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) Dabs = fmaxf(Dabs, redf[w]);
         if (a.approx) Dabs = 0.0f;
 
-        const float vstar = select_kth(K, false);
+        const float vstar = select_kth(K, false, a.approx ? 2 : 3);
         // at least K certainly accepted candidates have exact distances <= vstar
         const float vkey = canonical_key(vstar);
 
@@ -1431,7 +1436,7 @@ __global__ void __launch_bounds__(kSThreads, BMND_SCREEN_MIN_BLOCKS) blockmatch_
             // R smallest screening distances overall, the accepted (below the
             // threshold) first, then the best rejected, as the reference fills it
             __syncthreads();
-            const float v2 = select_kth(R, true);
+            const float v2 = select_kth(R, true, 3);
             const float v2key = canonical_key(v2);
             if (tid == 0) {
                 redi[0] = 0;
