@@ -154,6 +154,7 @@ SIGNATURES = {
     "bmnd_abi_version": (_I32, []),
     "bmnd_last_error": (ctypes.c_char_p, []),
     "bmnd_launch_count": (_I32, [_U64P]),
+    "bmnd_host_memory_direct": (_I32, [ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
     "bmnd_reference_schedule": (
         _I32,
         [_I32, _I32P, _I32P, _I32P, ctypes.c_double, _I32, _I32P, _I32P, _I32P, _I64, _I64P],
@@ -307,6 +308,15 @@ def mma_rates(configs=((16, 2), (48, 1), (48, 2), (96, 2), (128, 2), (256, 2)), 
         stream = torch.cuda.current_stream()
     check(lib().bmnd_mma_rates(n, cols, iss, out, scratch.data_ptr(), int(stream.cuda_stream)))
     return [(int(c[0]), int(c[1]), float(out[i])) for i, c in enumerate(configs)]
+
+
+def host_memory_direct(device: int) -> bool:
+    """True when the device reads ordinary (pageable) host memory through the
+    host's page tables, so host copies need no page-locked staging
+    (``bmnd_host_memory_direct``)."""
+    v = ctypes.c_int32(0)
+    check(lib().bmnd_host_memory_direct(int(device), ctypes.byref(v)))
+    return bool(v.value)
 
 
 def launch_count() -> int:

@@ -109,13 +109,18 @@ _REFS_CACHE: dict = {}
 
 
 class _Staging:
-    """Page-locked host buffers for the NumPy path of :func:`bmnd`, grown on
-    demand and reused: the input is copied into one and sent to the device
-    asynchronously, the result comes back through the other.  The host-side
-    copies are split over a few threads (NumPy releases the interpreter lock
-    while it copies), and the upload goes in slices, each slice's transfer
-    overlapping the copy of the next.  A lock makes concurrent host threads
-    take turns."""
+    """Host <-> device transfers of the NumPy path of :func:`bmnd`.
+
+    Where the device reads ordinary host memory through the host's page
+    tables (a Grace host over NVLink-C2C), the arrays are copied directly: a
+    64 MiB transfer then takes about 0.4 ms either way, the rate of a
+    page-locked one.  Elsewhere page-locked host buffers, grown on demand and
+    reused, carry the data: the input is copied into one and sent to the
+    device asynchronously, the result comes back through the other.  The
+    host-side copies are split over a few threads (NumPy releases the
+    interpreter lock while it copies), and the upload goes in slices, each
+    slice's transfer overlapping the copy of the next.  A lock makes
+    concurrent host threads take turns."""
 
     _SLICES = 8
 
@@ -123,6 +128,13 @@ class _Staging:
         self._lock = threading.Lock()
         self._bufs = {}
         self._pool = None
+        self._direct = {}
+
+    def _is_direct(self, device: int) -> bool:
+        d = self._direct.get(device)
+        if d is None:
+            d = self._direct[device] = _abi.host_memory_direct(device)
+        return d
 
     def _get(self, key, numel):
         torch = _torch()
@@ -153,6 +165,11 @@ class _Staging:
 
     def upload(self, arr: np.ndarray):
         torch = _torch()
+        device = torch.cuda.current_device()
+        if self._is_direct(device):
+            dev = torch.empty(arr.shape, dtype=torch.float32, device=device)
+            dev.copy_(torch.from_numpy(np.ascontiguousarray(arr, dtype=np.float32)))
+            return dev
         with self._lock:
             flat = arr.reshape(-1)
             host = self._get("in", flat.size)
@@ -172,8 +189,37 @@ class _Staging:
             torch.cuda.current_stream().synchronize()
         return dev
 
-    def download(self, t) -> np.ndarray:
+    def result_buffer(self, shape):
+        """A float32 host array of `shape` for a result that :meth:`download`
+        will fill directly, with its pages touched on worker threads while the
+        device computes (a fresh 64 MiB array otherwise takes about 3 ms of page
+        faults inside the copy).  Returns a future of the array, or None where
+        results go through the page-locked buffers."""
         torch = _torch()
+        n = int(np.prod(shape)) if len(shape) else 1
+        if n < (1 << 20) or not self._is_direct(torch.cuda.current_device()):
+            return None
+        out = np.empty(tuple(shape), dtype=np.float32)
+        flat = out.reshape(-1)
+        parts = self._SLICES
+        step = (n + parts - 1) // parts
+        pool = self._threads()
+        futs = [pool.submit(flat[i * step:(i + 1) * step].fill, 0.0) for i in range(parts)]
+
+        class _Ready:
+            def result(self_inner):
+                for f in futs:
+                    f.result()
+                return out
+
+        return _Ready()
+
+    def download(self, t, into=None) -> np.ndarray:
+        torch = _torch()
+        if self._is_direct(t.device.index if t.device.index is not None else torch.cuda.current_device()):
+            out = into.result() if into is not None else np.empty(tuple(t.shape), dtype=np.float32)
+            torch.from_numpy(out).copy_(t)
+            return out
         with self._lock:
             flat = t.reshape(-1)
             n = flat.numel()
@@ -213,8 +259,8 @@ def _cuda_ready() -> bool:
     return _CUDA_READY
 
 
-def _host_result(t) -> np.ndarray:
-    return _STAGING.download(t)
+def _host_result(t, into=None) -> np.ndarray:
+    return _STAGING.download(t, into)
 
 
 _NETS: dict = {}
@@ -672,6 +718,8 @@ def bmnd(
         dev = uploaded
     else:
         dev = _STAGING.upload(np.ascontiguousarray(vol))
+    # the host array of the result, made ready while the device computes
+    result_host = None if torch_input else _STAGING.result_buffer(shape)
     maps = None
     global_sigma = 0.0
     gauss = None
@@ -713,6 +761,6 @@ def bmnd(
         conv = (lambda t: t) if volume.is_cuda else (lambda t: t.cpu())
         return res, {"global": global_sigma, "ht": conv(maps["ht"]), "wiener": conv(maps["wiener"])}
     if maps is None:
-        return _host_result(out)
-    return _host_result(out), {"global": global_sigma, "ht": maps["ht"].cpu().numpy(),
+        return _host_result(out, result_host)
+    return _host_result(out, result_host), {"global": global_sigma, "ht": maps["ht"].cpu().numpy(),
                                "wiener": maps["wiener"].cpu().numpy()}

@@ -477,6 +477,15 @@ int32_t bmnd_launch_count(uint64_t* count) {
     return BMND_OK;
 }
 
+int32_t bmnd_host_memory_direct(int32_t device, int32_t* direct) {
+    clear_error();
+    if (!direct) return fail(BMND_ERR_INVALID_ARG, "null argument");
+    int v = 0;
+    BMND_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device));
+    *direct = v ? 1 : 0;
+    return BMND_OK;
+}
+
 int32_t bmnd_reference_schedule(int32_t ndim, const int32_t* counts, const int32_t* block,
                                 const int32_t* step, double shift_density,
                                 int32_t schedule_density, int32_t* out_abs, int32_t* out_shifted,

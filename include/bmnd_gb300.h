@@ -215,6 +215,12 @@ const char* bmnd_last_error(void);
  * the difference of two readings counts the launches between them. */
 int32_t bmnd_launch_count(uint64_t* count);
 
+/* *direct = 1 when `device` reads pageable host memory through the host's page
+ * tables (cudaDevAttrPageableMemoryAccessUsesHostPageTables, e.g. a Grace host
+ * over NVLink-C2C): copies from and to ordinary host memory then run at the
+ * link's rate and need no page-locked staging buffer; else 0. */
+int32_t bmnd_host_memory_direct(int32_t device, int32_t* direct);
+
 /*
  * Host-only.  GENERATED reference schedule: replaces get_reference_schedule
  * with mode="generated" (src/bmnd/shifts.py:405-423, :519-576, :229-266).
