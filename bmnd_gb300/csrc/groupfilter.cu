@@ -267,8 +267,8 @@ __device__ void group_axis_inplace(float* buf, int P, const float* G) {
 // block sum / w; the inverse adds and subtracts the detail down the pyramid.
 // The rounding differs from the matrix product, so only the fast path uses it.
 template <int N, int KIND>
-__device__ void haar_axis_fast(float* buf, int P) {
-    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+__device__ __forceinline__ void haar_column(float* buf, int p, int P) {
+    {
         float x[N];
 #pragma unroll
         for (int k = 0; k < N; ++k) x[k] = buf[k * P + p];
@@ -308,7 +308,35 @@ __device__ void haar_axis_fast(float* buf, int P) {
 #pragma unroll
         for (int k = 0; k < N; ++k) buf[k * P + p] = out[k];
     }
+}
+
+template <int N, int KIND>
+__device__ void haar_axis_fast(float* buf, int P) {
+    for (int p = threadIdx.x; p < P; p += blockDim.x) haar_column<N, KIND>(buf, p, P);
     __syncthreads();
+}
+
+// the forward Haar group axis of three groups in one sweep: s squared (kind
+// 2), x and r (kind 0; r may be null)
+template <int N>
+__device__ void haar_axis_fast3(float* s, float* x, float* r, int P) {
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        haar_column<N, 2>(s, p, P);
+        haar_column<N, 0>(x, p, P);
+        if (r) haar_column<N, 0>(r, p, P);
+    }
+    __syncthreads();
+}
+
+__device__ bool haar_axis_any3(float* s, float* x, float* r, int n, int P) {
+    switch (n) {
+        case 2: haar_axis_fast3<2>(s, x, r, P); return true;
+        case 4: haar_axis_fast3<4>(s, x, r, P); return true;
+        case 8: haar_axis_fast3<8>(s, x, r, P); return true;
+        case 16: haar_axis_fast3<16>(s, x, r, P); return true;
+        case 32: haar_axis_fast3<32>(s, x, r, P); return true;
+        default: return false;
+    }
 }
 
 template <int KIND>
@@ -355,6 +383,20 @@ __device__ void group_axis_any(float* buf, int n, int P, const float* G) {
 // transforms whole lines of B values (matrix in registers), so lines never
 // share a thread and the product overwrites its input
 template <int B, int INNER>
+__device__ __forceinline__ void space_line(float* buf, int base, const float (&m)[B * B]) {
+    float x[B];
+#pragma unroll
+    for (int k = 0; k < B; ++k) x[k] = buf[base + k * INNER];
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int k = 0; k < B; ++k) acc = fmaf(m[i * B + k], x[k], acc);
+        buf[base + i * INNER] = acc;
+    }
+}
+
+template <int B, int INNER>
 __device__ void space_axis_reg(float* buf, int total, const float* Msrc, bool square) {
     float m[B * B];
 #pragma unroll
@@ -366,17 +408,30 @@ __device__ void space_axis_reg(float* buf, int total, const float* Msrc, bool sq
     for (int line = threadIdx.x; line < lines; line += blockDim.x) {
         const int o = line / INNER;
         const int t = line - o * INNER;
+        space_line<B, INNER>(buf, o * B * INNER + t, m);
+    }
+    __syncthreads();
+}
+
+// the same axis of three groups in one sweep: s with the squared matrix, x and
+// r (may be null) with the matrix itself
+template <int B, int INNER>
+__device__ void space_axis_reg3(float* s, float* x, float* r, int total, const float* Msrc) {
+    float m[B * B], m2[B * B];
+#pragma unroll
+    for (int q = 0; q < B * B; ++q) {
+        const float v = Msrc[q];
+        m[q] = v;
+        m2[q] = mul_rn(v, v);
+    }
+    const int lines = total / B;
+    for (int line = threadIdx.x; line < lines; line += blockDim.x) {
+        const int o = line / INNER;
+        const int t = line - o * INNER;
         const int base = o * B * INNER + t;
-        float x[B];
-#pragma unroll
-        for (int k = 0; k < B; ++k) x[k] = buf[base + k * INNER];
-#pragma unroll
-        for (int i = 0; i < B; ++i) {
-            float acc = 0.0f;
-#pragma unroll
-            for (int k = 0; k < B; ++k) acc = fmaf(m[i * B + k], x[k], acc);
-            buf[base + i * INNER] = acc;
-        }
+        space_line<B, INNER>(s, base, m2);
+        space_line<B, INNER>(x, base, m);
+        if (r) space_line<B, INNER>(r, base, m);
     }
     __syncthreads();
 }
@@ -413,6 +468,13 @@ __device__ __forceinline__ void space_axis_fixed(float* buf, int n, const float*
     space_axis_reg<B, INNER>(buf, n * B0 * B1 * B2, M, square);
 }
 
+template <int ND, int B0, int B1, int B2, int D>
+__device__ __forceinline__ void space_axis_fixed3(float* s, float* x, float* r, int n, const float* M) {
+    constexpr int B = D == 0 ? B0 : (D == 1 ? B1 : B2);
+    constexpr int INNER = D == 0 ? (ND > 1 ? B1 : 1) * (ND > 2 ? B2 : 1) : (D == 1 ? (ND > 2 ? B2 : 1) : 1);
+    space_axis_reg3<B, INNER>(s, x, r, n * B0 * B1 * B2, M);
+}
+
 // separable transform of an (n, block...) group in place: the group axis
 // first, then the patch axes (transforms.py:209-255).  kind: 0 forward,
 // 1 inverse, 2 squared forward, 3 transposed inverse (poisson.py:84-114).
@@ -442,6 +504,29 @@ __device__ void transform_group(const GM& geo, const FilterArgs& a, unsigned cha
     } else {
         for (int d = 0; d < geo.nd(); ++d)
             space_axis_generic(geo, d, buf, n, F + d * BMND_MAX_EDGE * BMND_MAX_EDGE, square);
+    }
+}
+
+// The three forward transforms of the approximate path in one sweep of passes:
+// the variance group S squared (kind 2), the observation X and the pilot R
+// (kind 0, R may be null).  Only for compile-time patches with the Haar group
+// axis by its pyramid and a power-of-two group; returns false, having done
+// nothing, otherwise.  Every element goes through the same operations as in
+// transform_group, so the results are the same bits.
+template <int ND, int B0, int B1, int B2, class GM>
+__device__ bool transform_forward3(const GM& geo, const FilterArgs& a, unsigned char* smem, int n, float* S,
+                                   float* X, float* R) {
+    if constexpr (ND == 0) {
+        return false;
+    } else {
+        if (!(a.sp.fast_group_transform && a.sp.group_transform == BMND_GROUP_HAAR)) return false;
+        if (!haar_axis_any3(S, X, R, n, geo.P())) return false;
+        const float* F = sm<float>(smem, a.L.fw);
+        space_axis_fixed3<ND, B0, B1, B2, 0>(S, X, R, n, F);
+        if constexpr (ND > 1) space_axis_fixed3<ND, B0, B1, B2, 1>(S, X, R, n, F + BMND_MAX_EDGE * BMND_MAX_EDGE);
+        if constexpr (ND > 2)
+            space_axis_fixed3<ND, B0, B1, B2, 2>(S, X, R, n, F + 2 * BMND_MAX_EDGE * BMND_MAX_EDGE);
+        return true;
     }
 }
 
@@ -1208,6 +1293,7 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
     // The observation (and the pilot) are gathered here too, so the volume the
     // variance comes from is read once (its lists are no longer needed).
     bool gathered = false;
+    bool fused = false;  // X and R already forward-transformed with S
     if (!gauss && need_approx) {
         for (int e = tid; e < total; e += blockDim.x) {
             const int g = e / P;
@@ -1219,7 +1305,8 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
         }
         gathered = true;
         __syncthreads();
-        transform_group<ND, B0, B1, B2>(geo, a, smem, n, S, 2);
+        fused = transform_forward3<ND, B0, B1, B2>(geo, a, smem, n, S, X, wiener ? R : nullptr);
+        if (!fused) transform_group<ND, B0, B1, B2>(geo, a, smem, n, S, 2);
         for (int e = tid; e < total; e += blockDim.x) {
             const float v = S[e];
             S[e] = sqrtf(v > 0.0f ? v : 0.0f);
@@ -1290,8 +1377,10 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
         }
         __syncthreads();
     }
-    transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, 0);
-    if (wiener) transform_group<ND, B0, B1, B2>(geo, a, smem, n, R, 0);
+    if (!fused) {
+        transform_group<ND, B0, B1, B2>(geo, a, smem, n, X, 0);
+        if (wiener) transform_group<ND, B0, B1, B2>(geo, a, smem, n, R, 0);
+    }
     const int64_t probe_base = gid * static_cast<int64_t>(a.nmax) * P;
     if (a.probe.active) {
         for (int e = tid; e < total; e += blockDim.x) {
