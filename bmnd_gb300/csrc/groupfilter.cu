@@ -1016,14 +1016,18 @@ __global__ void __launch_bounds__(NT, NT == kThreads ? (ND >= 2 ? 3 : 2) : 1) gr
         const float* gtab = a.st + 2 * static_cast<int64_t>(P) * kron_stride(P) + group_table_offset(n);
         for (int e = tid; e < n * n; e += blockDim.x) G[e] = __ldg(gtab + e);
     }
-    for (int e = tid; e < BMND_MAX_DIMS * BMND_MAX_EDGE * BMND_MAX_EDGE; e += blockDim.x) {
-        Fw[e] = sp.spatial_fwd[e / (BMND_MAX_EDGE * BMND_MAX_EDGE)][e % (BMND_MAX_EDGE * BMND_MAX_EDGE)];
-        Fi[e] = sp.spatial_inv[e / (BMND_MAX_EDGE * BMND_MAX_EDGE)][e % (BMND_MAX_EDGE * BMND_MAX_EDGE)];
+    // only the b x b entries of each axis are read; the parameters live in the
+    // constant bank, where lanes reading different addresses take turns
+    for (int d = 0; d < geo.nd(); ++d) {
+        const int bb = geo.b(d) * geo.b(d);
+        for (int q = tid; q < bb; q += blockDim.x) {
+            Fw[d * BMND_MAX_EDGE * BMND_MAX_EDGE + q] = sp.spatial_fwd[d][q];
+            Fi[d * BMND_MAX_EDGE * BMND_MAX_EDGE + q] = sp.spatial_inv[d][q];
+        }
     }
-    for (int e = tid; e < P; e += blockDim.x) {
-        win[e] = sp.window[e];
-        mdiag[e] = sp.spatial_metric_diag[e];
-    }
+    for (int e = tid; e < P; e += blockDim.x) win[e] = sp.window[e];
+    if (sp.windowed_synthesis)  // the only reader of the metric diagonal
+        for (int e = tid; e < P; e += blockDim.x) mdiag[e] = sp.spatial_metric_diag[e];
     if (a.den_ro) {
         // matrices are stored densely, b x b row-major, per axis
         float* Fit = sm<float>(smem, a.L.fit);
