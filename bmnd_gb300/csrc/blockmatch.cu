@@ -1964,7 +1964,11 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
     for (int d = 0; d < a.ndim; ++d) wmax *= std::min<int64_t>(2 * a.radius[d] + 1, a.counts[d]);
     a.approx = precision == BMND_MATCH_APPROX || precision == BMND_MATCH_SUBSAMPLED;
     a.sub = precision == BMND_MATCH_SUBSAMPLED;
-    a.presel = std::min(4 * a.max_m, kSQueue);
+    // subsampled prescreen: candidates kept for the full form, 3K in 3-D (the
+    // sub-lattice holds 27 of 125 voxels; 256^3: 26.2 ms against 28.0 ms with
+    // 4K, +0.072 against +0.080 dB over the plain path), 4K in 2-D (16 of 64
+    // voxels, a noisier estimate)
+    a.presel = std::min((a.ndim == 3 ? 3 : 4) * a.max_m, kSQueue);
     if (a.null_moments) {
         // candidate standardisation: exact warp kernel, per-term evaluation
         a.use_table = 0;
