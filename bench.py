@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import gc
 import json
 import os
 import subprocess
@@ -432,7 +433,10 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         """W untimed calls, then K calls each bracketed by CUDA events on the
         launching stream, L2 flushed before each; returns (ms per call, last
         output).  ``counts`` (a list) receives the native library's kernel
-        launches over the K timed calls."""
+        launches over the K timed calls.  The garbage collector is paused
+        while the K calls run (as ``timeit`` does): a full collection over
+        this process's objects takes milliseconds and would stall the host
+        between a call's launches."""
         for _ in range(args.warmup):
             res = fn()
         torch.cuda.synchronize()
@@ -441,14 +445,19 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         torch.cuda.synchronize()
         n0 = _abi.launch_count()
         total = 0.0
-        for _ in range(args.steps):
-            flush.fill_(1)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            res = fn()
-            e1.record(stream)
-            e1.synchronize()
-            total += e0.elapsed_time(e1)
+        gc.collect()
+        gc.disable()
+        try:
+            for _ in range(args.steps):
+                flush.fill_(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                res = fn()
+                e1.record(stream)
+                e1.synchronize()
+                total += e0.elapsed_time(e1)
+        finally:
+            gc.enable()
         torch.cuda.synchronize()
         if counts is not None:
             counts.append(_abi.launch_count() - n0)
@@ -492,23 +501,34 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
                     pilot=fdet.get("pilot"), ms_fs2=ms_fs2, out_fs2=out_fs2, net=net)
     clocks = sampler.stop()
 
-    # end to end through the public API (host array in, host array out)
+    # end to end through the public API (host array in, host array out), with
+    # the garbage collector paused over the timed calls as in timed_loop
     e2e_steps = max(1, args.steps)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        host_out = bg.bmnd(noisy, profile, match_precision=args.precision, sigma=sigma)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    gc.collect()
+    gc.disable()
+    try:
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            host_out = bg.bmnd(noisy, profile, match_precision=args.precision, sigma=sigma)
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+    finally:
+        gc.enable()
     e2e_fast_s = None
     if fast is not None:
         # the public call a user makes: NumPy array in, NumPy array out, with the
         # argument checks, the copy to the device and the copy back inside
         bg.bmnd(noisy, profile, pilot="learned")
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            host_fast = bg.bmnd(noisy, profile, pilot="learned")
-        e2e_fast_s = (time.perf_counter() - t0) / e2e_steps
+        gc.collect()
+        gc.disable()
+        try:
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                host_fast = bg.bmnd(noisy, profile, pilot="learned")
+            e2e_fast_s = (time.perf_counter() - t0) / e2e_steps
+        finally:
+            gc.enable()
         assert host_fast.shape == noisy.shape
     if dist:
         e2e_s, e2e_fast_max = max_over_ranks([e2e_s, e2e_fast_s or 0.0], dist, "cuda")
