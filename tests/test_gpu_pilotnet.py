@@ -99,16 +99,18 @@ def test_tensor_memory_engine_matches_warp_mma(cuda, native, ndim, channels, lay
 
 def test_tensor_core_wait_runs_out_and_recovers(cuda, native):
     """Failure detection without a GPU fault: with the wait probe set, every
-    tcgen05 layer waits 2 ms on an mbarrier that nothing completes; the wait
-    runs out, the launches stop with their tensor memory freed, and the status
-    call reports BMND_ERR_TIMEOUT.  The next forward pass (probe off) runs and
-    equals the one before the probe bit for bit, which also shows that the
-    tensor memory was given back (an allocation would wait otherwise)."""
+    tcgen05 layer waits 2 ms on an mbarrier that nothing completes, in the
+    forward and in the gradient pass; the wait runs out, the launches stop with
+    their tensor memory freed, and the status call reports BMND_ERR_TIMEOUT.
+    The next forward and gradient passes (probe off) run and equal the ones
+    before the probe bit for bit, which also shows that the tensor memory was
+    given back (an allocation would wait otherwise)."""
     from bmnd_gb300 import _abi
     from bmnd_gb300.pilot import get_conv_engine, set_conv_engine
 
     rng = np.random.default_rng(11)
     x = cuda.from_numpy(rng.poisson(rng.uniform(1, 20, size=(1, 20, 36, 40))).astype(np.float32)).cuda()
+    t = 0.7 * x + 2.0
     net, _ = _net(cuda, 3, 48, 5, seed=12)
     lib = _abi.lib()
     old = get_conv_engine()
@@ -116,17 +118,29 @@ def test_tensor_core_wait_runs_out_and_recovers(cuda, native):
         set_conv_engine("tcgen05")
         before = net.forward(x).clone()
         net.check_status()
+        _, grad_before = net.gradient(x, t)
+        grad_before = grad_before.clone()
+        net.check_status(training=True)
         _abi.check(lib.bmnd_pilotnet_set_wait_probe(2_000_000))
         try:
             net.forward(x)
             with pytest.raises(_abi.BmndError) as info:
                 net.check_status()
             assert info.value.code == _abi.ERR_TIMEOUT
+            # the gradient pass: the tensor-core layers and weight gradients
+            # (512 tensor-memory columns each) time out the same way
+            net.gradient(x, t)
+            with pytest.raises(_abi.BmndError) as info:
+                net.check_status(training=True)
+            assert info.value.code == _abi.ERR_TIMEOUT
         finally:
             _abi.check(lib.bmnd_pilotnet_set_wait_probe(0))
         after = net.forward(x)
         net.check_status()
         assert cuda.equal(after, before)
+        _, grad_after = net.gradient(x, t)
+        net.check_status(training=True)
+        assert cuda.equal(grad_after, grad_before)
     finally:
         set_conv_engine(old)
     with pytest.raises(_abi.BmndError):
