@@ -174,6 +174,7 @@ extern "C" int32_t bmnd_mma_rates(int32_t count, const int32_t* n_cols, const in
             return fail(BMND_ERR_INVALID_ARG,
                         "mma rate: N must be 16..256 in steps of 16, 1..4 issuers, N x issuers <= 512");
     }
+    if (count == 0) return BMND_OK;
     int dev = 0, sms = 0;
     BMND_CUDA_TRY(cudaGetDevice(&dev));
     BMND_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

@@ -92,6 +92,24 @@ def test_native_errors_are_reported(native):
     assert native.bmnd_stage_workspace_bytes(ctypes.byref(p), 10, ctypes.byref(out)) == _abi.ERR_INVALID_ARG
 
 
+def test_measurement_entries_check_arguments_before_the_device(native):
+    """bmnd_mma_rates and bmnd_host_memory_direct reject bad arguments before
+    any CUDA call, so the checks run without a GPU."""
+    cols = (ctypes.c_int32 * 1)(40)      # not a multiple of 16
+    iss = (ctypes.c_int32 * 1)(2)
+    out = (ctypes.c_double * 1)()
+    sink = ctypes.c_int64(0)
+    assert native.bmnd_mma_rates(1, cols, iss, out, ctypes.byref(sink), 0) == _abi.ERR_INVALID_ARG
+    assert b"mma rate" in native.bmnd_last_error()
+    cols[0], iss[0] = 256, 3            # N x issuers above the 512 tensor-memory columns
+    assert native.bmnd_mma_rates(1, cols, iss, out, ctypes.byref(sink), 0) == _abi.ERR_INVALID_ARG
+    cols[0], iss[0] = 48, 5             # more issuing threads than warps 0..3
+    assert native.bmnd_mma_rates(1, cols, iss, out, ctypes.byref(sink), 0) == _abi.ERR_INVALID_ARG
+    assert native.bmnd_mma_rates(1, None, iss, out, ctypes.byref(sink), 0) == _abi.ERR_INVALID_ARG
+    assert native.bmnd_mma_rates(0, None, None, None, None, 0) == _abi.OK  # nothing to measure
+    assert native.bmnd_host_memory_direct(0, None) == _abi.ERR_INVALID_ARG
+
+
 def test_transform_matrices_match_reference():
     u = np.load(UNIT)
     for n in (4, 8):
