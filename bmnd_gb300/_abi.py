@@ -154,6 +154,7 @@ SIGNATURES = {
     "bmnd_abi_version": (_I32, []),
     "bmnd_last_error": (ctypes.c_char_p, []),
     "bmnd_launch_count": (_I32, [_U64P]),
+    "bmnd_device_alloc_count": (_I32, [_U64P]),
     "bmnd_host_memory_direct": (_I32, [ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
     "bmnd_reference_schedule": (
         _I32,
@@ -317,6 +318,13 @@ def host_memory_direct(device: int) -> bool:
     v = ctypes.c_int32(0)
     check(lib().bmnd_host_memory_direct(int(device), ctypes.byref(v)))
     return bool(v.value)
+
+
+def device_alloc_count() -> int:
+    """Device allocations the native library has made itself since it was loaded."""
+    n = ctypes.c_uint64(0)
+    check(lib().bmnd_device_alloc_count(ctypes.byref(n)))
+    return int(n.value)
 
 
 def launch_count() -> int:

@@ -20,9 +20,11 @@ namespace bmnd {
 namespace {
 thread_local std::string g_last_error;
 std::atomic<uint64_t> g_launches{0};
+std::atomic<uint64_t> g_device_allocs{0};
 }
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_device_alloc() { g_device_allocs.fetch_add(1, std::memory_order_relaxed); }
 void set_error(const std::string& msg) { g_last_error = msg; }
 void clear_error() { g_last_error.clear(); }
 int32_t fail(int32_t code, const std::string& msg) {
@@ -474,6 +476,13 @@ int32_t bmnd_launch_count(uint64_t* count) {
     clear_error();
     if (!count) return fail(BMND_ERR_INVALID_ARG, "null argument");
     *count = g_launches.load(std::memory_order_relaxed);
+    return BMND_OK;
+}
+
+int32_t bmnd_device_alloc_count(uint64_t* count) {
+    clear_error();
+    if (!count) return fail(BMND_ERR_INVALID_ARG, "null argument");
+    *count = g_device_allocs.load(std::memory_order_relaxed);
     return BMND_OK;
 }
 

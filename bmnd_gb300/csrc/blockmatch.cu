@@ -1904,6 +1904,7 @@ int32_t launch_ssd_tc(MatchArgs& a, cudaStream_t stream) {
     } else if (!a.no_alloc) {
         if (cudaMallocAsync(reinterpret_cast<void**>(&base), L.bytes, stream) == cudaSuccess) {
             owned = true;
+            note_device_alloc();
         } else {
             (void)cudaGetLastError();
             base = nullptr;
@@ -2007,6 +2008,7 @@ int32_t launch(MatchArgs& a, int code, int precision, cudaStream_t stream) {
             if (cudaMallocAsync(reinterpret_cast<void**>(&aux), static_cast<size_t>(need) * sizeof(float), stream) ==
                 cudaSuccess) {
                 aux_owned = true;
+                note_device_alloc();
             } else {
                 (void)cudaGetLastError();
                 aux = nullptr;

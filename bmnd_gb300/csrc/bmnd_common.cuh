@@ -24,6 +24,9 @@ int32_t fail(int32_t code, const std::string& msg);
 int32_t cuda_fail(cudaError_t err, const char* what);
 // counts kernel launches of this library (bmnd_launch_count)
 void note_launch();
+// counts the device allocations the library makes itself (fallbacks when a
+// caller's workspace has no room for a scratch array)
+void note_device_alloc();
 
 #define BMND_CUDA_TRY(expr)                                      \
     do {                                                         \

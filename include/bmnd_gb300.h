@@ -215,6 +215,11 @@ const char* bmnd_last_error(void);
  * the difference of two readings counts the launches between them. */
 int32_t bmnd_launch_count(uint64_t* count);
 
+/* Device allocations this library has made itself since it was loaded (a
+ * scratch array allocated on the stream when the caller's workspace has no
+ * room for it; bmnd_stage_noalloc never allocates). */
+int32_t bmnd_device_alloc_count(uint64_t* count);
+
 /* *direct = 1 when `device` reads pageable host memory through the host's page
  * tables (cudaDevAttrPageableMemoryAccessUsesHostPageTables, e.g. a Grace host
  * over NVLink-C2C): copies from and to ordinary host memory then run at the

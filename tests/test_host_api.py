@@ -35,10 +35,13 @@ def test_library_exports_every_declared_symbol(native):
 
 
 def test_launch_counter_reads_without_a_gpu(native):
-    """bmnd_launch_count needs no device; nothing has launched in a CPU-only process."""
+    """bmnd_launch_count and bmnd_device_alloc_count need no device."""
     n = _abi.launch_count()
     assert isinstance(n, int) and n >= 0
     assert _abi.launch_count() == n
+    a = _abi.device_alloc_count()
+    assert isinstance(a, int) and a >= 0
+    assert _abi.device_alloc_count() == a
 
 
 def test_struct_layout_matches_header(tmp_path):

@@ -50,10 +50,13 @@ def _no_alloc(torch, native, p, x, pilot, refs):
     from bmnd_gb300 import _abi
 
     out = torch.empty_like(x)
+    allocs = _abi.device_alloc_count()
     _abi.check(native.bmnd_stage_noalloc(ctypes.byref(p), x.data_ptr(),
                                          None if pilot is None else pilot.data_ptr(), refs.data_ptr(),
                                          refs.shape[0], out.data_ptr(), 0))
     torch.cuda.synchronize()
+    # the library made no device allocation of its own during the call
+    assert _abi.device_alloc_count() == allocs
     return out
 
 
